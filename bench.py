@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Benchmark: time-to-solution of the GLS map-making PCG on one GB300.
+
+Workload (default): 64 detectors, NSIDE 256, 48 segments x 131,072 samples
+(4.03e8 samples), FP32 operator with FP64 P^T sums and CG scalars, seeded
+synthetic scan/sky/1-over-f noise (sanepic_gb300.synth).  One step = one
+solve from x0 = 0 to |r|/|b| <= 1e-6 (crit = |r|^2/|b|^2 <= 1e-12):
+  value: b = P^T N^-1 d plus the PCG, inputs already resident in HBM,
+         CUDA-event time on the library's stream (the bench's torch stream);
+  e2e:   the same through the C ABI from host buffers: pointing, noise and
+         TOD uploaded (host->device) every step, maps read back.
+The dominant kernel (noise filter with the fused projection P) is timed live
+with CUDA events for the roofline; its algorithmic bytes are 16 B/sample
+(int32 pixel + 2 x FP32 cos/sin in, FP32 out) plus the map and filter rows.
+
+--impl reference times the reference's CPU algorithm on the host cores: the
+oracle port (the FP64 restatement of sanepic.cc's operator, same operation
+order), one process per core as the reference's MPI workers, on a bounded
+sample of the workload, projected linearly in samples to the full problem.
+(The reference binary itself is built only where its source is available; the
+GPU host has neither the source nor an x86 CPU.)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from sanepic_gb300 import synth  # noqa: E402
+
+METRIC = "time-to-solution at rel. residual 1e-6: learned-precond vs plain PCG, 1 GB300"
+STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
+# Iterations the reference's own preconditioner (the scalar diagonal,
+# sanepic.cc:1351-1355) needs to reach |r|/|b| = 1e-6 on this workload,
+# measured with the library's reference-diagonal mode (same algorithm).
+REFERENCE_ITERS_TO_1E6 = None
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi") is None:
+            return self
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        self.proc = subprocess.Popen(
+            ["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+             "--format=csv,noheader,nounits", "-lms", "200"],
+            stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"), f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    import sanepic_gb300 as sg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    spec = synth.spec_from_name(args.config)
+    t0 = time.time()
+    prob = synth.make_problem(spec)
+    gen_s = time.time() - t0
+    stream = torch.cuda.current_stream()
+    dets = sg.detectors_from_angles(prob["angles"])
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def upload(mm):
+        mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+        for d in range(spec.ndet):
+            mm.set_noise(d, prob["ispf"][d])
+            mm.set_tod(d, prob["tod"][d])
+
+    mm = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                     omega=prob["omega"], precision=spec.precision, device=local)
+    mm.set_stream(stream.cuda_stream)
+    upload(mm)
+
+    def device_step(precond):
+        mm.rhs()
+        return mm.solve(precond=precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+
+    # ---- value: inputs resident, CUDA events on the launching stream -------
+    for _ in range(args.warmup):
+        device_step(args.precond)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps, launches = [], 0
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            rep = device_step(args.precond)
+            reps.append(rep)
+            launches += rep["kernel_launches"] + 2  # + filter and P^T of the RHS
+        ev1.record(stream)
+        barrier()
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    clocks = clk.summary()
+    sec = ms_step / 1e3
+    if world > 1:
+        t = torch.tensor([sec], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    iters = reps[-1]["iterations"]
+    # ---- roofline of the dominant kernel (same stream, live) -----------------
+    prof = mm.profile_operator(reps=5)
+    ns_all = spec.ndet * spec.nseg * spec.ns
+    npix = mm.npix
+    esz = 4 if spec.precision == "f32" else 8
+    filt_bytes = ns_all * (4 + 2 * esz + esz) + npix * 4 * esz + spec.ndet * (spec.ns // 2 + 1) * esz
+    pt_bytes = ns_all * (4 + 2 * esz + esz) + npix * 3 * 8 + (npix + 1) * 8 + npix * 4
+    hbm, peak_kind = peaks()
+    achieved = filt_bytes / (prof["filter_ms"] * 1e-3) / 1e9
+    # ---- plain block-Jacobi vs the reference's diagonal (same workload) -------
+    extra = {}
+    if args.compare_diag:
+        rep_d = device_step("diag")
+        extra["diag_precond"] = {"iterations": rep_d["iterations"],
+                                 "seconds": rep_d["device_seconds"],
+                                 "converged": bool(rep_d["converged"])}
+        device_step(args.precond)
+    # ---- e2e through the C ABI with host buffers ------------------------------
+    h2d = (3 * prob["ra"].size * 8 + spec.ndet * prob["ispf"][0].size * 8
+           + spec.ndet * prob["tod"][0].size * 8)
+    d2h = 3 * 12 * spec.nside ** 2 * 8
+    e2e = []
+    for i in range(args.e2e_steps):
+        barrier()
+        te = time.perf_counter()
+        upload(mm)
+        device_step(args.precond)
+        maps = [mm.get_map(k) for k in ("I", "Q", "U")]
+        barrier()
+        e2e.append(time.perf_counter() - te)
+    e2e_s = float(np.median(e2e))
+    line = {
+        "metric": METRIC, "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": spec.precision == "f32" and "f32" or "f64",
+        "data": "synthetic (seeded spin+precession scan, iid sky, 1/f noise)",
+        "config": {"workload": args.config, "ndet": spec.ndet, "nside": spec.nside,
+                   "nseg": spec.nseg, "ns": spec.ns, "samples": ns_all, "npix_obs": npix,
+                   "precond": args.precond, "stop": "|r|/|b| <= 1e-6",
+                   "iterations": iters, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (pointing alone %.1f GB)" % (ns_all * 12 / 1e9)},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "kernel": "k_noise_filter",
+                     "peak_kind": peak_kind, "filter_ms": prof["filter_ms"],
+                     "pt_ms": prof["pt_ms"],
+                     "pt_GBps": pt_bytes / (prof["pt_ms"] * 1e-3) / 1e9},
+        "clocks": clocks,
+        "iter_per_sec": reps[-1]["iter_per_sec"],
+        "generation_s": gen_s,
+    }
+    line.update(extra)
+    if not args.no_cpu_baseline and rank == 0:
+        line["cpu_baseline"] = reference_cpu(
+            args, spec, iters_for_projection=extra.get("diag_precond", {}).get("iterations")
+            or REFERENCE_ITERS_TO_1E6)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    mm.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+def _port_worker(task):
+    """One host core of the CPU baseline: the oracle port's operator (the
+    reference's deproject + FFT weighting + scatter, FP64, same operation
+    order) on one segment of the workload, timed over `reps` applications."""
+    spec_kw, seg_problem, reps = task
+    import oracle  # the CPU checker; only this leg of bench.py uses it
+    spec = synth.ProblemSpec(**spec_kw)
+    spec.problem = seg_problem
+    prob = synth.make_problem(spec)
+    s = oracle.Setup(prob)
+    x = np.random.default_rng(seg_problem).standard_normal(3 * s.npix)
+    s.apply(x)
+    t = time.perf_counter()
+    for _ in range(reps):
+        s.apply(x)
+    return (time.perf_counter() - t) / reps, spec.ndet * spec.nseg * spec.ns
+
+
+def reference_cpu(args, spec, iters_for_projection=None):
+    """CPU baseline: the oracle port on every host core (one process per core,
+    each owning whole segments, as the reference's MPI workers do,
+    sanepic.cc:623-632), timed on a bounded sample of the workload and
+    projected linearly in samples to the full problem."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 2
+    workers = max(1, cores - 1)  # the reference's rank 0 holds no data
+    ndet_s = 8
+    spec_kw = dict(name="sample", ndet=ndet_s, nside=spec.nside, nseg=1, ns=spec.ns,
+                   hwp=spec.hwp, fknee=spec.fknee, alpha=spec.alpha,
+                   fknee_range=spec.fknee_range, alpha_range=spec.alpha_range)
+    reps = 3
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        res = pool.map(_port_worker, [(spec_kw, 100 + w, reps) for w in range(workers)])
+    t_apply = max(r[0] for r in res)           # workers run concurrently
+    n_sample = sum(r[1] for r in res)
+    n_full = spec.ndet * spec.nseg * spec.ns
+    rate = n_sample / t_apply                   # sample-applies per second, all cores
+    t_iter_full = 1.1 * n_full / rate           # + one true-residual apply per 10 iterations
+    proj = iters_for_projection * t_iter_full if iters_for_projection else None
+    return {"value": proj, "unit": "s", "cores": workers, "kind": "port",
+            "sample": (f"{workers} processes x (1 segment x {ndet_s} detectors x {spec.ns} "
+                       f"samples), {reps} operator applications each; projected linearly in "
+                       f"samples to {n_full:.3g} samples x {iters_for_projection} iterations of "
+                       f"the reference's diagonal-preconditioned PCG"),
+            "sample_applies_per_second": rate, "seconds_per_iteration_full": t_iter_full}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    spec = synth.spec_from_name(args.config)
+    cb = reference_cpu(args, spec, iters_for_projection=REFERENCE_ITERS_TO_1E6 or args.ref_iters)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": cb["value"] * 1e3 if cb["value"] else None,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": {"workload": args.config},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    if cb["value"] is None:
+        line["unavailable"] = cb["sample"]
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2_64det_nside256")
+    ap.add_argument("--precond", default="bj3")
+    ap.add_argument("--maxiter", type=int, default=2000)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--compare-diag", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-iters", type=int, default=None)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,169 @@
+/*
+ * sanepic_gpu.h -- C ABI of libsanepic_gpu, the GB300 (sm_103a) map-making
+ * library that replaces the reference's PCG hot path (patanch/SANEPIC,
+ * src/sanepic.cc).  Plain pointers and sizes only; callers own every host
+ * buffer (it is copied in or out), the library owns all device memory.
+ *
+ * The reference has no library interface: its hot path sits between its
+ * binary readers and map writers inside main().  Each entry point below names
+ * the part of sanepic.cc it replaces.  The drop-in `sanepic` executable
+ * (same getopt string, files and outputs) is built on these calls.
+ *
+ * Errors: every int-returning call returns SG_OK (0) or a negative SG_ERR_*
+ * code and never exits the process (the reference calls exit()).  The last
+ * error message of a context is available from sg_last_error().
+ * Threading: one context per host thread; contexts share no global state.
+ * Layouts: per-sample arrays are [det][seg][sample] (sanepic.cc:749, 874);
+ * compact maps are [I | Q | U], npix each, observed pixels in ascending RING
+ * order (sanepic.cc:904-921); full maps are 12*nside^2 RING doubles with 0 at
+ * unobserved pixels (sanepic.cc:2364-2388).
+ */
+#ifndef SANEPIC_GPU_H
+#define SANEPIC_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_OK 0
+#define SG_ERR_ARG (-1)         /* invalid argument or size */
+#define SG_ERR_CUDA (-2)        /* a CUDA call failed (message has details) */
+#define SG_ERR_STATE (-3)       /* call out of order (e.g. solve before rhs) */
+#define SG_ERR_POINTING (-4)    /* theta outside [0, pi]: the reference exits */
+#define SG_ERR_UNSUPPORTED (-5) /* e.g. ns not a power of two in [256, 131072] */
+#define SG_ERR_PRECOND (-6)     /* zero preconditioner entry (sanepic.cc:1344) */
+#define SG_ERR_NOT_CONVERGED (-7)
+
+#define SG_F64 0 /* every per-sample quantity in FP64 */
+#define SG_F32 1 /* TOD, cos/sin, FFT in FP32; P^T sums and CG in FP64 */
+
+#define SG_PRECOND_BJ3 0  /* 3x3 block-Jacobi (not in the reference) */
+#define SG_PRECOND_DIAG 1 /* the reference's diagonal, sanepic.cc:1351-1355 */
+#define SG_PRECOND_LEARNED 2 /* BJ3 + trained MLP correction, flexible PCG */
+
+/* map kinds for sg_get_map (output names: sanepic.cc:1618-1690, 1786-1801) */
+#define SG_MAP_I 0
+#define SG_MAP_Q 1
+#define SG_MAP_U 2
+#define SG_MAP_NVAR 3
+#define SG_MAP_Q_NVAR 4
+#define SG_MAP_U_NVAR 5
+#define SG_MAP_HITS 6
+#define SG_MAP_POL_HITS 7
+#define SG_MAP_COS2P 8
+#define SG_MAP_SIN2P 9
+
+typedef struct sg_ctx sg_ctx;
+
+typedef struct sg_desc {
+  long ns;          /* -l samples per segment (power of two, 256..131072) */
+  long nseg;        /* -n number of segments */
+  long ndet;        /* -d number of detectors */
+  long nside;       /* -N HEALPix nside */
+  int pol;          /* -p, must be 1 (pol=0 is broken in the reference) */
+  int hwp;          /* -h */
+  double omega;     /* -w HWP step, rad/sample (sanepic.cc:765) */
+  int precision;    /* SG_F64 or SG_F32 */
+  int device;       /* CUDA device ordinal */
+} sg_desc;
+
+typedef struct sg_det {
+  double offx; /* lel * pi/180 (sanepic.cc:460) */
+  double offy; /* xel * pi/180 (sanepic.cc:461) */
+  double psi;  /* detector angle, rad (sanepic.cc:462) */
+} sg_det;
+
+typedef struct sg_solve_opts {
+  int precond;       /* SG_PRECOND_* */
+  double stop_crit;  /* stop when |r|^2/|b|^2 <= stop_crit (reference 1e-15) */
+  int maxiter;       /* reference: 2000 (sanepic.cc:1415) */
+  int refresh_every; /* true residual b - A x every k iterations (reference 10) */
+  int verbose;       /* print the reference's "iter = ..., crit = ..." lines */
+  const double *x0;  /* -I start map, compact [3*npix], or NULL for zeros */
+  int use_graph;     /* replay each iteration from a captured CUDA graph */
+} sg_solve_opts;
+
+typedef struct sg_report {
+  int iterations;
+  int converged;
+  double crit;          /* final |r|^2/|b|^2 */
+  double var00;         /* |b|^2 */
+  double solve_seconds; /* wall time of the iterations */
+  double iter_per_sec;
+  double setup_seconds; /* preconditioner build inside sg_solve */
+  double device_seconds;  /* CUDA-event time of the iterations on the GPU */
+  long kernel_launches;   /* kernels this library launched during the solve */
+} sg_report;
+
+/* Creates a context on desc->device.  Replaces the parameter handling of
+ * main (sanepic.cc:315-446) and the MPI layout (sanepic.cc:591-632). */
+int sg_create(sg_ctx **ctx, const sg_desc *desc);
+
+/* Run this context's work on an existing CUDA stream (a cudaStream_t passed
+ * as void*; NULL restores the context's own stream).  The caller keeps
+ * ownership.  No reference counterpart (the reference has no GPU). */
+int sg_set_stream(sg_ctx *ctx, void *cuda_stream);
+
+/* Boresight pointing (full timelines of nsamp_total samples, read at
+ * isampmin[iseg], sanepic.cc:680-692; NULL isampmin = i*ns) and per-detector
+ * offsets/angles.  Runs the pointing expansion, HEALPix ang2pix, indpix
+ * compaction, hit counts and cross-link sums on the GPU.  Replaces
+ * sanepic.cc:452-464, 722-773, 828-951, 2594-2597, 2613-2626. */
+int sg_set_pointing(sg_ctx *ctx, const double *ra, const double *dec, const double *psi,
+                    long nsamp_total, const long *isampmin, const sg_det *dets);
+
+/* Inverse-noise spectrum of one detector (nssp values, the -u file).
+ * Replaces sanepic.cc:507-539 (including the bin-0 override, 536-537). */
+int sg_set_noise(sg_ctx *ctx, long det, const double *ispf, long nssp);
+
+/* TOD of one detector (full timeline; NaNs patched as sanepic.cc:784-790).
+ * Replaces sanepic.cc:776-803. */
+int sg_set_tod(sg_ctx *ctx, long det, const double *tod, long nsamp_total);
+
+/* b = P^T N^-1 d (sanepic.cc:1069-1125).  chi2 (may be NULL) receives the
+ * reference's chi2_0 = 2 sum |F d|^2 SpN (sanepic.cc:1089-1110). */
+int sg_rhs(sg_ctx *ctx, double *chi2);
+
+/* Number of observed pixels (npix, sanepic.cc:915). */
+long sg_npix(const sg_ctx *ctx);
+
+/* y = P^T N^-1 P x for a compact host vector [3*npix] (one operator pass,
+ * sanepic.cc:1428-1448); masked != 0 applies the pol degeneracy mask
+ * (sanepic.cc:1455-1459). */
+int sg_apply(sg_ctx *ctx, const double *x, double *y, int masked);
+
+/* N^-1 applied tile by tile to a [ndet][nseg][ns] host array (the
+ * r2c -> x SpN -> c2r of sanepic.cc:2429-2436, 2549-2582). */
+int sg_noise_filter(sg_ctx *ctx, const double *in, double *out);
+
+/* Preconditioned CG (sanepic.cc:1177-1761). */
+int sg_solve(sg_ctx *ctx, const sg_solve_opts *opts, sg_report *report);
+
+/* A full 12*nside^2 RING map (write_reduced_map, sanepic.cc:2364-2388). */
+int sg_get_map(sg_ctx *ctx, int kind, double *out_full);
+
+/* The compact solution [3*npix], i.e. the map__A_* output (sanepic.cc:1786-1788). */
+int sg_get_solution(sg_ctx *ctx, double *out_compact);
+
+/* RING pixel of every sample [ndet][nseg][ns] (the reference's datatopix). */
+int sg_get_pixels(sg_ctx *ctx, long *ring_pix);
+
+/* indpix [12*nside^2] (sanepic.cc:904-915). */
+int sg_get_indpix(sg_ctx *ctx, long *indpix);
+
+/* crit = |r|^2/|b|^2 after each iteration of the last solve (up to max). */
+int sg_get_crit_history(sg_ctx *ctx, double *out, int max);
+
+/* Diagnostics: average CUDA-event time (ms) of the two operator kernels over
+ * `reps` applications of A to the current search direction: ms[0] = noise
+ * filter with the fused projection P, ms[1] = P^T.  Overwrites only scratch
+ * buffers.  No reference counterpart (the reference has no profiling). */
+int sg_profile_operator(sg_ctx *ctx, int reps, double *ms);
+
+const char *sg_last_error(const sg_ctx *ctx);
+void sg_destroy(sg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

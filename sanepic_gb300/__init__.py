@@ -1,0 +1,265 @@
+"""sanepic_gb300 -- GB300-native GLS map-maker (the PCG hot path of SANEPIC).
+
+Python mirror of the C ABI in include/sanepic_gpu.h, over ctypes.  The compute
+runs only in libsanepic_gpu.so (hand-written sm_103a kernels); if that library
+is missing this package raises instead of falling back to anything else.
+
+    mm = MapMaker(ns, nseg, ndet, nside, precision="f32")
+    mm.set_pointing(ra, dec, psi, dets)     # boresight timelines + detectors
+    mm.set_noise(det, ispf); mm.set_tod(det, tod)
+    mm.rhs(); rep = mm.solve(precond="bj3", stop_crit=1e-12)
+    I = mm.get_map("I")
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsanepic_gpu.so")
+
+D2PI = 6.2831853071795864769252867665590057683943387987502
+
+SG_OK = 0
+ERRORS = {-1: "SG_ERR_ARG", -2: "SG_ERR_CUDA", -3: "SG_ERR_STATE", -4: "SG_ERR_POINTING",
+          -5: "SG_ERR_UNSUPPORTED", -6: "SG_ERR_PRECOND", -7: "SG_ERR_NOT_CONVERGED"}
+PRECISION = {"f64": 0, "f32": 1}
+PRECOND = {"bj3": 0, "diag": 1, "learned": 2}
+MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
+        "POL_HITS": 7, "COS2P": 8, "SIN2P": 9}
+
+# every symbol include/sanepic_gpu.h declares
+EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
+           "sg_apply", "sg_noise_filter", "sg_solve", "sg_get_map", "sg_get_solution",
+           "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
+           "sg_last_error", "sg_destroy"]
+
+
+class SanepicError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SgDesc(ctypes.Structure):
+    _fields_ = [("ns", ctypes.c_long), ("nseg", ctypes.c_long), ("ndet", ctypes.c_long),
+                ("nside", ctypes.c_long), ("pol", ctypes.c_int), ("hwp", ctypes.c_int),
+                ("omega", ctypes.c_double), ("precision", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class SgDet(ctypes.Structure):
+    _fields_ = [("offx", ctypes.c_double), ("offy", ctypes.c_double), ("psi", ctypes.c_double)]
+
+
+class SgSolveOpts(ctypes.Structure):
+    _fields_ = [("precond", ctypes.c_int), ("stop_crit", ctypes.c_double),
+                ("maxiter", ctypes.c_int), ("refresh_every", ctypes.c_int),
+                ("verbose", ctypes.c_int), ("x0", ctypes.POINTER(ctypes.c_double)),
+                ("use_graph", ctypes.c_int)]
+
+
+class SgReport(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("crit", ctypes.c_double), ("var00", ctypes.c_double),
+                ("solve_seconds", ctypes.c_double), ("iter_per_sec", ctypes.c_double),
+                ("setup_seconds", ctypes.c_double), ("device_seconds", ctypes.c_double),
+                ("kernel_launches", ctypes.c_long)]
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    """Load libsanepic_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with sanepic_gb300.build.build() "
+                           "(there is no CPU fallback)")
+    L = ctypes.CDLL(p)
+    c_p = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    lp = ctypes.POINTER(ctypes.c_long)
+    L.sg_create.argtypes = [ctypes.POINTER(c_p), ctypes.POINTER(SgDesc)]
+    L.sg_set_stream.argtypes = [c_p, c_p]
+    L.sg_set_pointing.argtypes = [c_p, dp, dp, dp, ctypes.c_long, lp, ctypes.POINTER(SgDet)]
+    L.sg_set_noise.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
+    L.sg_set_tod.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
+    L.sg_rhs.argtypes = [c_p, dp]
+    L.sg_npix.argtypes = [c_p]
+    L.sg_npix.restype = ctypes.c_long
+    L.sg_apply.argtypes = [c_p, dp, dp, ctypes.c_int]
+    L.sg_noise_filter.argtypes = [c_p, dp, dp]
+    L.sg_solve.argtypes = [c_p, ctypes.POINTER(SgSolveOpts), ctypes.POINTER(SgReport)]
+    L.sg_get_map.argtypes = [c_p, ctypes.c_int, dp]
+    L.sg_get_solution.argtypes = [c_p, dp]
+    L.sg_get_pixels.argtypes = [c_p, lp]
+    L.sg_get_indpix.argtypes = [c_p, lp]
+    L.sg_get_crit_history.argtypes = [c_p, dp, ctypes.c_int]
+    L.sg_profile_operator.argtypes = [c_p, ctypes.c_int, dp]
+    L.sg_last_error.argtypes = [c_p]
+    L.sg_last_error.restype = ctypes.c_char_p
+    L.sg_destroy.argtypes = [c_p]
+    if path is None:
+        _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class MapMaker:
+    """One map-making problem on one GPU (a context of the C ABI)."""
+
+    def __init__(self, ns: int, nseg: int, ndet: int, nside: int, hwp: bool = False,
+                 omega: float = 0.0, precision: str = "f32", device: int = 0):
+        self.L = load_library()
+        self.ns, self.nseg, self.ndet, self.nside = ns, nseg, ndet, nside
+        self.precision = precision
+        desc = SgDesc(ns, nseg, ndet, nside, 1, int(bool(hwp)), float(omega),
+                      PRECISION[precision], device)
+        h = ctypes.c_void_p()
+        rc = self.L.sg_create(ctypes.byref(h), ctypes.byref(desc))
+        self.h = h
+        if rc != SG_OK:
+            msg = self.L.sg_last_error(h).decode() if h.value else "sg_create failed"
+            self.close()
+            raise SanepicError(rc, msg)
+
+    def _check(self, rc: int):
+        if rc < 0:
+            raise SanepicError(rc, self.L.sg_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.sg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: Optional[int]):
+        """Run on an existing cudaStream_t (an integer handle), None = own stream."""
+        self._check(self.L.sg_set_stream(self.h, ctypes.c_void_p(stream_handle or None)))
+
+    # ---- inputs -----------------------------------------------------------
+    def set_pointing(self, ra, dec, psi, dets: Sequence, isampmin=None):
+        ra, dec, psi = _f64(ra), _f64(dec), _f64(psi)
+        arr = (SgDet * self.ndet)(*[SgDet(*map(float, d)) for d in dets])
+        isp = None
+        if isampmin is not None:
+            self._isamp = np.ascontiguousarray(isampmin, dtype=np.int64)
+            isp = self._isamp.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
+        self._check(self.L.sg_set_pointing(self.h, _dp(ra), _dp(dec), _dp(psi), ra.size, isp, arr))
+        self.npix = int(self.L.sg_npix(self.h))
+
+    def set_noise(self, det: int, ispf):
+        ispf = _f64(ispf)
+        self._check(self.L.sg_set_noise(self.h, det, _dp(ispf), ispf.size))
+
+    def set_tod(self, det: int, tod):
+        tod = _f64(tod)
+        self._check(self.L.sg_set_tod(self.h, det, _dp(tod), tod.size))
+
+    # ---- operator -----------------------------------------------------------
+    def rhs(self) -> float:
+        chi2 = ctypes.c_double(0.0)
+        self._check(self.L.sg_rhs(self.h, ctypes.byref(chi2)))
+        return chi2.value
+
+    def apply(self, x, masked: bool = False) -> np.ndarray:
+        x = _f64(x)
+        y = np.empty(3 * self.npix)
+        self._check(self.L.sg_apply(self.h, _dp(x), _dp(y), int(masked)))
+        return y
+
+    def noise_filter(self, arr) -> np.ndarray:
+        a = _f64(arr).reshape(-1)
+        out = np.empty_like(a)
+        self._check(self.L.sg_noise_filter(self.h, _dp(a), _dp(out)))
+        return out
+
+    def solve(self, precond: str = "bj3", stop_crit: float = 1e-15, maxiter: int = 2000,
+              refresh_every: int = 10, verbose: bool = False, x0=None,
+              use_graph: bool = True) -> dict:
+        x0p = None
+        if x0 is not None:
+            self._x0 = _f64(x0)
+            x0p = _dp(self._x0)
+        o = SgSolveOpts(PRECOND[precond], stop_crit, maxiter, refresh_every, int(verbose),
+                        x0p, int(use_graph))
+        rep = SgReport()
+        self._check(self.L.sg_solve(self.h, ctypes.byref(o), ctypes.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in SgReport._fields_}
+
+    # ---- outputs ------------------------------------------------------------
+    def get_map(self, kind: str) -> np.ndarray:
+        out = np.empty(12 * self.nside * self.nside)
+        self._check(self.L.sg_get_map(self.h, MAPS[kind], _dp(out)))
+        return out
+
+    def solution(self) -> np.ndarray:
+        out = np.empty(3 * self.npix)
+        self._check(self.L.sg_get_solution(self.h, _dp(out)))
+        return out
+
+    def pixels(self) -> np.ndarray:
+        out = np.empty(self.ndet * self.nseg * self.ns, dtype=np.int64)
+        self._check(self.L.sg_get_pixels(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
+        return out
+
+    def indpix(self) -> np.ndarray:
+        out = np.empty(12 * self.nside * self.nside, dtype=np.int64)
+        self._check(self.L.sg_get_indpix(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
+        return out
+
+    def profile_operator(self, reps: int = 5) -> dict:
+        ms = np.zeros(2)
+        self._check(self.L.sg_profile_operator(self.h, reps, _dp(ms)))
+        return {"filter_ms": float(ms[0]), "pt_ms": float(ms[1])}
+
+    def crit_history(self, max_n: int = 100000) -> np.ndarray:
+        out = np.empty(max_n)
+        n = self._check(self.L.sg_get_crit_history(self.h, _dp(out), max_n))
+        return out[:n].copy()
+
+
+def detectors_from_angles(angles_deg, offsets=None):
+    """sg_det rows (offx, offy, psi) as the reference derives them
+    (sanepic.cc:458-463): zero offsets unless given, psi = angle in radians."""
+    rows = []
+    for d, a in enumerate(angles_deg):
+        ox, oy = (0.0, 0.0) if offsets is None else offsets[d]
+        rows.append((ox, oy, float(a) / 180.0 * D2PI / 2.0))
+    return rows
+
+
+def from_problem(prob, precision: Optional[str] = None, device: int = 0,
+                 with_tod: bool = True) -> MapMaker:
+    """A MapMaker loaded with an in-memory problem (see sanepic_gb300.synth)."""
+    spec = prob["spec"]
+    prec = precision or spec.precision
+    mm = MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                  omega=prob["omega"], precision=prec, device=device)
+    mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], detectors_from_angles(prob["angles"]),
+                    prob.get("isampmin"))
+    for d in range(spec.ndet):
+        mm.set_noise(d, prob["ispf"][d])
+        if with_tod and "tod" in prob:
+            mm.set_tod(d, prob["tod"][d])
+    return mm

@@ -1,0 +1,919 @@
+// sg_api.cu -- host side of libsanepic_gpu: the context, the setup pipeline
+// and the PCG driver behind the C ABI in include/sanepic_gpu.h.
+//
+// All device memory is owned here (cudaMalloc at setup, nothing allocated
+// inside the iteration loop).  One CG iteration is a fixed sequence of
+// launches on one stream -- noise filter (P fused into its load), P^T, three
+// vector kernels -- captured once into a CUDA graph and replayed; the host
+// reads back one scalar per iteration to test convergence.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/sanepic_gpu.h"
+#include "sg_kernels.h"
+
+using namespace sg;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t n) {
+    release();
+    bytes = n;
+    if (n == 0) return cudaSuccess;
+    return cudaMalloc(&p, n);
+  }
+  template <typename U>
+  U* as() const {
+    return reinterpret_cast<U*>(p);
+  }
+};
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+const double kD2PI = 6.2831853071795864769252867665590057683943387987502;
+
+}  // namespace
+
+struct sg_ctx {
+  sg_desc desc{};
+  std::string err;
+  cudaStream_t st = nullptr;
+  cudaStream_t own_st = nullptr;  // the stream the context created
+  int f32 = 0;       // precision
+  int esize = 8;     // bytes per real
+  long long ns = 0, nseg = 0, ndet = 0, ntiles = 0, nsamp = 0, npixfull = 0;
+  int logm = 0, S = 1, nclusters = 1;
+  long long npix = 0;
+  std::vector<int> indpix_host;
+  std::vector<long long> isampmin;
+
+  DevBuf pix, cs, y, tod, csr_off, csr_idx, csr_cs, hits, indpix, sumcross;
+  DevBuf filt, tw_lo, tw_hi, g0, ntab;
+  DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
+  cplx<float> wn1f{1.f, 0.f};
+  cplx<double> wn1d{1.0, 0.0};
+  CgScalars* sc_host = nullptr;  // pinned
+
+  bool have_pointing = false, have_rhs = false, have_solution = false;
+  bool have_bj3 = false, have_diag = false;
+  std::vector<char> have_noise, have_tod;
+  std::vector<double> crit_hist;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+  std::map<std::pair<int, int>, long long> graph_launches;
+  long long launches = 0;  // kernels launched by this context
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(SG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  ~sg_ctx() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (sc_host) cudaFreeHost(sc_host);
+    if (own_st) cudaStreamDestroy(own_st);
+  }
+
+  // ---- operator pieces ---------------------------------------------------
+  template <typename T>
+  FilterArgs<T> filter_args(int mode, const T* in, T* out, long long ntiles_, int nseg_,
+                            int filt_abs) {
+    FilterArgs<T> a{};
+    a.ntiles = ntiles_;
+    a.nseg = nseg_;
+    a.mode = mode;
+    a.filt_abs = filt_abs;
+    a.tod = in;
+    a.pix = pix.as<int>();
+    a.cs = cs.as<T>();
+    a.map = dmap.as<T>();
+    a.filt = filt.as<T>();
+    a.out = out;
+    a.tw_lo = tw_lo.as<cplx<T>>();
+    a.tw_hi = tw_hi.as<cplx<T>>();
+    return a;
+  }
+
+  cudaError_t launch_filter(int mode, const void* in, void* out, long long ntiles_, int nseg_,
+                            int filt_abs) {
+    const int ncl = (int)std::min<long long>(nclusters, ntiles_);
+    launches++;
+    if (f32) {
+      auto a = filter_args<float>(mode, (const float*)in, (float*)out, ntiles_, nseg_, filt_abs);
+      a.wn1 = wn1f;
+      return filter_launch<float>(a, logm, S, ncl, st);
+    }
+    auto a = filter_args<double>(mode, (const double*)in, (double*)out, ntiles_, nseg_, filt_abs);
+    a.wn1 = wn1d;
+    return filter_launch<double>(a, logm, S, ncl, st);
+  }
+
+  cudaError_t launch_pt(const void* yy, double* out, bool masked) {
+    const int* h = masked ? hits.as<int>() : nullptr;
+    launches++;
+    if (f32)
+      return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(),
+                              csr_cs.as<float>(), (const float*)yy, npix, h, out, st);
+    return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(),
+                             csr_cs.as<double>(), (const double*)yy, npix, h, out, st);
+  }
+
+  cudaError_t to_map(const double* v) {
+    launches++;
+    if (f32) return to_map4<float>(v, npix, dmap.as<float>(), st);
+    return to_map4<double>(v, npix, dmap.as<double>(), st);
+  }
+
+  // out = A v (masked or not); v is a device compact vector
+  cudaError_t apply_dev(const double* v, double* out, bool masked) {
+    cudaError_t e = to_map(v);
+    if (e == cudaSuccess) e = launch_filter(kLoadProj, nullptr, y.p, ntiles, (int)nseg, 0);
+    if (e == cudaSuccess) e = launch_pt(y.p, out, masked);
+    return e;
+  }
+
+  CgVecs vecs(int precond) {
+    CgVecs v{};
+    v.npix = npix;
+    v.x = x.as<double>();
+    v.r = r.as<double>();
+    v.d = d.as<double>();
+    v.q = q.as<double>();
+    v.z = z.as<double>();
+    v.rprev = rprev.as<double>();
+    v.b = b.as<double>();
+    v.minv = minv.as<double>();
+    v.mdiag = mdiag.as<double>();
+    v.hits_true = hits.as<int>();
+    v.precond = precond;
+    v.part = part.as<double>();
+    v.sc = sc.as<CgScalars>();
+    return v;
+  }
+
+  // one PCG iteration (sanepic.cc:1417-1610) as a launch sequence
+  cudaError_t enqueue_iteration(int precond, bool refresh) {
+    CgVecs v = vecs(precond);
+    cudaError_t e = launch_filter(kLoadProj, nullptr, y.p, ntiles, (int)nseg, 0);
+    if (e == cudaSuccess) e = launch_pt(y.p, q.as<double>(), true);
+    if (e == cudaSuccess) e = cg_step_a(v, st);
+    if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 0, st);
+    launches += 3;  // step a, b, c
+    if (refresh) {
+      if (e == cudaSuccess) e = apply_dev(x.as<double>(), q.as<double>(), true);
+      if (e == cudaSuccess) e = cg_refresh_r(v, 0, st);
+      launches++;
+    }
+    if (e == cudaSuccess)
+      e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 0, st)
+              : cg_step_c<double>(v, dmap.as<double>(), 0, st);
+    return e;
+  }
+
+  cudaError_t run_iteration(int precond, bool refresh, bool use_graph) {
+    if (!use_graph) return enqueue_iteration(precond, refresh);
+    auto key = std::make_pair(precond, refresh ? 1 : 0);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      cudaGraph_t g;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return e;
+      const long long before = launches;
+      e = enqueue_iteration(precond, refresh);
+      graph_launches[key] = launches - before;
+      launches = before;
+      cudaError_t e2 = cudaStreamEndCapture(st, &g);
+      if (e != cudaSuccess) return e;
+      if (e2 != cudaSuccess) return e2;
+      cudaGraphExec_t ge;
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return e;
+      it = graphs.emplace(key, ge).first;
+    }
+    launches += graph_launches[key];
+    return cudaGraphLaunch(it->second, st);
+  }
+};
+
+// ---------------------------------------------------------------------------
+static bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+extern "C" int sg_create(sg_ctx** out, const sg_desc* desc) {
+  if (!out || !desc) return SG_ERR_ARG;
+  *out = nullptr;
+  sg_ctx* c = new sg_ctx();
+  c->desc = *desc;
+  auto bad = [&](int code, const char* msg) {
+    // a failed create still returns the context so sg_last_error works
+    c->err = msg;
+    *out = c;
+    return code;
+  };
+  if (desc->pol != 1) return bad(SG_ERR_UNSUPPORTED, "pol must be 1 (pol=0 is broken in the reference)");
+  if (!is_pow2(desc->ns) || desc->ns < 256 || desc->ns > 131072)
+    return bad(SG_ERR_UNSUPPORTED, "ns must be a power of two in [256, 131072]");
+  if (desc->nseg < 1 || desc->ndet < 1) return bad(SG_ERR_ARG, "nseg and ndet must be >= 1");
+  if (desc->nside < 1 || desc->nside > 8192) return bad(SG_ERR_ARG, "nside out of range");
+  const long long nsamp = (long long)desc->ns * desc->nseg * desc->ndet;
+  if (nsamp >= (1LL << 32)) return bad(SG_ERR_UNSUPPORTED, "more than 2^32 samples");
+  cudaError_t e = cudaSetDevice(desc->device);
+  if (e != cudaSuccess) return bad(SG_ERR_CUDA, cudaGetErrorString(e));
+  e = cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bad(SG_ERR_CUDA, cudaGetErrorString(e));
+  c->st = c->own_st;
+  c->f32 = desc->precision == SG_F32;
+  c->esize = c->f32 ? 4 : 8;
+  c->ns = desc->ns;
+  c->nseg = desc->nseg;
+  c->ndet = desc->ndet;
+  c->ntiles = c->nseg * c->ndet;
+  c->nsamp = nsamp;
+  c->npixfull = 12LL * desc->nside * desc->nside;
+  const long long M = c->ns / 2;
+  int logm = 0;
+  while ((1LL << logm) < M) logm++;
+  c->logm = logm;
+  const long long emax = c->f32 ? 8192 : 4096;  // complex elements per CTA buffer
+  c->S = (int)std::max<long long>(1, M / emax);
+  c->nclusters = c->f32 ? filter_max_clusters<float>(logm, c->S)
+                        : filter_max_clusters<double>(logm, c->S);
+  if (c->nclusters <= 0) return bad(SG_ERR_CUDA, "noise-filter kernel cannot be scheduled");
+  c->have_noise.assign(c->ndet, 0);
+  c->have_tod.assign(c->ndet, 0);
+  // twiddle tables W_M^j = W_M^{64 jh} W_M^{jl}, computed in FP64
+  {
+    std::vector<double> lo(2 * 64), hi(2 * (M / 64));
+    for (int jl = 0; jl < 64; jl++) {
+      double a = kD2PI * (double)jl / (double)M;
+      lo[2 * jl] = cos(a);
+      lo[2 * jl + 1] = -sin(a);
+    }
+    for (long long jh = 0; jh < M / 64; jh++) {
+      double a = kD2PI * (double)(64 * jh) / (double)M;
+      hi[2 * jh] = cos(a);
+      hi[2 * jh + 1] = -sin(a);
+    }
+    const double a1 = kD2PI / (double)(2 * M);
+    c->wn1d = cplx<double>{cos(a1), -sin(a1)};
+    c->wn1f = cplx<float>{(float)cos(a1), (float)-sin(a1)};
+    if ((e = c->tw_lo.alloc(lo.size() * c->esize)) != cudaSuccess ||
+        (e = c->tw_hi.alloc(hi.size() * c->esize)) != cudaSuccess)
+      return bad(SG_ERR_CUDA, cudaGetErrorString(e));
+    if (c->f32) {
+      std::vector<float> lf(lo.begin(), lo.end()), hf(hi.begin(), hi.end());
+      cudaMemcpy(c->tw_lo.p, lf.data(), lf.size() * 4, cudaMemcpyHostToDevice);
+      cudaMemcpy(c->tw_hi.p, hf.data(), hf.size() * 4, cudaMemcpyHostToDevice);
+    } else {
+      cudaMemcpy(c->tw_lo.p, lo.data(), lo.size() * 8, cudaMemcpyHostToDevice);
+      cudaMemcpy(c->tw_hi.p, hi.data(), hi.size() * 8, cudaMemcpyHostToDevice);
+    }
+  }
+  if ((e = c->filt.alloc((size_t)c->ndet * (M + 1) * c->esize)) != cudaSuccess ||
+      (e = c->g0.alloc(sizeof(double) * c->ndet)) != cudaSuccess ||
+      (e = c->y.alloc((size_t)nsamp * c->esize)) != cudaSuccess ||
+      (e = c->tod.alloc((size_t)nsamp * c->esize)) != cudaSuccess)
+    return bad(SG_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = cudaMallocHost(&c->sc_host, sizeof(CgScalars))) != cudaSuccess)
+    return bad(SG_ERR_CUDA, cudaGetErrorString(e));
+  *out = c;
+  return SG_OK;
+}
+
+extern "C" void sg_destroy(sg_ctx* c) { delete c; }
+
+extern "C" int sg_set_stream(sg_ctx* c, void* stream) {
+  if (!c) return SG_ERR_ARG;
+  cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c->own_st;
+  if (s != c->st) {
+    cudaStreamSynchronize(c->st);
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();  // graphs were captured on the old stream
+    c->graph_launches.clear();
+    c->st = s;
+  }
+  return SG_OK;
+}
+
+extern "C" const char* sg_last_error(const sg_ctx* c) {
+  return c ? c->err.c_str() : "null context";
+}
+
+extern "C" long sg_npix(const sg_ctx* c) { return c ? (long)c->npix : -1; }
+
+// ---------------------------------------------------------------------------
+extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
+                               const double* psi, long nsamp_total, const long* isampmin,
+                               const sg_det* dets) {
+  if (!c) return SG_ERR_ARG;
+  if (!ra || !dec || !psi || !dets) return c->fail(SG_ERR_ARG, "null pointing array");
+  cudaSetDevice(c->desc.device);
+  const long long ns = c->ns, nseg = c->nseg, ndet = c->ndet, nsd = ns * nseg;
+  c->isampmin.resize(nseg);
+  for (long long g = 0; g < nseg; g++) {
+    c->isampmin[g] = isampmin ? isampmin[g] : g * ns;
+    if (c->isampmin[g] < 0 || c->isampmin[g] + ns > nsamp_total)
+      return c->fail(SG_ERR_ARG, "segment %lld [%lld, %lld] outside the %ld-sample timeline",
+                     g, c->isampmin[g], c->isampmin[g] + ns - 1, nsamp_total);
+  }
+  // per-segment boresight, psi NaN-patched within the segment (sanepic.cc:722-727)
+  std::vector<double> hra(nsd), hdec(nsd), hpsi(nsd);
+  for (long long g = 0; g < nseg; g++) {
+    const long long o = c->isampmin[g];
+    memcpy(&hra[g * ns], ra + o, sizeof(double) * ns);
+    memcpy(&hdec[g * ns], dec + o, sizeof(double) * ns);
+    memcpy(&hpsi[g * ns], psi + o, sizeof(double) * ns);
+    for (long long i = 1; i < ns; i++) {
+      double& v = hpsi[g * ns + i];
+      if (!(v > 0) && !(v <= 0.0)) v = hpsi[g * ns + i - 1];
+    }
+  }
+  // detectors grouped by identical offsets share the pixelisation
+  std::vector<int> grp_off, grp_det;
+  {
+    std::vector<char> used(ndet, 0);
+    for (long long dd = 0; dd < ndet; dd++) {
+      if (used[dd]) continue;
+      grp_off.push_back((int)grp_det.size());
+      for (long long e2 = dd; e2 < ndet; e2++)
+        if (!used[e2] && dets[e2].offx == dets[dd].offx && dets[e2].offy == dets[dd].offy) {
+          used[e2] = 1;
+          grp_det.push_back((int)e2);
+        }
+    }
+    grp_off.push_back((int)grp_det.size());
+  }
+  std::vector<double> offx(ndet), offy(ndet), pdet(ndet);
+  for (long long dd = 0; dd < ndet; dd++) {
+    offx[dd] = dets[dd].offx;
+    offy[dd] = dets[dd].offy;
+    pdet[dd] = dets[dd].psi;
+  }
+  cudaError_t e;
+  DevBuf dra, ddec, dpsi, doffx, doffy, dpdet, dgoff, dgdet, ring, psip, psipfp, flag, count,
+      scratch, npix_dev;
+  const long long nsamp = c->nsamp;
+  const bool hwp = c->desc.hwp != 0;
+#define SG_TRY(x)                                   \
+  do {                                              \
+    e = (x);                                        \
+    if (e != cudaSuccess) return c->cuda_fail(e, #x); \
+  } while (0)
+  SG_TRY(dra.alloc(sizeof(double) * nsd));
+  SG_TRY(ddec.alloc(sizeof(double) * nsd));
+  SG_TRY(dpsi.alloc(sizeof(double) * nsd));
+  SG_TRY(doffx.alloc(sizeof(double) * ndet));
+  SG_TRY(doffy.alloc(sizeof(double) * ndet));
+  SG_TRY(dpdet.alloc(sizeof(double) * ndet));
+  SG_TRY(dgoff.alloc(sizeof(int) * grp_off.size()));
+  SG_TRY(dgdet.alloc(sizeof(int) * grp_det.size()));
+  SG_TRY(ring.alloc(sizeof(int) * nsamp));
+  SG_TRY(psip.alloc(sizeof(double) * nsamp));
+  if (hwp) SG_TRY(psipfp.alloc(sizeof(double) * nsamp));
+  SG_TRY(flag.alloc(sizeof(int)));
+  SG_TRY(cudaMemcpyAsync(dra.p, hra.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(ddec.p, hdec.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(dpsi.p, hpsi.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(doffx.p, offx.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(doffy.p, offy.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(dpdet.p, pdet.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(dgoff.p, grp_off.data(), sizeof(int) * grp_off.size(), cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemcpyAsync(dgdet.p, grp_det.data(), sizeof(int) * grp_det.size(), cudaMemcpyHostToDevice, c->st));
+  SG_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), c->st));
+  PointingArgs pa{};
+  pa.ns = ns;
+  pa.nseg = (int)nseg;
+  pa.ndet = (int)ndet;
+  pa.ra = dra.as<double>();
+  pa.dec = ddec.as<double>();
+  pa.psi = dpsi.as<double>();
+  pa.offx = doffx.as<double>();
+  pa.offy = doffy.as<double>();
+  pa.psidet = dpdet.as<double>();
+  pa.hwp = hwp ? 1 : 0;
+  pa.omega = c->desc.omega;
+  pa.nside = c->desc.nside;
+  pa.ring_pix = ring.as<int>();
+  pa.psip = psip.as<double>();
+  pa.psipfp = hwp ? psipfp.as<double>() : nullptr;
+  pa.error_flag = flag.as<int>();
+  SG_TRY(pointing_launch_groups(pa, (int)grp_off.size() - 1, dgoff.as<int>(), dgdet.as<int>(),
+                                c->st));
+  int hflag = 0;
+  SG_TRY(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  SG_TRY(cudaStreamSynchronize(c->st));
+  if (hflag)
+    return c->fail(SG_ERR_POINTING, "theta out of range in ang2pix (the reference exits here)");
+  dra.release();
+  ddec.release();
+  dpsi.release();
+  // NaN pointing: reuse the previous pixel in the reference's loop order
+  // (det, seg, sample; sanepic.cc:851-873).  Rare, so done on the host.
+  {
+    std::vector<int> hr(nsamp);
+    SG_TRY(cudaMemcpy(hr.data(), ring.p, sizeof(int) * nsamp, cudaMemcpyDeviceToHost));
+    bool any = false;
+    int prev = 0;
+    for (long long i = 0; i < nsamp; i++) {
+      if (hr[i] < 0) {
+        hr[i] = prev;
+        any = true;
+      }
+      prev = hr[i];
+    }
+    if (any)
+      SG_TRY(cudaMemcpy(ring.p, hr.data(), sizeof(int) * nsamp, cudaMemcpyHostToDevice));
+  }
+  // indpix, compact pixels, hit counts
+  SG_TRY(count.alloc(sizeof(int) * c->npixfull));
+  SG_TRY(cudaMemsetAsync(count.p, 0, sizeof(int) * c->npixfull, c->st));
+  SG_TRY(hist_launch(ring.as<int>(), nsamp, count.as<int>(), c->st));
+  SG_TRY(c->indpix.alloc(sizeof(int) * c->npixfull));
+  const size_t tb = indpix_tmp_bytes(c->npixfull);
+  SG_TRY(scratch.alloc(tb));
+  SG_TRY(npix_dev.alloc(sizeof(long long)));
+  SG_TRY(indpix_launch(count.as<int>(), c->npixfull, c->indpix.as<int>(),
+                       npix_dev.as<long long>(), scratch.p, tb, c->st));
+  long long npix = 0;
+  SG_TRY(cudaMemcpyAsync(&npix, npix_dev.p, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+  SG_TRY(cudaStreamSynchronize(c->st));
+  c->npix = npix;
+  c->indpix_host.resize(c->npixfull);
+  SG_TRY(cudaMemcpy(c->indpix_host.data(), c->indpix.p, sizeof(int) * c->npixfull,
+                    cudaMemcpyDeviceToHost));
+  SG_TRY(c->pix.alloc(sizeof(int) * nsamp));
+  SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), nsamp, c->pix.as<int>(), c->st));
+  SG_TRY(c->hits.alloc(sizeof(int) * npix));
+  SG_TRY(hits_launch(count.as<int>(), c->indpix.as<int>(), c->npixfull, c->hits.as<int>(), c->st));
+  // pixel-sorted sample index (CSR) for P^T
+  const size_t ctb = csr_tmp_bytes(nsamp, npix);
+  SG_TRY(scratch.alloc(ctb));
+  SG_TRY(c->csr_off.alloc(sizeof(long long) * (npix + 1)));
+  SG_TRY(c->csr_idx.alloc(sizeof(uint32_t) * nsamp));
+  SG_TRY(csr_build(c->pix.as<int>(), nsamp, npix, c->hits.as<int>(), c->csr_off.as<long long>(),
+                   c->csr_idx.as<uint32_t>(), scratch.p, ctb, c->st));
+  scratch.release();
+  // angles: (cos 2psip, sin 2psip) in time order and in CSR order
+  SG_TRY(c->cs.alloc((size_t)2 * nsamp * c->esize));
+  SG_TRY(c->csr_cs.alloc((size_t)2 * nsamp * c->esize));
+  if (c->f32) {
+    SG_TRY(angles_launch<float>(psip.as<double>(), nsamp, c->cs.as<float>(), c->st));
+    SG_TRY(gather_cs_launch<float>(c->cs.as<float>(), c->csr_idx.as<uint32_t>(), nsamp,
+                                   c->csr_cs.as<float>(), c->st));
+  } else {
+    SG_TRY(angles_launch<double>(psip.as<double>(), nsamp, c->cs.as<double>(), c->st));
+    SG_TRY(gather_cs_launch<double>(c->cs.as<double>(), c->csr_idx.as<uint32_t>(), nsamp,
+                                    c->csr_cs.as<double>(), c->st));
+  }
+  // cross-link sums with psipFP (sanepic.cc:1258, 2594-2597)
+  SG_TRY(c->sumcross.alloc(sizeof(double) * 3 * npix));
+  SG_TRY(sumcross_launch(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                         hwp ? psipfp.as<double>() : psip.as<double>(), npix,
+                         c->sumcross.as<double>(), c->st));
+  // CG vectors
+  const size_t vb = sizeof(double) * 3 * npix;
+  SG_TRY(c->x.alloc(vb));
+  SG_TRY(c->r.alloc(vb));
+  SG_TRY(c->d.alloc(vb));
+  SG_TRY(c->q.alloc(vb));
+  SG_TRY(c->z.alloc(vb));
+  SG_TRY(c->rprev.alloc(vb));
+  SG_TRY(c->b.alloc(vb));
+  SG_TRY(c->minv.alloc(sizeof(double) * 6 * npix));
+  SG_TRY(c->mdiag.alloc(vb));
+  SG_TRY(c->mp_raw.alloc(vb));
+  SG_TRY(c->part.alloc(sizeof(double) * 4 * kCgBlocks));
+  SG_TRY(c->sc.alloc(sizeof(CgScalars)));
+  SG_TRY(c->dmap.alloc((size_t)4 * npix * c->esize));
+  SG_TRY(cudaMemsetAsync(c->x.p, 0, vb, c->st));
+  SG_TRY(cudaStreamSynchronize(c->st));
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+  c->have_pointing = true;
+  c->have_rhs = c->have_solution = c->have_bj3 = c->have_diag = false;
+  return SG_OK;
+}
+
+extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) {
+  if (!c) return SG_ERR_ARG;
+  if (det < 0 || det >= c->ndet || !ispf || nssp < 2)
+    return c->fail(SG_ERR_ARG, "bad detector index or noise spectrum");
+  cudaSetDevice(c->desc.device);
+  const long long ns = c->ns, M = ns / 2;
+  std::vector<double> spn(M + 1);
+  for (long long k = 0; k <= M; k++) {
+    const long long idx = (long long)((double)k / nssp * ns);  // sanepic.cc:535
+    if (idx < 0 || idx >= nssp)
+      return c->fail(SG_ERR_ARG, "noise spectrum of %ld values is too short for ns=%lld", nssp, ns);
+    spn[k] = ispf[idx] / (double)ns / (double)ns;
+  }
+  spn[0] = ispf[1] * 1e-6 / (double)ns / (double)ns;  // sanepic.cc:536-537
+  // diagonal of the circulant N^-1 in the time domain: c2r(spn)[0]
+  double g = spn[0];
+  for (long long k = 1; k < M; k++) g += 2.0 * spn[k];
+  g += spn[M];
+  cudaError_t e;
+  if (c->f32) {
+    std::vector<float> f(spn.begin(), spn.end());
+    e = cudaMemcpy(c->filt.as<float>() + det * (M + 1), f.data(), 4 * (M + 1), cudaMemcpyHostToDevice);
+  } else {
+    e = cudaMemcpy(c->filt.as<double>() + det * (M + 1), spn.data(), 8 * (M + 1),
+                   cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(c->g0.as<double>() + det, &g, 8, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
+  c->have_noise[det] = 1;
+  c->have_bj3 = c->have_diag = c->have_rhs = false;
+  return SG_OK;
+}
+
+extern "C" int sg_set_tod(sg_ctx* c, long det, const double* tod, long nsamp_total) {
+  if (!c) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "set the pointing before the TOD");
+  if (det < 0 || det >= c->ndet || !tod) return c->fail(SG_ERR_ARG, "bad detector or TOD");
+  cudaSetDevice(c->desc.device);
+  const long long ns = c->ns, nseg = c->nseg, nsd = ns * nseg;
+  std::vector<double> h(nsd);
+  for (long long g = 0; g < nseg; g++) {
+    const long long o = c->isampmin[g];
+    if (o + ns > nsamp_total) return c->fail(SG_ERR_ARG, "TOD shorter than the segment list");
+    memcpy(&h[g * ns], tod + o, sizeof(double) * ns);
+    for (long long i = 1; i < ns; i++) {  // sanepic.cc:784-790
+      double& v = h[g * ns + i];
+      if (!(v > 0) && !(v <= 0.0)) v = h[g * ns + i - 1];
+    }
+  }
+  cudaError_t e;
+  if (c->f32) {
+    std::vector<float> f(h.begin(), h.end());
+    e = cudaMemcpy(c->tod.as<float>() + det * nsd, f.data(), 4 * nsd, cudaMemcpyHostToDevice);
+  } else {
+    e = cudaMemcpy(c->tod.as<double>() + det * nsd, h.data(), 8 * nsd, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "set_tod");
+  c->have_tod[det] = 1;
+  c->have_rhs = false;
+  return SG_OK;
+}
+
+static int check_ready(sg_ctx* c, bool need_tod) {
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  for (long long dd = 0; dd < c->ndet; dd++) {
+    if (!c->have_noise[dd]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", dd);
+    if (need_tod && !c->have_tod[dd]) return c->fail(SG_ERR_STATE, "TOD of detector %lld not set", dd);
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
+  if (!c) return SG_ERR_ARG;
+  int rc = check_ready(c, true);
+  if (rc) return rc;
+  cudaSetDevice(c->desc.device);
+  cudaError_t e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+  if (e == cudaSuccess) e = c->launch_pt(c->y.p, c->b.as<double>(), true);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "rhs");
+  if (chi2) *chi2 = NAN;  // not computed on this path yet
+  c->have_rhs = true;
+  return SG_OK;
+}
+
+extern "C" int sg_apply(sg_ctx* c, const double* xin, double* yout, int masked) {
+  if (!c) return SG_ERR_ARG;
+  int rc = check_ready(c, false);
+  if (rc) return rc;
+  if (!xin || !yout) return c->fail(SG_ERR_ARG, "null vector");
+  cudaSetDevice(c->desc.device);
+  const size_t vb = sizeof(double) * 3 * c->npix;
+  cudaError_t e = cudaMemcpyAsync(c->z.p, xin, vb, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = c->apply_dev(c->z.as<double>(), c->q.as<double>(), masked != 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(yout, c->q.p, vb, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "apply");
+  return SG_OK;
+}
+
+extern "C" int sg_noise_filter(sg_ctx* c, const double* in, double* out) {
+  if (!c) return SG_ERR_ARG;
+  if (!in || !out) return c->fail(SG_ERR_ARG, "null array");
+  for (long long dd = 0; dd < c->ndet; dd++)
+    if (!c->have_noise[dd]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", dd);
+  cudaSetDevice(c->desc.device);
+  const long long n = c->nsamp;
+  DevBuf din;
+  cudaError_t e = din.alloc((size_t)n * c->esize);
+  if (e != cudaSuccess) return c->cuda_fail(e, "noise_filter alloc");
+  if (c->f32) {
+    std::vector<float> f(in, in + n);
+    e = cudaMemcpy(din.p, f.data(), 4 * n, cudaMemcpyHostToDevice);
+  } else {
+    e = cudaMemcpy(din.p, in, 8 * n, cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = c->launch_filter(kLoadTod, din.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e == cudaSuccess) {
+    if (c->f32) {
+      std::vector<float> f(n);
+      e = cudaMemcpy(f.data(), c->y.p, 4 * n, cudaMemcpyDeviceToHost);
+      for (long long i = 0; i < n; i++) out[i] = f[i];
+    } else {
+      e = cudaMemcpy(out, c->y.p, 8 * n, cudaMemcpyDeviceToHost);
+    }
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "noise_filter");
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+static int build_bj3(sg_ctx* c) {
+  if (c->have_bj3) return SG_OK;
+  cudaError_t e;
+  if (c->f32)
+    e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                          c->csr_cs.as<float>(), c->npix, c->ns * c->nseg, (int)c->nseg,
+                          c->g0.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
+  else
+    e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                           c->csr_cs.as<double>(), c->npix, c->ns * c->nseg, (int)c->nseg,
+                           c->g0.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "bj3 build");
+  c->have_bj3 = true;
+  return SG_OK;
+}
+
+// The reference's diagonal (also needed for the NVAR outputs).
+static int build_diag(sg_ctx* c) {
+  if (c->have_diag) return SG_OK;
+  cudaError_t e;
+  const long long ns = c->ns, npix = c->npix;
+  // N_ = c2r(|SpN|) per detector: the filter with |h| applied to a unit impulse
+  if ((e = c->ntab.alloc((size_t)c->ndet * ns * c->esize)) != cudaSuccess)
+    return c->cuda_fail(e, "diag alloc");
+  e = c->launch_filter(kLoadDelta, nullptr, c->ntab.p, c->ndet, 1, 1);
+  if (e == cudaSuccess) {
+    if (c->f32)
+      e = diag_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
+                             (int)c->nseg, c->ntab.as<float>(), c->mp_raw.as<double>(), c->st);
+    else
+      e = diag_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
+                              (int)c->nseg, c->ntab.as<double>(), c->mp_raw.as<double>(), c->st);
+  }
+  if (e == cudaSuccess) e = mask_qu(c->mp_raw.as<double>(), c->hits.as<int>(), npix, c->st);
+  std::vector<double> mp(3 * npix);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(mp.data(), c->mp_raw.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost,
+                        c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "diag build");
+  for (long long m = 0; m < npix; m++)
+    if (mp[m] == 0.0) return c->fail(SG_ERR_PRECOND, "Mp[%lld] has elements = 0", m);
+  for (auto& v : mp) v = v != 0.0 ? 1.0 / v : 0.0;
+  e = cudaMemcpy(c->mdiag.p, mp.data(), sizeof(double) * 3 * npix, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return c->cuda_fail(e, "diag upload");
+  c->ntab.release();
+  c->have_diag = true;
+  return SG_OK;
+}
+
+extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
+  if (!c || !o) return SG_ERR_ARG;
+  int rc = check_ready(c, false);
+  if (rc) return rc;
+  if (!c->have_rhs) return c->fail(SG_ERR_STATE, "call sg_rhs before sg_solve");
+  if (o->precond != SG_PRECOND_BJ3 && o->precond != SG_PRECOND_DIAG)
+    return c->fail(SG_ERR_UNSUPPORTED, "preconditioner %d not available", o->precond);
+  cudaSetDevice(c->desc.device);
+  const double t0 = now_s();
+  rc = (o->precond == SG_PRECOND_BJ3) ? build_bj3(c) : build_diag(c);
+  if (rc) return rc;
+  const int pc = (o->precond == SG_PRECOND_BJ3) ? 1 : 0;
+  const long long npix = c->npix;
+  const size_t vb = sizeof(double) * 3 * npix;
+  cudaError_t e;
+  // x0 (masked, sanepic.cc:1209-1227, 1316-1330), r = A x0
+  if (o->x0) {
+    e = cudaMemcpyAsync(c->x.p, o->x0, vb, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = mask_qu(c->x.as<double>(), c->hits.as<int>(), npix, c->st);
+    if (e == cudaSuccess) e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
+  } else {
+    e = cudaMemsetAsync(c->x.p, 0, vb, c->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->r.p, 0, vb, c->st);
+  }
+  CgVecs v = c->vecs(pc);
+  if (!c->ev0) cudaEventCreate(&c->ev0);
+  if (!c->ev1) cudaEventCreate(&c->ev1);
+  const long long launches0 = c->launches;
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->st);
+  if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v, c->st) : cg_init<double>(v, c->st);
+  c->launches += 2;
+  if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "solve init");
+  const double t1 = now_s();
+  const double var00 = c->sc_host->var00, delta0 = c->sc_host->delta0;
+  double crit = c->sc_host->var / var00;
+  const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
+  const int maxiter = o->maxiter > 0 ? o->maxiter : 2000;
+  c->crit_hist.clear();
+  int iter = 0;
+  while ((iter < maxiter && crit > o->stop_crit) || iter == 0) {
+    const bool refresh = (iter % refresh_every) == 0;
+    e = c->run_iteration(pc, refresh, o->use_graph != 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "solve iteration");
+    crit = c->sc_host->var / var00;
+    c->crit_hist.push_back(crit);
+    if (o->verbose)
+      printf("iter = %d, crit = %10.15g, crit2 = %10.15g\n", iter, crit,
+             c->sc_host->delta / delta0);
+    if (c->sc_host->flag)
+      return c->fail(SG_ERR_NOT_CONVERGED, "CG breakdown at iteration %d (flag %d)", iter,
+                     c->sc_host->flag);
+    iter++;
+  }
+  e = cudaEventRecord(c->ev1, c->st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
+  float dev_ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&dev_ms, c->ev0, c->ev1);
+  if (e != cudaSuccess) return c->cuda_fail(e, "solve timing");
+  const double t2 = now_s();
+  c->have_solution = true;
+  if (rep) {
+    rep->iterations = iter;
+    rep->converged = crit <= o->stop_crit;
+    rep->crit = crit;
+    rep->var00 = var00;
+    rep->solve_seconds = t2 - t1;
+    rep->iter_per_sec = iter / (t2 - t1 > 0 ? t2 - t1 : 1e-30);
+    rep->setup_seconds = t1 - t0;
+    rep->device_seconds = dev_ms * 1e-3;
+    rep->kernel_launches = (long)(c->launches - launches0);
+  }
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+static void expand(const sg_ctx* c, const double* compact, double* full) {
+  for (long long p = 0; p < c->npixfull; p++) {
+    const int m = c->indpix_host[p];
+    full[p] = m >= 0 ? compact[m] : 0.0;
+  }
+}
+
+extern "C" int sg_get_map(sg_ctx* c, int kind, double* out) {
+  if (!c || !out) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  cudaSetDevice(c->desc.device);
+  const long long npix = c->npix;
+  std::vector<double> v(3 * npix);
+  cudaError_t e = cudaSuccess;
+  const double* blk = nullptr;
+  switch (kind) {
+    case SG_MAP_I:
+    case SG_MAP_Q:
+    case SG_MAP_U:
+      if (!c->have_solution) return c->fail(SG_ERR_STATE, "no solution yet");
+      e = cudaMemcpy(v.data(), c->x.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost);
+      blk = v.data() + (kind - SG_MAP_I) * npix;
+      break;
+    case SG_MAP_NVAR:
+    case SG_MAP_Q_NVAR:
+    case SG_MAP_U_NVAR: {
+      int rc = build_diag(c);
+      if (rc) return rc;
+      e = cudaMemcpy(v.data(), c->mdiag.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost);
+      blk = v.data() + (kind - SG_MAP_NVAR) * npix;
+      break;
+    }
+    case SG_MAP_HITS:
+    case SG_MAP_POL_HITS: {
+      std::vector<int> h(npix);
+      e = cudaMemcpy(h.data(), c->hits.p, sizeof(int) * npix, cudaMemcpyDeviceToHost);
+      for (long long m = 0; m < npix; m++) v[m] = 2.0 * h[m];  // doubled (Q1)
+      blk = v.data();
+      break;
+    }
+    case SG_MAP_COS2P:
+    case SG_MAP_SIN2P: {
+      std::vector<int> h(npix);
+      e = cudaMemcpy(v.data(), c->sumcross.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(h.data(), c->hits.p, sizeof(int) * npix, cudaMemcpyDeviceToHost);
+      if (kind == SG_MAP_SIN2P)
+        for (long long m = 0; m < npix; m++)
+          if (h[m] < 2) v[npix + m] = 0.0;  // Q2 (sanepic.cc:1325-1328)
+      blk = v.data() + (kind - SG_MAP_COS2P) * npix;
+      break;
+    }
+    default:
+      return c->fail(SG_ERR_ARG, "unknown map kind %d", kind);
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "get_map");
+  expand(c, blk, out);
+  return SG_OK;
+}
+
+extern "C" int sg_get_solution(sg_ctx* c, double* out) {
+  if (!c || !out) return SG_ERR_ARG;
+  if (!c->have_solution) return c->fail(SG_ERR_STATE, "no solution yet");
+  cudaError_t e = cudaMemcpy(out, c->x.p, sizeof(double) * 3 * c->npix, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "get_solution");
+}
+
+extern "C" int sg_get_pixels(sg_ctx* c, long* ring_out) {
+  if (!c || !ring_out) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  std::vector<int> comp(c->nsamp);
+  cudaError_t e = cudaMemcpy(comp.data(), c->pix.p, sizeof(int) * c->nsamp, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return c->cuda_fail(e, "get_pixels");
+  std::vector<long> inv(c->npix, -1);
+  for (long long p = 0; p < c->npixfull; p++)
+    if (c->indpix_host[p] >= 0) inv[c->indpix_host[p]] = (long)p;
+  for (long long i = 0; i < c->nsamp; i++) ring_out[i] = inv[comp[i]];
+  return SG_OK;
+}
+
+extern "C" int sg_get_indpix(sg_ctx* c, long* out) {
+  if (!c || !out) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  for (long long p = 0; p < c->npixfull; p++) out[p] = c->indpix_host[p];
+  return SG_OK;
+}
+
+extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
+  if (!c || !ms || reps < 1) return SG_ERR_ARG;
+  int rc = check_ready(c, false);
+  if (rc) return rc;
+  cudaSetDevice(c->desc.device);
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaError_t e = c->to_map(c->d.as<double>());
+  float t_filter = 0.f, t_pt = 0.f;
+  for (int i = 0; i < reps && e == cudaSuccess; i++) {
+    float a = 0.f, b2 = 0.f;
+    e = cudaEventRecord(e0, c->st);
+    if (e == cudaSuccess) e = c->launch_filter(kLoadProj, nullptr, c->y.p, c->ntiles, (int)c->nseg, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
+    if (e == cudaSuccess) e = c->launch_pt(c->y.p, c->q.as<double>(), true);
+    if (e == cudaSuccess) e = cudaEventRecord(e2, c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e2);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&a, e0, e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b2, e1, e2);
+    t_filter += a;
+    t_pt += b2;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  if (e != cudaSuccess) return c->cuda_fail(e, "profile_operator");
+  ms[0] = t_filter / reps;
+  ms[1] = t_pt / reps;
+  return SG_OK;
+}
+
+extern "C" int sg_get_crit_history(sg_ctx* c, double* out, int max) {
+  if (!c || !out) return SG_ERR_ARG;
+  const int n = std::min<int>(max, (int)c->crit_hist.size());
+  for (int i = 0; i < n; i++) out[i] = c->crit_hist[i];
+  return n;
+}

@@ -1,0 +1,150 @@
+// sg_kernels.h -- device kernel entry points of the map-making library
+// (internal; the public C ABI is include/sanepic_gpu.h).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "sg_cplx.cuh"
+
+namespace sg {
+
+// ---- noise filter (sg_filter.cu) --------------------------------------------
+enum { kLoadTod = 0, kLoadProj = 1, kLoadDelta = 2 };
+
+template <typename T>
+struct FilterArgs {
+  long long ntiles;  // (det, seg) tiles, each ns = 2M samples, tile-major
+  int nseg;          // det = tile / nseg selects the filter row
+  int mode;          // kLoadTod / kLoadProj / kLoadDelta
+  int filt_abs;      // multiply by |h| instead of h
+  const T* tod;      // kLoadTod: [ntiles][ns]
+  const int* pix;    // kLoadProj: compact pixel per sample
+  const T* cs;       // kLoadProj: (cos 2psi, sin 2psi) per sample
+  const T* map;      // kLoadProj: [npix][4] = (I, Q, U, 0)
+  const T* filt;     // [ndet][M+1]
+  T* out;            // [ntiles][ns]
+  const cplx<T>* tw_lo;
+  const cplx<T>* tw_hi;
+  cplx<T> wn1;
+};
+
+template <typename T>
+cudaError_t filter_launch(const FilterArgs<T>& a, int logm, int S, int nclusters,
+                          cudaStream_t st);
+template <typename T>
+int filter_max_clusters(int logm, int S);
+size_t filter_smem_bytes(int logm, int S, int esize);
+
+// ---- pointing expansion + pixelisation (sg_pointing.cu, FP64, no FMA) --------
+struct PointingArgs {
+  long long ns;          // samples per segment
+  int nseg, ndet;
+  const double* ra;      // [nseg][ns] boresight, psi already NaN-patched
+  const double* dec;
+  const double* psi;
+  const double* offx;    // [ndet] radians
+  const double* offy;
+  const double* psidet;
+  int hwp;
+  double omega;
+  long long nside;
+  int* ring_pix;         // [ndet][nseg][ns]; -1 invalid (NaN), -2 out of range
+  double* psip;          // [ndet][nseg][ns] or nullptr
+  double* psipfp;        // [ndet][nseg][ns] or nullptr
+  int* error_flag;       // set to 1 when theta is outside [0, pi]
+};
+// grp_off [ngroups+1] / grp_det: detectors grouped by identical (offx, offy)
+cudaError_t pointing_launch_groups(const PointingArgs& a, int ngroups, const int* grp_off,
+                                   const int* grp_det, cudaStream_t st);
+
+// ---- setup helpers (sg_setup.cu) ------------------------------------------------
+cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream_t st);
+// count[npixfull] -> indpix[npixfull] (-1 unobserved), returns npix through *npix_dev
+cudaError_t indpix_launch(const int* count, long long npixfull, int* indpix,
+                          long long* npix_dev, void* tmp, size_t tmp_bytes, cudaStream_t st);
+size_t indpix_tmp_bytes(long long npixfull);
+cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, int* pix,
+                           cudaStream_t st);
+// hits_true[m] = count[ring(m)] via indpix
+cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull,
+                        int* hits_true, cudaStream_t st);
+// CSR by pixel: keys sorted; csr_off [npix+1], csr_idx [n]
+size_t csr_tmp_bytes(long long n, long long npix);
+cudaError_t csr_build(const int* pix, long long n, long long npix, const int* hits_true,
+                      long long* csr_off, uint32_t* csr_idx, void* tmp, size_t tmp_bytes,
+                      cudaStream_t st);
+template <typename T>
+cudaError_t gather_cs_launch(const T* cs, const uint32_t* csr_idx, long long n, T* csr_cs,
+                             cudaStream_t st);
+// (cos 2psi, sin 2psi) per sample in precision T from psip (FP64)
+template <typename T>
+cudaError_t angles_launch(const double* psip, long long n, T* cs, cudaStream_t st);
+// COS2P/SIN2P sums (sanepic.cc:2594-2597) over the CSR, FP64
+cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx,
+                            const double* psipfp, long long npix, double* sumcross,
+                            cudaStream_t st);
+// 3x3 block-Jacobi build+invert; minv [6][npix] (00 01 02 11 12 22)
+template <typename T>
+cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
+                       long long npix, long long tile_len, int nseg, const double* g0,
+                       const int* hits_true, double* minv, cudaStream_t st);
+// reference diagonal (compute_diagPtNPCorr x2, sanepic.cc:2680-2762): Mp [3][npix]
+template <typename T>
+cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
+                        long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st);
+
+// ---- P^T (sg_pt.cu) ------------------------------------------------------------
+// q[c*npix + m] = sum over samples of pixel m of w_c * y (w = 1, cos, sin),
+// Q/U zeroed where the pol mask applies (hits_true < 2).
+template <typename T>
+cudaError_t pt_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
+                      const T* y, long long npix, const int* hits_true, double* q,
+                      cudaStream_t st);
+
+// ---- CG vector algebra (sg_cg.cu) ------------------------------------------------
+struct CgScalars {
+  double delta;      // current r^T z
+  double delta_old;  // previous r^T z
+  double delta0;
+  double var;        // r^T r
+  double var00;      // b^T b
+  double alpha, beta, rtq;
+  int flag;          // bit 0: d^T A d <= 0, bit 1: r^T z <= 0
+  int pad;
+};
+constexpr int kCgBlocks = 304;  // 2 x 152 SMs, grid-stride
+constexpr int kCgThreads = 256;
+
+struct CgVecs {
+  long long npix;
+  double* x;
+  double* r;
+  double* d;
+  double* q;
+  double* z;            // preconditioned residual
+  double* rprev;        // flexible PCG: previous residual (or nullptr)
+  const double* b;
+  const double* minv;   // bj3 [6][npix] (00 01 02 11 12 22)
+  const double* mdiag;  // reference diagonal, inverted [3][npix]
+  const int* hits_true;
+  int precond;          // 0 diag, 1 bj3, 2 z supplied externally
+  double* part;         // [4][kCgBlocks] partial sums
+  CgScalars* sc;
+};
+// r = b - r (r holds the masked A x0); z = M r; d = z; scalars
+template <typename T>
+cudaError_t cg_init(const CgVecs& v, cudaStream_t st);
+cudaError_t cg_step_a(const CgVecs& v, cudaStream_t st);  // partial q.d
+cudaError_t cg_step_b(const CgVecs& v, int refresh, int flexible, cudaStream_t st);
+cudaError_t cg_refresh_r(const CgVecs& v, int flexible, cudaStream_t st);  // r = b - q
+cudaError_t cg_dots(const CgVecs& v, int flexible, cudaStream_t st);
+template <typename T>
+cudaError_t cg_step_c(const CgVecs& v, T* dmap, int flexible, cudaStream_t st);
+template <typename T>
+cudaError_t to_map4(const double* x, long long npix, T* map, cudaStream_t st);
+cudaError_t mask_qu(double* v, const int* hits_true, long long npix, cudaStream_t st);
+cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStream_t st);
+
+}  // namespace sg

@@ -1,0 +1,347 @@
+// sg_setup.cu -- one-time setup kernels: observed-pixel compaction (indpix),
+// the pixel-sorted sample index (CSR) used by the deterministic P^T, hit
+// counts, cross-link sums and the two preconditioners.
+//
+// Reference counterparts: pixon/indpix sanepic.cc:828-915, hits 2613-2626,
+// sumCross 2594-2597, compute_diagPtNPCorr 2680-2762.  The 3x3 block-Jacobi
+// preconditioner has no reference counterpart.
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+
+#include "sg_kernels.h"
+
+namespace sg {
+
+static unsigned grid_for(long long n, int threads, long long cap = 152LL * 32) {
+  long long b = (n + threads - 1) / threads;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+__global__ void k_hist(const int* ring_pix, long long n, int* count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int p = ring_pix[i];
+    if (p >= 0) atomicAdd(count + p, 1);
+  }
+}
+
+cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream_t st) {
+  k_hist<<<grid_for(n, 256), 256, 0, st>>>(ring_pix, n, count);
+  return cudaGetLastError();
+}
+
+__global__ void k_flags(const int* count, long long n, int* flags) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    flags[i] = count[i] != 0 ? 1 : 0;
+}
+
+__global__ void k_indpix_finish(const int* count, const int* scan, long long npixfull,
+                                int* indpix, long long* npix) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npixfull;
+       i += (long long)gridDim.x * blockDim.x) {
+    indpix[i] = count[i] != 0 ? scan[i] : -1;
+    if (i == npixfull - 1) *npix = (long long)scan[i] + (count[i] != 0 ? 1 : 0);
+  }
+}
+
+size_t indpix_tmp_bytes(long long npixfull) {
+  size_t cub_bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int*)nullptr, (int*)nullptr,
+                                (long long)npixfull);
+  return cub_bytes + sizeof(int) * (size_t)npixfull + 256;
+}
+
+cudaError_t indpix_launch(const int* count, long long npixfull, int* indpix, long long* npix,
+                          void* tmp, size_t tmp_bytes, cudaStream_t st) {
+  int* scan = reinterpret_cast<int*>(tmp);
+  void* cub_tmp = reinterpret_cast<char*>(tmp) + ((sizeof(int) * npixfull + 255) / 256) * 256;
+  size_t cub_bytes = tmp_bytes - ((sizeof(int) * npixfull + 255) / 256) * 256;
+  k_flags<<<grid_for(npixfull, 256), 256, 0, st>>>(count, npixfull, scan);
+  cudaError_t e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, scan, scan,
+                                                (long long)npixfull, st);
+  if (e != cudaSuccess) return e;
+  k_indpix_finish<<<grid_for(npixfull, 256), 256, 0, st>>>(count, scan, npixfull, indpix, npix);
+  return cudaGetLastError();
+}
+
+__global__ void k_compact(const int* ring_pix, const int* indpix, long long n, int* pix) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    pix[i] = indpix[ring_pix[i]];
+}
+
+cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, int* pix,
+                           cudaStream_t st) {
+  k_compact<<<grid_for(n, 256), 256, 0, st>>>(ring_pix, indpix, n, pix);
+  return cudaGetLastError();
+}
+
+__global__ void k_hits(const int* count, const int* indpix, long long npixfull, int* hits) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npixfull;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int m = indpix[i];
+    if (m >= 0) hits[m] = count[i];
+  }
+}
+
+cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull, int* hits,
+                        cudaStream_t st) {
+  k_hits<<<grid_for(npixfull, 256), 256, 0, st>>>(count, indpix, npixfull, hits);
+  return cudaGetLastError();
+}
+
+// ---- CSR: samples sorted by (pixel, sample index) ---------------------------
+// Keys (pixel << 32 | sample) are unique, so the order is fully determined.
+__global__ void k_make_keys(const int* pix, long long n, unsigned long long* keys) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    keys[i] = ((unsigned long long)(unsigned)pix[i] << 32) | (unsigned long long)i;
+}
+
+__global__ void k_keys_to_idx(const unsigned long long* keys, long long n, uint32_t* idx) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    idx[i] = (uint32_t)(keys[i] & 0xffffffffULL);
+}
+
+static int bits_for(long long v) {
+  int b = 0;
+  while ((1LL << b) <= v) b++;
+  return b;
+}
+
+size_t csr_tmp_bytes(long long n, long long npix) {
+  size_t sort_bytes = 0, scan_bytes = 0;
+  cub::DoubleBuffer<unsigned long long> db(nullptr, nullptr);
+  cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, db, n, 0, 64);
+  cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (long long*)nullptr, (long long*)nullptr,
+                                npix + 1);
+  size_t cub_bytes = sort_bytes > scan_bytes ? sort_bytes : scan_bytes;
+  return 2 * sizeof(unsigned long long) * (size_t)n + cub_bytes + 1024;
+}
+
+__global__ void k_counts_ll(const int* hits, long long npix, long long* off) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i <= npix;
+       i += (long long)gridDim.x * blockDim.x)
+    off[i] = i < npix ? (long long)hits[i] : 0;
+}
+
+cudaError_t csr_build(const int* pix, long long n, long long npix, const int* hits,
+                      long long* csr_off, uint32_t* csr_idx, void* tmp, size_t tmp_bytes,
+                      cudaStream_t st) {
+  char* base = reinterpret_cast<char*>(tmp);
+  unsigned long long* k0 = reinterpret_cast<unsigned long long*>(base);
+  unsigned long long* k1 = k0 + n;
+  char* cub_tmp = reinterpret_cast<char*>(k1 + n);
+  size_t cub_bytes = tmp_bytes - 2 * sizeof(unsigned long long) * (size_t)n;
+  k_make_keys<<<grid_for(n, 256), 256, 0, st>>>(pix, n, k0);
+  cub::DoubleBuffer<unsigned long long> db(k0, k1);
+  const int nbits = 32 + bits_for(npix);
+  cudaError_t e = cub::DeviceRadixSort::SortKeys(cub_tmp, cub_bytes, db, n, 0, nbits, st);
+  if (e != cudaSuccess) return e;
+  k_keys_to_idx<<<grid_for(n, 256), 256, 0, st>>>(db.Current(), n, csr_idx);
+  // offsets: exclusive scan of the per-pixel counts
+  long long* cnt = reinterpret_cast<long long*>(db.Alternate());  // reuse as scratch
+  k_counts_ll<<<grid_for(npix + 1, 256), 256, 0, st>>>(hits, npix, cnt);
+  e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt, csr_off, npix + 1, st);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void k_gather_cs(const T* cs, const uint32_t* idx, long long n, T* out) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx[j];
+    out[2 * j] = cs[2 * i];
+    out[2 * j + 1] = cs[2 * i + 1];
+  }
+}
+
+template <typename T>
+cudaError_t gather_cs_launch(const T* cs, const uint32_t* csr_idx, long long n, T* csr_cs,
+                             cudaStream_t st) {
+  k_gather_cs<T><<<grid_for(n, 256), 256, 0, st>>>(cs, csr_idx, n, csr_cs);
+  return cudaGetLastError();
+}
+template cudaError_t gather_cs_launch<float>(const float*, const uint32_t*, long long, float*,
+                                             cudaStream_t);
+template cudaError_t gather_cs_launch<double>(const double*, const uint32_t*, long long,
+                                              double*, cudaStream_t);
+
+// cos/sin(2 psip) as the reference evaluates them (sanepic.cc:2601-2605, FP64),
+// rounded to T.  For FP32 storage the FP64 angle is first reduced modulo 2pi
+// (exact fmod) so that HWP angles of ~1e6 rad stay on the fast path.
+template <typename T>
+__global__ void k_angles(const double* psip, long long n, T* cs) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double a = 2.0 * (psip[i] + 0.0);
+    if (sizeof(T) == 4) a = fmod(a, 6.2831853071795864769252867665590057683943387987502);
+    double s, c;
+    sincos(a, &s, &c);
+    cs[2 * i] = (T)c;
+    cs[2 * i + 1] = (T)s;
+  }
+}
+
+template <typename T>
+cudaError_t angles_launch(const double* psip, long long n, T* cs, cudaStream_t st) {
+  k_angles<T><<<grid_for(n, 256), 256, 0, st>>>(psip, n, cs);
+  return cudaGetLastError();
+}
+template cudaError_t angles_launch<float>(const double*, long long, float*, cudaStream_t);
+template cudaError_t angles_launch<double>(const double*, long long, double*, cudaStream_t);
+
+// ---- per-pixel reductions over the CSR (one warp per pixel) -----------------
+__global__ void k_sumcross(const long long* off, const uint32_t* idx, const double* psipfp,
+                           long long npix, double* out) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long m = warp; m < npix; m += nwarps) {
+    double c = 0.0, s = 0.0;
+    for (long long j = off[m] + lane; j < off[m + 1]; j += 32) {
+      double sn, cs;
+      sincos(2.0 * (psipfp[idx[j]] + 0.0), &sn, &cs);
+      c += cs;
+      s += sn;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (lane == 0) {
+      out[m] = c;
+      out[npix + m] = s;
+      out[2 * npix + m] = 0.0;
+    }
+  }
+}
+
+cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx,
+                            const double* psipfp, long long npix, double* sumcross,
+                            cudaStream_t st) {
+  k_sumcross<<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(csr_off, csr_idx, psipfp,
+                                                                   npix, sumcross);
+  return cudaGetLastError();
+}
+
+// 3x3 block-Jacobi: A_p = sum g0[det] w w^T, w = (1, c, s); inverse in FP64.
+template <typename T>
+__global__ void k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix,
+                      long long tile_len, const double* g0, const int* hits, double* minv) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long m = warp; m < npix; m += nwarps) {
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (long long j = off[m] + lane; j < off[m + 1]; j += 32) {
+      const double g = g0[idx[j] / tile_len];
+      const double c = (double)ccs[2 * j], s = (double)ccs[2 * j + 1];
+      a[0] += g;
+      a[1] += g * c;
+      a[2] += g * s;
+      a[3] += g * c * c;
+      a[4] += g * c * s;
+      a[5] += g * s * s;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 6; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+    if (lane == 0) {
+      double o6[6] = {0, 0, 0, 0, 0, 0};
+      if (hits[m] < 2) {
+        o6[0] = a[0] != 0.0 ? 1.0 / a[0] : 0.0;
+      } else {
+        const double c00 = a[3] * a[5] - a[4] * a[4];
+        const double c01 = a[2] * a[4] - a[1] * a[5];
+        const double c02 = a[1] * a[4] - a[2] * a[3];
+        const double c11 = a[0] * a[5] - a[2] * a[2];
+        const double c12 = a[1] * a[2] - a[0] * a[4];
+        const double c22 = a[0] * a[3] - a[1] * a[1];
+        const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+        const double scale = a[0] * a[0] * a[0];
+        if (!(det > 1e-12 * scale)) {
+          o6[0] = 1.0 / a[0];
+          o6[3] = a[3] > 0.0 ? 1.0 / a[3] : 0.0;
+          o6[5] = a[5] > 0.0 ? 1.0 / a[5] : 0.0;
+        } else {
+          const double id = 1.0 / det;
+          o6[0] = c00 * id;
+          o6[1] = c01 * id;
+          o6[2] = c02 * id;
+          o6[3] = c11 * id;
+          o6[4] = c12 * id;
+          o6[5] = c22 * id;
+        }
+      }
+      for (int k = 0; k < 6; k++) minv[k * npix + m] = o6[k];
+    }
+  }
+}
+
+template <typename T>
+cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
+                       long long npix, long long tile_len, int nseg, const double* g0,
+                       const int* hits_true, double* minv, cudaStream_t st) {
+  (void)nseg;
+  k_bj3<T><<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(
+      csr_off, csr_idx, csr_cs, npix, tile_len, g0, hits_true, minv);
+  return cudaGetLastError();
+}
+template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*,
+                                       long long, long long, int, const double*, const int*,
+                                       double*, cudaStream_t);
+template cudaError_t bj3_launch<double>(const long long*, const uint32_t*, const double*,
+                                        long long, long long, int, const double*, const int*,
+                                        double*, cudaStream_t);
+
+// Reference diagonal: for every tile and pixel, sum over sample pairs (i, j)
+// of that pixel in the tile with |i - j| < ns/2 of N_[|i - j|], N_ = c2r|SpN|
+// (sanepic.cc:2698-2752).  The reference adds it twice (Q1) and sets the Q/U
+// blocks to I/2 (sanepic.cc:2561-2565).  One thread per pixel; the sample
+// list is sorted by sample index, so a tile's samples are contiguous.
+template <typename T>
+__global__ void k_diag(const long long* off, const uint32_t* idx, long long npix, long long ns,
+                       int nseg, const T* ntab, double* Mp) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < npix;
+       m += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    long long j0 = off[m];
+    const long long jend = off[m + 1];
+    while (j0 < jend) {
+      const long long tile = idx[j0] / ns;
+      long long j1 = j0;
+      while (j1 < jend && (long long)(idx[j1] / ns) == tile) j1++;
+      const T* nt = ntab + (tile / nseg) * ns;
+      for (long long a = j0; a < j1; a++) {
+        const long long ia = idx[a] % ns;
+        for (long long b = j0; b < j1; b++) {
+          const long long ib = idx[b] % ns;
+          const long long dd = ia > ib ? ia - ib : ib - ia;
+          if (dd < ns / 2) acc += (double)nt[dd];
+        }
+      }
+      j0 = j1;
+    }
+    Mp[m] = 2.0 * acc;
+    Mp[npix + m] = acc;
+    Mp[2 * npix + m] = acc;
+  }
+}
+
+template <typename T>
+cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
+                        long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st) {
+  k_diag<T><<<grid_for(npix, 128), 128, 0, st>>>(csr_off, csr_idx, npix, ns, nseg, ntab, Mp);
+  return cudaGetLastError();
+}
+template cudaError_t diag_launch<float>(const long long*, const uint32_t*, long long, long long,
+                                        int, const float*, double*, cudaStream_t);
+template cudaError_t diag_launch<double>(const long long*, const uint32_t*, long long,
+                                         long long, int, const double*, double*, cudaStream_t);
+
+}  // namespace sg

@@ -23,6 +23,7 @@ expects and returns the matching command-line arguments.
 """
 from __future__ import annotations
 
+import concurrent.futures
 import dataclasses
 import math
 import os
@@ -223,10 +224,12 @@ def make_tod(prob, noise_seed_base: Optional[int] = None, dets=None) -> np.ndarr
     sky = prob["sky"]
     I, Q, U = sky[0][pix], sky[1][pix], sky[2][pix]
     tidx = np.arange(nsamp, dtype=np.float64)
-    dets = range(spec.ndet) if dets is None else dets
+    dets = list(range(spec.ndet) if dets is None else dets)
     out = np.empty((len(dets), nsamp))
     base = 2000 + 1000 * spec.problem if noise_seed_base is None else noise_seed_base
-    for j, d in enumerate(dets):
+
+    def one(j):
+        d = dets[j]
         pdet = prob["psi"] + prob["angles"][d] / 180.0 * D2PI / 2.0
         if spec.hwp:
             pdet = -pdet + 2.0 * prob["omega"] * tidx
@@ -239,6 +242,15 @@ def make_tod(prob, noise_seed_base: Optional[int] = None, dets=None) -> np.ndarr
                 n = np.fft.irfft(np.fft.rfft(w) * amp, n=ns)
                 tod[g * ns:(g + 1) * ns] += n
         out[j] = tod
+
+    # detectors are independent (own seed each): generate them on threads
+    workers = min(len(dets), os.cpu_count() or 1)
+    if workers > 1 and nsamp * len(dets) > 4_000_000:
+        with concurrent.futures.ThreadPoolExecutor(max_workers=workers) as ex:
+            list(ex.map(one, range(len(dets))))
+    else:
+        for j in range(len(dets)):
+            one(j)
     return out
 
 

@@ -1,0 +1,160 @@
+"""GPU parity: libsanepic_gpu (called through the C ABI) against the CPU
+oracle and the reference's own outputs (tests/golden)."""
+import numpy as np
+import pytest
+
+import oracle
+import sanepic_gb300 as sg
+from golden_util import NAMES, load_log, load_outputs, load_problem, rel_rms
+from sanepic_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    sg.build.build()
+
+
+def small_problem(ndet=2, nside=16, nseg=4, ns=2048, hwp=False, problem=7, fknee=0.1,
+                  precision="f64"):
+    spec = synth.ProblemSpec("t", ndet=ndet, nside=nside, nseg=nseg, ns=ns, hwp=hwp,
+                             fknee=fknee, alpha=1.0, problem=problem, precision=precision)
+    return synth.make_problem(spec)
+
+
+# ---- pixelisation -------------------------------------------------------------
+@pytest.mark.parametrize("name", NAMES)
+def test_pixels_bit_exact(name):
+    prob = load_problem(name)
+    mm = sg.from_problem(prob, precision="f64")
+    s = oracle.Setup(prob)
+    assert np.array_equal(mm.pixels(), s.pix)
+    assert np.array_equal(mm.indpix(), s.indpix)
+    assert mm.npix == s.npix
+
+
+def test_pixels_bit_exact_1det_nside64_full_size():
+    spec = synth.spec_from_name("c1_1det_nside64")
+    prob = synth.make_problem(spec, with_tod=False)
+    mm = sg.from_problem(prob, with_tod=False)
+    s = oracle.Setup(prob)
+    assert np.array_equal(mm.pixels(), s.pix)
+
+
+def test_pixels_with_detector_offsets_and_hwp():
+    prob = small_problem(ndet=3, hwp=True)
+    offs = [(0.0, 0.0), (0.01, -0.02), (0.01, -0.02)]
+    mm = sg.MapMaker(prob["spec"].ns, prob["spec"].nseg, 3, prob["spec"].nside, hwp=True,
+                     omega=prob["omega"], precision="f64")
+    mm.set_pointing(prob["ra"], prob["dec"], prob["psi"],
+                    sg.detectors_from_angles(prob["angles"], offs))
+    s = oracle.Setup(prob, det_offsets=offs)
+    assert np.array_equal(mm.pixels(), s.pix)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_reference_hits_and_weights(name):
+    prob = load_problem(name)
+    ref = load_outputs(name)
+    mm = sg.from_problem(prob, precision="f64")
+    assert np.array_equal(mm.get_map("HITS"), ref["HITS"])
+    assert np.array_equal(mm.get_map("POL_HITS"), ref["POL_HITS"])
+    for k in ("COS2P", "SIN2P", "NVAR", "Q_NVAR", "U_NVAR"):
+        assert rel_rms(mm.get_map(k), ref[k]) < 1e-10, k
+
+
+# ---- noise filter (FFT) ---------------------------------------------------------
+@pytest.mark.parametrize("ns,prec", [(256, "f64"), (2048, "f64"), (16384, "f64"),
+                                     (65536, "f64"), (1024, "f32"), (32768, "f32"),
+                                     (131072, "f32")])
+def test_noise_filter_vs_oracle(ns, prec):
+    prob = small_problem(ndet=2, nseg=2, ns=ns, precision=prec)
+    s = oracle.Setup(prob)
+    mm = sg.from_problem(prob, precision=prec, with_tod=False)
+    rng = np.random.default_rng(ns)
+    x = rng.standard_normal(2 * 2 * ns)
+    got = mm.noise_filter(x)
+    want = np.concatenate([s.noise_filter(d, x[(d * 2 + g) * ns:(d * 2 + g + 1) * ns])
+                           for d in range(2) for g in range(2)])
+    tol = 1e-12 if prec == "f64" else 2e-6
+    assert rel_rms(got, want) < tol
+
+
+# ---- operator ---------------------------------------------------------------------
+@pytest.mark.parametrize("prec,ns", [("f64", 2048), ("f64", 65536), ("f32", 4096),
+                                     ("f32", 131072)])
+def test_apply_vs_oracle(prec, ns):
+    nseg = 2 if ns >= 65536 else 4
+    prob = small_problem(ndet=2, nseg=nseg, ns=ns, precision=prec, nside=32)
+    s = oracle.Setup(prob)
+    mm = sg.from_problem(prob, precision=prec, with_tod=False)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(3 * s.npix)
+    got = mm.apply(x)
+    want = s.apply(x)
+    tol = 1e-11 if prec == "f64" else 1e-5
+    assert rel_rms(got, want) < tol
+    # A is symmetric: x^T A y = y^T A x
+    y = rng.standard_normal(3 * s.npix)
+    a, b = x @ mm.apply(y), y @ mm.apply(x)
+    assert abs(a - b) <= (1e-10 if prec == "f64" else 1e-5) * max(abs(a), abs(b))
+
+
+def test_apply_bitwise_deterministic():
+    prob = small_problem(ndet=4, nseg=4, ns=4096, precision="f32", nside=32)
+    mm = sg.from_problem(prob, precision="f32", with_tod=False)
+    x = np.random.default_rng(3).standard_normal(3 * mm.npix)
+    y1, y2 = mm.apply(x), mm.apply(x)
+    assert np.array_equal(y1, y2)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_rhs_and_solution_vs_reference(name):
+    prob = load_problem(name)
+    ref = load_outputs(name)
+    log = load_log(name)
+    mm = sg.from_problem(prob, precision="f64")
+    mm.rhs()
+    rep = mm.solve(precond="diag", stop_crit=1e-15, maxiter=2000)
+    crit = mm.crit_history()
+    ref_crit = np.array([c[1] for c in log["crit"]])
+    n = min(10, len(ref_crit))
+    np.testing.assert_allclose(crit[:n], ref_crit[:n], rtol=1e-6)
+    assert abs(rep["iterations"] - log["iterations"]) <= max(3, log["iterations"] // 10)
+    assert rel_rms(mm.get_map("I"), ref["I"], remove_monopole=True) < 1e-6
+    assert rel_rms(mm.get_map("Q"), ref["Q"]) < 1e-6
+    assert rel_rms(mm.get_map("U"), ref["U"]) < 1e-6
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_bj3_solve_vs_oracle(prec):
+    prob = small_problem(ndet=4, nseg=8, ns=4096, precision=prec, nside=16, fknee=0.05)
+    s = oracle.Setup(prob)
+    b, _ = s.rhs(prob["tod"])
+    mm = sg.from_problem(prob, precision=prec)
+    mm.rhs()
+    # same stopping point on both sides (|r|/|b| = 1e-6), then a deeper one
+    checks = [(1e-12, 1e-5)] + ([(1e-14, 1e-6)] if prec == "f64" else [])
+    for stop, tol in checks:
+        xo, it_o, _ = s.pcg(b, precond="bj3", stop_crit=stop, maxiter=500)
+        rep = mm.solve(precond="bj3", stop_crit=stop, maxiter=500)
+        assert rep["converged"]
+        assert abs(rep["iterations"] - it_o) <= 2
+        x = mm.solution()
+        npix = s.npix
+        for c in range(3):
+            blk = slice(c * npix, (c + 1) * npix)
+            err = rel_rms(x[blk], xo[blk], remove_monopole=(c == 0))
+            assert err < tol, (stop, c, err)
+
+
+def test_graph_and_eager_agree():
+    prob = small_problem(ndet=2, nseg=4, ns=2048, precision="f32")
+    mm = sg.from_problem(prob, precision="f32")
+    mm.rhs()
+    mm.solve(precond="bj3", stop_crit=1e-10, use_graph=True)
+    a = mm.solution()
+    mm.solve(precond="bj3", stop_crit=1e-10, use_graph=False)
+    b = mm.solution()
+    assert np.array_equal(a, b)
