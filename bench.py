@@ -200,7 +200,7 @@ def run_ours(args):
         maps = [mm.get_map(k) for k in ("I", "Q", "U")]
         barrier()
         e2e.append(time.perf_counter() - te)
-    e2e_s = float(np.median(e2e))
+    e2e_s = float(np.median(e2e)) if e2e else None
     line = {
         "metric": METRIC, "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False,

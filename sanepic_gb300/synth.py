@@ -63,6 +63,10 @@ PRESETS: Dict[str, ProblemSpec] = {
     "c2_64det_nside256": ProblemSpec("c2_64det_nside256", 64, 256, 48, 131072,
                                      fknee_range=(0.02, 0.2),
                                      alpha_range=(1.0, 2.0), precision="f32"),
+    # the same tiles with 8 detectors: a small case for profiling captures
+    "c2_8det_nside256": ProblemSpec("c2_8det_nside256", 8, 256, 48, 131072,
+                                    fknee_range=(0.02, 0.2),
+                                    alpha_range=(1.0, 2.0), precision="f32"),
     # 256 detectors, NSIDE 512, 48 x 131,072 samples, HWP, FP32
     "c3_256det_nside512_hwp": ProblemSpec("c3_256det_nside512_hwp", 256, 512,
                                           48, 131072, hwp=True, fknee=0.05,

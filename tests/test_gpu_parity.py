@@ -5,6 +5,7 @@ import pytest
 
 import oracle
 import sanepic_gb300 as sg
+from sanepic_gb300 import build
 from golden_util import NAMES, load_log, load_outputs, load_problem, rel_rms
 from sanepic_gb300 import synth
 
@@ -13,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module", autouse=True)
 def _lib():
-    sg.build.build()
+    build.build()
 
 
 def small_problem(ndet=2, nside=16, nseg=4, ns=2048, hwp=False, problem=7, fknee=0.1,
