@@ -136,6 +136,23 @@ int sg_apply(sg_ctx *ctx, const double *x, double *y, int masked);
  * r2c -> x SpN -> c2r of sanepic.cc:2429-2436, 2549-2582). */
 int sg_noise_filter(sg_ctx *ctx, const double *in, double *out);
 
+/* N^-1 (r2c -> x h -> c2r, as sg_noise_filter) on ntiles tiles of ns FP32
+ * samples that the caller already holds in DEVICE memory, allocating no GPU
+ * memory: for callers that cannot call cudaMalloc -- applications whose GPU
+ * memory belongs to their own pool, code running while a CUDA graph is being
+ * captured, real-time loops that cannot take cudaMalloc's synchronisation.
+ * No counterpart in the reference (it has no GPU code).
+ * in/out: [ntiles][ns]; filt: [ntiles / tiles_per_filter][ns/2 + 1] inverse-
+ * noise rows (tile t uses row t / tiles_per_filter); stream: a cudaStream_t or
+ * NULL.  The work is enqueued on the stream of the current device.
+ * Limit: ns a power of two in [256, 131072]; larger ns returns
+ * SG_ERR_UNSUPPORTED.  The FFT twiddle table lives in one 8.5 KiB
+ * library-static device array per GPU, shared by every call: calls that
+ * overlap on the GPU race on it.  The first call on a device looks the array
+ * up (cudaGetSymbolAddress), so make it before any stream capture. */
+int sg_noise_filter_noalloc(const float *in, float *out, const float *filt, long ns,
+                            long ntiles, long tiles_per_filter, void *stream);
+
 /* Preconditioned CG (sanepic.cc:1177-1761). */
 int sg_solve(sg_ctx *ctx, const sg_solve_opts *opts, sg_report *report);
 

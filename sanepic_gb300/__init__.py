@@ -33,7 +33,7 @@ MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
 
 # every symbol include/sanepic_gpu.h declares
 EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
-           "sg_apply", "sg_noise_filter", "sg_solve", "sg_get_map", "sg_get_solution",
+           "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_last_error", "sg_destroy"]
 
@@ -96,6 +96,8 @@ def load_library(path: Optional[str] = None):
     L.sg_npix.restype = ctypes.c_long
     L.sg_apply.argtypes = [c_p, dp, dp, ctypes.c_int]
     L.sg_noise_filter.argtypes = [c_p, dp, dp]
+    L.sg_noise_filter_noalloc.argtypes = [c_p, c_p, c_p, ctypes.c_long, ctypes.c_long,
+                                          ctypes.c_long, c_p]
     L.sg_solve.argtypes = [c_p, ctypes.POINTER(SgSolveOpts), ctypes.POINTER(SgReport)]
     L.sg_get_map.argtypes = [c_p, ctypes.c_int, dp]
     L.sg_get_solution.argtypes = [c_p, dp]
@@ -237,6 +239,17 @@ class MapMaker:
         out = np.empty(max_n)
         n = self._check(self.L.sg_get_crit_history(self.h, _dp(out), max_n))
         return out[:n].copy()
+
+
+def noise_filter_noalloc(in_ptr: int, out_ptr: int, filt_ptr: int, ns: int, ntiles: int,
+                         tiles_per_filter: int, stream: Optional[int] = None) -> int:
+    """sg_noise_filter_noalloc on raw device pointers (FP32): N^-1 applied to
+    caller-owned device buffers without any GPU allocation.  Returns the C
+    status code (0 on success)."""
+    L = load_library()
+    return L.sg_noise_filter_noalloc(ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr),
+                                     ctypes.c_void_p(filt_ptr), ns, ntiles, tiles_per_filter,
+                                     ctypes.c_void_p(stream or None))
 
 
 def detectors_from_angles(angles_deg, offsets=None):

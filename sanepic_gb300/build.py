@@ -28,6 +28,7 @@ UNITS = {
     "sg_pt.cu": [],
     "sg_cg.cu": [],
     "sg_api.cu": [],
+    "sg_noalloc.cu": [],
     "sg_pointing.cu": ["--fmad=false"],
 }
 LIB = os.path.join(LIBDIR, "libsanepic_gpu.so")
