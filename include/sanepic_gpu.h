@@ -171,10 +171,10 @@ int sg_get_indpix(sg_ctx *ctx, long *indpix);
 /* crit = |r|^2/|b|^2 after each iteration of the last solve (up to max). */
 int sg_get_crit_history(sg_ctx *ctx, double *out, int max);
 
-/* Diagnostics: average CUDA-event time (ms) of the two operator kernels over
- * `reps` applications of A to the current search direction: ms[0] = noise
- * filter with the fused projection P, ms[1] = P^T.  Overwrites only scratch
- * buffers.  No reference counterpart (the reference has no profiling). */
+/* Diagnostics: average CUDA-event time (ms) of the three operator kernels over
+ * `reps` applications of A to the current search direction: ms[0] = P,
+ * ms[1] = noise filter N^-1, ms[2] = P^T.  Overwrites only scratch buffers.
+ * No reference counterpart (the reference has no profiling). */
 int sg_profile_operator(sg_ctx *ctx, int reps, double *ms);
 
 const char *sg_last_error(const sg_ctx *ctx);

@@ -231,9 +231,9 @@ class MapMaker:
         return out
 
     def profile_operator(self, reps: int = 5) -> dict:
-        ms = np.zeros(2)
+        ms = np.zeros(3)
         self._check(self.L.sg_profile_operator(self.h, reps, _dp(ms)))
-        return {"filter_ms": float(ms[0]), "pt_ms": float(ms[1])}
+        return {"p_ms": float(ms[0]), "filter_ms": float(ms[1]), "pt_ms": float(ms[2])}
 
     def crit_history(self, max_n: int = 100000) -> np.ndarray:
         out = np.empty(max_n)

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/sanepic_gpu.h"
+#include "sg_healpix.h"
 #include "sg_kernels.h"
 
 using namespace sg;
@@ -69,7 +70,9 @@ struct sg_ctx {
   long long ns = 0, nseg = 0, ndet = 0, ntiles = 0, nsamp = 0, npixfull = 0;
   int logm = 0, S = 1, nclusters = 1;
   long long npix = 0;
-  std::vector<int> indpix_host;
+  std::vector<int> indpix_host;        // RING pixel -> RING-order compact index (reference)
+  std::vector<long long> int2ring;     // internal index -> RING pixel
+  std::vector<long long> int2ringc;    // internal index -> RING-order compact index
   std::vector<long long> isampmin;
 
   DevBuf pix, cs, y, tod, csr_off, csr_idx, csr_cs, hits, indpix, sumcross;
@@ -106,6 +109,16 @@ struct sg_ctx {
     if (ev1) cudaEventDestroy(ev1);
     if (sc_host) cudaFreeHost(sc_host);
     if (own_st) cudaStreamDestroy(own_st);
+  }
+
+  // compact vectors [I|Q|U]: RING-order compact (API) <-> internal order
+  void to_internal(const double* ringc, double* out) const {
+    for (int cc = 0; cc < 3; cc++)
+      for (long long m = 0; m < npix; m++) out[cc * npix + m] = ringc[cc * npix + int2ringc[m]];
+  }
+  void to_ring(const double* internal, double* out) const {
+    for (int cc = 0; cc < 3; cc++)
+      for (long long m = 0; m < npix; m++) out[cc * npix + int2ringc[m]] = internal[cc * npix + m];
   }
 
   // ---- operator pieces ---------------------------------------------------
@@ -146,10 +159,10 @@ struct sg_ctx {
     const int* h = masked ? hits.as<int>() : nullptr;
     launches++;
     if (f32)
-      return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(),
-                              csr_cs.as<float>(), (const float*)yy, npix, h, out, st);
-    return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(),
-                             csr_cs.as<double>(), (const double*)yy, npix, h, out, st);
+      return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
+                              (const float*)yy, npix, h, out, st);
+    return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<double>(),
+                             (const double*)yy, npix, h, out, st);
   }
 
   cudaError_t to_map(const double* v) {
@@ -158,11 +171,26 @@ struct sg_ctx {
     return to_map4<double>(v, npix, dmap.as<double>(), st);
   }
 
+  // y = P map (time order), then N^-1 in place on y
+  cudaError_t launch_project() {
+    launches++;
+    if (f32) return project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), nsamp,
+                                          y.as<float>(), st);
+    return project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), nsamp,
+                                  y.as<double>(), st);
+  }
+
+  cudaError_t apply_map(double* out, bool masked) {
+    cudaError_t e = launch_project();
+    if (e == cudaSuccess) e = launch_filter(kLoadTod, y.p, y.p, ntiles, (int)nseg, 0);
+    if (e == cudaSuccess) e = launch_pt(y.p, out, masked);
+    return e;
+  }
+
   // out = A v (masked or not); v is a device compact vector
   cudaError_t apply_dev(const double* v, double* out, bool masked) {
     cudaError_t e = to_map(v);
-    if (e == cudaSuccess) e = launch_filter(kLoadProj, nullptr, y.p, ntiles, (int)nseg, 0);
-    if (e == cudaSuccess) e = launch_pt(y.p, out, masked);
+    if (e == cudaSuccess) e = apply_map(out, masked);
     return e;
   }
 
@@ -188,8 +216,7 @@ struct sg_ctx {
   // one PCG iteration (sanepic.cc:1417-1610) as a launch sequence
   cudaError_t enqueue_iteration(int precond, bool refresh) {
     CgVecs v = vecs(precond);
-    cudaError_t e = launch_filter(kLoadProj, nullptr, y.p, ntiles, (int)nseg, 0);
-    if (e == cudaSuccess) e = launch_pt(y.p, q.as<double>(), true);
+    cudaError_t e = apply_map(q.as<double>(), true);
     if (e == cudaSuccess) e = cg_step_a(v, st);
     if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 0, st);
     launches += 3;  // step a, b, c
@@ -385,7 +412,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   }
   cudaError_t e;
   DevBuf dra, ddec, dpsi, doffx, doffy, dpdet, dgoff, dgdet, ring, psip, psipfp, flag, count,
-      scratch, npix_dev;
+      scratch;
   const long long nsamp = c->nsamp;
   const bool hwp = c->desc.hwp != 0;
 #define SG_TRY(x)                                   \
@@ -462,19 +489,37 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(count.alloc(sizeof(int) * c->npixfull));
   SG_TRY(cudaMemsetAsync(count.p, 0, sizeof(int) * c->npixfull, c->st));
   SG_TRY(hist_launch(ring.as<int>(), nsamp, count.as<int>(), c->st));
-  SG_TRY(c->indpix.alloc(sizeof(int) * c->npixfull));
-  const size_t tb = indpix_tmp_bytes(c->npixfull);
-  SG_TRY(scratch.alloc(tb));
-  SG_TRY(npix_dev.alloc(sizeof(long long)));
-  SG_TRY(indpix_launch(count.as<int>(), c->npixfull, c->indpix.as<int>(),
-                       npix_dev.as<long long>(), scratch.p, tb, c->st));
-  long long npix = 0;
-  SG_TRY(cudaMemcpyAsync(&npix, npix_dev.p, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+  // indpix in the reference's RING order (sanepic.cc:904-915), and the
+  // library's internal numbering: observed pixels in NESTED order
+  std::vector<int> hcount(c->npixfull);
+  SG_TRY(cudaMemcpyAsync(hcount.data(), count.p, sizeof(int) * c->npixfull,
+                         cudaMemcpyDeviceToHost, c->st));
   SG_TRY(cudaStreamSynchronize(c->st));
+  c->indpix_host.assign(c->npixfull, -1);
+  long long npix = 0;
+  for (long long p = 0; p < c->npixfull; p++)
+    if (hcount[p] != 0) c->indpix_host[p] = (int)npix++;
   c->npix = npix;
-  c->indpix_host.resize(c->npixfull);
-  SG_TRY(cudaMemcpy(c->indpix_host.data(), c->indpix.p, sizeof(int) * c->npixfull,
-                    cudaMemcpyDeviceToHost));
+  c->int2ring.resize(npix);
+  {
+    std::vector<std::pair<long long, long long>> key;  // (nested, ring)
+    key.reserve(npix);
+    const long long ns_ = c->desc.nside;
+    const bool pow2 = (ns_ & (ns_ - 1)) == 0;
+    for (long long p = 0; p < c->npixfull; p++)
+      if (hcount[p] != 0) key.emplace_back(pow2 ? hp_ring2nest(ns_, p) : p, p);
+    std::sort(key.begin(), key.end());
+    for (long long m = 0; m < npix; m++) c->int2ring[m] = key[m].second;
+  }
+  c->int2ringc.resize(npix);
+  std::vector<int> indpix_int(c->npixfull, -1);
+  for (long long m = 0; m < npix; m++) {
+    indpix_int[c->int2ring[m]] = (int)m;
+    c->int2ringc[m] = c->indpix_host[c->int2ring[m]];
+  }
+  SG_TRY(c->indpix.alloc(sizeof(int) * c->npixfull));
+  SG_TRY(cudaMemcpy(c->indpix.p, indpix_int.data(), sizeof(int) * c->npixfull,
+                    cudaMemcpyHostToDevice));
   SG_TRY(c->pix.alloc(sizeof(int) * nsamp));
   SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), nsamp, c->pix.as<int>(), c->st));
   SG_TRY(c->hits.alloc(sizeof(int) * npix));
@@ -620,11 +665,14 @@ extern "C" int sg_apply(sg_ctx* c, const double* xin, double* yout, int masked) 
   if (!xin || !yout) return c->fail(SG_ERR_ARG, "null vector");
   cudaSetDevice(c->desc.device);
   const size_t vb = sizeof(double) * 3 * c->npix;
-  cudaError_t e = cudaMemcpyAsync(c->z.p, xin, vb, cudaMemcpyHostToDevice, c->st);
+  std::vector<double> tmp(3 * c->npix);
+  c->to_internal(xin, tmp.data());
+  cudaError_t e = cudaMemcpyAsync(c->z.p, tmp.data(), vb, cudaMemcpyHostToDevice, c->st);
   if (e == cudaSuccess) e = c->apply_dev(c->z.as<double>(), c->q.as<double>(), masked != 0);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(yout, c->q.p, vb, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), c->q.p, vb, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "apply");
+  c->to_ring(tmp.data(), yout);
   return SG_OK;
 }
 
@@ -726,8 +774,11 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   const size_t vb = sizeof(double) * 3 * npix;
   cudaError_t e;
   // x0 (masked, sanepic.cc:1209-1227, 1316-1330), r = A x0
+  std::vector<double> x0i;
   if (o->x0) {
-    e = cudaMemcpyAsync(c->x.p, o->x0, vb, cudaMemcpyHostToDevice, c->st);
+    x0i.resize(3 * npix);
+    c->to_internal(o->x0, x0i.data());
+    e = cudaMemcpyAsync(c->x.p, x0i.data(), vb, cudaMemcpyHostToDevice, c->st);
     if (e == cudaSuccess) e = mask_qu(c->x.as<double>(), c->hits.as<int>(), npix, c->st);
     if (e == cudaSuccess) e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
   } else {
@@ -793,10 +844,8 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
 
 // ---------------------------------------------------------------------------
 static void expand(const sg_ctx* c, const double* compact, double* full) {
-  for (long long p = 0; p < c->npixfull; p++) {
-    const int m = c->indpix_host[p];
-    full[p] = m >= 0 ? compact[m] : 0.0;
-  }
+  for (long long p = 0; p < c->npixfull; p++) full[p] = 0.0;
+  for (long long m = 0; m < c->npix; m++) full[c->int2ring[m]] = compact[m];
 }
 
 extern "C" int sg_get_map(sg_ctx* c, int kind, double* out) {
@@ -854,8 +903,12 @@ extern "C" int sg_get_map(sg_ctx* c, int kind, double* out) {
 extern "C" int sg_get_solution(sg_ctx* c, double* out) {
   if (!c || !out) return SG_ERR_ARG;
   if (!c->have_solution) return c->fail(SG_ERR_STATE, "no solution yet");
-  cudaError_t e = cudaMemcpy(out, c->x.p, sizeof(double) * 3 * c->npix, cudaMemcpyDeviceToHost);
-  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "get_solution");
+  std::vector<double> tmp(3 * c->npix);
+  cudaError_t e =
+      cudaMemcpy(tmp.data(), c->x.p, sizeof(double) * 3 * c->npix, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return c->cuda_fail(e, "get_solution");
+  c->to_ring(tmp.data(), out);
+  return SG_OK;
 }
 
 extern "C" int sg_get_pixels(sg_ctx* c, long* ring_out) {
@@ -864,10 +917,7 @@ extern "C" int sg_get_pixels(sg_ctx* c, long* ring_out) {
   std::vector<int> comp(c->nsamp);
   cudaError_t e = cudaMemcpy(comp.data(), c->pix.p, sizeof(int) * c->nsamp, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return c->cuda_fail(e, "get_pixels");
-  std::vector<long> inv(c->npix, -1);
-  for (long long p = 0; p < c->npixfull; p++)
-    if (c->indpix_host[p] >= 0) inv[c->indpix_host[p]] = (long)p;
-  for (long long i = 0; i < c->nsamp; i++) ring_out[i] = inv[comp[i]];
+  for (long long i = 0; i < c->nsamp; i++) ring_out[i] = (long)c->int2ring[comp[i]];
   return SG_OK;
 }
 
@@ -883,31 +933,28 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   int rc = check_ready(c, false);
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
-  cudaEvent_t e0, e1, e2;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventCreate(&e2);
+  cudaEvent_t ev[4];
+  for (auto& x : ev) cudaEventCreate(&x);
   cudaError_t e = c->to_map(c->d.as<double>());
-  float t_filter = 0.f, t_pt = 0.f;
+  float tot[3] = {0.f, 0.f, 0.f};
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
-    float a = 0.f, b2 = 0.f;
-    e = cudaEventRecord(e0, c->st);
-    if (e == cudaSuccess) e = c->launch_filter(kLoadProj, nullptr, c->y.p, c->ntiles, (int)c->nseg, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
+    e = cudaEventRecord(ev[0], c->st);
+    if (e == cudaSuccess) e = c->launch_project();
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
+    if (e == cudaSuccess) e = c->launch_filter(kLoadTod, c->y.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
     if (e == cudaSuccess) e = c->launch_pt(c->y.p, c->q.as<double>(), true);
-    if (e == cudaSuccess) e = cudaEventRecord(e2, c->st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(e2);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&a, e0, e1);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&b2, e1, e2);
-    t_filter += a;
-    t_pt += b2;
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+      float t = 0.f;
+      e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      tot[k] += t;
+    }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
+  for (auto& x : ev) cudaEventDestroy(x);
   if (e != cudaSuccess) return c->cuda_fail(e, "profile_operator");
-  ms[0] = t_filter / reps;
-  ms[1] = t_pt / reps;
+  for (int k = 0; k < 3; k++) ms[k] = tot[k] / reps;
   return SG_OK;
 }
 

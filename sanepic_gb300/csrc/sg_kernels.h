@@ -36,6 +36,7 @@ cudaError_t filter_launch(const FilterArgs<T>& a, int logm, int S, int nclusters
 template <typename T>
 int filter_max_clusters(int logm, int S);
 size_t filter_smem_bytes(int logm, int S, int esize);
+int filter_cluster_size(int logm, int esize);
 
 // ---- pointing expansion + pixelisation (sg_pointing.cu, FP64, no FMA) --------
 struct PointingArgs {
@@ -61,10 +62,6 @@ cudaError_t pointing_launch_groups(const PointingArgs& a, int ngroups, const int
 
 // ---- setup helpers (sg_setup.cu) ------------------------------------------------
 cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream_t st);
-// count[npixfull] -> indpix[npixfull] (-1 unobserved), returns npix through *npix_dev
-cudaError_t indpix_launch(const int* count, long long npixfull, int* indpix,
-                          long long* npix_dev, void* tmp, size_t tmp_bytes, cudaStream_t st);
-size_t indpix_tmp_bytes(long long npixfull);
 cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, int* pix,
                            cudaStream_t st);
 // hits_true[m] = count[ring(m)] via indpix
@@ -95,7 +92,11 @@ template <typename T>
 cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
                         long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st);
 
-// ---- P^T (sg_pt.cu) ------------------------------------------------------------
+// ---- P and P^T (sg_pt.cu) --------------------------------------------------------
+// t[i] = I[pix_i] + cos_i Q[pix_i] + sin_i U[pix_i]; map is [npix][4]; n % 4 == 0
+template <typename T>
+cudaError_t project_launch(const int* pix, const T* cs, const T* map, long long n, T* t,
+                           cudaStream_t st);
 // q[c*npix + m] = sum over samples of pixel m of w_c * y (w = 1, cos, sin),
 // Q/U zeroed where the pol mask applies (hits_true < 2).
 template <typename T>

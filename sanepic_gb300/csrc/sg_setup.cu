@@ -32,41 +32,6 @@ cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream
   return cudaGetLastError();
 }
 
-__global__ void k_flags(const int* count, long long n, int* flags) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    flags[i] = count[i] != 0 ? 1 : 0;
-}
-
-__global__ void k_indpix_finish(const int* count, const int* scan, long long npixfull,
-                                int* indpix, long long* npix) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npixfull;
-       i += (long long)gridDim.x * blockDim.x) {
-    indpix[i] = count[i] != 0 ? scan[i] : -1;
-    if (i == npixfull - 1) *npix = (long long)scan[i] + (count[i] != 0 ? 1 : 0);
-  }
-}
-
-size_t indpix_tmp_bytes(long long npixfull) {
-  size_t cub_bytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, (int*)nullptr, (int*)nullptr,
-                                (long long)npixfull);
-  return cub_bytes + sizeof(int) * (size_t)npixfull + 256;
-}
-
-cudaError_t indpix_launch(const int* count, long long npixfull, int* indpix, long long* npix,
-                          void* tmp, size_t tmp_bytes, cudaStream_t st) {
-  int* scan = reinterpret_cast<int*>(tmp);
-  void* cub_tmp = reinterpret_cast<char*>(tmp) + ((sizeof(int) * npixfull + 255) / 256) * 256;
-  size_t cub_bytes = tmp_bytes - ((sizeof(int) * npixfull + 255) / 256) * 256;
-  k_flags<<<grid_for(npixfull, 256), 256, 0, st>>>(count, npixfull, scan);
-  cudaError_t e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, scan, scan,
-                                                (long long)npixfull, st);
-  if (e != cudaSuccess) return e;
-  k_indpix_finish<<<grid_for(npixfull, 256), 256, 0, st>>>(count, scan, npixfull, indpix, npix);
-  return cudaGetLastError();
-}
-
 __global__ void k_compact(const int* ring_pix, const int* indpix, long long n, int* pix) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
