@@ -175,13 +175,19 @@ def run_ours(args):
     ns_all = spec.ndet * spec.nseg * spec.ns
     npix = mm.npix
     esz = 4 if spec.precision == "f32" else 8
-    # algorithmic bytes per launch (each input read once, each output written once)
+    # algorithmic bytes per launch (each input read once, each output written once).
+    # Detectors sharing focal-plane offsets share one pixel stream: pixel index,
+    # base angle and the CSR live per group sample (ng), y per detector sample.
+    ngrp = 1  # the synthetic detectors all sit on the boresight
+    ng = ngrp * spec.nseg * spec.ns
     kbytes = {
-        "k_project": ns_all * (4 + 2 * esz + esz) + npix * 4 * esz,
+        "k_project": ng * (4 + 2 * esz) + ns_all * esz + npix * 4 * esz,
         "k_noise_filter": ns_all * 2 * esz + spec.ndet * (spec.ns // 2 + 1) * esz,
-        "k_pt": ns_all * (4 + 2 * esz + esz) + npix * (3 * 8 + 8 + 4),
+        "k_detsum": ns_all * esz + ng * 4 * esz,
+        "k_pt": ng * (4 + 2 * esz + 4 * esz) + npix * (3 * 8 + 8 + 4),
     }
-    kms = {"k_project": prof["p_ms"], "k_noise_filter": prof["filter_ms"], "k_pt": prof["pt_ms"]}
+    kms = {"k_project": prof["p_ms"], "k_noise_filter": prof["filter_ms"],
+           "k_detsum": prof["detsum_ms"], "k_pt": prof["pt_ms"]}
     hbm, peak_kind = peaks()
     kernels = {k: {"ms": kms[k], "GBps": kbytes[k] / (kms[k] * 1e-3) / 1e9,
                    "bytes": kbytes[k]} for k in kbytes}

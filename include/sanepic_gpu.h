@@ -93,6 +93,8 @@ typedef struct sg_report {
   double setup_seconds; /* preconditioner build inside sg_solve */
   double device_seconds;  /* CUDA-event time of the iterations on the GPU */
   long kernel_launches;   /* kernels this library launched during the solve */
+  int breakdown;          /* nonzero: stopped early because d^T A d <= 0 (bit 0) or
+                             r^T M r <= 0 (bit 1) -- the residual reached rounding level */
 } sg_report;
 
 /* Creates a context on desc->device.  Replaces the parameter handling of
@@ -171,9 +173,10 @@ int sg_get_indpix(sg_ctx *ctx, long *indpix);
 /* crit = |r|^2/|b|^2 after each iteration of the last solve (up to max). */
 int sg_get_crit_history(sg_ctx *ctx, double *out, int max);
 
-/* Diagnostics: average CUDA-event time (ms) of the three operator kernels over
+/* Diagnostics: average CUDA-event time (ms) of the four operator kernels over
  * `reps` applications of A to the current search direction: ms[0] = P,
- * ms[1] = noise filter N^-1, ms[2] = P^T.  Overwrites only scratch buffers.
+ * ms[1] = noise filter N^-1, ms[2] = per-sample detector sums, ms[3] = P^T.
+ * Overwrites only scratch buffers.
  * No reference counterpart (the reference has no profiling). */
 int sg_profile_operator(sg_ctx *ctx, int reps, double *ms);
 

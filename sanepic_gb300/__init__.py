@@ -67,7 +67,7 @@ class SgReport(ctypes.Structure):
                 ("crit", ctypes.c_double), ("var00", ctypes.c_double),
                 ("solve_seconds", ctypes.c_double), ("iter_per_sec", ctypes.c_double),
                 ("setup_seconds", ctypes.c_double), ("device_seconds", ctypes.c_double),
-                ("kernel_launches", ctypes.c_long)]
+                ("kernel_launches", ctypes.c_long), ("breakdown", ctypes.c_int)]
 
 
 _lib = None
@@ -231,9 +231,10 @@ class MapMaker:
         return out
 
     def profile_operator(self, reps: int = 5) -> dict:
-        ms = np.zeros(3)
+        ms = np.zeros(4)
         self._check(self.L.sg_profile_operator(self.h, reps, _dp(ms)))
-        return {"p_ms": float(ms[0]), "filter_ms": float(ms[1]), "pt_ms": float(ms[2])}
+        return {"p_ms": float(ms[0]), "filter_ms": float(ms[1]), "detsum_ms": float(ms[2]),
+                "pt_ms": float(ms[3])}
 
     def crit_history(self, max_n: int = 100000) -> np.ndarray:
         out = np.empty(max_n)

@@ -75,7 +75,15 @@ struct sg_ctx {
   std::vector<long long> int2ringc;    // internal index -> RING-order compact index
   std::vector<long long> isampmin;
 
+  // Detectors with identical focal-plane offsets share one pixel stream (an
+  // offset group).  pix, cs, csr_* live per group sample (ngsamp of them);
+  // y and tod per detector sample (nsamp).
+  int ngroups = 0;
+  long long ngsamp = 0;
+  std::vector<int> grp_off_h, grp_det_h;
+  std::vector<double> g0_h, psidet_h;
   DevBuf pix, cs, y, tod, csr_off, csr_idx, csr_cs, hits, indpix, sumcross;
+  DevBuf grp_off, grp_det, dcs, ys, gconst;
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
   cplx<float> wn1f{1.f, 0.f};
@@ -131,9 +139,6 @@ struct sg_ctx {
     a.mode = mode;
     a.filt_abs = filt_abs;
     a.tod = in;
-    a.pix = pix.as<int>();
-    a.cs = cs.as<T>();
-    a.map = dmap.as<T>();
     a.filt = filt.as<T>();
     a.out = out;
     a.tw_lo = tw_lo.as<cplx<T>>();
@@ -155,14 +160,31 @@ struct sg_ctx {
     return filter_launch<double>(a, logm, S, ncl, st);
   }
 
-  cudaError_t launch_pt(const void* yy, double* out, bool masked) {
+  // per group sample detector sums of y, then the CSR reduction into a map
+  cudaError_t launch_detsum() {
+    launches++;
+    if (f32)
+      return detsum_launch<float>(y.as<float>(), ngsamp, ns * nseg, grp_off.as<int>(),
+                                  grp_det.as<int>(), dcs.as<float>(), ys.as<float>(), st);
+    return detsum_launch<double>(y.as<double>(), ngsamp, ns * nseg, grp_off.as<int>(),
+                                 grp_det.as<int>(), dcs.as<double>(), ys.as<double>(), st);
+  }
+
+  cudaError_t launch_pt(double* out, bool masked) {
     const int* h = masked ? hits.as<int>() : nullptr;
     launches++;
     if (f32)
       return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
-                              (const float*)yy, npix, h, out, st);
+                              ys.as<float>(), npix, h, out, st);
     return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<double>(),
-                             (const double*)yy, npix, h, out, st);
+                             ys.as<double>(), npix, h, out, st);
+  }
+
+  // out = P^T y (y in time order, one row per detector)
+  cudaError_t pt_of_y(double* out, bool masked) {
+    cudaError_t e = launch_detsum();
+    if (e == cudaSuccess) e = launch_pt(out, masked);
+    return e;
   }
 
   cudaError_t to_map(const double* v) {
@@ -171,19 +193,22 @@ struct sg_ctx {
     return to_map4<double>(v, npix, dmap.as<double>(), st);
   }
 
-  // y = P map (time order), then N^-1 in place on y
+  // y = P map (time order, every detector), then N^-1 in place on y
   cudaError_t launch_project() {
     launches++;
-    if (f32) return project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), nsamp,
-                                          y.as<float>(), st);
-    return project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), nsamp,
-                                  y.as<double>(), st);
+    if (f32)
+      return project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
+                                   ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
+                                   dcs.as<float>(), y.as<float>(), st);
+    return project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
+                                  ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
+                                  dcs.as<double>(), y.as<double>(), st);
   }
 
   cudaError_t apply_map(double* out, bool masked) {
     cudaError_t e = launch_project();
     if (e == cudaSuccess) e = launch_filter(kLoadTod, y.p, y.p, ntiles, (int)nseg, 0);
-    if (e == cudaSuccess) e = launch_pt(y.p, out, masked);
+    if (e == cudaSuccess) e = pt_of_y(out, masked);
     return e;
   }
 
@@ -370,6 +395,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   if (!ra || !dec || !psi || !dets) return c->fail(SG_ERR_ARG, "null pointing array");
   cudaSetDevice(c->desc.device);
   const long long ns = c->ns, nseg = c->nseg, ndet = c->ndet, nsd = ns * nseg;
+  const bool hwp = c->desc.hwp != 0;
   c->isampmin.resize(nseg);
   for (long long g = 0; g < nseg; g++) {
     c->isampmin[g] = isampmin ? isampmin[g] : g * ns;
@@ -389,106 +415,131 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
       if (!(v > 0) && !(v <= 0.0)) v = hpsi[g * ns + i - 1];
     }
   }
-  // detectors grouped by identical offsets share the pixelisation
-  std::vector<int> grp_off, grp_det;
-  {
-    std::vector<char> used(ndet, 0);
-    for (long long dd = 0; dd < ndet; dd++) {
-      if (used[dd]) continue;
-      grp_off.push_back((int)grp_det.size());
-      for (long long e2 = dd; e2 < ndet; e2++)
-        if (!used[e2] && dets[e2].offx == dets[dd].offx && dets[e2].offy == dets[dd].offy) {
-          used[e2] = 1;
-          grp_det.push_back((int)e2);
-        }
-    }
-    grp_off.push_back((int)grp_det.size());
-  }
-  std::vector<double> offx(ndet), offy(ndet), pdet(ndet);
-  for (long long dd = 0; dd < ndet; dd++) {
-    offx[dd] = dets[dd].offx;
-    offy[dd] = dets[dd].offy;
-    pdet[dd] = dets[dd].psi;
-  }
   cudaError_t e;
-  DevBuf dra, ddec, dpsi, doffx, doffy, dpdet, dgoff, dgdet, ring, psip, psipfp, flag, count,
-      scratch;
-  const long long nsamp = c->nsamp;
-  const bool hwp = c->desc.hwp != 0;
-#define SG_TRY(x)                                   \
-  do {                                              \
-    e = (x);                                        \
+#define SG_TRY(x)                                     \
+  do {                                                \
+    e = (x);                                          \
     if (e != cudaSuccess) return c->cuda_fail(e, #x); \
   } while (0)
+  DevBuf dra, ddec, dpsi, doffx, doffy, ring, psio, flag, count, scratch, gsz, gsc, gss;
   SG_TRY(dra.alloc(sizeof(double) * nsd));
   SG_TRY(ddec.alloc(sizeof(double) * nsd));
   SG_TRY(dpsi.alloc(sizeof(double) * nsd));
-  SG_TRY(doffx.alloc(sizeof(double) * ndet));
-  SG_TRY(doffy.alloc(sizeof(double) * ndet));
-  SG_TRY(dpdet.alloc(sizeof(double) * ndet));
-  SG_TRY(dgoff.alloc(sizeof(int) * grp_off.size()));
-  SG_TRY(dgdet.alloc(sizeof(int) * grp_det.size()));
-  SG_TRY(ring.alloc(sizeof(int) * nsamp));
-  SG_TRY(psip.alloc(sizeof(double) * nsamp));
-  if (hwp) SG_TRY(psipfp.alloc(sizeof(double) * nsamp));
   SG_TRY(flag.alloc(sizeof(int)));
   SG_TRY(cudaMemcpyAsync(dra.p, hra.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
   SG_TRY(cudaMemcpyAsync(ddec.p, hdec.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
   SG_TRY(cudaMemcpyAsync(dpsi.p, hpsi.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(doffx.p, offx.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(doffy.p, offy.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(dpdet.p, pdet.data(), sizeof(double) * ndet, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(dgoff.p, grp_off.data(), sizeof(int) * grp_off.size(), cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(dgdet.p, grp_det.data(), sizeof(int) * grp_det.size(), cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), c->st));
-  PointingArgs pa{};
-  pa.ns = ns;
-  pa.nseg = (int)nseg;
-  pa.ndet = (int)ndet;
-  pa.ra = dra.as<double>();
-  pa.dec = ddec.as<double>();
-  pa.psi = dpsi.as<double>();
-  pa.offx = doffx.as<double>();
-  pa.offy = doffy.as<double>();
-  pa.psidet = dpdet.as<double>();
-  pa.hwp = hwp ? 1 : 0;
-  pa.omega = c->desc.omega;
-  pa.nside = c->desc.nside;
-  pa.ring_pix = ring.as<int>();
-  pa.psip = psip.as<double>();
-  pa.psipfp = hwp ? psipfp.as<double>() : nullptr;
-  pa.error_flag = flag.as<int>();
-  SG_TRY(pointing_launch_groups(pa, (int)grp_off.size() - 1, dgoff.as<int>(), dgdet.as<int>(),
-                                c->st));
-  int hflag = 0;
-  SG_TRY(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-  SG_TRY(cudaStreamSynchronize(c->st));
-  if (hflag)
-    return c->fail(SG_ERR_POINTING, "theta out of range in ang2pix (the reference exits here)");
+  // offset groups: detectors with identical (offx, offy) share the pixelisation
+  // (pass 1); if any pointing sample is NaN, every detector gets its own
+  // stream (pass 2) so the reference's previous-pixel rule, which carries
+  // across detectors, is applied exactly.
+  std::vector<int> hring;
+  for (int pass = 0; pass < 2; pass++) {
+    std::vector<int> goff, gdet;
+    std::vector<char> used(ndet, 0);
+    for (long long dd = 0; dd < ndet; dd++) {
+      if (used[dd]) continue;
+      goff.push_back((int)gdet.size());
+      for (long long e2 = dd; e2 < ndet; e2++)
+        if (!used[e2] && (pass == 1 ? e2 == dd
+                                    : (dets[e2].offx == dets[dd].offx &&
+                                       dets[e2].offy == dets[dd].offy))) {
+          used[e2] = 1;
+          gdet.push_back((int)e2);
+        }
+    }
+    goff.push_back((int)gdet.size());
+    const int G = (int)goff.size() - 1;
+    std::vector<double> offx(G), offy(G);
+    for (int g = 0; g < G; g++) {
+      offx[g] = dets[gdet[goff[g]]].offx;
+      offy[g] = dets[gdet[goff[g]]].offy;
+    }
+    const long long ng = (long long)G * nsd;
+    SG_TRY(doffx.alloc(sizeof(double) * G));
+    SG_TRY(doffy.alloc(sizeof(double) * G));
+    SG_TRY(ring.alloc(sizeof(int) * ng));
+    SG_TRY(psio.alloc(sizeof(double) * ng));
+    SG_TRY(cudaMemcpyAsync(doffx.p, offx.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+    SG_TRY(cudaMemcpyAsync(doffy.p, offy.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
+    SG_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), c->st));
+    PointingArgs pa{};
+    pa.ns = ns;
+    pa.nseg = (int)nseg;
+    pa.ngroups = G;
+    pa.ra = dra.as<double>();
+    pa.dec = ddec.as<double>();
+    pa.psi = dpsi.as<double>();
+    pa.offx = doffx.as<double>();
+    pa.offy = doffy.as<double>();
+    pa.nside = c->desc.nside;
+    pa.ring_pix = ring.as<int>();
+    pa.psio = psio.as<double>();
+    pa.error_flag = flag.as<int>();
+    SG_TRY(pointing_launch(pa, c->st));
+    int hflag = 0;
+    SG_TRY(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaStreamSynchronize(c->st));
+    if (hflag)
+      return c->fail(SG_ERR_POINTING, "theta out of range in ang2pix (the reference exits here)");
+    hring.resize(ng);
+    SG_TRY(cudaMemcpy(hring.data(), ring.p, sizeof(int) * ng, cudaMemcpyDeviceToHost));
+    bool any_invalid = false;
+    for (long long i = 0; i < ng && !any_invalid; i++) any_invalid = hring[i] < 0;
+    c->ngroups = G;
+    c->ngsamp = ng;
+    c->grp_off_h = goff;
+    c->grp_det_h = gdet;
+    if (!any_invalid) break;
+    if (pass == 1 || G == ndet) {
+      // NaN pointing: reuse the previous pixel in the reference's loop order
+      // (det, seg, sample; sanepic.cc:851-873), streams are per detector here
+      int prev = 0;
+      for (long long i = 0; i < ng; i++) {
+        if (hring[i] < 0) hring[i] = prev;
+        prev = hring[i];
+      }
+      SG_TRY(cudaMemcpy(ring.p, hring.data(), sizeof(int) * ng, cudaMemcpyHostToDevice));
+      break;
+    }
+  }
   dra.release();
   ddec.release();
   dpsi.release();
-  // NaN pointing: reuse the previous pixel in the reference's loop order
-  // (det, seg, sample; sanepic.cc:851-873).  Rare, so done on the host.
+  const int G = c->ngroups;
+  const long long ng = c->ngsamp;
+  std::vector<int> gsize(G);
+  for (int g = 0; g < G; g++) gsize[g] = c->grp_off_h[g + 1] - c->grp_off_h[g];
+  SG_TRY(gsz.alloc(sizeof(int) * G));
+  SG_TRY(cudaMemcpy(gsz.p, gsize.data(), sizeof(int) * G, cudaMemcpyHostToDevice));
+  SG_TRY(c->grp_off.alloc(sizeof(int) * (G + 1)));
+  SG_TRY(c->grp_det.alloc(sizeof(int) * ndet));
+  SG_TRY(cudaMemcpy(c->grp_off.p, c->grp_off_h.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice));
+  SG_TRY(cudaMemcpy(c->grp_det.p, c->grp_det_h.data(), sizeof(int) * ndet, cudaMemcpyHostToDevice));
+  // detector rotations: the detector's angle relative to its group's base
+  // angle phi is +psi_det, or -psi_det under a half-wave plate
+  // (psip = -(psi_o + psi_det) + 2 omega t, sanepic.cc:765)
+  c->psidet_h.resize(ndet);
   {
-    std::vector<int> hr(nsamp);
-    SG_TRY(cudaMemcpy(hr.data(), ring.p, sizeof(int) * nsamp, cudaMemcpyDeviceToHost));
-    bool any = false;
-    int prev = 0;
-    for (long long i = 0; i < nsamp; i++) {
-      if (hr[i] < 0) {
-        hr[i] = prev;
-        any = true;
-      }
-      prev = hr[i];
+    std::vector<double> r(2 * ndet);
+    for (long long dd = 0; dd < ndet; dd++) {
+      c->psidet_h[dd] = dets[dd].psi;
+      const double a = 2.0 * (hwp ? -dets[dd].psi : dets[dd].psi);
+      r[2 * dd] = cos(a);
+      r[2 * dd + 1] = sin(a);
     }
-    if (any)
-      SG_TRY(cudaMemcpy(ring.p, hr.data(), sizeof(int) * nsamp, cudaMemcpyHostToDevice));
+    SG_TRY(c->dcs.alloc((size_t)2 * ndet * c->esize));
+    if (c->f32) {
+      std::vector<float> f(r.begin(), r.end());
+      SG_TRY(cudaMemcpy(c->dcs.p, f.data(), 4 * f.size(), cudaMemcpyHostToDevice));
+    } else {
+      SG_TRY(cudaMemcpy(c->dcs.p, r.data(), 8 * r.size(), cudaMemcpyHostToDevice));
+    }
   }
-  // indpix, compact pixels, hit counts
+  // detector samples per RING pixel
   SG_TRY(count.alloc(sizeof(int) * c->npixfull));
   SG_TRY(cudaMemsetAsync(count.p, 0, sizeof(int) * c->npixfull, c->st));
-  SG_TRY(hist_launch(ring.as<int>(), nsamp, count.as<int>(), c->st));
+  SG_TRY(hist_launch(ring.as<int>(), ng, nsd, gsz.as<int>(), count.as<int>(), c->st));
   // indpix in the reference's RING order (sanepic.cc:904-915), and the
   // library's internal numbering: observed pixels in NESTED order
   std::vector<int> hcount(c->npixfull);
@@ -520,35 +571,51 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(c->indpix.alloc(sizeof(int) * c->npixfull));
   SG_TRY(cudaMemcpy(c->indpix.p, indpix_int.data(), sizeof(int) * c->npixfull,
                     cudaMemcpyHostToDevice));
-  SG_TRY(c->pix.alloc(sizeof(int) * nsamp));
-  SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), nsamp, c->pix.as<int>(), c->st));
+  SG_TRY(c->pix.alloc(sizeof(int) * ng));
+  SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), ng, c->pix.as<int>(), c->st));
   SG_TRY(c->hits.alloc(sizeof(int) * npix));
   SG_TRY(hits_launch(count.as<int>(), c->indpix.as<int>(), c->npixfull, c->hits.as<int>(), c->st));
-  // pixel-sorted sample index (CSR) for P^T
-  const size_t ctb = csr_tmp_bytes(nsamp, npix);
+  ring.release();
+  // pixel-sorted group-sample index (CSR) for P^T
+  const size_t ctb = csr_tmp_bytes(ng, npix);
   SG_TRY(scratch.alloc(ctb));
   SG_TRY(c->csr_off.alloc(sizeof(long long) * (npix + 1)));
-  SG_TRY(c->csr_idx.alloc(sizeof(uint32_t) * nsamp));
-  SG_TRY(csr_build(c->pix.as<int>(), nsamp, npix, c->hits.as<int>(), c->csr_off.as<long long>(),
+  SG_TRY(c->csr_idx.alloc(sizeof(uint32_t) * ng));
+  SG_TRY(csr_build(c->pix.as<int>(), ng, npix, c->csr_off.as<long long>(),
                    c->csr_idx.as<uint32_t>(), scratch.p, ctb, c->st));
   scratch.release();
-  // angles: (cos 2psip, sin 2psip) in time order and in CSR order
-  SG_TRY(c->cs.alloc((size_t)2 * nsamp * c->esize));
-  SG_TRY(c->csr_cs.alloc((size_t)2 * nsamp * c->esize));
+  // base angles (cos 2phi, sin 2phi) in time order and in CSR order
+  SG_TRY(c->cs.alloc((size_t)2 * ng * c->esize));
+  SG_TRY(c->csr_cs.alloc((size_t)2 * ng * c->esize));
   if (c->f32) {
-    SG_TRY(angles_launch<float>(psip.as<double>(), nsamp, c->cs.as<float>(), c->st));
-    SG_TRY(gather_cs_launch<float>(c->cs.as<float>(), c->csr_idx.as<uint32_t>(), nsamp,
+    SG_TRY(base_angles_launch<float>(psio.as<double>(), ng, ns, nsd, hwp ? 1 : 0, c->desc.omega,
+                                     c->cs.as<float>(), c->st));
+    SG_TRY(gather_cs_launch<float>(c->cs.as<float>(), c->csr_idx.as<uint32_t>(), ng,
                                    c->csr_cs.as<float>(), c->st));
   } else {
-    SG_TRY(angles_launch<double>(psip.as<double>(), nsamp, c->cs.as<double>(), c->st));
-    SG_TRY(gather_cs_launch<double>(c->cs.as<double>(), c->csr_idx.as<uint32_t>(), nsamp,
+    SG_TRY(base_angles_launch<double>(psio.as<double>(), ng, ns, nsd, hwp ? 1 : 0, c->desc.omega,
+                                      c->cs.as<double>(), c->st));
+    SG_TRY(gather_cs_launch<double>(c->cs.as<double>(), c->csr_idx.as<uint32_t>(), ng,
                                     c->csr_cs.as<double>(), c->st));
   }
-  // cross-link sums with psipFP (sanepic.cc:1258, 2594-2597)
+  // cross-link sums with psipFP = psi_o + psi_det (sanepic.cc:760-762, 2594-2597)
+  {
+    std::vector<double> sc_(G, 0.0), ss_(G, 0.0);
+    for (int g = 0; g < G; g++)
+      for (int k = c->grp_off_h[g]; k < c->grp_off_h[g + 1]; k++) {
+        sc_[g] += cos(2.0 * c->psidet_h[c->grp_det_h[k]]);
+        ss_[g] += sin(2.0 * c->psidet_h[c->grp_det_h[k]]);
+      }
+    SG_TRY(gsc.alloc(sizeof(double) * G));
+    SG_TRY(gss.alloc(sizeof(double) * G));
+    SG_TRY(cudaMemcpy(gsc.p, sc_.data(), sizeof(double) * G, cudaMemcpyHostToDevice));
+    SG_TRY(cudaMemcpy(gss.p, ss_.data(), sizeof(double) * G, cudaMemcpyHostToDevice));
+  }
   SG_TRY(c->sumcross.alloc(sizeof(double) * 3 * npix));
-  SG_TRY(sumcross_launch(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
-                         hwp ? psipfp.as<double>() : psip.as<double>(), npix,
-                         c->sumcross.as<double>(), c->st));
+  SG_TRY(sumcross_launch(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), psio.as<double>(),
+                         nsd, gsc.as<double>(), gss.as<double>(), npix, c->sumcross.as<double>(),
+                         c->st));
+  SG_TRY(c->ys.alloc((size_t)4 * ng * c->esize));
   // CG vectors
   const size_t vb = sizeof(double) * 3 * npix;
   SG_TRY(c->x.alloc(vb));
@@ -568,6 +635,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(cudaStreamSynchronize(c->st));
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
+  c->graph_launches.clear();
   c->have_pointing = true;
   c->have_rhs = c->have_solution = c->have_bj3 = c->have_diag = false;
   return SG_OK;
@@ -600,6 +668,8 @@ extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) 
                    cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) e = cudaMemcpy(c->g0.as<double>() + det, &g, 8, cudaMemcpyHostToDevice);
+  if (c->g0_h.size() != (size_t)c->ndet) c->g0_h.assign(c->ndet, 0.0);
+  c->g0_h[det] = g;
   if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
   c->have_noise[det] = 1;
   c->have_bj3 = c->have_diag = c->have_rhs = false;
@@ -650,7 +720,7 @@ extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
   cudaError_t e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
-  if (e == cudaSuccess) e = c->launch_pt(c->y.p, c->b.as<double>(), true);
+  if (e == cudaSuccess) e = c->pt_of_y(c->b.as<double>(), true);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "rhs");
   if (chi2) *chi2 = NAN;  // not computed on this path yet
@@ -710,15 +780,35 @@ extern "C" int sg_noise_filter(sg_ctx* c, const double* in, double* out) {
 // ---------------------------------------------------------------------------
 static int build_bj3(sg_ctx* c) {
   if (c->have_bj3) return SG_OK;
-  cudaError_t e;
-  if (c->f32)
-    e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
-                          c->csr_cs.as<float>(), c->npix, c->ns * c->nseg, (int)c->nseg,
-                          c->g0.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
-  else
-    e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
-                           c->csr_cs.as<double>(), c->npix, c->ns * c->nseg, (int)c->nseg,
-                           c->g0.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
+  // group constants (sum g0, sum g0 cos 2d', sum g0 sin 2d', sum g0 cos 4d',
+  // sum g0 sin 4d') over each group's detectors, d' = the detector rotation
+  const int G = c->ngroups;
+  std::vector<double> gc(5 * G, 0.0);
+  for (int g = 0; g < G; g++)
+    for (int k = c->grp_off_h[g]; k < c->grp_off_h[g + 1]; k++) {
+      const int dd = c->grp_det_h[k];
+      const double d2 = 2.0 * (c->desc.hwp ? -c->psidet_h[dd] : c->psidet_h[dd]);
+      const double g0 = c->g0_h[dd];
+      gc[g] += g0;
+      gc[G + g] += g0 * cos(d2);
+      gc[2 * G + g] += g0 * sin(d2);
+      gc[3 * G + g] += g0 * cos(2.0 * d2);
+      gc[4 * G + g] += g0 * sin(2.0 * d2);
+    }
+  cudaError_t e = c->gconst.alloc(sizeof(double) * 5 * G);
+  if (e == cudaSuccess) e = cudaMemcpy(c->gconst.p, gc.data(), sizeof(double) * 5 * G,
+                                       cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    if (c->f32)
+      e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                            c->csr_cs.as<float>(), c->npix, c->ns * c->nseg, G,
+                            c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
+    else
+      e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                             c->csr_cs.as<double>(), c->npix, c->ns * c->nseg, G,
+                             c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(),
+                             c->st);
+  }
   if (e != cudaSuccess) return c->cuda_fail(e, "bj3 build");
   c->have_bj3 = true;
   return SG_OK;
@@ -733,13 +823,23 @@ static int build_diag(sg_ctx* c) {
   if ((e = c->ntab.alloc((size_t)c->ndet * ns * c->esize)) != cudaSuccess)
     return c->cuda_fail(e, "diag alloc");
   e = c->launch_filter(kLoadDelta, nullptr, c->ntab.p, c->ndet, 1, 1);
+  // the group's pixel stream is shared, so the detectors' tables add up
+  DevBuf gtab;
+  if (e == cudaSuccess) e = gtab.alloc((size_t)c->ngroups * ns * c->esize);
   if (e == cudaSuccess) {
-    if (c->f32)
-      e = diag_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
-                             (int)c->nseg, c->ntab.as<float>(), c->mp_raw.as<double>(), c->st);
-    else
-      e = diag_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
-                              (int)c->nseg, c->ntab.as<double>(), c->mp_raw.as<double>(), c->st);
+    if (c->f32) {
+      e = group_ntab_launch<float>(c->ntab.as<float>(), ns, c->ngroups, c->grp_off.as<int>(),
+                                   c->grp_det.as<int>(), gtab.as<float>(), c->st);
+      if (e == cudaSuccess)
+        e = diag_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
+                               (int)c->nseg, gtab.as<float>(), c->mp_raw.as<double>(), c->st);
+    } else {
+      e = group_ntab_launch<double>(c->ntab.as<double>(), ns, c->ngroups, c->grp_off.as<int>(),
+                                    c->grp_det.as<int>(), gtab.as<double>(), c->st);
+      if (e == cudaSuccess)
+        e = diag_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), npix, ns,
+                                (int)c->nseg, gtab.as<double>(), c->mp_raw.as<double>(), c->st);
+    }
   }
   if (e == cudaSuccess) e = mask_qu(c->mp_raw.as<double>(), c->hits.as<int>(), npix, c->st);
   std::vector<double> mp(3 * npix);
@@ -816,10 +916,10 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     if (o->verbose)
       printf("iter = %d, crit = %10.15g, crit2 = %10.15g\n", iter, crit,
              c->sc_host->delta / delta0);
-    if (c->sc_host->flag)
-      return c->fail(SG_ERR_NOT_CONVERGED, "CG breakdown at iteration %d (flag %d)", iter,
-                     c->sc_host->flag);
     iter++;
+    // d^T A d <= 0 or r^T z <= 0: the recurrence has hit rounding level (or a
+    // non-SPD preconditioner); stop with the current map
+    if (c->sc_host->flag) break;
   }
   e = cudaEventRecord(c->ev1, c->st);
   if (e == cudaSuccess) e = cudaEventSynchronize(c->ev1);
@@ -838,6 +938,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     rep->setup_seconds = t1 - t0;
     rep->device_seconds = dev_ms * 1e-3;
     rep->kernel_launches = (long)(c->launches - launches0);
+    rep->breakdown = c->sc_host->flag;
   }
   return SG_OK;
 }
@@ -914,10 +1015,16 @@ extern "C" int sg_get_solution(sg_ctx* c, double* out) {
 extern "C" int sg_get_pixels(sg_ctx* c, long* ring_out) {
   if (!c || !ring_out) return SG_ERR_ARG;
   if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
-  std::vector<int> comp(c->nsamp);
-  cudaError_t e = cudaMemcpy(comp.data(), c->pix.p, sizeof(int) * c->nsamp, cudaMemcpyDeviceToHost);
+  std::vector<int> comp(c->ngsamp);
+  cudaError_t e =
+      cudaMemcpy(comp.data(), c->pix.p, sizeof(int) * c->ngsamp, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return c->cuda_fail(e, "get_pixels");
-  for (long long i = 0; i < c->nsamp; i++) ring_out[i] = (long)c->int2ring[comp[i]];
+  const long long nsd = c->ns * c->nseg;
+  for (int g = 0; g < c->ngroups; g++)
+    for (int k = c->grp_off_h[g]; k < c->grp_off_h[g + 1]; k++) {
+      const long long dd = c->grp_det_h[k];
+      for (long long w = 0; w < nsd; w++) ring_out[dd * nsd + w] = (long)c->int2ring[comp[g * nsd + w]];
+    }
   return SG_OK;
 }
 
@@ -933,20 +1040,22 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   int rc = check_ready(c, false);
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
-  cudaEvent_t ev[4];
+  cudaEvent_t ev[5];
   for (auto& x : ev) cudaEventCreate(&x);
   cudaError_t e = c->to_map(c->d.as<double>());
-  float tot[3] = {0.f, 0.f, 0.f};
+  float tot[4] = {0.f, 0.f, 0.f, 0.f};
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
     e = cudaEventRecord(ev[0], c->st);
     if (e == cudaSuccess) e = c->launch_project();
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
     if (e == cudaSuccess) e = c->launch_filter(kLoadTod, c->y.p, c->y.p, c->ntiles, (int)c->nseg, 0);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-    if (e == cudaSuccess) e = c->launch_pt(c->y.p, c->q.as<double>(), true);
+    if (e == cudaSuccess) e = c->launch_detsum();
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], c->st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
-    for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+    if (e == cudaSuccess) e = c->launch_pt(c->q.as<double>(), true);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4], c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+    for (int k = 0; k < 4 && e == cudaSuccess; k++) {
       float t = 0.f;
       e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
       tot[k] += t;
@@ -954,7 +1063,7 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   }
   for (auto& x : ev) cudaEventDestroy(x);
   if (e != cudaSuccess) return c->cuda_fail(e, "profile_operator");
-  for (int k = 0; k < 3; k++) ms[k] = tot[k] / reps;
+  for (int k = 0; k < 4; k++) ms[k] = tot[k] / reps;
   return SG_OK;
 }
 

@@ -39,69 +39,83 @@ size_t filter_smem_bytes(int logm, int S, int esize);
 int filter_cluster_size(int logm, int esize);
 
 // ---- pointing expansion + pixelisation (sg_pointing.cu, FP64, no FMA) --------
+// Per offset group g (detectors with identical (offx, offy)) and group sample
+// w = iseg * ns + ii: RING pixel and psi_o (the angle before the detector's
+// own angle is added, sanepic.cc:742-759).
 struct PointingArgs {
   long long ns;          // samples per segment
-  int nseg, ndet;
+  int nseg, ngroups;
   const double* ra;      // [nseg][ns] boresight, psi already NaN-patched
   const double* dec;
   const double* psi;
-  const double* offx;    // [ndet] radians
+  const double* offx;    // [ngroups] radians
   const double* offy;
-  const double* psidet;
-  int hwp;
-  double omega;
   long long nside;
-  int* ring_pix;         // [ndet][nseg][ns]; -1 invalid (NaN), -2 out of range
-  double* psip;          // [ndet][nseg][ns] or nullptr
-  double* psipfp;        // [ndet][nseg][ns] or nullptr
+  int* ring_pix;         // [ngroups][nseg][ns]; -1 invalid (NaN), -2 out of range
+  double* psio;          // [ngroups][nseg][ns]
   int* error_flag;       // set to 1 when theta is outside [0, pi]
 };
-// grp_off [ngroups+1] / grp_det: detectors grouped by identical (offx, offy)
-cudaError_t pointing_launch_groups(const PointingArgs& a, int ngroups, const int* grp_off,
-                                   const int* grp_det, cudaStream_t st);
+cudaError_t pointing_launch(const PointingArgs& a, cudaStream_t st);
 
 // ---- setup helpers (sg_setup.cu) ------------------------------------------------
-cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream_t st);
+// Group samples are indexed gs = g * nsd + iseg * ns + ii (nsd = nseg * ns).
+// detector samples per RING pixel (each group sample counts gsize[g] times)
+cudaError_t hist_launch(const int* ring_pix, long long n, long long nsd, const int* gsize,
+                        int* count, cudaStream_t st);
 cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, int* pix,
                            cudaStream_t st);
 // hits_true[m] = count[ring(m)] via indpix
 cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull,
                         int* hits_true, cudaStream_t st);
-// CSR by pixel: keys sorted; csr_off [npix+1], csr_idx [n]
+// CSR by pixel over group samples: csr_off [npix+1], csr_idx [n]
 size_t csr_tmp_bytes(long long n, long long npix);
-cudaError_t csr_build(const int* pix, long long n, long long npix, const int* hits_true,
+cudaError_t csr_build(const int* pix, long long n, long long npix,
                       long long* csr_off, uint32_t* csr_idx, void* tmp, size_t tmp_bytes,
                       cudaStream_t st);
 template <typename T>
 cudaError_t gather_cs_launch(const T* cs, const uint32_t* csr_idx, long long n, T* csr_cs,
                              cudaStream_t st);
-// (cos 2psi, sin 2psi) per sample in precision T from psip (FP64)
+// (cos 2phi, sin 2phi) of the group base angle per group sample
 template <typename T>
-cudaError_t angles_launch(const double* psip, long long n, T* cs, cudaStream_t st);
-// COS2P/SIN2P sums (sanepic.cc:2594-2597) over the CSR, FP64
-cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx,
-                            const double* psipfp, long long npix, double* sumcross,
-                            cudaStream_t st);
-// 3x3 block-Jacobi build+invert; minv [6][npix] (00 01 02 11 12 22)
+cudaError_t base_angles_launch(const double* psio, long long n, long long ns, long long nsd,
+                               int hwp, double omega, T* cs, cudaStream_t st);
+// COS2P/SIN2P sums over the CSR; gsc/gss [ngroups] = group sums of cos/sin 2psi_det
+cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, const double* psio,
+                            long long nsd, const double* gsc, const double* gss, long long npix,
+                            double* sumcross, cudaStream_t st);
+// 3x3 block-Jacobi build+invert; gconst [5][ngroups]; minv [6][npix] (00 01 02 11 12 22)
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
-                       long long npix, long long tile_len, int nseg, const double* g0,
+                       long long npix, long long nsd, int ngroups, const double* gconst,
                        const int* hits_true, double* minv, cudaStream_t st);
-// reference diagonal (compute_diagPtNPCorr x2, sanepic.cc:2680-2762): Mp [3][npix]
+// per-group sum of the detectors' N_ tables: out [ngroups][ns]
+template <typename T>
+cudaError_t group_ntab_launch(const T* ntab, long long ns, int ngroups, const int* grp_off,
+                              const int* grp_det, T* out, cudaStream_t st);
+// reference diagonal (compute_diagPtNPCorr x2, sanepic.cc:2680-2762): Mp [3][npix];
+// ntab is per group [ngroups][ns] (group tile = idx / ns, group = tile / nseg)
 template <typename T>
 cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
                         long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st);
 
-// ---- P and P^T (sg_pt.cu) --------------------------------------------------------
-// t[i] = I[pix_i] + cos_i Q[pix_i] + sin_i U[pix_i]; map is [npix][4]; n % 4 == 0
+// ---- P, detector sums, P^T (sg_pt.cu) ------------------------------------------
+// Groups: grp_off [ngroups+1] / grp_det list the detectors of each offset group;
+// dcs [ndet] = (cos 2d', sin 2d') rotates the group base angle to the detector's.
+// P: t[det][w] = I + cos(2phi+2d') Q + sin(2phi+2d') U at the group's pixel
+// (n = group samples, multiple of 4); map is [npix][4].
 template <typename T>
-cudaError_t project_launch(const int* pix, const T* cs, const T* map, long long n, T* t,
-                           cudaStream_t st);
-// q[c*npix + m] = sum over samples of pixel m of w_c * y (w = 1, cos, sin),
-// Q/U zeroed where the pol mask applies (hits_true < 2).
+cudaError_t project_launch(const int* gpix, const T* gcs, const T* map, long long n,
+                           long long nsd, const int* grp_off, const int* grp_det, const T* dcs,
+                           T* t, cudaStream_t st);
+// detector sums per group sample: ys[gs] = (sum y, sum cos2d' y, sum sin2d' y, 0)
+template <typename T>
+cudaError_t detsum_launch(const T* y, long long n, long long nsd, const int* grp_off,
+                          const int* grp_det, const T* dcs, T* ys, cudaStream_t st);
+// q[c*npix + m]: sums over the group samples of pixel m of (S0, cos2phi A - sin2phi B,
+// sin2phi A + cos2phi B); Q/U zeroed where the pol mask applies (hits_true < 2).
 template <typename T>
 cudaError_t pt_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
-                      const T* y, long long npix, const int* hits_true, double* q,
+                      const T* ys, long long npix, const int* hits_true, double* q,
                       cudaStream_t st);
 
 // ---- CG vector algebra (sg_cg.cu) ------------------------------------------------

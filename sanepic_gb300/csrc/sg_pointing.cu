@@ -11,10 +11,11 @@
 // atan2/asin, which can move a pixel index only for a sample within ~1e-16
 // of a pixel boundary.
 //
-// Detectors that share (offx, offy) have identical pixels (the boresight
-// files are common to all detectors, sanepic.cc:680-692), so each thread
-// computes one boresight sample once per offset group and writes every
-// member detector.
+// Detectors that share (offx, offy) have identical pixels and differ only by
+// the constant angle psi[idet] added after pointingshift (the boresight files
+// are common to all detectors, sanepic.cc:680-692, 757-766), so the kernel
+// works per offset group: one RING pixel and one FP64 angle psi_o per group
+// sample; the per-detector angle is applied later as a rotation.
 #include <cuda_runtime.h>
 
 #include "sg_kernels.h"
@@ -63,17 +64,14 @@ __device__ __forceinline__ int ang2pix_ring_dev(long long nside, double theta, d
   return ipix1 - 1;
 }
 
-__global__ void k_pointing(PointingArgs a, int ngroups, const int* grp_off,
-                           const int* grp_det) {
+__global__ void k_pointing(PointingArgs a) {
   const long long nsd = a.ns * a.nseg;
-  const long long total = nsd * ngroups;
+  const long long total = nsd * a.ngroups;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
     const int g = (int)(e / nsd);
-    const long long w = e % nsd;          // iseg * ns + ii
-    const long long iseg = w / a.ns, ii = w % a.ns;
-    const int lead = grp_det[grp_off[g]];
-    const double x = a.offx[lead], y = a.offy[lead];
+    const long long w = e % nsd;  // iseg * ns + ii
+    const double x = a.offx[g], y = a.offy[g];
     // pointingshift with nn = 1 (sanepic.cc:3419-3471)
     const double thetap = SG_D2PI / 4.0 - a.dec[w];
     const double phip = a.ra[w];
@@ -129,25 +127,16 @@ __global__ void k_pointing(PointingArgs a, int ngroups, const int* grp_off,
       pix = ang2pix_ring_dev(a.nside, theta, phi);
       if (pix < 0 || pix > 12 * (int)a.nside * (int)a.nside - 1) pix = -1;
     }
-    for (int m = grp_off[g]; m < grp_off[g + 1]; m++) {
-      const int d = grp_det[m];
-      const long long pos = (long long)d * nsd + w;
-      a.ring_pix[pos] = pix;
-      const double pd = psi_o + a.psidet[d];
-      double ps = pd;
-      if (a.hwp) ps = -(psi_o + a.psidet[d]) + 2.0 * a.omega * (double)(ii + a.ns * iseg);
-      if (a.psip) a.psip[pos] = ps;
-      if (a.psipfp) a.psipfp[pos] = pd;
-    }
+    a.ring_pix[e] = pix;
+    a.psio[e] = psi_o;
   }
 }
 
-cudaError_t pointing_launch_groups(const PointingArgs& a, int ngroups, const int* grp_off,
-                                   const int* grp_det, cudaStream_t st) {
-  const long long total = a.ns * a.nseg * (long long)ngroups;
+cudaError_t pointing_launch(const PointingArgs& a, cudaStream_t st) {
+  const long long total = a.ns * a.nseg * (long long)a.ngroups;
   long long blocks = (total + 255) / 256;
   if (blocks > 152 * 64) blocks = 152 * 64;
-  k_pointing<<<(unsigned)blocks, 256, 0, st>>>(a, ngroups, grp_off, grp_det);
+  k_pointing<<<(unsigned)blocks, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
 

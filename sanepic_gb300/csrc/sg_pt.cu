@@ -10,8 +10,10 @@
 // MPI_Reduce of the map over ranks (sanepic.cc:1448): for every observed
 // pixel m
 //   q_I[m] = sum y_i,  q_Q[m] = sum cos(2psi_i) y_i,  q_U[m] = sum sin(2psi_i) y_i
-// over the samples i that hit m, read through the pixel-sorted sample index
-// (CSR built once at setup; the pointing never changes).  One warp per
+// over the samples i that hit m.  Detectors that share a pixel stream (an
+// offset group) are first summed per group sample (k_detsum), so P^T walks
+// the group samples, read through the pixel-sorted index (CSR built once at
+// setup; the pointing never changes).  One warp per
 // pixel: the lanes stride through its samples in a fixed order (several
 // independent gathers in flight per lane) and the warp combines lanes with a
 // fixed xor tree, so the result is bitwise identical run to run.  A block
@@ -39,56 +41,90 @@ struct alignas(4 * sizeof(T)) pmap4 {
   T I, Q, U, pad;
 };
 
-__global__ void __launch_bounds__(256) k_project_f32(const int4* __restrict__ pix,
-                                                     const float4* __restrict__ cs,
+// Four group samples per thread: one pixel/angle load and one map gather per
+// sample, then the P value of every detector of the group (coalesced writes).
+__global__ void __launch_bounds__(256) k_project_f32(const int4* __restrict__ gpix,
+                                                     const float4* __restrict__ gcs,
                                                      const pmap4<float>* __restrict__ map,
-                                                     long long n4, float4* __restrict__ t) {
+                                                     long long n4, long long nsd4,
+                                                     const int* __restrict__ grp_off,
+                                                     const int* __restrict__ grp_det,
+                                                     const float2* __restrict__ dcs,
+                                                     float4* __restrict__ t) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
        i += (long long)gridDim.x * blockDim.x) {
-    const int4 p = __ldcs(pix + i);
-    const float4 a = __ldcs(cs + 2 * i), b = __ldcs(cs + 2 * i + 1);
+    const int g = (int)(i / nsd4);
+    const long long w4 = i - (long long)g * nsd4;
+    const int4 p = __ldcs(gpix + i);
+    const float4 ca = __ldcs(gcs + 2 * i), cb = __ldcs(gcs + 2 * i + 1);
     const pmap4<float> m0 = map[p.x], m1 = map[p.y], m2 = map[p.z], m3 = map[p.w];
-    float4 o;
-    o.x = m0.I + a.x * m0.Q + a.y * m0.U;
-    o.y = m1.I + a.z * m1.Q + a.w * m1.U;
-    o.z = m2.I + b.x * m2.Q + b.y * m2.U;
-    o.w = m3.I + b.z * m3.Q + b.w * m3.U;
-    __stcs(t + i, o);
+    // t_det = a + cos2d' b + sin2d' e with a = I, b = c Q + s U, e = c U - s Q
+    const float4 a = make_float4(m0.I, m1.I, m2.I, m3.I);
+    const float4 b = make_float4(ca.x * m0.Q + ca.y * m0.U, ca.z * m1.Q + ca.w * m1.U,
+                                 cb.x * m2.Q + cb.y * m2.U, cb.z * m3.Q + cb.w * m3.U);
+    const float4 e = make_float4(ca.x * m0.U - ca.y * m0.Q, ca.z * m1.U - ca.w * m1.Q,
+                                 cb.x * m2.U - cb.y * m2.Q, cb.z * m3.U - cb.w * m3.Q);
+    for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
+      const int d = grp_det[k];
+      const float2 r = dcs[d];
+      float4 o;
+      o.x = a.x + r.x * b.x + r.y * e.x;
+      o.y = a.y + r.x * b.y + r.y * e.y;
+      o.z = a.z + r.x * b.z + r.y * e.z;
+      o.w = a.w + r.x * b.w + r.y * e.w;
+      __stcs(t + (long long)d * nsd4 + w4, o);
+    }
   }
 }
 
-__global__ void __launch_bounds__(256) k_project_f64(const int* __restrict__ pix,
-                                                     const double2* __restrict__ cs,
+__global__ void __launch_bounds__(256) k_project_f64(const int* __restrict__ gpix,
+                                                     const double2* __restrict__ gcs,
                                                      const pmap4<double>* __restrict__ map,
-                                                     long long n, double* __restrict__ t) {
+                                                     long long n, long long nsd,
+                                                     const int* __restrict__ grp_off,
+                                                     const int* __restrict__ grp_det,
+                                                     const double2* __restrict__ dcs,
+                                                     double* __restrict__ t) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const pmap4<double> m = map[pix[i]];
-    const double2 w = cs[i];
-    t[i] = m.I + (w.x * m.Q + w.y * m.U);
+    const int g = (int)(i / nsd);
+    const long long w = i - (long long)g * nsd;
+    const pmap4<double> m = map[gpix[i]];
+    const double2 c = gcs[i];
+    const double b = c.x * m.Q + c.y * m.U, e = c.x * m.U - c.y * m.Q;
+    for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
+      const int d = grp_det[k];
+      const double2 r = dcs[d];
+      t[(long long)d * nsd + w] = m.I + (r.x * b + r.y * e);
+    }
   }
 }
 
 template <>
-cudaError_t project_launch<float>(const int* pix, const float* cs, const float* map, long long n,
-                                  float* t, cudaStream_t st) {
-  const long long n4 = n / 4;  // n is a multiple of 4 (ns >= 256)
+cudaError_t project_launch<float>(const int* gpix, const float* gcs, const float* map,
+                                  long long n, long long nsd, const int* grp_off,
+                                  const int* grp_det, const float* dcs, float* t,
+                                  cudaStream_t st) {
+  const long long n4 = n / 4;  // nsd is a multiple of 4 (ns >= 256)
   long long blocks = (n4 + 255) / 256;
   if (blocks > 152LL * 16) blocks = 152LL * 16;
   k_project_f32<<<(unsigned)blocks, 256, 0, st>>>(
-      reinterpret_cast<const int4*>(pix), reinterpret_cast<const float4*>(cs),
-      reinterpret_cast<const pmap4<float>*>(map), n4, reinterpret_cast<float4*>(t));
+      reinterpret_cast<const int4*>(gpix), reinterpret_cast<const float4*>(gcs),
+      reinterpret_cast<const pmap4<float>*>(map), n4, nsd / 4, grp_off, grp_det,
+      reinterpret_cast<const float2*>(dcs), reinterpret_cast<float4*>(t));
   return cudaGetLastError();
 }
 
 template <>
-cudaError_t project_launch<double>(const int* pix, const double* cs, const double* map,
-                                   long long n, double* t, cudaStream_t st) {
+cudaError_t project_launch<double>(const int* gpix, const double* gcs, const double* map,
+                                   long long n, long long nsd, const int* grp_off,
+                                   const int* grp_det, const double* dcs, double* t,
+                                   cudaStream_t st) {
   long long blocks = (n + 255) / 256;
   if (blocks > 152LL * 16) blocks = 152LL * 16;
-  k_project_f64<<<(unsigned)blocks, 256, 0, st>>>(pix, reinterpret_cast<const double2*>(cs),
-                                                  reinterpret_cast<const pmap4<double>*>(map), n,
-                                                  t);
+  k_project_f64<<<(unsigned)blocks, 256, 0, st>>>(
+      gpix, reinterpret_cast<const double2*>(gcs), reinterpret_cast<const pmap4<double>*>(map),
+      n, nsd, grp_off, grp_det, reinterpret_cast<const double2*>(dcs), t);
   return cudaGetLastError();
 }
 
@@ -115,6 +151,93 @@ __device__ __forceinline__ ff ff_shfl_xor(ff a, int o) {
   return ff{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
 }
 
+// ---- detector sums ------------------------------------------------------------
+// Per group sample: S0 = sum y_det, A = sum cos2d' y_det, B = sum sin2d' y_det over
+// the group's detectors (Neumaier-compensated FP32, fixed detector order), so
+// that P^T only visits the group's samples: cos 2(phi + d') = c C - s S and
+// sin 2(phi + d') = s C + c S with (C, S) the detector rotation.
+__global__ void __launch_bounds__(256) k_detsum_f32(const float4* __restrict__ y, long long n4,
+                                                    long long nsd4,
+                                                    const int* __restrict__ grp_off,
+                                                    const int* __restrict__ grp_det,
+                                                    const float2* __restrict__ dcs,
+                                                    float4* __restrict__ ys) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(i / nsd4);
+    const long long w4 = i - (long long)g * nsd4;
+    ff s0[4], sa[4], sb[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) s0[k] = sa[k] = sb[k] = ff{0.f, 0.f};
+    for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
+      const int d = grp_det[k];
+      const float2 r = dcs[d];
+      const float4 v = __ldcs(y + (long long)d * nsd4 + w4);
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        ff_add_f(s0[q], vv[q]);
+        ff_add_f(sa[q], r.x * vv[q]);
+        ff_add_f(sb[q], r.y * vv[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      ys[4 * i + q] = make_float4(s0[q].hi + s0[q].lo, sa[q].hi + sa[q].lo, sb[q].hi + sb[q].lo,
+                                  0.f);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_detsum_f64(const double* __restrict__ y, long long n,
+                                                    long long nsd,
+                                                    const int* __restrict__ grp_off,
+                                                    const int* __restrict__ grp_det,
+                                                    const double2* __restrict__ dcs,
+                                                    double* __restrict__ ys) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(i / nsd);
+    const long long w = i - (long long)g * nsd;
+    double s0 = 0.0, sa = 0.0, sb = 0.0;
+    for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
+      const int d = grp_det[k];
+      const double v = y[(long long)d * nsd + w];
+      s0 += v;
+      sa += dcs[d].x * v;
+      sb += dcs[d].y * v;
+    }
+    ys[4 * i] = s0;
+    ys[4 * i + 1] = sa;
+    ys[4 * i + 2] = sb;
+    ys[4 * i + 3] = 0.0;
+  }
+}
+
+template <>
+cudaError_t detsum_launch<float>(const float* y, long long n, long long nsd, const int* grp_off,
+                                 const int* grp_det, const float* dcs, float* ys,
+                                 cudaStream_t st) {
+  const long long n4 = n / 4;
+  long long blocks = (n4 + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  k_detsum_f32<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const float4*>(y), n4, nsd / 4,
+                                                 grp_off, grp_det,
+                                                 reinterpret_cast<const float2*>(dcs),
+                                                 reinterpret_cast<float4*>(ys));
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t detsum_launch<double>(const double* y, long long n, long long nsd,
+                                  const int* grp_off, const int* grp_det, const double* dcs,
+                                  double* ys, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  k_detsum_f64<<<(unsigned)blocks, 256, 0, st>>>(y, n, nsd, grp_off, grp_det,
+                                                 reinterpret_cast<const double2*>(dcs), ys);
+  return cudaGetLastError();
+}
+
 // ---- P^T --------------------------------------------------------------------------
 constexpr int kPtUnroll = 4;
 constexpr int kPtPix = 32;  // pixels per block (4 per warp)
@@ -122,7 +245,7 @@ constexpr int kPtPix = 32;  // pixels per block (4 per warp)
 __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ off,
                                                 const uint32_t* __restrict__ idx,
                                                 const float2* __restrict__ ccs,
-                                                const float* __restrict__ y, long long npix,
+                                                const float4* __restrict__ ys, long long npix,
                                                 const int* __restrict__ hits,
                                                 double* __restrict__ q) {
   __shared__ float sh[kPtPix][6];
@@ -136,28 +259,28 @@ __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ of
       long long j = off[m] + lane;
       for (; j + 32 * (kPtUnroll - 1) < jend; j += 32 * kPtUnroll) {
         uint32_t ii[kPtUnroll];
-        float v[kPtUnroll];
+        float4 v[kPtUnroll];
         float2 wv[kPtUnroll];
 #pragma unroll
         for (int u = 0; u < kPtUnroll; u++) ii[u] = __ldcs(idx + j + 32 * u);
 #pragma unroll
         for (int u = 0; u < kPtUnroll; u++) {
-          v[u] = __ldg(y + ii[u]);
+          v[u] = __ldg(ys + ii[u]);
           wv[u] = __ldcs(ccs + j + 32 * u);
         }
 #pragma unroll
         for (int u = 0; u < kPtUnroll; u++) {
-          ff_add_f(a0, v[u]);
-          ff_add_f(a1, wv[u].x * v[u]);
-          ff_add_f(a2, wv[u].y * v[u]);
+          ff_add_f(a0, v[u].x);
+          ff_add_f(a1, wv[u].x * v[u].y - wv[u].y * v[u].z);
+          ff_add_f(a2, wv[u].y * v[u].y + wv[u].x * v[u].z);
         }
       }
       for (; j < jend; j += 32) {
-        const float v = __ldg(y + __ldcs(idx + j));
+        const float4 v = __ldg(ys + __ldcs(idx + j));
         const float2 wv = __ldcs(ccs + j);
-        ff_add_f(a0, v);
-        ff_add_f(a1, wv.x * v);
-        ff_add_f(a2, wv.y * v);
+        ff_add_f(a0, v.x);
+        ff_add_f(a1, wv.x * v.y - wv.y * v.z);
+        ff_add_f(a2, wv.y * v.y + wv.x * v.z);
       }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -189,7 +312,7 @@ __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ of
 }
 
 __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint32_t* idx,
-                                                const double2* ccs, const double* y,
+                                                const double2* ccs, const double* ys,
                                                 long long npix, const int* hits, double* q) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -198,11 +321,11 @@ __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     const long long j1 = off[m + 1];
     for (long long j = off[m] + lane; j < j1; j += 32) {
-      const double v = __ldg(y + idx[j]);
+      const double* v = ys + 4 * (long long)idx[j];
       const double2 w = ccs[j];
-      a0 += v;
-      a1 += w.x * v;
-      a2 += w.y * v;
+      a0 += v[0];
+      a1 += w.x * v[1] - w.y * v[2];
+      a2 += w.y * v[1] + w.x * v[2];
     }
     for (int o = 16; o > 0; o >>= 1) {
       a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -220,23 +343,24 @@ __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint
 
 template <>
 cudaError_t pt_launch<float>(const long long* csr_off, const uint32_t* csr_idx,
-                             const float* csr_cs, const float* y, long long npix,
+                             const float* csr_cs, const float* ys, long long npix,
                              const int* hits_true, double* q, cudaStream_t st) {
   const long long blocks = (npix + kPtPix - 1) / kPtPix;
   k_pt_f32<<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,
-                                             reinterpret_cast<const float2*>(csr_cs), y, npix,
+                                             reinterpret_cast<const float2*>(csr_cs),
+                                             reinterpret_cast<const float4*>(ys), npix,
                                              hits_true, q);
   return cudaGetLastError();
 }
 
 template <>
 cudaError_t pt_launch<double>(const long long* csr_off, const uint32_t* csr_idx,
-                              const double* csr_cs, const double* y, long long npix,
+                              const double* csr_cs, const double* ys, long long npix,
                               const int* hits_true, double* q, cudaStream_t st) {
   long long blocks = (npix * 32 + 255) / 256;
   if (blocks > 152LL * 8 * 16) blocks = 152LL * 8 * 16;
   k_pt_f64<<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,
-                                             reinterpret_cast<const double2*>(csr_cs), y, npix,
+                                             reinterpret_cast<const double2*>(csr_cs), ys, npix,
                                              hits_true, q);
   return cudaGetLastError();
 }

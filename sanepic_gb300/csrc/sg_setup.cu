@@ -19,16 +19,20 @@ static unsigned grid_for(long long n, int threads, long long cap = 152LL * 32) {
   return (unsigned)b;
 }
 
-__global__ void k_hist(const int* ring_pix, long long n, int* count) {
+// detector samples per RING pixel: each group sample counts once per member
+// detector (integer atomics: the result does not depend on their order)
+__global__ void k_hist(const int* ring_pix, long long n, long long nsd, const int* gsize,
+                       int* count) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const int p = ring_pix[i];
-    if (p >= 0) atomicAdd(count + p, 1);
+    if (p >= 0) atomicAdd(count + p, gsize[i / nsd]);
   }
 }
 
-cudaError_t hist_launch(const int* ring_pix, long long n, int* count, cudaStream_t st) {
-  k_hist<<<grid_for(n, 256), 256, 0, st>>>(ring_pix, n, count);
+cudaError_t hist_launch(const int* ring_pix, long long n, long long nsd, const int* gsize,
+                        int* count, cudaStream_t st) {
+  k_hist<<<grid_for(n, 256), 256, 0, st>>>(ring_pix, n, nsd, gsize, count);
   return cudaGetLastError();
 }
 
@@ -79,22 +83,26 @@ static int bits_for(long long v) {
 }
 
 size_t csr_tmp_bytes(long long n, long long npix) {
-  size_t sort_bytes = 0, scan_bytes = 0;
+  (void)npix;
+  size_t sort_bytes = 0;
   cub::DoubleBuffer<unsigned long long> db(nullptr, nullptr);
   cub::DeviceRadixSort::SortKeys(nullptr, sort_bytes, db, n, 0, 64);
-  cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (long long*)nullptr, (long long*)nullptr,
-                                npix + 1);
-  size_t cub_bytes = sort_bytes > scan_bytes ? sort_bytes : scan_bytes;
-  return 2 * sizeof(unsigned long long) * (size_t)n + cub_bytes + 1024;
+  return 2 * sizeof(unsigned long long) * (size_t)n + sort_bytes + 1024;
 }
 
-__global__ void k_counts_ll(const int* hits, long long npix, long long* off) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i <= npix;
-       i += (long long)gridDim.x * blockDim.x)
-    off[i] = i < npix ? (long long)hits[i] : 0;
+// row starts of the CSR: the first sorted key of every pixel (every observed
+// pixel has at least one sample, so every entry is written)
+__global__ void k_offsets(const unsigned long long* keys, long long n, long long npix,
+                          long long* off) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    const long long p = (long long)(keys[j] >> 32);
+    if (j == 0 || (long long)(keys[j - 1] >> 32) != p) off[p] = j;
+    if (j == n - 1) off[npix] = n;
+  }
 }
 
-cudaError_t csr_build(const int* pix, long long n, long long npix, const int* hits,
+cudaError_t csr_build(const int* pix, long long n, long long npix,
                       long long* csr_off, uint32_t* csr_idx, void* tmp, size_t tmp_bytes,
                       cudaStream_t st) {
   char* base = reinterpret_cast<char*>(tmp);
@@ -108,11 +116,7 @@ cudaError_t csr_build(const int* pix, long long n, long long npix, const int* hi
   cudaError_t e = cub::DeviceRadixSort::SortKeys(cub_tmp, cub_bytes, db, n, 0, nbits, st);
   if (e != cudaSuccess) return e;
   k_keys_to_idx<<<grid_for(n, 256), 256, 0, st>>>(db.Current(), n, csr_idx);
-  // offsets: exclusive scan of the per-pixel counts
-  long long* cnt = reinterpret_cast<long long*>(db.Alternate());  // reuse as scratch
-  k_counts_ll<<<grid_for(npix + 1, 256), 256, 0, st>>>(hits, npix, cnt);
-  e = cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, cnt, csr_off, npix + 1, st);
-  if (e != cudaSuccess) return e;
+  k_offsets<<<grid_for(n, 256), 256, 0, st>>>(db.Current(), n, npix, csr_off);
   return cudaGetLastError();
 }
 
@@ -137,14 +141,19 @@ template cudaError_t gather_cs_launch<float>(const float*, const uint32_t*, long
 template cudaError_t gather_cs_launch<double>(const double*, const uint32_t*, long long,
                                               double*, cudaStream_t);
 
-// cos/sin(2 psip) as the reference evaluates them (sanepic.cc:2601-2605, FP64),
-// rounded to T.  For FP32 storage the FP64 angle is first reduced modulo 2pi
-// (exact fmod) so that HWP angles of ~1e6 rad stay on the fast path.
+// cos/sin of twice the group's base angle phi per group sample, rounded to T:
+// phi = psi_o, or with a half-wave plate phi = -psi_o + 2 omega (ii + ns iseg)
+// (sanepic.cc:757-766); the detector's own angle is applied as a rotation.
+// For FP32 storage the FP64 angle is first reduced modulo 2pi (exact fmod)
+// so that HWP angles of ~1e6 rad stay on the fast path.
 template <typename T>
-__global__ void k_angles(const double* psip, long long n, T* cs) {
+__global__ void k_base_angles(const double* psio, long long n, long long ns, long long nsd,
+                              int hwp, double omega, T* cs) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    double a = 2.0 * (psip[i] + 0.0);
+    double phi = psio[i];
+    if (hwp) phi = -phi + 2.0 * omega * (double)(i % nsd);  // i % nsd = ii + ns * iseg
+    double a = 2.0 * phi;
     if (sizeof(T) == 4) a = fmod(a, 6.2831853071795864769252867665590057683943387987502);
     double s, c;
     sincos(a, &s, &c);
@@ -154,26 +163,37 @@ __global__ void k_angles(const double* psip, long long n, T* cs) {
 }
 
 template <typename T>
-cudaError_t angles_launch(const double* psip, long long n, T* cs, cudaStream_t st) {
-  k_angles<T><<<grid_for(n, 256), 256, 0, st>>>(psip, n, cs);
+cudaError_t base_angles_launch(const double* psio, long long n, long long ns, long long nsd,
+                               int hwp, double omega, T* cs, cudaStream_t st) {
+  (void)ns;
+  k_base_angles<T><<<grid_for(n, 256), 256, 0, st>>>(psio, n, ns, nsd, hwp, omega, cs);
   return cudaGetLastError();
 }
-template cudaError_t angles_launch<float>(const double*, long long, float*, cudaStream_t);
-template cudaError_t angles_launch<double>(const double*, long long, double*, cudaStream_t);
+template cudaError_t base_angles_launch<float>(const double*, long long, long long, long long,
+                                               int, double, float*, cudaStream_t);
+template cudaError_t base_angles_launch<double>(const double*, long long, long long, long long,
+                                                int, double, double*, cudaStream_t);
 
 // ---- per-pixel reductions over the CSR (one warp per pixel) -----------------
-__global__ void k_sumcross(const long long* off, const uint32_t* idx, const double* psipfp,
-                           long long npix, double* out) {
+// COS2P/SIN2P (sanepic.cc:2594-2597): per pixel, the sum over detector
+// samples of cos/sin(2 (psi_o + psi_det)).  Per group sample that is
+// cos 2psi_o SC - sin 2psi_o SS (and sin 2psi_o SC + cos 2psi_o SS) with
+// SC, SS the group's sums of cos/sin(2 psi_det).  FP64, warp per pixel.
+__global__ void k_sumcross(const long long* off, const uint32_t* idx, const double* psio,
+                           long long nsd, const double* gsc, const double* gss, long long npix,
+                           double* out) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long m = warp; m < npix; m += nwarps) {
     double c = 0.0, s = 0.0;
     for (long long j = off[m] + lane; j < off[m + 1]; j += 32) {
+      const long long gs = idx[j];
+      const int g = (int)(gs / nsd);
       double sn, cs;
-      sincos(2.0 * (psipfp[idx[j]] + 0.0), &sn, &cs);
-      c += cs;
-      s += sn;
+      sincos(2.0 * (psio[gs] + 0.0), &sn, &cs);
+      c += cs * gsc[g] - sn * gss[g];
+      s += sn * gsc[g] + cs * gss[g];
     }
     for (int o = 16; o > 0; o >>= 1) {
       c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -187,32 +207,41 @@ __global__ void k_sumcross(const long long* off, const uint32_t* idx, const doub
   }
 }
 
-cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx,
-                            const double* psipfp, long long npix, double* sumcross,
-                            cudaStream_t st) {
-  k_sumcross<<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(csr_off, csr_idx, psipfp,
-                                                                   npix, sumcross);
+cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, const double* psio,
+                            long long nsd, const double* gsc, const double* gss, long long npix,
+                            double* sumcross, cudaStream_t st) {
+  k_sumcross<<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(csr_off, csr_idx, psio, nsd,
+                                                                   gsc, gss, npix, sumcross);
   return cudaGetLastError();
 }
 
-// 3x3 block-Jacobi: A_p = sum g0[det] w w^T, w = (1, c, s); inverse in FP64.
+// 3x3 block-Jacobi: A_p = sum over detector samples of g0_det w w^T,
+// w = (1, cos 2a, sin 2a), a = phi + delta_det.  Summed over a group's
+// detectors in closed form from five group constants
+//   gc = (sum g0, sum g0 cos 2d, sum g0 sin 2d, sum g0 cos 4d, sum g0 sin 4d)
+// with cos^2 = (1 + cos 4a)/2, cos sin = sin 4a / 2.  Inverse in FP64.
 template <typename T>
 __global__ void k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix,
-                      long long tile_len, const double* g0, const int* hits, double* minv) {
+                      long long nsd, int ngroups, const double* gc, const int* hits,
+                      double* minv) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long m = warp; m < npix; m += nwarps) {
     double a[6] = {0, 0, 0, 0, 0, 0};
     for (long long j = off[m] + lane; j < off[m + 1]; j += 32) {
-      const double g = g0[idx[j] / tile_len];
-      const double c = (double)ccs[2 * j], s = (double)ccs[2 * j + 1];
-      a[0] += g;
-      a[1] += g * c;
-      a[2] += g * s;
-      a[3] += g * c * c;
-      a[4] += g * c * s;
-      a[5] += g * s * s;
+      const int g = (int)(idx[j] / nsd);
+      const double G0 = gc[g], G2c = gc[ngroups + g], G2s = gc[2 * ngroups + g];
+      const double G4c = gc[3 * ngroups + g], G4s = gc[4 * ngroups + g];
+      const double c2 = (double)ccs[2 * j], s2 = (double)ccs[2 * j + 1];
+      const double c4 = c2 * c2 - s2 * s2, s4 = 2.0 * c2 * s2;
+      const double C4 = c4 * G4c - s4 * G4s, S4 = s4 * G4c + c4 * G4s;
+      a[0] += G0;
+      a[1] += c2 * G2c - s2 * G2s;
+      a[2] += s2 * G2c + c2 * G2s;
+      a[3] += 0.5 * (G0 + C4);
+      a[4] += 0.5 * S4;
+      a[5] += 0.5 * (G0 - C4);
     }
     for (int o = 16; o > 0; o >>= 1)
       for (int k = 0; k < 6; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
@@ -250,19 +279,45 @@ __global__ void k_bj3(const long long* off, const uint32_t* idx, const T* ccs, l
 
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
-                       long long npix, long long tile_len, int nseg, const double* g0,
+                       long long npix, long long nsd, int ngroups, const double* gconst,
                        const int* hits_true, double* minv, cudaStream_t st) {
-  (void)nseg;
   k_bj3<T><<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(
-      csr_off, csr_idx, csr_cs, npix, tile_len, g0, hits_true, minv);
+      csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv);
   return cudaGetLastError();
 }
-template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*,
-                                       long long, long long, int, const double*, const int*,
-                                       double*, cudaStream_t);
+template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*, long long,
+                                       long long, int, const double*, const int*, double*,
+                                       cudaStream_t);
 template cudaError_t bj3_launch<double>(const long long*, const uint32_t*, const double*,
                                         long long, long long, int, const double*, const int*,
                                         double*, cudaStream_t);
+
+// N_ of every detector summed over its group: the pixel stream is common to
+// the group, so the reference's per-detector pair sums add up per group.
+template <typename T>
+__global__ void k_group_ntab(const T* ntab, long long ns, int ngroups, const int* grp_off,
+                             const int* grp_det, T* out) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ns * ngroups;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(e / ns);
+    const long long t = e % ns;
+    double acc = 0.0;
+    for (int m = grp_off[g]; m < grp_off[g + 1]; m++) acc += (double)ntab[grp_det[m] * ns + t];
+    out[e] = (T)acc;
+  }
+}
+
+template <typename T>
+cudaError_t group_ntab_launch(const T* ntab, long long ns, int ngroups, const int* grp_off,
+                              const int* grp_det, T* out, cudaStream_t st) {
+  k_group_ntab<T><<<grid_for(ns * ngroups, 256), 256, 0, st>>>(ntab, ns, ngroups, grp_off,
+                                                              grp_det, out);
+  return cudaGetLastError();
+}
+template cudaError_t group_ntab_launch<float>(const float*, long long, int, const int*,
+                                              const int*, float*, cudaStream_t);
+template cudaError_t group_ntab_launch<double>(const double*, long long, int, const int*,
+                                               const int*, double*, cudaStream_t);
 
 // Reference diagonal: for every tile and pixel, sum over sample pairs (i, j)
 // of that pixel in the tile with |i - j| < ns/2 of N_[|i - j|], N_ = c2r|SpN|
