@@ -81,6 +81,13 @@ typedef struct sg_solve_opts {
   int verbose;       /* print the reference's "iter = ..., crit = ..." lines */
   const double *x0;  /* -I start map, compact [3*npix], or NULL for zeros */
   int use_graph;     /* replay each iteration from a captured CUDA graph */
+  /* Called after every iteration with the values the reference prints
+   * (sanepic.cc:1607-1609; chi2 is refreshed every refresh_every iterations,
+   * sanepic.cc:1483-1546), or NULL.  A nonzero return ends the solve.  Inside
+   * the call, sg_get_solution and sg_get_map(I, Q, U) read the current map
+   * (the reference's per-iteration map writes, sanepic.cc:1709-1745). */
+  int (*on_iteration)(void *user, int iter, double crit, double crit2, double chi2);
+  void *user;
 } sg_solve_opts;
 
 typedef struct sg_report {

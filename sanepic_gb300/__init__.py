@@ -55,11 +55,16 @@ class SgDet(ctypes.Structure):
     _fields_ = [("offx", ctypes.c_double), ("offy", ctypes.c_double), ("psi", ctypes.c_double)]
 
 
+ITER_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                           ctypes.c_double, ctypes.c_double)
+
+
 class SgSolveOpts(ctypes.Structure):
     _fields_ = [("precond", ctypes.c_int), ("stop_crit", ctypes.c_double),
                 ("maxiter", ctypes.c_int), ("refresh_every", ctypes.c_int),
                 ("verbose", ctypes.c_int), ("x0", ctypes.POINTER(ctypes.c_double)),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("on_iteration", ITER_CB),
+                ("user", ctypes.c_void_p)]
 
 
 class SgReport(ctypes.Structure):
@@ -198,16 +203,29 @@ class MapMaker:
 
     def solve(self, precond: str = "bj3", stop_crit: float = 1e-15, maxiter: int = 2000,
               refresh_every: int = 10, verbose: bool = False, x0=None,
-              use_graph: bool = True) -> dict:
+              use_graph: bool = True, on_iteration=None) -> dict:
+        """Run PCG.  The report dict also holds `history`: one
+        (iter, crit, crit2, chi2) row per iteration (the reference's printed
+        line).  on_iteration(iter, crit, crit2, chi2) -> bool (True stops)
+        runs after each iteration."""
         x0p = None
         if x0 is not None:
             self._x0 = _f64(x0)
             x0p = _dp(self._x0)
+        hist = []
+
+        def _cb(_user, it, crit, crit2, chi2):
+            hist.append((it, crit, crit2, chi2))
+            return int(bool(on_iteration(it, crit, crit2, chi2))) if on_iteration else 0
+
+        cb = ITER_CB(_cb)
         o = SgSolveOpts(PRECOND[precond], stop_crit, maxiter, refresh_every, int(verbose),
-                        x0p, int(use_graph))
+                        x0p, int(use_graph), cb, None)
         rep = SgReport()
         self._check(self.L.sg_solve(self.h, ctypes.byref(o), ctypes.byref(rep)))
-        return {k: getattr(rep, k) for k, _ in SgReport._fields_}
+        out = {k: getattr(rep, k) for k, _ in SgReport._fields_}
+        out["history"] = np.array(hist, dtype=np.float64).reshape(-1, 4)
+        return out
 
     # ---- outputs ------------------------------------------------------------
     def get_map(self, kind: str) -> np.ndarray:

@@ -86,6 +86,7 @@ struct sg_ctx {
   DevBuf grp_off, grp_det, dcs, ys, gconst;
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
+  DevBuf chi2p;  // per-CTA chi^2 partials of the noise filter
   cplx<float> wn1f{1.f, 0.f};
   cplx<double> wn1d{1.0, 0.0};
   CgScalars* sc_host = nullptr;  // pinned
@@ -132,13 +133,15 @@ struct sg_ctx {
   // ---- operator pieces ---------------------------------------------------
   template <typename T>
   FilterArgs<T> filter_args(int mode, const T* in, T* out, long long ntiles_, int nseg_,
-                            int filt_abs) {
+                            int filt_abs, const T* sub, double* chi2_part) {
     FilterArgs<T> a{};
     a.ntiles = ntiles_;
     a.nseg = nseg_;
     a.mode = mode;
     a.filt_abs = filt_abs;
     a.tod = in;
+    a.sub = sub;
+    a.chi2_part = chi2_part;
     a.filt = filt.as<T>();
     a.out = out;
     a.tw_lo = tw_lo.as<cplx<T>>();
@@ -146,18 +149,29 @@ struct sg_ctx {
     return a;
   }
 
+  // chi2_out (device double) receives 2 sum h |X|^2 over all tiles when set
   cudaError_t launch_filter(int mode, const void* in, void* out, long long ntiles_, int nseg_,
-                            int filt_abs) {
+                            int filt_abs, const void* sub = nullptr, double* chi2_out = nullptr) {
     const int ncl = (int)std::min<long long>(nclusters, ntiles_);
+    double* part = chi2_out ? chi2p.as<double>() : nullptr;
+    cudaError_t e;
     launches++;
     if (f32) {
-      auto a = filter_args<float>(mode, (const float*)in, (float*)out, ntiles_, nseg_, filt_abs);
+      auto a = filter_args<float>(mode, (const float*)in, (float*)out, ntiles_, nseg_, filt_abs,
+                                  (const float*)sub, part);
       a.wn1 = wn1f;
-      return filter_launch<float>(a, logm, S, ncl, st);
+      e = filter_launch<float>(a, logm, S, ncl, st);
+    } else {
+      auto a = filter_args<double>(mode, (const double*)in, (double*)out, ntiles_, nseg_,
+                                   filt_abs, (const double*)sub, part);
+      a.wn1 = wn1d;
+      e = filter_launch<double>(a, logm, S, ncl, st);
     }
-    auto a = filter_args<double>(mode, (const double*)in, (double*)out, ntiles_, nseg_, filt_abs);
-    a.wn1 = wn1d;
-    return filter_launch<double>(a, logm, S, ncl, st);
+    if (e == cudaSuccess && chi2_out) {
+      launches++;
+      e = chi2_sum(part, S * ncl, chi2_out, st);
+    }
+    return e;
   }
 
   // per group sample detector sums of y, then the CSR reduction into a map
@@ -246,8 +260,15 @@ struct sg_ctx {
     if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 0, st);
     launches += 3;  // step a, b, c
     if (refresh) {
-      if (e == cudaSuccess) e = apply_dev(x.as<double>(), q.as<double>(), true);
-      if (e == cudaSuccess) e = cg_refresh_r(v, 0, st);
+      // true residual r = P^T N^-1 (d - P x) in one operator pass; the filter
+      // also yields chi^2 of the residual timeline (sanepic.cc:1483-1572)
+      if (e == cudaSuccess) e = to_map(x.as<double>());
+      if (e == cudaSuccess) e = launch_project();
+      if (e == cudaSuccess)
+        e = launch_filter(kLoadTodMinus, tod.p, y.p, ntiles, (int)nseg, 0, y.p,
+                          &sc.as<CgScalars>()->chi2);
+      if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
+      if (e == cudaSuccess) e = cg_refresh_r(v, 0, 1, st);
       launches++;
     }
     if (e == cudaSuccess)
@@ -358,7 +379,8 @@ extern "C" int sg_create(sg_ctx** out, const sg_desc* desc) {
   if ((e = c->filt.alloc((size_t)c->ndet * (M + 1) * c->esize)) != cudaSuccess ||
       (e = c->g0.alloc(sizeof(double) * c->ndet)) != cudaSuccess ||
       (e = c->y.alloc((size_t)nsamp * c->esize)) != cudaSuccess ||
-      (e = c->tod.alloc((size_t)nsamp * c->esize)) != cudaSuccess)
+      (e = c->tod.alloc((size_t)nsamp * c->esize)) != cudaSuccess ||
+      (e = c->chi2p.alloc(sizeof(double) * c->S * c->nclusters)) != cudaSuccess)
     return bad(SG_ERR_CUDA, cudaGetErrorString(e));
   if ((e = cudaMallocHost(&c->sc_host, sizeof(CgScalars))) != cudaSuccess)
     return bad(SG_ERR_CUDA, cudaGetErrorString(e));
@@ -719,11 +741,15 @@ extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
   int rc = check_ready(c, true);
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
-  cudaError_t e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+  double* dchi2 = &c->sc.as<CgScalars>()->chi2;
+  cudaError_t e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0,
+                                   nullptr, dchi2);
   if (e == cudaSuccess) e = c->pt_of_y(c->b.as<double>(), true);
+  double h = 0.0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dchi2, sizeof(double), cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "rhs");
-  if (chi2) *chi2 = NAN;  // not computed on this path yet
+  if (chi2) *chi2 = h;  // chi2_0 (sanepic.cc:1089-1110)
   c->have_rhs = true;
   return SG_OK;
 }
@@ -903,6 +929,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
   const int maxiter = o->maxiter > 0 ? o->maxiter : 2000;
   c->crit_hist.clear();
+  c->have_solution = true;  // the callback may read the current map
   int iter = 0;
   while ((iter < maxiter && crit > o->stop_crit) || iter == 0) {
     const bool refresh = (iter % refresh_every) == 0;
@@ -913,10 +940,13 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     if (e != cudaSuccess) return c->cuda_fail(e, "solve iteration");
     crit = c->sc_host->var / var00;
     c->crit_hist.push_back(crit);
+    const double crit2 = c->sc_host->delta / delta0, chi2 = c->sc_host->chi2;
     if (o->verbose)
-      printf("iter = %d, crit = %10.15g, crit2 = %10.15g\n", iter, crit,
-             c->sc_host->delta / delta0);
+      printf("iter = %d, crit = %10.15g, crit2 = %10.15g, chi2 = %10.15g\n", iter, crit, crit2,
+             chi2);
+    const int stop = o->on_iteration ? o->on_iteration(o->user, iter, crit, crit2, chi2) : 0;
     iter++;
+    if (stop) break;
     // d^T A d <= 0 or r^T z <= 0: the recurrence has hit rounding level (or a
     // non-SPD preconditioner); stop with the current map
     if (c->sc_host->flag) break;

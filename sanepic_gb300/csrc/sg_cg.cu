@@ -207,8 +207,9 @@ cudaError_t cg_step_b(const CgVecs& v, int refresh, int flexible, cudaStream_t s
   return cudaGetLastError();
 }
 
-// refresh: r = b - q (q = masked A x), z = M r, partial dots
-__global__ void __launch_bounds__(kCgThreads) k_refresh_r(CgVecs v, int flexible) {
+// refresh: r = b - q (q = masked A x), or r = q (q = masked P^T N^-1 (d - P x)),
+// z = M r, partial dots
+__global__ void __launch_bounds__(kCgThreads) k_refresh_r(CgVecs v, int flexible, int direct) {
   const long long n = v.npix;
   double acc[3] = {0.0, 0.0, 0.0};
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
@@ -218,7 +219,7 @@ __global__ void __launch_bounds__(kCgThreads) k_refresh_r(CgVecs v, int flexible
     for (int c = 0; c < 3; c++) {
       const long long i = c * n + m;
       if (flexible) v.rprev[i] = v.r[i];
-      r[c] = v.b[i] - v.q[i];
+      r[c] = direct ? v.q[i] : v.b[i] - v.q[i];
       v.r[i] = r[c];
     }
     if (v.precond != 2) {
@@ -237,8 +238,29 @@ __global__ void __launch_bounds__(kCgThreads) k_refresh_r(CgVecs v, int flexible
   block_reduce_store<3>(acc, v.part + kCgBlocks, kCgBlocks);
 }
 
-cudaError_t cg_refresh_r(const CgVecs& v, int flexible, cudaStream_t st) {
-  k_refresh_r<<<kCgBlocks, kCgThreads, 0, st>>>(v, flexible);
+cudaError_t cg_refresh_r(const CgVecs& v, int flexible, int direct, cudaStream_t st) {
+  k_refresh_r<<<kCgBlocks, kCgThreads, 0, st>>>(v, flexible, direct);
+  return cudaGetLastError();
+}
+
+// chi^2 (sanepic.cc:1089-1110, 1542-1546): the filter leaves one partial per
+// CTA; one block adds them in a fixed order.
+__global__ void __launch_bounds__(kCgThreads) k_chi2_sum(const double* part, int n, double* out) {
+  __shared__ double sh[kCgThreads / 32];
+  double x = 0.0;
+  for (int i = threadIdx.x; i < n; i += kCgThreads) x += part[i];
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kCgThreads / 32; w++) s += sh[w];
+    *out = 2.0 * s;
+  }
+}
+
+cudaError_t chi2_sum(const double* part, int n, double* out, cudaStream_t st) {
+  k_chi2_sum<<<1, kCgThreads, 0, st>>>(part, n, out);
   return cudaGetLastError();
 }
 

@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
 
   const int cluster_id = blockIdx.x / S;
   const int nclusters = gridDim.x / S;
+  double chi2 = 0.0;  // sum of h[k] |X[k]|^2 over this thread's bins
   for (long long tile = cluster_id; tile < p.ntiles; tile += nclusters) {
     const long long base = tile * (long long)(2 * M);
     const int det = (int)(tile / p.nseg);
@@ -128,6 +129,9 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       cplx<T> v;
       if (p.mode == kLoadTod) {
         v = *reinterpret_cast<const cplx<T>*>(p.tod + s0);
+      } else if (p.mode == kLoadTodMinus) {
+        v = *reinterpret_cast<const cplx<T>*>(p.tod + s0) -
+            *reinterpret_cast<const cplx<T>*>(p.sub + s0);
       } else if (p.mode == kLoadProj) {
         const int2 pp = *reinterpret_cast<const int2*>(p.pix + s0);
         const cplx<T> cs0 = *reinterpret_cast<const cplx<T>*>(p.cs + 2 * s0);
@@ -217,6 +221,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
     // ---- 5. real-spectrum split, multiply by h, re-pack for c2r -----------
     {
       const T* h = p.filt + (long long)det * (M + 1);
+      T c2 = T(0);
       for (int e = tid; e < E; e += NT) {
         const int t = e % Rs, pos = e / Rs;
         const int k2 = pos / C2 + C1 * (pos % C2);
@@ -229,7 +234,9 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
             h0 = h0 < T(0) ? -h0 : h0;
             hM = hM < T(0) ? -hM : hM;
           }
-          const T y0 = h0 * (z.x + z.y), yM = hM * (z.x - z.y);
+          const T x0 = z.x + z.y, xM = z.x - z.y;
+          c2 += h0 * x0 * x0 + hM * xM * xM;
+          const T y0 = h0 * x0, yM = hM * xM;
           buf[pos * PC + t] = cplx<T>{y0 + yM, y0 - yM};
           continue;
         }
@@ -258,6 +265,8 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         const cplx<T> wO = cmul(wk, Ov);
         const cplx<T> Xk = Ev + wO;
         const cplx<T> Xm = cconj(Ev - wO);
+        // bin M/2 pairs with itself: count it once
+        c2 += hk * (Xk.x * Xk.x + Xk.y * Xk.y) + (k == kp ? T(0) : hm * (Xm.x * Xm.x + Xm.y * Xm.y));
         const cplx<T> Yk = cscale(Xk, hk), Ym = cscale(Xm, hm);
         const cplx<T> P = Yk + cconj(Ym), Q = Yk - cconj(Ym);
         const cplx<T> cwQ = cmulc(Q, wk);
@@ -265,6 +274,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         buf[pos * PC + t] = P + iwQ;
         buf[posp * PC + tp] = cconj(P - iwQ);
       }
+      chi2 += (double)c2;
     }
     __syncthreads();
     // ---- 6. inverse row FFTs and the W_M^-1 twiddle ------------------------
@@ -350,6 +360,17 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       *reinterpret_cast<cplx<T>*>(p.out + s0) = buf[n1 * PA + c];
     }
     __syncthreads();
+  }
+  if (p.chi2_part) {
+    __shared__ double red[kFilterWarps];
+    for (int o = 16; o > 0; o >>= 1) chi2 += __shfl_xor_sync(0xffffffffu, chi2, o);
+    if ((tid & 31) == 0) red[tid >> 5] = chi2;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < kFilterWarps; w++) s += red[w];
+      p.chi2_part[blockIdx.x] = s;
+    }
   }
   // peers may still read this CTA's shared memory: keep it alive
   cluster_arrive();

@@ -11,15 +11,17 @@
 namespace sg {
 
 // ---- noise filter (sg_filter.cu) --------------------------------------------
-enum { kLoadTod = 0, kLoadProj = 1, kLoadDelta = 2 };
+enum { kLoadTod = 0, kLoadProj = 1, kLoadDelta = 2, kLoadTodMinus = 3 };
 
 template <typename T>
 struct FilterArgs {
   long long ntiles;  // (det, seg) tiles, each ns = 2M samples, tile-major
   int nseg;          // det = tile / nseg selects the filter row
-  int mode;          // kLoadTod / kLoadProj / kLoadDelta
+  int mode;          // kLoadTod / kLoadProj / kLoadDelta / kLoadTodMinus
   int filt_abs;      // multiply by |h| instead of h
-  const T* tod;      // kLoadTod: [ntiles][ns]
+  const T* tod;      // kLoadTod, kLoadTodMinus: [ntiles][ns]
+  const T* sub;      // kLoadTodMinus: the input is tod - sub
+  double* chi2_part; // if set: per-CTA sums of h[k] |X[k]|^2, k = 0..ns/2 [gridDim]
   const int* pix;    // kLoadProj: compact pixel per sample
   const T* cs;       // kLoadProj: (cos 2psi, sin 2psi) per sample
   const T* map;      // kLoadProj: [npix][4] = (I, Q, U, 0)
@@ -126,6 +128,7 @@ struct CgScalars {
   double var;        // r^T r
   double var00;      // b^T b
   double alpha, beta, rtq;
+  double chi2;       // 2 sum h |F(d - P x)|^2 at the last refresh
   int flag;          // bit 0: d^T A d <= 0, bit 1: r^T z <= 0
   int pad;
 };
@@ -153,7 +156,10 @@ template <typename T>
 cudaError_t cg_init(const CgVecs& v, cudaStream_t st);
 cudaError_t cg_step_a(const CgVecs& v, cudaStream_t st);  // partial q.d
 cudaError_t cg_step_b(const CgVecs& v, int refresh, int flexible, cudaStream_t st);
-cudaError_t cg_refresh_r(const CgVecs& v, int flexible, cudaStream_t st);  // r = b - q
+// refresh: r = b - q, or r = q when q already holds the residual (direct)
+cudaError_t cg_refresh_r(const CgVecs& v, int flexible, int direct, cudaStream_t st);
+// out = 2 * sum of n per-CTA chi^2 partials (fixed order)
+cudaError_t chi2_sum(const double* part, int n, double* out, cudaStream_t st);
 cudaError_t cg_dots(const CgVecs& v, int flexible, cudaStream_t st);
 template <typename T>
 cudaError_t cg_step_c(const CgVecs& v, T* dmap, int flexible, cudaStream_t st);
