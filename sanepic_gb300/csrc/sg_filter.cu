@@ -1,11 +1,13 @@
 // sg_filter.cu -- per-(detector, segment) noise weighting N^-1 as one fused
-// GB300 kernel: load (TOD, or the projection P of a map) -> real FFT ->
-// multiply by the inverse-noise spectrum -> inverse real FFT -> store.
+// GB300 kernel: load (TOD, TOD minus a projection, or the projection P of a
+// map) -> real FFT -> multiply by the inverse-noise spectrum -> inverse real
+// FFT -> store, optionally accumulating chi^2 of the input.
 //
 // Replaces the reference's write_tfAS + the first half of do_PtNd
 // (sanepic.cc:2390-2445, 2522-2582): per tile of ns samples it computes
 //   y = c2r( h . r2c(x) ),   h[k] = SpN_all[k] (k <= ns/2, sanepic.cc:533-537)
-// with FFTW's unnormalised conventions (r2c sign -1, c2r sign +1).
+// with FFTW's unnormalised conventions (r2c sign -1, c2r sign +1), and the
+// chi^2 terms sum_k h[k] |r2c(x)[k]|^2 of sanepic.cc:1089-1110, 1528-1546.
 //
 // Algorithm.  The real tile x (N = ns samples) is packed as M = N/2 complex
 // points z[m] = x[2m] + i x[2m+1].  The length-M complex FFT is a four-step
@@ -15,23 +17,28 @@
 // pass and a set of R/S rows for the row pass; the transposes between the
 // passes go through distributed shared memory (no HBM round trip, no TMA
 // multicast).  Rows are dealt out in pairs (k1, R-k1) so that every
-// frequency k and its real-FFT partner M-k live in the same warp, which lets
-// the split into the real spectrum, the multiply by h and the re-packing for
-// the inverse all happen in place.
+// frequency k and its real-FFT partner M-k live in the same CTA.
 //
-// Scheduling.  All 512 threads of a CTA cooperate on every pass with the
-// batch index (column, or row) fastest across lanes, which makes every
-// shared-memory access of the radix passes conflict-free.  The transposes
-// are staged through registers (coalesced DSMEM reads), so one shared buffer
-// per CTA suffices (~76 KB with the twiddle tables): two CTAs of different
-// clusters share an SM (32 warps), and one cluster's barrier waits overlap
-// the other's arithmetic.  Each sub-FFT (length R or C) is two in-register
-// radix passes (sizes 2..16); the forward sub-FFT leaves its output
-// digit-reversed and the inverse consumes it that way.  Twiddles come from
-// two shared-memory tables (W_M^j = W_M^{64 jh} W_M^{jl}) built in FP64 on
-// the host.  The projection P runs as its own streaming kernel (sg_pt.cu);
-// this kernel can also load a map projection itself (kLoadProj), which the
-// library uses only for small problems.
+// Each sub-FFT (length R or C) is two in-register radix passes (sizes
+// 2..16) through shared memory; the forward sub-FFT leaves its output
+// digit-reversed and the inverse consumes it that way.  Every pass works on
+// "units" (one small DFT each) with the batch index fastest across lanes, so
+// the shared-memory accesses are conflict-free, and in FP32 a thread carries
+// two units at once for instruction-level parallelism.  256 threads per CTA
+// with up to 128 registers each: two CTAs of different clusters share an SM,
+// so one cluster's barrier waits overlap the other's arithmetic.
+//
+// The last forward row pass, the real-spectrum split, the multiply by h, the
+// re-packing for the inverse and the first inverse row pass are one register
+// phase: the unit holding frequencies k and the unit holding M-k sit in
+// lanes l and l^17 of one warp (l^16 for row R/2) and swap their values with
+// shuffles.  Only row 0, whose partners are in the same row, goes through
+// shared memory.
+//
+// Twiddles: the inner ones (W_R, W_C) come from per-length shared tables,
+// the four-step ones (W_M) from two shared tables (W_M^j = W_M^{64 jh} W_M^{jl})
+// built in FP64 on the host, the real-FFT split twiddle W_N^k from one table
+// value per unit times a per-digit table.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -50,7 +57,7 @@ struct alignas(4 * sizeof(T)) map4 {
   T I, Q, U, pad;
 };
 
-constexpr int kFilterThreads = 512;
+constexpr int kFilterThreads = 256;
 constexpr int kFilterWarps = kFilterThreads / 32;
 constexpr int kTwLo = 64;
 
@@ -72,6 +79,26 @@ __device__ __forceinline__ int row_of(int i) {
   return (i & 1) ? R - p : p;
 }
 
+// 32-bit shared-window addresses of a peer CTA's shared memory (mapa), and
+// loads through them: keeps the transposes' addresses in one register each.
+__device__ __forceinline__ uint32_t cluster_map(const void* local, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n"
+               : "=r"(r)
+               : "r"((uint32_t)__cvta_generic_to_shared(local)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ cplx<float> ld_cluster(uint32_t addr, cplx<float>*) {
+  cplx<float> v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ cplx<double> ld_cluster(uint32_t addr, cplx<double>*) {
+  cplx<double> v;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];\n" : "=d"(v.x), "=d"(v.y) : "r"(addr));
+  return v;
+}
+
 __device__ __forceinline__ void cluster_arrive() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
 }
@@ -89,8 +116,64 @@ struct Geo {
   static constexpr int E = M / S;                // complex points per CTA
   static constexpr int BUF = (R * PA > C * PC) ? R * PA : C * PC;
   static constexpr int XE = (E + kFilterThreads - 1) / kFilterThreads;  // per thread
-  static_assert(Rs >= 2 && Rs % 2 == 0 && Cs >= 1, "tile too small");
+  // shared twiddle tables: lo, hi, W_R, W_C, W_N^{R C1 i} (i < C2)
+  static constexpr int TWN = kTwLo + M / kTwLo + R + C + C2;
+  static_assert(Rs >= 16 && Rs % 16 == 0, "the fused spectrum phase needs 16-row blocks");
+  static_assert(C1 >= 2 && (Rs * C1) % 32 == 0, "fused phase: whole warps of units");
+  static_assert(Cs >= 1, "tile too small");
 };
+
+// Runs U units through load -> DFT<P> -> store; with PAIR a thread carries
+// two units at once (independent instruction streams for latency hiding).
+template <typename T, int P, bool INV, int U, bool PAIR, class Ld, class St>
+__device__ __forceinline__ void run_pass(int tid, Ld ld, St st) {
+  constexpr int NT = kFilterThreads;
+  if constexpr (PAIR) {
+    for (int u0 = tid; u0 < U; u0 += 2 * NT) {
+      const int u1 = u0 + NT;
+      const bool two = (U % (2 * NT) == 0) || u1 < U;
+      cplx<T> a[P], b[P];
+      ld(u0, a);
+      if (two) ld(u1, b);
+      SgDft<P, INV, T>::run(a);
+      if (two) SgDft<P, INV, T>::run(b);
+      st(u0, a);
+      if (two) st(u1, b);
+    }
+  } else {
+    for (int u = tid; u < U; u += NT) {
+      cplx<T> a[P];
+      ld(u, a);
+      SgDft<P, INV, T>::run(a);
+      st(u, a);
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int src) {
+  return __shfl_sync(0xffffffffu, v, src);
+}
+
+// One real-FFT frequency pair (k, M-k) of the packed spectrum z: split into
+// the r2c values X[k], X[M-k], multiply by h, re-pack for the inverse.
+// Returns the re-packed value at the slot of `own` (k if own_is_k, else M-k)
+// and the r2c value X at that slot (for chi^2).  wk = W_N^k, k < M-k.
+template <typename T>
+__device__ __forceinline__ cplx<T> split_filter(cplx<T> zk, cplx<T> zm, T hk, T hm, cplx<T> wk,
+                                                bool own_is_k, cplx<T>& xown) {
+  const cplx<T> Ev{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
+  const cplx<T> Ov{T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x)};
+  const cplx<T> wO = cmul(wk, Ov);
+  const cplx<T> Xk = Ev + wO;
+  const cplx<T> Xm = cconj(Ev - wO);
+  xown = own_is_k ? Xk : Xm;
+  const cplx<T> Yk = cscale(Xk, hk), Ym = cscale(Xm, hm);
+  const cplx<T> P = Yk + cconj(Ym), Q = Yk - cconj(Ym);
+  const cplx<T> cwQ = cmulc(Q, wk);
+  const cplx<T> iwQ{-cwQ.y, cwQ.x};
+  return own_is_k ? P + iwQ : cconj(P - iwQ);
+}
 
 template <typename T, int LOGR, int LOGC, int S>
 __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
@@ -99,6 +182,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
   constexpr int R = G::R, C = G::C, M = G::M, R1 = G::R1, R2 = G::R2, C1 = G::C1, C2 = G::C2;
   constexpr int Cs = G::Cs, Rs = G::Rs, PA = G::PA, PC = G::PC, E = G::E;
   constexpr int NT = kFilterThreads;
+  constexpr bool PAIR = sizeof(T) == 4;
   cg::cluster_group cl = cg::this_cluster();
   const int j = (int)cl.block_rank();
   const int tid = threadIdx.x;
@@ -107,10 +191,17 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
   cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* twlo = buf + G::BUF;
   cplx<T>* twhi = twlo + kTwLo;
+  cplx<T>* twr = twhi + M / kTwLo;  // W_R^i, i < R
+  cplx<T>* twc = twr + R;           // W_C^i, i < C
+  cplx<T>* twd = twc + C;           // W_N^{R C1 i}, i < C2
   for (int i = tid; i < kTwLo; i += NT) twlo[i] = p.tw_lo[i];
   for (int i = tid; i < M / kTwLo; i += NT) twhi[i] = p.tw_hi[i];
   __syncthreads();
   const Tw<T> tw{twlo, twhi};
+  for (int i = tid; i < R; i += NT) twr[i] = tw((i * C) & (M - 1));
+  for (int i = tid; i < C; i += NT) twc[i] = tw((i * R) & (M - 1));
+  for (int i = tid; i < C2; i += NT) twd[i] = tw(((R * C1 / 2) * i) & (M - 1));
+  __syncthreads();
   const cplx<T> wn1 = p.wn1;
 
   const int cluster_id = blockIdx.x / S;
@@ -119,8 +210,9 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
   for (long long tile = cluster_id; tile < p.ntiles; tile += nclusters) {
     const long long base = tile * (long long)(2 * M);
     const int det = (int)(tile / p.nseg);
+    const T* h = p.filt + (long long)det * (M + 1);
     // ---- 1. load: z[C n1 + n2] = x[2n] + i x[2n+1], this CTA's columns ----
-#pragma unroll 4
+#pragma unroll 16
     for (int it = 0; it < G::XE; it++) {
       const int e = it * NT + tid;
       if (E % NT != 0 && e >= E) break;
@@ -147,43 +239,50 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       buf[n1 * PA + c] = v;
     }
     __syncthreads();
-    // ---- 2. forward column FFTs (length R) and the W_M twiddle ------------
-    for (int u = tid; u < Cs * R2; u += NT) {
-      const int c = u % Cs, n2 = u / Cs;
-      cplx<T> a[R1];
+    // ---- 2. forward column pass 1: DFT_R1 over n1, twiddle W_R^{n2 k} ------
+    run_pass<T, R1, false, Cs * R2, PAIR>(
+        tid,
+        [&](int u, auto& a) {
+          const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-      for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
-      SgDft<R1, false, T>::run(a);
+          for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
+        },
+        [&](int u, auto& a) {
+          const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-      for (int k = 0; k < R1; k++)
-        buf[(R2 * k + n2) * PA + c] = (k == 0 || n2 == 0) ? a[k] : cmul(a[k], tw((n2 * k * C) & (M - 1)));
-    }
+          for (int k = 0; k < R1; k++)
+            buf[(R2 * k + n2) * PA + c] =
+                (k == 0 || n2 == 0) ? a[k] : cmul(a[k], twr[(n2 * k) & (R - 1)]);
+        });
     __syncthreads();
-    for (int u = tid; u < Cs * R1; u += NT) {
-      const int c = u % Cs, ka = u / Cs;
-      const int n2g = j * Cs + c;
-      cplx<T> b[R2];
+    // ---- 3. forward column pass 2: DFT_R2, four-step twiddle W_M ------------
+    run_pass<T, R2, false, Cs * R1, PAIR>(
+        tid,
+        [&](int u, auto& b) {
+          const int c = u % Cs, ka = u / Cs;
 #pragma unroll
-      for (int i = 0; i < R2; i++) b[i] = buf[(R2 * ka + i) * PA + c];
-      SgDft<R2, false, T>::run(b);
+          for (int i = 0; i < R2; i++) b[i] = buf[(R2 * ka + i) * PA + c];
+        },
+        [&](int u, auto& b) {
+          const int c = u % Cs, ka = u / Cs;
+          const int n2g = j * Cs + c;
 #pragma unroll
-      for (int kb = 0; kb < R2; kb++)
-        buf[(R2 * ka + kb) * PA + c] = cmul(b[kb], tw((n2g * (ka + R1 * kb)) & (M - 1)));
-    }
+          for (int kb = 0; kb < R2; kb++)
+            buf[(R2 * ka + kb) * PA + c] = cmul(b[kb], tw((n2g * (ka + R1 * kb)) & (M - 1)));
+        });
     cluster_arrive();
     cluster_wait();
-    // ---- 3. transpose A -> C through registers -----------------------------
+    // ---- 4. transpose A -> C through registers -----------------------------
     {
       cplx<T> v[G::XE];
 #pragma unroll
       for (int it = 0; it < G::XE; it++) {
-        const int e = it * NT + tid;           // over (t, q, c) with c fastest
+        const int e = it * NT + tid;  // over (t, q, c) with c fastest
         if (E % NT != 0 && e >= E) break;
         const int c = e % Cs, r = e / Cs, q = r % S, t = r / S;
         const int k1 = row_of<R>(j * Rs + t);
         const int posr = R2 * (k1 % R1) + k1 / R1;
-        const cplx<T>* src = cl.map_shared_rank(buf, q);
-        v[it] = src[posr * PA + c];
+        v[it] = ld_cluster(cluster_map(buf + posr * PA + c, q), (cplx<T>*)nullptr);
       }
       cluster_arrive();
       cluster_wait();
@@ -196,124 +295,148 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       }
     }
     __syncthreads();
-    // ---- 4. forward row FFTs (length C) -----------------------------------
-    for (int u = tid; u < Rs * C2; u += NT) {
-      const int t = u % Rs, n2 = u / Rs;
-      cplx<T> a[C1];
+    // ---- 5. forward row pass 1: DFT_C1 over n1, twiddle W_C^{n2 k} ---------
+    run_pass<T, C1, false, Rs * C2, PAIR>(
+        tid,
+        [&](int u, auto& a) {
+          const int t = u % Rs, n2 = u / Rs;
 #pragma unroll
-      for (int i = 0; i < C1; i++) a[i] = buf[(C2 * i + n2) * PC + t];
-      SgDft<C1, false, T>::run(a);
+          for (int i = 0; i < C1; i++) a[i] = buf[(C2 * i + n2) * PC + t];
+        },
+        [&](int u, auto& a) {
+          const int t = u % Rs, n2 = u / Rs;
 #pragma unroll
-      for (int k = 0; k < C1; k++)
-        buf[(C2 * k + n2) * PC + t] = (k == 0 || n2 == 0) ? a[k] : cmul(a[k], tw((n2 * k * R) & (M - 1)));
-    }
+          for (int k = 0; k < C1; k++)
+            buf[(C2 * k + n2) * PC + t] =
+                (k == 0 || n2 == 0) ? a[k] : cmul(a[k], twc[(n2 * k) & (C - 1)]);
+        });
     __syncthreads();
-    for (int u = tid; u < Rs * C1; u += NT) {
-      const int t = u % Rs, ka = u / Rs;
-      cplx<T> b[C2];
-#pragma unroll
-      for (int i = 0; i < C2; i++) b[i] = buf[(C2 * ka + i) * PC + t];
-      SgDft<C2, false, T>::run(b);
-#pragma unroll
-      for (int kb = 0; kb < C2; kb++) buf[(C2 * ka + kb) * PC + t] = b[kb];
-    }
-    __syncthreads();
-    // ---- 5. real-spectrum split, multiply by h, re-pack for c2r -----------
+    // ---- 6. forward row pass 2 + spectrum + inverse row pass 1, in registers --
+    // unit (t, ka): lanes l < 16 take ka = q, lanes l >= 16 take C1-1-q, so
+    // the partner unit (t^1, C1-1-ka) is lane l^17 (row R/2: (t, C1-1-ka),
+    // lane l^16); its element C2-1-i holds frequency M - k_i.
     {
-      const T* h = p.filt + (long long)det * (M + 1);
       T c2 = T(0);
-      for (int e = tid; e < E; e += NT) {
-        const int t = e % Rs, pos = e / Rs;
-        const int k2 = pos / C2 + C1 * (pos % C2);
+      constexpr int TB = Rs / 16;
+      for (int u = tid; u < Rs * C1; u += NT) {
+        const int l = u & 31, g = u >> 5;
+        const int t = 16 * (g % TB) + (l & 15);
+        const int q = g / TB;
+        const int ka = (l < 16) ? q : C1 - 1 - q;
         const int k1 = row_of<R>(j * Rs + t);
-        const int k = k1 + R * k2;
-        if (k == 0) {
-          const cplx<T> z = buf[pos * PC + t];
-          T h0 = h[0], hM = h[M];
-          if (p.filt_abs) {
-            h0 = h0 < T(0) ? -h0 : h0;
-            hM = hM < T(0) ? -hM : hM;
-          }
-          const T x0 = z.x + z.y, xM = z.x - z.y;
-          c2 += h0 * x0 * x0 + hM * xM * xM;
-          const T y0 = h0 * x0, yM = hM * xM;
-          buf[pos * PC + t] = cplx<T>{y0 + yM, y0 - yM};
-          continue;
+        cplx<T> z[C2];
+#pragma unroll
+        for (int i = 0; i < C2; i++) z[i] = buf[(C2 * ka + i) * PC + t];
+        SgDft<C2, false, T>::run(z);
+        const bool row0 = (j == 0 && t == 0);
+        const int src = (j == 0 && t == 1) ? (l ^ 16) : (l ^ 17);
+        const int kb0 = k1 + R * ka;  // k_i = kb0 + R C1 i
+        T hk[C2];
+#pragma unroll
+        for (int i = 0; i < C2; i++) hk[i] = h[kb0 + R * C1 * i];
+        cplx<T> wb = tw(kb0 >> 1);
+        if (kb0 & 1) wb = cmul(wb, wn1);  // W_N^{kb0}
+        cplx<T> zo[C2];
+#pragma unroll
+        for (int i = 0; i < C2; i++) {
+          const cplx<T> zp{shfl(z[C2 - 1 - i].x, src), shfl(z[C2 - 1 - i].y, src)};
+          const T hp = shfl(hk[C2 - 1 - i], src);
+          const int k = kb0 + R * C1 * i;
+          const bool lo = k <= M - k;  // this unit holds the smaller frequency
+          const cplx<T> wk = cmul(wb, twd[i]);          // W_N^k
+          const cplx<T> ws = lo ? wk : cplx<T>{-wk.x, wk.y};  // W_N^{M-k} = -conj(W_N^k)
+          cplx<T> x;
+          zo[i] = split_filter(lo ? z[i] : zp, lo ? zp : z[i], lo ? hk[i] : hp, lo ? hp : hk[i],
+                               ws, lo, x);
+          if (!row0) c2 += hk[i] * (x.x * x.x + x.y * x.y);
         }
-        int k2p, tp;
-        if (k1 == 0) {
-          k2p = C - k2;
-          tp = t;
+        if (!row0) {
+          SgDft<C2, true, T>::run(zo);
+#pragma unroll
+          for (int n2 = 0; n2 < C2; n2++)
+            buf[(C2 * ka + n2) * PC + t] =
+                (ka == 0 || n2 == 0) ? zo[n2] : cmulc(zo[n2], twc[(n2 * ka) & (C - 1)]);
         } else {
-          k2p = C - 1 - k2;
-          tp = (j == 0 && t < 2) ? t : (t ^ 1);
+#pragma unroll
+          for (int i = 0; i < C2; i++) buf[(C2 * ka + i) * PC + t] = z[i];
         }
-        const int kp = M - k;
-        if (k > kp) continue;
-        const int posp = C2 * (k2p % C1) + k2p / C1;
-        const cplx<T> zk = buf[pos * PC + t];
-        const cplx<T> zm = buf[posp * PC + tp];
-        T hk = h[k], hm = h[kp];
-        if (p.filt_abs) {
-          hk = hk < T(0) ? -hk : hk;
-          hm = hm < T(0) ? -hm : hm;
+      }
+      // row 0's lanes paired with row R/2 above and kept only their forward
+      // values; row 0 is finished here through shared memory
+      __syncthreads();
+      if (j == 0) {
+        // row 0 (k1 = 0, t = 0): partners k2 <-> C - k2 within the row
+        T c0 = T(0);
+        for (int pos = tid; pos < C; pos += NT) {
+          const int k2 = pos / C2 + C1 * (pos % C2);
+          if (k2 == 0) {  // bins 0 and M
+            const cplx<T> zz = buf[0];
+            const T h0 = h[0], hM = h[M];
+            const T x0 = zz.x + zz.y, xM = zz.x - zz.y;
+            c0 += h0 * x0 * x0 + hM * xM * xM;
+            const T y0 = h0 * x0, yM = hM * xM;
+            buf[0] = cplx<T>{y0 + yM, y0 - yM};
+            continue;
+          }
+          const int k2p = C - k2;
+          if (k2 > k2p) continue;
+          const int posp = C2 * (k2p % C1) + k2p / C1;
+          const int k = R * k2;
+          const cplx<T> zk = buf[pos * PC], zm = buf[posp * PC];
+          const T hk0 = h[k], hm0 = h[M - k];
+          const cplx<T> wk = tw(k >> 1);  // R even: k even
+          cplx<T> xk, xm;
+          const cplx<T> ok = split_filter(zk, zm, hk0, hm0, wk, true, xk);
+          const cplx<T> om = split_filter(zk, zm, hk0, hm0, wk, false, xm);
+          c0 += hk0 * (xk.x * xk.x + xk.y * xk.y) +
+                (k2 == k2p ? T(0) : hm0 * (xm.x * xm.x + xm.y * xm.y));
+          buf[pos * PC] = ok;
+          buf[posp * PC] = om;
         }
-        const cplx<T> Ev{T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y)};
-        const cplx<T> Ov{T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x)};
-        cplx<T> wk = tw(k >> 1);
-        if (k & 1) wk = cmul(wk, wn1);
-        const cplx<T> wO = cmul(wk, Ov);
-        const cplx<T> Xk = Ev + wO;
-        const cplx<T> Xm = cconj(Ev - wO);
-        // bin M/2 pairs with itself: count it once
-        c2 += hk * (Xk.x * Xk.x + Xk.y * Xk.y) + (k == kp ? T(0) : hm * (Xm.x * Xm.x + Xm.y * Xm.y));
-        const cplx<T> Yk = cscale(Xk, hk), Ym = cscale(Xm, hm);
-        const cplx<T> P = Yk + cconj(Ym), Q = Yk - cconj(Ym);
-        const cplx<T> cwQ = cmulc(Q, wk);
-        const cplx<T> iwQ{-cwQ.y, cwQ.x};
-        buf[pos * PC + t] = P + iwQ;
-        buf[posp * PC + tp] = cconj(P - iwQ);
+        chi2 += (double)c0;
+        __syncthreads();
+        for (int a1 = tid; a1 < C1; a1 += NT) {  // inverse row pass 1 of row 0
+          cplx<T> b[C2];
+#pragma unroll
+          for (int i = 0; i < C2; i++) b[i] = buf[(C2 * a1 + i) * PC];
+          SgDft<C2, true, T>::run(b);
+#pragma unroll
+          for (int n2 = 0; n2 < C2; n2++)
+            buf[(C2 * a1 + n2) * PC] =
+                (a1 == 0 || n2 == 0) ? b[n2] : cmulc(b[n2], twc[(n2 * a1) & (C - 1)]);
+        }
+        __syncthreads();
       }
       chi2 += (double)c2;
     }
-    __syncthreads();
-    // ---- 6. inverse row FFTs and the W_M^-1 twiddle ------------------------
-    for (int u = tid; u < Rs * C1; u += NT) {
-      const int t = u % Rs, a1 = u / Rs;
-      cplx<T> b[C2];
+    // ---- 7. inverse row pass 2: DFT_C1, conj four-step twiddle W_M^{n k1} ---
+    run_pass<T, C1, true, Rs * C2, PAIR>(
+        tid,
+        [&](int u, auto& a) {
+          const int t = u % Rs, n2 = u / Rs;
 #pragma unroll
-      for (int i = 0; i < C2; i++) b[i] = buf[(C2 * a1 + i) * PC + t];
-      SgDft<C2, true, T>::run(b);
+          for (int i = 0; i < C1; i++) a[i] = buf[(C2 * i + n2) * PC + t];
+        },
+        [&](int u, auto& a) {
+          const int t = u % Rs, n2 = u / Rs;
+          const int k1 = row_of<R>(j * Rs + t);
 #pragma unroll
-      for (int n2 = 0; n2 < C2; n2++)
-        buf[(C2 * a1 + n2) * PC + t] = (a1 == 0 || n2 == 0) ? b[n2] : cmulc(b[n2], tw((n2 * a1 * R) & (M - 1)));
-    }
-    __syncthreads();
-    for (int u = tid; u < Rs * C2; u += NT) {
-      const int t = u % Rs, n2 = u / Rs;
-      const int k1 = row_of<R>(j * Rs + t);
-      cplx<T> a[C1];
-#pragma unroll
-      for (int i = 0; i < C1; i++) a[i] = buf[(C2 * i + n2) * PC + t];
-      SgDft<C1, true, T>::run(a);
-#pragma unroll
-      for (int n1 = 0; n1 < C1; n1++) {
-        const int n = C2 * n1 + n2;
-        buf[n * PC + t] = cmulc(a[n1], tw((n * k1) & (M - 1)));
-      }
-    }
+          for (int n1 = 0; n1 < C1; n1++) {
+            const int n = C2 * n1 + n2;
+            buf[n * PC + t] = cmulc(a[n1], tw((n * k1) & (M - 1)));
+          }
+        });
     cluster_arrive();
     cluster_wait();
-    // ---- 7. transpose C -> A through registers -----------------------------
+    // ---- 8. transpose C -> A through registers -----------------------------
     {
       cplx<T> v[G::XE];
 #pragma unroll
       for (int it = 0; it < G::XE; it++) {
-        const int e = it * NT + tid;           // over (q, c, t) with t fastest
+        const int e = it * NT + tid;  // over (q, c, t) with t fastest
         if (E % NT != 0 && e >= E) break;
         const int t = e % Rs, r = e / Rs, c = r % Cs, q = r / Cs;
-        const cplx<T>* src = cl.map_shared_rank(buf, q);
-        v[it] = src[(j * Cs + c) * PC + t];
+        v[it] = ld_cluster(cluster_map(buf + (j * Cs + c) * PC + t, q), (cplx<T>*)nullptr);
       }
       cluster_arrive();
       cluster_wait();
@@ -328,30 +451,38 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       }
     }
     __syncthreads();
-    // ---- 8. inverse column FFTs --------------------------------------------
-    for (int u = tid; u < Cs * R1; u += NT) {
-      const int c = u % Cs, a1 = u / Cs;
-      cplx<T> b[R2];
+    // ---- 9. inverse column pass 1: DFT_R2, conj twiddle W_R^{n2 a1} --------
+    run_pass<T, R2, true, Cs * R1, PAIR>(
+        tid,
+        [&](int u, auto& b) {
+          const int c = u % Cs, a1 = u / Cs;
 #pragma unroll
-      for (int i = 0; i < R2; i++) b[i] = buf[(R2 * a1 + i) * PA + c];
-      SgDft<R2, true, T>::run(b);
+          for (int i = 0; i < R2; i++) b[i] = buf[(R2 * a1 + i) * PA + c];
+        },
+        [&](int u, auto& b) {
+          const int c = u % Cs, a1 = u / Cs;
 #pragma unroll
-      for (int n2 = 0; n2 < R2; n2++)
-        buf[(R2 * a1 + n2) * PA + c] = (a1 == 0 || n2 == 0) ? b[n2] : cmulc(b[n2], tw((n2 * a1 * C) & (M - 1)));
-    }
+          for (int n2 = 0; n2 < R2; n2++)
+            buf[(R2 * a1 + n2) * PA + c] =
+                (a1 == 0 || n2 == 0) ? b[n2] : cmulc(b[n2], twr[(n2 * a1) & (R - 1)]);
+        });
     __syncthreads();
-    for (int u = tid; u < Cs * R2; u += NT) {
-      const int c = u % Cs, n2 = u / Cs;
-      cplx<T> a[R1];
+    // ---- 10. inverse column pass 2: DFT_R1 ----------------------------------
+    run_pass<T, R1, true, Cs * R2, PAIR>(
+        tid,
+        [&](int u, auto& a) {
+          const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-      for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
-      SgDft<R1, true, T>::run(a);
+          for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
+        },
+        [&](int u, auto& a) {
+          const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-      for (int n1 = 0; n1 < R1; n1++) buf[(R2 * n1 + n2) * PA + c] = a[n1];
-    }
+          for (int n1 = 0; n1 < R1; n1++) buf[(R2 * n1 + n2) * PA + c] = a[n1];
+        });
     __syncthreads();
-    // ---- 9. store ------------------------------------------------------------
-#pragma unroll 4
+    // ---- 11. store -------------------------------------------------------------
+#pragma unroll 16
     for (int it = 0; it < G::XE; it++) {
       const int e = it * NT + tid;
       if (E % NT != 0 && e >= E) break;
@@ -376,12 +507,11 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
   cluster_arrive();
   cluster_wait();
 }
-
 // ---------------------------------------------------------------------------
 template <typename T, int LOGR, int LOGC, int S>
 static size_t smem_bytes() {
   using G = Geo<LOGR, LOGC, S>;
-  return sizeof(cplx<T>) * ((size_t)G::BUF + kTwLo + G::M / kTwLo);
+  return sizeof(cplx<T>) * ((size_t)G::BUF + G::TWN);
 }
 
 template <typename T, int LOGR, int LOGC, int S>
@@ -443,8 +573,9 @@ static int max_clusters_one() {
 size_t filter_smem_bytes(int logm, int S, int esize) {
   const int logr = (logm + 1) / 2, logc = logm / 2;
   const size_t R = 1u << logr, C = 1u << logc, M = R * C;
+  const size_t C2 = C >> ((logc + 1) / 2);
   const size_t buf = std::max(R * (C / S + 1), C * (R / S + 1));
-  return (size_t)esize * 2 * (buf + kTwLo + M / kTwLo);
+  return (size_t)esize * 2 * (buf + kTwLo + M / kTwLo + R + C + C2);
 }
 
 int filter_cluster_size(int logm, int esize) {
