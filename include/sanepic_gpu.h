@@ -102,6 +102,8 @@ typedef struct sg_report {
   long kernel_launches;   /* kernels this library launched during the solve */
   int breakdown;          /* nonzero: stopped early because d^T A d <= 0 (bit 0) or
                              r^T M r <= 0 (bit 1) -- the residual reached rounding level */
+  int fallback_iter;      /* SG_PRECOND_LEARNED: iteration at which the solve fell back
+                             to plain block-Jacobi PCG, or -1 */
 } sg_report;
 
 /* Creates a context on desc->device.  Replaces the parameter handling of
@@ -161,6 +163,63 @@ int sg_noise_filter(sg_ctx *ctx, const double *in, double *out);
  * up (cudaGetSymbolAddress), so make it before any stream capture. */
 int sg_noise_filter_noalloc(const float *in, float *out, const float *filt, long ns,
                             long ntiles, long tiles_per_filter, void *stream);
+
+/* ---- learned preconditioner (no reference counterpart) ----------------------
+ * A 4-layer MLP (768 -> 256 -> 256 -> 256 -> 768, BF16 weights on the tensor
+ * cores, FP32 accumulate) maps 3 x 256-pixel nested-HEALPix patches of the
+ * block-Jacobi-preconditioned residual to a correction; SG_PRECOND_LEARNED
+ * uses M_bj3 r + correction inside flexible PCG and falls back to plain
+ * block-Jacobi PCG if r^T z turns non-positive.  Needs nside a power of two
+ * >= 16. */
+typedef struct sg_learn_opts {
+  int npairs;        /* residual/solution pairs from the plain solver (0: 512) */
+  long seed;         /* first synthetic sky/noise seed (0: 5000) */
+  int steps;         /* Adam steps (0: 1500) */
+  int batch;         /* patches per step, multiple of 128 (0: 4096) */
+  float lr;          /* Adam learning rate (0: 1e-3) */
+  double pair_crit;  /* plain-solver |r|^2/|b|^2 that defines each solution (0: 1e-13) */
+  double val_crit;   /* stop of the validation solves (0: 1e-12) */
+  int force;         /* nonzero: use the network even if validation shows no gain */
+} sg_learn_opts;
+
+typedef struct sg_learn_report {
+  int pairs, skies; /* pairs kept, synthetic skies solved */
+  long rows;        /* training patches (pairs x observed patches) */
+  int steps;
+  float loss_first, loss_last;  /* batch MSE (normalised units) at the first / last step */
+  double gen_seconds, train_seconds;
+  double gemm_tflop;            /* tensor-core work of the training, TFLOP */
+  /* validation on a held-out synthetic sky and noise realisation */
+  int val_plain_iters, val_learned_iters;
+  double val_plain_ms, val_learned_ms;  /* CUDA-event time of each solve */
+  int enabled;  /* 1: SG_PRECOND_LEARNED uses the network; 0: it runs plain
+                   block-Jacobi PCG because the network did not beat it */
+} sg_learn_report;
+
+/* Generates training data on this context's pointing and noise model
+ * (synthetic skies and noise on the GPU; the residuals of plain block-Jacobi
+ * solves run to pair_crit) and trains the network with the library's own
+ * forward/backward kernels: each step maximises the A-cosine
+ * (r^T z)^2 / ((z^T A z)(r^T M_bj3 r)) of the corrected direction z for one
+ * stored residual, differentiated through one application of A.  Plain PCG
+ * then judges the result on a held-out problem (report->enabled).
+ * `batch` is unused (one residual's patches per step).
+ * Overwrites b and the solution: call sg_rhs again before sg_solve. */
+int sg_learn_train(sg_ctx *ctx, const sg_learn_opts *opts, sg_learn_report *report);
+long sg_learn_nparams(void);
+/* FP32 parameters, per layer W [out x in] row-major then b [out]. */
+int sg_learn_get_params(sg_ctx *ctx, float *params);
+int sg_learn_set_params(sg_ctx *ctx, const float *params);
+
+/* Tests and measurements on host arrays.  sg_mlp_gemm_host: C[M x N] =
+ * A[M x K] . B[N x K]^T, BF16 bit patterns in, FP32 out (M, N multiples of
+ * 128, K of 64); with reps > 0, *ms = mean CUDA-event time of one GEMM.
+ * sg_mlp_grad_host: one forward + backward of the network (B rows, a
+ * multiple of 128): Y [B x 768], loss = mean (Y - T)^2, grads like params. */
+int sg_mlp_gemm_host(const unsigned short *A, const unsigned short *B, float *C, int M, int N,
+                     int K, int reps, double *ms);
+int sg_mlp_grad_host(const float *params, const float *X, const float *T, int B, float *Y,
+                     float *loss, float *grads);
 
 /* Preconditioned CG (sanepic.cc:1177-1761). */
 int sg_solve(sg_ctx *ctx, const sg_solve_opts *opts, sg_report *report);

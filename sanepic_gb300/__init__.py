@@ -35,7 +35,8 @@ MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
 EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
-           "sg_last_error", "sg_destroy"]
+           "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
+           "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_last_error", "sg_destroy"]
 
 
 class SanepicError(RuntimeError):
@@ -72,7 +73,24 @@ class SgReport(ctypes.Structure):
                 ("crit", ctypes.c_double), ("var00", ctypes.c_double),
                 ("solve_seconds", ctypes.c_double), ("iter_per_sec", ctypes.c_double),
                 ("setup_seconds", ctypes.c_double), ("device_seconds", ctypes.c_double),
-                ("kernel_launches", ctypes.c_long), ("breakdown", ctypes.c_int)]
+                ("kernel_launches", ctypes.c_long), ("breakdown", ctypes.c_int),
+                ("fallback_iter", ctypes.c_int)]
+
+
+class SgLearnOpts(ctypes.Structure):
+    _fields_ = [("npairs", ctypes.c_int), ("seed", ctypes.c_long), ("steps", ctypes.c_int),
+                ("batch", ctypes.c_int), ("lr", ctypes.c_float), ("pair_crit", ctypes.c_double),
+                ("val_crit", ctypes.c_double), ("force", ctypes.c_int)]
+
+
+class SgLearnReport(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_int), ("skies", ctypes.c_int), ("rows", ctypes.c_long),
+                ("steps", ctypes.c_int), ("loss_first", ctypes.c_float),
+                ("loss_last", ctypes.c_float), ("gen_seconds", ctypes.c_double),
+                ("train_seconds", ctypes.c_double), ("gemm_tflop", ctypes.c_double),
+                ("val_plain_iters", ctypes.c_int), ("val_learned_iters", ctypes.c_int),
+                ("val_plain_ms", ctypes.c_double), ("val_learned_ms", ctypes.c_double),
+                ("enabled", ctypes.c_int)]
 
 
 _lib = None
@@ -110,12 +128,25 @@ def load_library(path: Optional[str] = None):
     L.sg_get_indpix.argtypes = [c_p, lp]
     L.sg_get_crit_history.argtypes = [c_p, dp, ctypes.c_int]
     L.sg_profile_operator.argtypes = [c_p, ctypes.c_int, dp]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.sg_learn_train.argtypes = [c_p, ctypes.POINTER(SgLearnOpts), ctypes.POINTER(SgLearnReport)]
+    L.sg_learn_nparams.argtypes = []
+    L.sg_learn_nparams.restype = ctypes.c_long
+    L.sg_learn_get_params.argtypes = [c_p, fp]
+    L.sg_learn_set_params.argtypes = [c_p, fp]
+    L.sg_mlp_gemm_host.argtypes = [ctypes.POINTER(ctypes.c_ushort), ctypes.POINTER(ctypes.c_ushort),
+                                   fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    L.sg_mlp_grad_host.argtypes = [fp, fp, fp, ctypes.c_int, fp, fp, fp]
     L.sg_last_error.argtypes = [c_p]
     L.sg_last_error.restype = ctypes.c_char_p
     L.sg_destroy.argtypes = [c_p]
     if path is None:
         _lib = L
     return L
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def _dp(a: np.ndarray):
@@ -248,6 +279,27 @@ class MapMaker:
         self._check(self.L.sg_get_indpix(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
         return out
 
+    # ---- learned preconditioner ---------------------------------------------
+    def learn_train(self, npairs: int = 512, seed: int = 5000, steps: int = 1500,
+                    batch: int = 0, lr: float = 1e-3, pair_crit: float = 1e-13,
+                    val_crit: float = 1e-12, force: bool = False) -> dict:
+        """Make residual/solution pairs with the plain solver on synthetic skies,
+        train the network on the GPU and validate it against plain PCG on a
+        held-out problem.  Overwrites b: call rhs() again afterwards."""
+        o = SgLearnOpts(npairs, seed, steps, batch, lr, pair_crit, val_crit, int(force))
+        rep = SgLearnReport()
+        self._check(self.L.sg_learn_train(self.h, ctypes.byref(o), ctypes.byref(rep)))
+        return {k: getattr(rep, k) for k, _ in SgLearnReport._fields_}
+
+    def learn_params(self) -> np.ndarray:
+        out = np.empty(int(self.L.sg_learn_nparams()), dtype=np.float32)
+        self._check(self.L.sg_learn_get_params(self.h, _fp(out)))
+        return out
+
+    def set_learn_params(self, params) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.L.sg_learn_set_params(self.h, _fp(p)))
+
     def profile_operator(self, reps: int = 5) -> dict:
         ms = np.zeros(4)
         self._check(self.L.sg_profile_operator(self.h, reps, _dp(ms)))
@@ -295,3 +347,40 @@ def from_problem(prob, precision: Optional[str] = None, device: int = 0,
         if with_tod and "tod" in prob:
             mm.set_tod(d, prob["tod"][d])
     return mm
+
+
+# ---- tensor-core GEMM and network gradients on host arrays (tests, measurements) ----
+def mlp_nparams() -> int:
+    return int(load_library().sg_learn_nparams())
+
+
+def gemm_bf16(a_bits: np.ndarray, b_bits: np.ndarray, reps: int = 0):
+    """C = A . B^T for BF16 bit patterns A [M, K], B [N, K] (uint16).  Returns
+    (C float32 [M, N], mean milliseconds per GEMM when reps > 0)."""
+    A = np.ascontiguousarray(a_bits, dtype=np.uint16)
+    B = np.ascontiguousarray(b_bits, dtype=np.uint16)
+    M, K = A.shape
+    N = B.shape[0]
+    C = np.empty((M, N), dtype=np.float32)
+    ms = ctypes.c_double(0.0)
+    rc = load_library().sg_mlp_gemm_host(A.ctypes.data_as(ctypes.POINTER(ctypes.c_ushort)),
+                                         B.ctypes.data_as(ctypes.POINTER(ctypes.c_ushort)),
+                                         _fp(C), M, N, K, reps, ctypes.byref(ms))
+    if rc:
+        raise SanepicError(rc, "sg_mlp_gemm_host failed")
+    return C, ms.value
+
+
+def mlp_grad(params: np.ndarray, X: np.ndarray, T: np.ndarray):
+    """One forward + backward of the network: returns (Y, loss, grads)."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    Y = np.empty_like(X)
+    g = np.empty_like(p)
+    loss = ctypes.c_float(0.0)
+    rc = load_library().sg_mlp_grad_host(_fp(p), _fp(X), _fp(T), X.shape[0], _fp(Y),
+                                         ctypes.byref(loss), _fp(g))
+    if rc:
+        raise SanepicError(rc, "sg_mlp_grad_host failed")
+    return Y, float(loss.value), g

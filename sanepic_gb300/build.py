@@ -29,6 +29,9 @@ UNITS = {
     "sg_cg.cu": [],
     "sg_api.cu": [],
     "sg_noalloc.cu": [],
+    "sg_gemm.cu": [],
+    "sg_mlp.cu": [],
+    "sg_learn.cu": [],
     "sg_pointing.cu": ["--fmad=false"],
 }
 LIB = os.path.join(LIBDIR, "libsanepic_gpu.so")

@@ -319,6 +319,38 @@ cudaError_t cg_step_c(const CgVecs& v, T* dmap, int flexible, cudaStream_t st) {
 template cudaError_t cg_step_c<float>(const CgVecs&, float*, int, cudaStream_t);
 template cudaError_t cg_step_c<double>(const CgVecs&, double*, int, cudaStream_t);
 
+// restart the search direction from an externally supplied z: d = z,
+// delta = delta0 = r.z (partials from cg_dots)
+template <typename T>
+__global__ void __launch_bounds__(kCgThreads) k_reinit_d(CgVecs v, T* dmap) {
+  const double rz = reduce_partials(v.part + kCgBlocks);
+  const long long n = v.npix;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+       m += (long long)gridDim.x * blockDim.x) {
+    double d[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      d[c] = v.z[c * n + m];
+      v.d[c * n + m] = d[c];
+    }
+    store_map<T>(dmap, m, d[0], d[1], d[2]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    v.sc->delta = rz;
+    v.sc->delta0 = rz;
+    v.sc->delta_old = rz;
+    if (!(rz > 0.0)) v.sc->flag |= 2;
+  }
+}
+
+template <typename T>
+cudaError_t cg_reinit_d(const CgVecs& v, T* dmap, cudaStream_t st) {
+  k_reinit_d<T><<<kCgBlocks, kCgThreads, 0, st>>>(v, dmap);
+  return cudaGetLastError();
+}
+template cudaError_t cg_reinit_d<float>(const CgVecs&, float*, cudaStream_t);
+template cudaError_t cg_reinit_d<double>(const CgVecs&, double*, cudaStream_t);
+
 template <typename T>
 __global__ void k_to_map4(const double* x, long long n, T* map) {
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;

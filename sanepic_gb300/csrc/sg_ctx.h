@@ -1,0 +1,353 @@
+// sg_ctx.h -- the library context behind the C ABI (internal): problem
+// sizes, the pixelisation, device buffers, the operator pieces A = P^T N^-1 P
+// and the PCG iteration as a launch sequence (captured in CUDA graphs).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/sanepic_gpu.h"
+#include "sg_kernels.h"
+#include "sg_mlp.h"
+
+using namespace sg;
+
+namespace sg {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t n) {
+    release();
+    bytes = n;
+    if (n == 0) return cudaSuccess;
+    return cudaMalloc(&p, n);
+  }
+  template <typename U>
+  U* as() const {
+    return reinterpret_cast<U*>(p);
+  }
+};
+
+inline double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+constexpr double kD2PI = 6.2831853071795864769252867665590057683943387987502;
+
+}  // namespace sg
+
+struct sg_ctx {
+  sg_desc desc{};
+  std::string err;
+  cudaStream_t st = nullptr;
+  cudaStream_t own_st = nullptr;  // the stream the context created
+  int f32 = 0;       // precision
+  int esize = 8;     // bytes per real
+  long long ns = 0, nseg = 0, ndet = 0, ntiles = 0, nsamp = 0, npixfull = 0;
+  int logm = 0, S = 1, nclusters = 1;
+  long long npix = 0;
+  std::vector<int> indpix_host;        // RING pixel -> RING-order compact index (reference)
+  std::vector<long long> int2ring;     // internal index -> RING pixel
+  std::vector<long long> int2ringc;    // internal index -> RING-order compact index
+  std::vector<long long> isampmin;
+
+  // Detectors with identical focal-plane offsets share one pixel stream (an
+  // offset group).  pix, cs, csr_* live per group sample (ngsamp of them);
+  // y and tod per detector sample (nsamp).
+  int ngroups = 0;
+  long long ngsamp = 0;
+  std::vector<int> grp_off_h, grp_det_h;
+  std::vector<double> g0_h, psidet_h;
+  DevBuf pix, cs, y, tod, csr_off, csr_idx, csr_cs, hits, indpix, sumcross;
+  DevBuf grp_off, grp_det, dcs, ys, gconst;
+  DevBuf filt, tw_lo, tw_hi, g0, ntab;
+  DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
+  DevBuf chi2p;  // per-CTA chi^2 partials of the noise filter
+  std::vector<double> spn_h;  // host copy of the filter rows [ndet][M+1] (FP64)
+
+  // learned preconditioner: the network, the nested patch geometry
+  // (patch_idx [npatch_pad][256] internal pixel or -1), per-patch scales, and
+  // the synthetic timeline used while generating training pairs
+  std::unique_ptr<Mlp> mlp;
+  DevBuf patch_idx, patch_sig, tod_syn, filt_noise;
+  int npatch = 0, npatch_pad = 0;
+  bool have_mlp = false, use_syn = false;
+  bool learned_enabled = false;  // validation: the network beat plain PCG
+  const void* tod_active() const { return use_syn ? tod_syn.p : tod.p; }
+  cplx<float> wn1f{1.f, 0.f};
+  cplx<double> wn1d{1.0, 0.0};
+  CgScalars* sc_host = nullptr;  // pinned
+
+  bool have_pointing = false, have_rhs = false, have_solution = false;
+  bool have_bj3 = false, have_diag = false;
+  std::vector<char> have_noise, have_tod;
+  std::vector<double> crit_hist;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+  std::map<std::pair<int, int>, long long> graph_launches;
+  long long launches = 0;  // kernels launched by this context
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* what) {
+    return fail(SG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  ~sg_ctx() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (sc_host) cudaFreeHost(sc_host);
+    if (own_st) cudaStreamDestroy(own_st);
+  }
+
+  // compact vectors [I|Q|U]: RING-order compact (API) <-> internal order
+  void to_internal(const double* ringc, double* out) const {
+    for (int cc = 0; cc < 3; cc++)
+      for (long long m = 0; m < npix; m++) out[cc * npix + m] = ringc[cc * npix + int2ringc[m]];
+  }
+  void to_ring(const double* internal, double* out) const {
+    for (int cc = 0; cc < 3; cc++)
+      for (long long m = 0; m < npix; m++) out[cc * npix + int2ringc[m]] = internal[cc * npix + m];
+  }
+
+  // ---- operator pieces ---------------------------------------------------
+  template <typename T>
+  FilterArgs<T> filter_args(int mode, const T* in, T* out, long long ntiles_, int nseg_,
+                            int filt_abs, const T* sub, double* chi2_part,
+                            const T* table = nullptr) {
+    FilterArgs<T> a{};
+    a.ntiles = ntiles_;
+    a.nseg = nseg_;
+    a.mode = mode;
+    a.filt_abs = filt_abs;
+    a.tod = in;
+    a.sub = sub;
+    a.chi2_part = chi2_part;
+    a.filt = table ? table : filt.as<T>();
+    a.out = out;
+    a.tw_lo = tw_lo.as<cplx<T>>();
+    a.tw_hi = tw_hi.as<cplx<T>>();
+    return a;
+  }
+
+  // chi2_out (device double) receives 2 sum h |X|^2 over all tiles when set
+  cudaError_t launch_filter(int mode, const void* in, void* out, long long ntiles_, int nseg_,
+                            int filt_abs, const void* sub = nullptr, double* chi2_out = nullptr,
+                            const void* table = nullptr) {
+    const int ncl = (int)std::min<long long>(nclusters, ntiles_);
+    double* part = chi2_out ? chi2p.as<double>() : nullptr;
+    cudaError_t e;
+    launches++;
+    if (f32) {
+      auto a = filter_args<float>(mode, (const float*)in, (float*)out, ntiles_, nseg_, filt_abs,
+                                  (const float*)sub, part, (const float*)table);
+      a.wn1 = wn1f;
+      e = filter_launch<float>(a, logm, S, ncl, st);
+    } else {
+      auto a = filter_args<double>(mode, (const double*)in, (double*)out, ntiles_, nseg_,
+                                   filt_abs, (const double*)sub, part, (const double*)table);
+      a.wn1 = wn1d;
+      e = filter_launch<double>(a, logm, S, ncl, st);
+    }
+    if (e == cudaSuccess && chi2_out) {
+      launches++;
+      e = chi2_sum(part, S * ncl, chi2_out, st);
+    }
+    return e;
+  }
+
+  // per group sample detector sums of y, then the CSR reduction into a map
+  cudaError_t launch_detsum() {
+    launches++;
+    if (f32)
+      return detsum_launch<float>(y.as<float>(), ngsamp, ns * nseg, grp_off.as<int>(),
+                                  grp_det.as<int>(), dcs.as<float>(), ys.as<float>(), st);
+    return detsum_launch<double>(y.as<double>(), ngsamp, ns * nseg, grp_off.as<int>(),
+                                 grp_det.as<int>(), dcs.as<double>(), ys.as<double>(), st);
+  }
+
+  cudaError_t launch_pt(double* out, bool masked) {
+    const int* h = masked ? hits.as<int>() : nullptr;
+    launches++;
+    if (f32)
+      return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
+                              ys.as<float>(), npix, h, out, st);
+    return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<double>(),
+                             ys.as<double>(), npix, h, out, st);
+  }
+
+  // out = P^T y (y in time order, one row per detector)
+  cudaError_t pt_of_y(double* out, bool masked) {
+    cudaError_t e = launch_detsum();
+    if (e == cudaSuccess) e = launch_pt(out, masked);
+    return e;
+  }
+
+  cudaError_t to_map(const double* v) {
+    launches++;
+    if (f32) return to_map4<float>(v, npix, dmap.as<float>(), st);
+    return to_map4<double>(v, npix, dmap.as<double>(), st);
+  }
+
+  // y = P map (time order, every detector), then N^-1 in place on y
+  cudaError_t launch_project() {
+    launches++;
+    if (f32)
+      return project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
+                                   ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
+                                   dcs.as<float>(), y.as<float>(), st);
+    return project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
+                                  ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
+                                  dcs.as<double>(), y.as<double>(), st);
+  }
+
+  cudaError_t apply_map(double* out, bool masked) {
+    cudaError_t e = launch_project();
+    if (e == cudaSuccess) e = launch_filter(kLoadTod, y.p, y.p, ntiles, (int)nseg, 0);
+    if (e == cudaSuccess) e = pt_of_y(out, masked);
+    return e;
+  }
+
+  // out = A v (masked or not); v is a device compact vector
+  cudaError_t apply_dev(const double* v, double* out, bool masked) {
+    cudaError_t e = to_map(v);
+    if (e == cudaSuccess) e = apply_map(out, masked);
+    return e;
+  }
+
+  CgVecs vecs(int precond) {
+    CgVecs v{};
+    v.npix = npix;
+    v.x = x.as<double>();
+    v.r = r.as<double>();
+    v.d = d.as<double>();
+    v.q = q.as<double>();
+    v.z = z.as<double>();
+    v.rprev = rprev.as<double>();
+    v.b = b.as<double>();
+    v.minv = minv.as<double>();
+    v.mdiag = mdiag.as<double>();
+    v.hits_true = hits.as<int>();
+    v.precond = precond;
+    v.part = part.as<double>();
+    v.sc = sc.as<CgScalars>();
+    return v;
+  }
+
+  // one PCG iteration (sanepic.cc:1417-1610) as a launch sequence
+  cudaError_t enqueue_iteration(int precond, bool refresh) {
+    if (precond == 2) return enqueue_learned_iteration(refresh);
+    CgVecs v = vecs(precond);
+    cudaError_t e = apply_map(q.as<double>(), true);
+    if (e == cudaSuccess) e = cg_step_a(v, st);
+    if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 0, st);
+    launches += 3;  // step a, b, c
+    if (refresh) {
+      // true residual r = P^T N^-1 (d - P x) in one operator pass; the filter
+      // also yields chi^2 of the residual timeline (sanepic.cc:1483-1572)
+      if (e == cudaSuccess) e = to_map(x.as<double>());
+      if (e == cudaSuccess) e = launch_project();
+      if (e == cudaSuccess)
+        e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
+                          &sc.as<CgScalars>()->chi2);
+      if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
+      if (e == cudaSuccess) e = cg_refresh_r(v, 0, 1, st);
+      launches++;
+    }
+    if (e == cudaSuccess)
+      e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 0, st)
+              : cg_step_c<double>(v, dmap.as<double>(), 0, st);
+    return e;
+  }
+
+  // flexible PCG with z = M_bj3 r + network correction (Polak-Ribiere beta)
+  cudaError_t enqueue_learned_iteration(bool refresh) {
+    CgVecs v = vecs(2);
+    cudaError_t e = apply_map(q.as<double>(), true);
+    if (e == cudaSuccess) e = cg_step_a(v, st);
+    if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 1, st);
+    launches += 2;
+    if (refresh) {
+      if (e == cudaSuccess) e = to_map(x.as<double>());
+      if (e == cudaSuccess) e = launch_project();
+      if (e == cudaSuccess)
+        e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
+                          &sc.as<CgScalars>()->chi2);
+      if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
+      if (e == cudaSuccess) e = cg_refresh_r(v, 1, 1, st);
+      launches++;
+    }
+    if (e == cudaSuccess) e = learned_z();
+    if (e == cudaSuccess) e = cg_dots(v, 1, st);
+    if (e == cudaSuccess)
+      e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 1, st)
+              : cg_step_c<double>(v, dmap.as<double>(), 1, st);
+    launches += 2;
+    return e;
+  }
+  cudaError_t learned_z();  // z = M_bj3 r + correction (sg_learn.cu)
+
+  // captured iterations hold raw device pointers: drop them whenever a buffer
+  // they use is reallocated
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    graph_launches.clear();
+  }
+
+  cudaError_t run_iteration(int precond, bool refresh, bool use_graph) {
+    if (!use_graph) return enqueue_iteration(precond, refresh);
+    auto key = std::make_pair(precond, refresh ? 1 : 0);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      cudaGraph_t g;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return e;
+      const long long before = launches;
+      e = enqueue_iteration(precond, refresh);
+      graph_launches[key] = launches - before;
+      launches = before;
+      cudaError_t e2 = cudaStreamEndCapture(st, &g);
+      if (e != cudaSuccess) return e;
+      if (e2 != cudaSuccess) return e2;
+      cudaGraphExec_t ge;
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return e;
+      it = graphs.emplace(key, ge).first;
+    }
+    launches += graph_launches[key];
+    return cudaGraphLaunch(it->second, st);
+  }
+};
+
+int build_bj3(sg_ctx* c);  // 3x3 block-Jacobi blocks for the current pointing and noise
+int ensure_patches(sg_ctx* c);  // nested patch geometry of the learned preconditioner

@@ -163,9 +163,21 @@ cudaError_t chi2_sum(const double* part, int n, double* out, cudaStream_t st);
 cudaError_t cg_dots(const CgVecs& v, int flexible, cudaStream_t st);
 template <typename T>
 cudaError_t cg_step_c(const CgVecs& v, T* dmap, int flexible, cudaStream_t st);
+// d = z, delta = delta0 = r.z after cg_dots (start of a flexible PCG)
+template <typename T>
+cudaError_t cg_reinit_d(const CgVecs& v, T* dmap, cudaStream_t st);
 template <typename T>
 cudaError_t to_map4(const double* x, long long npix, T* map, cudaStream_t st);
 cudaError_t mask_qu(double* v, const int* hits_true, long long npix, cudaStream_t st);
 cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStream_t st);
+
+// ---- tensor-core BF16 GEMM (sg_gemm.cu) -----------------------------------------
+// C[M x N] (FP32, row-major, ldc = N) = A[M x K] . B[N x K]^T (+ C if beta);
+// A, B row-major BF16 with K contiguous; M % 128 == 0, N % 128 == 0, K % 64 == 0.
+// *err (device int) receives a nonzero code if a pipeline wait timed out.
+bool gemm_shape_ok(int M, int N, int K);
+cudaError_t gemm_prepare();  // one-time kernel attributes on the current device
+cudaError_t gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int beta,
+                      int* err, cudaStream_t st);
 
 }  // namespace sg

@@ -1,0 +1,681 @@
+// sg_learn.cu -- the learned preconditioner (no reference counterpart).
+//
+// Inside flexible PCG the preconditioner is
+//     z = M_bj3 r + sum_p  s_p * f(u_p),   u_p = (M_bj3 r)|_p / s_p
+// where p runs over nested-HEALPix patches of 256 pixels (a 16 x 16 block of
+// one base face), (M_bj3 r)|_p is the block-Jacobi-preconditioned residual on
+// the patch's I, Q and U (768 values, 0 where a pixel is not observed), s_p
+// its RMS, and f the MLP of sg_mlp.h.  The plain block-Jacobi PCG stays the
+// fallback: if r^T z turns non-positive the solve restarts from the current
+// map with block-Jacobi alone.
+//
+// Training data come from the plain solver: for each synthetic sky (seeded,
+// iid I/Q/U) and noise realisation the library makes the timeline
+// d = P sky + n on the GPU (n: white Gaussian shaped by the detectors' own
+// noise spectra), solves with block-Jacobi PCG to a tight tolerance and keeps
+// the residual r_k of every iteration.  Each training step takes one stored
+// residual and maximises the A-cosine of the corrected direction,
+//     (r^T z)^2 / ((z^T A z) (r^T M_bj3 r)),
+// the share of the A-norm error that one CG step along z removes; the
+// gradient goes through one application of the real operator A and the
+// network's own backward pass.  The correction carries no per-patch mean, so
+// the network does not inject the near-null large-scale modes.  After
+// training, plain PCG judges the network on a held-out problem and the
+// learned mode is used only if it was faster.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <random>
+
+#include "sg_ctx.h"
+#include "sg_healpix.h"
+#include "sg_kernels.h"
+#include "sg_mlp.h"
+
+namespace sg {
+namespace {
+
+constexpr int kT = 256;
+
+__device__ __forceinline__ uint16_t bf16_rn(float f) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(f));
+}
+
+// one block of 256 threads per patch; thread j = nested slot j
+__global__ void __launch_bounds__(kPatch)
+    k_patch_gather(const double* __restrict__ z, const int* __restrict__ idx, int npatch,
+                   long long npix, uint16_t* X, float* sig) {
+  __shared__ double red[kPatch / 32];
+  __shared__ int cnt[kPatch / 32];
+  const int p = blockIdx.x, j = threadIdx.x;
+  const int m = (p < npatch) ? idx[(size_t)p * kPatch + j] : -1;
+  double zc[3] = {0.0, 0.0, 0.0};
+  if (m >= 0) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) zc[c] = z[c * npix + m];
+  }
+  double ss = zc[0] * zc[0] + zc[1] * zc[1] + zc[2] * zc[2];
+  int ob = m >= 0;
+  for (int o = 16; o > 0; o >>= 1) {
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    ob += __shfl_xor_sync(0xffffffffu, ob, o);
+  }
+  if ((j & 31) == 0) {
+    red[j >> 5] = ss;
+    cnt[j >> 5] = ob;
+  }
+  __syncthreads();
+  double sst = 0.0;
+  int obt = 0;
+  for (int w = 0; w < kPatch / 32; w++) {
+    sst += red[w];
+    obt += cnt[w];
+  }
+  const double s = (obt > 0 && sst > 0.0) ? sqrt(sst / (3.0 * obt)) : 1.0;
+  const double inv = 1.0 / s;
+#pragma unroll
+  for (int c = 0; c < 3; c++) X[(size_t)p * kIn + c * kPatch + j] = bf16_rn((float)(zc[c] * inv));
+  if (j == 0) sig[p] = (float)s;
+}
+
+// z += s_p (f(u_p) - its patch mean) on observed pixels; Q/U stay 0 where
+// the pol mask applies (and do not enter their means there)
+__global__ void __launch_bounds__(kPatch)
+    k_patch_scatter(const float* __restrict__ Y, const float* __restrict__ sig,
+                    const int* __restrict__ idx, long long npix, const int* __restrict__ hits,
+                    double* z) {
+  __shared__ double red[kPatch / 32];
+  __shared__ int cnt[kPatch / 32];
+  const int p = blockIdx.x, j = threadIdx.x;
+  const int m = idx[(size_t)p * kPatch + j];
+  const bool pol = m >= 0 && hits[m] >= 2;
+  const double s = sig[p];
+  const float* y = Y + (size_t)p * kIn;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const bool on = (c == 0) ? (m >= 0) : pol;
+    double v = on ? (double)y[c * kPatch + j] : 0.0;
+    int k = on;
+    double vs = v;
+    for (int o = 16; o > 0; o >>= 1) {
+      vs += __shfl_xor_sync(0xffffffffu, vs, o);
+      k += __shfl_xor_sync(0xffffffffu, k, o);
+    }
+    if ((j & 31) == 0) {
+      red[j >> 5] = vs;
+      cnt[j >> 5] = k;
+    }
+    __syncthreads();
+    double tot = 0.0;
+    int kt = 0;
+    for (int w = 0; w < kPatch / 32; w++) {
+      tot += red[w];
+      kt += cnt[w];
+    }
+    __syncthreads();
+    if (on) z[c * npix + m] += s * (v - tot / kt);
+  }
+}
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+
+// unit-variance white Gaussian noise (Box-Muller on a counter-based hash)
+template <typename T>
+__global__ void k_white(T* out, long long n, uint64_t seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; 2 * i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t u = mix64(seed ^ mix64((uint64_t)i));
+    const float u1 = ((float)(u >> 40) + 0.5f) * (1.f / 16777216.f);
+    const float u2 = ((float)(u & 0xFFFFFF) + 0.5f) * (1.f / 16777216.f);
+    const float r = sqrtf(-2.f * logf(u1));
+    float sn, cs;
+    sincospif(2.f * u2, &sn, &cs);
+    out[2 * i] = (T)(r * cs);
+    if (2 * i + 1 < n) out[2 * i + 1] = (T)(r * sn);
+  }
+}
+
+template <typename T>
+__global__ void k_add(T* a, const T* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    a[i] += b[i];
+}
+
+// partial dots per block: [0] r.zf, [1] zf.az, [2] r.zb
+__global__ void __launch_bounds__(kT) k_dot3(const double* r, const double* zf, const double* az,
+                                             const double* zb, long long n, double* part) {
+  __shared__ double sh[3][kT / 32];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    a0 += r[i] * zf[i];
+    a1 += zf[i] * az[i];
+    a2 += r[i] * zb[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = a0;
+    sh[1][threadIdx.x >> 5] = a1;
+    sh[2][threadIdx.x >> 5] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; w++) t += sh[threadIdx.x][w];
+    part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// every block re-reduces the partials (fixed order); gz = dL/dz for
+// L = -a^2 / (b n): dL/dz = (-2 a r + 2 (a^2 / b) A z) / (b n)
+__global__ void __launch_bounds__(kT) k_cos_grad(const double* part, const double* r,
+                                                 const double* az, long long n3, double* gz,
+                                                 double* scal) {
+  __shared__ double tot[3];
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int i = 0; i < (int)gridDim.x; i++) t += part[threadIdx.x * gridDim.x + i];
+    tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+  const double a = tot[0], b = tot[1], nr = tot[2];
+  const bool ok = b > 0.0 && nr > 0.0;
+  const double c1 = ok ? -2.0 * a / (b * nr) : 0.0;
+  const double c2 = ok ? 2.0 * a * a / (b * b * nr) : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+       i += (long long)gridDim.x * blockDim.x)
+    gz[i] = c1 * r[i] + c2 * az[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = ok ? -a * a / (b * nr) : 0.0;
+}
+
+// transpose of k_patch_scatter: dL/dy = s_p (g - its mean over the applied slots)
+__global__ void __launch_bounds__(kPatch)
+    k_patch_grad(const double* __restrict__ gz, const float* __restrict__ sig,
+                 const int* __restrict__ idx, long long npix, const int* __restrict__ hits,
+                 float* dY) {
+  __shared__ double red[kPatch / 32];
+  __shared__ int cnt[kPatch / 32];
+  const int p = blockIdx.x, j = threadIdx.x;
+  const int m = idx[(size_t)p * kPatch + j];
+  const bool pol = m >= 0 && hits[m] >= 2;
+  const double s = sig[p];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const bool on = (c == 0) ? (m >= 0) : pol;
+    const double g = on ? gz[c * npix + m] : 0.0;
+    double gs = g;
+    int k = on;
+    for (int o = 16; o > 0; o >>= 1) {
+      gs += __shfl_xor_sync(0xffffffffu, gs, o);
+      k += __shfl_xor_sync(0xffffffffu, k, o);
+    }
+    if ((j & 31) == 0) {
+      red[j >> 5] = gs;
+      cnt[j >> 5] = k;
+    }
+    __syncthreads();
+    double tot = 0.0;
+    int kt = 0;
+    for (int w = 0; w < kPatch / 32; w++) {
+      tot += red[w];
+      kt += cnt[w];
+    }
+    __syncthreads();
+    dY[(size_t)p * kIn + c * kPatch + j] = on ? (float)(s * (g - tot / kt)) : 0.f;
+  }
+}
+
+int grid_for(long long n) {
+  const long long b = (n + kT - 1) / kT;
+  return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+}  // namespace
+
+// nested patches over the observed pixels; needs nside a power of two >= 16
+static int build_patches(sg_ctx* c) {
+  const long long nside = c->desc.nside;
+  if ((nside & (nside - 1)) != 0 || nside < 16)
+    return c->fail(SG_ERR_UNSUPPORTED, "learned preconditioner needs nside a power of two >= 16");
+  const long long nall = 12 * nside * nside / kPatch;
+  std::vector<int> full(nall * kPatch, -1);
+  for (long long m = 0; m < c->npix; m++) full[hp_ring2nest(nside, c->int2ring[m])] = (int)m;
+  std::vector<int> idx;
+  idx.reserve(full.size());
+  int np = 0;
+  for (long long p = 0; p < nall; p++) {
+    bool any = false;
+    for (int j = 0; j < kPatch && !any; j++) any = full[p * kPatch + j] >= 0;
+    if (!any) continue;
+    idx.insert(idx.end(), full.begin() + p * kPatch, full.begin() + (p + 1) * kPatch);
+    np++;
+  }
+  const int pad = (np + 127) / 128 * 128;
+  idx.resize((size_t)pad * kPatch, -1);
+  c->drop_graphs();  // learned iterations captured earlier point at the old geometry
+  cudaError_t e = c->patch_idx.alloc(sizeof(int) * idx.size());
+  if (e == cudaSuccess) e = c->patch_sig.alloc(sizeof(float) * pad);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->patch_idx.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return c->cuda_fail(e, "patch geometry");
+  c->npatch = np;
+  c->npatch_pad = pad;
+  return SG_OK;
+}
+
+}  // namespace sg
+
+// z = M_bj3 r + network correction (graph-capturable: no host sync)
+cudaError_t sg_ctx::learned_z() {
+  CgVecs vb = vecs(1);
+  cudaError_t e = apply_precond(vb, r.as<double>(), z.as<double>(), st);
+  if (e != cudaSuccess) return e;
+  k_patch_gather<<<npatch_pad, kPatch, 0, st>>>(z.as<double>(), patch_idx.as<int>(), npatch,
+                                               npix, mlp->x, patch_sig.as<float>());
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = mlp->forward(npatch_pad, st);
+  if (e != cudaSuccess) return e;
+  k_patch_scatter<<<npatch, kPatch, 0, st>>>(mlp->y, patch_sig.as<float>(), patch_idx.as<int>(),
+                                             npix, hits.as<int>(), z.as<double>());
+  launches += 3 + 8;  // precond, gather, scatter, 4 GEMMs + 4 bias/activation kernels
+  return cudaGetLastError();
+}
+
+namespace {
+
+// h_noise[k] = 1 / (ns^2 sqrt(h[k])): shapes unit white noise into noise whose
+// inverse spectrum is the detector's filter row (bin 0 takes bin 1's value,
+// since h[0] carries the reference's 1e-6 override)
+int make_noise_table(sg_ctx* c) {
+  const long long M = c->ns / 2;
+  const double ns2 = (double)c->ns * (double)c->ns;
+  std::vector<double> t(c->ndet * (M + 1));
+  for (long long d = 0; d < c->ndet; d++)
+    for (long long k = 0; k <= M; k++) {
+      const double hk = c->spn_h[d * (M + 1) + (k == 0 ? 1 : k)];
+      t[d * (M + 1) + k] = hk > 0.0 ? 1.0 / (ns2 * std::sqrt(hk)) : 0.0;
+    }
+  cudaError_t e = c->filt_noise.alloc(t.size() * c->esize);
+  if (e == cudaSuccess) {
+    if (c->f32) {
+      std::vector<float> f(t.begin(), t.end());
+      e = cudaMemcpy(c->filt_noise.p, f.data(), 4 * f.size(), cudaMemcpyHostToDevice);
+    } else {
+      e = cudaMemcpy(c->filt_noise.p, t.data(), 8 * t.size(), cudaMemcpyHostToDevice);
+    }
+  }
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "noise table");
+}
+
+// d = P sky + n for one seed, into tod_syn; b = P^T N^-1 d
+cudaError_t synth_rhs(sg_ctx* c, uint64_t seed) {
+  const long long npix = c->npix;
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<double> ni(0.0, 100e-6), nqu(0.0, 10e-6);
+  std::vector<double> sky(3 * npix);
+  for (long long m = 0; m < npix; m++) sky[m] = ni(rng);
+  for (long long m = npix; m < 3 * npix; m++) sky[m] = nqu(rng);
+  cudaError_t e = cudaMemcpyAsync(c->x.p, sky.data(), 8 * sky.size(), cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = c->to_map(c->x.as<double>());
+  if (e == cudaSuccess) e = c->launch_project();
+  if (e != cudaSuccess) return e;
+  const long long n = c->nsamp;
+  if (c->f32) {
+    k_white<float><<<grid_for(n / 2), kT, 0, c->st>>>(c->tod_syn.as<float>(), n, mix64(seed));
+  } else {
+    k_white<double><<<grid_for(n / 2), kT, 0, c->st>>>(c->tod_syn.as<double>(), n, mix64(seed));
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = c->launch_filter(kLoadTod, c->tod_syn.p, c->tod_syn.p, c->ntiles, (int)c->nseg, 0,
+                         nullptr, nullptr, c->filt_noise.p);
+  if (e != cudaSuccess) return e;
+  if (c->f32)
+    k_add<float><<<grid_for(n), kT, 0, c->st>>>(c->tod_syn.as<float>(), c->y.as<float>(), n);
+  else
+    k_add<double><<<grid_for(n), kT, 0, c->st>>>(c->tod_syn.as<double>(), c->y.as<double>(), n);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = c->launch_filter(kLoadTod, c->tod_syn.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+  if (e == cudaSuccess) e = c->pt_of_y(c->b.as<double>(), true);
+  return e;
+}
+
+}  // namespace
+
+namespace {
+
+struct ValSolve {
+  int iters = 0;
+  double ms = 0.0;
+  bool converged = false;
+};
+
+// PCG from x = 0 on the current b (block-Jacobi, or block-Jacobi + network),
+// timed with CUDA events on the context's stream
+cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
+  const long long n3 = 3 * c->npix;
+  CgVecs v1 = c->vecs(1), v2 = c->vecs(2);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t e = cudaMemsetAsync(c->x.p, 0, 8 * n3, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->r.p, 0, 8 * n3, c->st);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, c->st);
+  if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
+  if (pc == 2) {
+    if (e == cudaSuccess) e = c->learned_z();
+    if (e == cudaSuccess) e = cg_dots(v2, 0, c->st);
+    if (e == cudaSuccess)
+      e = c->f32 ? cg_reinit_d<float>(v2, c->dmap.as<float>(), c->st)
+                 : cg_reinit_d<double>(v2, c->dmap.as<double>(), c->st);
+  } else if (e == cudaSuccess) {
+    e = c->to_map(c->d.as<double>());
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  const double var00 = c->sc_host->var00;
+  int it = 0;
+  for (; it < 1000 && e == cudaSuccess; it++) {
+    e = c->run_iteration(pc, it % 10 == 0, false);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) break;
+    if (c->sc_host->var / var00 <= stop) {
+      out.converged = true;
+      it++;
+      break;
+    }
+    if (c->sc_host->flag) {
+      it++;
+      break;
+    }
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  out.iters = it;
+  out.ms = ms;
+  return e;
+}
+
+}  // namespace
+
+extern "C" long sg_learn_nparams(void) { return (long)mlp_nparams(); }
+
+extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report* rep) {
+  if (!c || !o) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  for (long long d = 0; d < c->ndet; d++)
+    if (!c->have_noise[d]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", d);
+  const int npairs = o->npairs > 0 ? o->npairs : 512;
+  const uint64_t seed0 = o->seed > 0 ? (uint64_t)o->seed : 5000;
+  const int steps = o->steps > 0 ? o->steps : 1500;
+  const float lr = o->lr > 0.f ? o->lr : 1e-3f;
+  const double pair_crit = o->pair_crit > 0.0 ? o->pair_crit : 1e-13;
+  cudaSetDevice(c->desc.device);
+  const double t0 = now_s();
+  int rc = build_bj3(c);
+  if (rc) return rc;
+  rc = build_patches(c);
+  if (rc) return rc;
+  rc = make_noise_table(c);
+  if (rc) return rc;
+  const long long npix = c->npix, n3 = 3 * npix;
+  DevBuf bank, rec_x, zb, zf, az, gz, dy, scal, part;
+  cudaError_t e = c->tod_syn.alloc((size_t)c->nsamp * c->esize);
+  if (e == cudaSuccess) e = bank.alloc((size_t)npairs * n3 * 8);
+  if (e != cudaSuccess) return c->cuda_fail(e, "training buffers");
+
+  // ---- residual/solution pairs from the plain block-Jacobi solver ----------
+  // (the residuals r_k of every iteration are kept; the solve to pair_crit
+  // defines which residuals occur)
+  c->use_syn = true;
+  CgVecs v = c->vecs(1);
+  int pairs = 0, skies = 0;
+  while (pairs < npairs && skies < 4 * npairs && e == cudaSuccess) {
+    e = synth_rhs(c, seed0 + skies);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->x.p, 0, 8 * n3, c->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->r.p, 0, 8 * n3, c->st);
+    if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v, c->st) : cg_init<double>(v, c->st);
+    if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) break;
+    const double var00 = c->sc_host->var00;
+    for (int it = 0; it < 400 && pairs < npairs; it++) {
+      e = c->run_iteration(1, it % 10 == 0, false);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bank.as<double>() + (size_t)pairs * n3, c->r.p, 8 * n3,
+                            cudaMemcpyDeviceToDevice, c->st);
+      pairs++;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost,
+                            c->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+      if (e != cudaSuccess) break;
+      if (c->sc_host->var / var00 <= pair_crit || c->sc_host->flag) break;
+    }
+    skies++;
+  }
+  c->use_syn = false;
+  c->have_rhs = false;
+  c->have_solution = false;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "training pairs");
+  const double t1 = now_s();
+
+  // ---- training: maximise the A-cosine of the corrected direction ------------
+  // For a residual r and z = M_bj3 r + correction, one CG step from r removes
+  // (r^T z)^2 / (z^T A z) of the squared A-norm error.  The loss
+  //   L = -(r^T z)^2 / ((z^T A z) (r^T M_bj3 r))
+  // is differentiated through the real operator A (one application per step).
+  c->drop_graphs();
+  c->mlp.reset(new Mlp());
+  Mlp& net = *c->mlp;
+  const int B = c->npatch_pad;
+  e = net.init(B, 4000, c->st);
+  if (e == cudaSuccess) e = zb.alloc(8 * n3);
+  if (e == cudaSuccess) e = zf.alloc(8 * n3);
+  if (e == cudaSuccess) e = az.alloc(8 * n3);
+  if (e == cudaSuccess) e = gz.alloc(8 * n3);
+  if (e == cudaSuccess) e = dy.alloc((size_t)B * kIn * 4);
+  if (e == cudaSuccess) e = scal.alloc(8 * 4);
+  if (e == cudaSuccess) e = part.alloc(8 * 3 * kCgBlocks);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dy.p, 0, (size_t)B * kIn * 4, c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "network init");
+  float loss_first = 0.f, loss_last = 0.f;
+  for (int s = 0; s < steps && e == cudaSuccess; s++) {
+    const long long k = (long long)(mix64(seed0 * 7919ULL + (uint64_t)s) % (uint64_t)pairs);
+    const double* r = bank.as<double>() + (size_t)k * n3;
+    e = apply_precond(v, r, zb.as<double>(), c->st);
+    if (e != cudaSuccess) break;
+    k_patch_gather<<<B, kPatch, 0, c->st>>>(zb.as<double>(), c->patch_idx.as<int>(), c->npatch,
+                                            npix, net.x, c->patch_sig.as<float>());
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = net.forward(B, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(zf.p, zb.p, 8 * n3, cudaMemcpyDeviceToDevice, c->st);
+    if (e != cudaSuccess) break;
+    k_patch_scatter<<<c->npatch, kPatch, 0, c->st>>>(net.y, c->patch_sig.as<float>(),
+                                                     c->patch_idx.as<int>(), npix,
+                                                     c->hits.as<int>(), zf.as<double>());
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = c->apply_dev(zf.as<double>(), az.as<double>(), true);
+    if (e != cudaSuccess) break;
+    k_dot3<<<kCgBlocks, kT, 0, c->st>>>(r, zf.as<double>(), az.as<double>(), zb.as<double>(), n3,
+                                        part.as<double>());
+    k_cos_grad<<<kCgBlocks, kT, 0, c->st>>>(part.as<double>(), r, az.as<double>(), n3,
+                                            gz.as<double>(), scal.as<double>());
+    k_patch_grad<<<c->npatch, kPatch, 0, c->st>>>(gz.as<double>(), c->patch_sig.as<float>(),
+                                                  c->patch_idx.as<int>(), npix,
+                                                  c->hits.as<int>(), dy.as<float>());
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = net.backward_dy(B, dy.as<float>(), c->st);
+    const float frac = (float)s / (float)steps;
+    const float lr_s = frac < 0.7f ? lr : lr * (1.f - 0.9f * (frac - 0.7f) / 0.3f);
+    if (e == cudaSuccess) e = net.adam(lr_s, c->st);
+    if (e == cudaSuccess && (s == 0 || s == steps - 1)) {
+      double l = 0.0;
+      e = cudaMemcpyAsync(&l, scal.p, 8, cudaMemcpyDeviceToHost, c->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+      (s == 0 ? loss_first : loss_last) = (float)l;
+    }
+  }
+  int gerr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&gerr, net.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return c->cuda_fail(e, "training");
+  if (gerr) return c->fail(SG_ERR_CUDA, "tensor-core GEMM pipeline timed out (code %d)", gerr);
+  const double t2 = now_s();
+  c->have_mlp = true;
+
+  // ---- validation: plain PCG judges the network on a held-out problem ------------
+  const double vcrit = o->val_crit > 0.0 ? o->val_crit : 1e-12;
+  ValSolve vp, vl;
+  c->use_syn = true;
+  e = synth_rhs(c, seed0 + 1000003);
+  if (e == cudaSuccess) e = val_solve(c, 1, vcrit, vp);
+  if (e == cudaSuccess) e = val_solve(c, 2, vcrit, vl);
+  c->use_syn = false;
+  c->tod_syn.release();
+  c->have_solution = false;
+  if (e != cudaSuccess) return c->cuda_fail(e, "validation");
+  c->learned_enabled = o->force != 0 || (vl.converged && vl.ms < vp.ms);
+  if (rep) {
+    rep->val_plain_iters = vp.iters;
+    rep->val_learned_iters = vl.iters;
+    rep->val_plain_ms = vp.ms;
+    rep->val_learned_ms = vl.ms;
+    rep->enabled = c->learned_enabled ? 1 : 0;
+  }
+  if (rep) {
+    rep->pairs = pairs;
+    rep->skies = skies;
+    rep->rows = (long)pairs * c->npatch;
+    rep->steps = steps;
+    rep->loss_first = loss_first;
+    rep->loss_last = loss_last;
+    rep->gen_seconds = t1 - t0;
+    rep->train_seconds = t2 - t1;
+    rep->gemm_tflop = (double)net.gemm_flops * 1e-12;
+  }
+  return SG_OK;
+}
+
+static int ensure_net(sg_ctx* c) {
+  if (c->mlp) return SG_OK;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  int rc = c->npatch_pad ? SG_OK : build_patches(c);
+  if (rc) return rc;
+  c->drop_graphs();
+  c->mlp.reset(new Mlp());
+  cudaError_t e = c->mlp->init(c->npatch_pad, 4000, c->st);
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "network init");
+}
+
+extern "C" int sg_learn_get_params(sg_ctx* c, float* params) {
+  if (!c || !params) return SG_ERR_ARG;
+  if (!c->have_mlp) return c->fail(SG_ERR_STATE, "no trained network");
+  cudaSetDevice(c->desc.device);
+  cudaError_t e = cudaMemcpy(params, c->mlp->w32, 4 * mlp_nparams(), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "get params");
+}
+
+extern "C" int sg_learn_set_params(sg_ctx* c, const float* params) {
+  if (!c || !params) return SG_ERR_ARG;
+  cudaSetDevice(c->desc.device);
+  int rc = ensure_net(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->mlp->w32, params, 4 * mlp_nparams(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = c->mlp->sync_weights(c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return c->cuda_fail(e, "set params");
+  c->have_mlp = true;
+  c->learned_enabled = true;  // an explicitly loaded network is used as given
+  return SG_OK;
+}
+
+int ensure_patches(sg_ctx* c) {
+  if (c->npatch_pad) return SG_OK;
+  return build_patches(c);
+}
+
+// ---- host-array entry points for tests and measurements --------------------------
+extern "C" int sg_mlp_gemm_host(const unsigned short* A, const unsigned short* B, float* C, int M,
+                                int N, int K, int reps, double* ms) {
+  if (!A || !B || !C || !gemm_shape_ok(M, N, K)) return SG_ERR_ARG;
+  DevBuf da, db, dc, derr;
+  cudaError_t e = da.alloc((size_t)M * K * 2);
+  if (e == cudaSuccess) e = db.alloc((size_t)N * K * 2);
+  if (e == cudaSuccess) e = dc.alloc((size_t)M * N * 4);
+  if (e == cudaSuccess) e = derr.alloc(sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(da.p, A, (size_t)M * K * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db.p, B, (size_t)N * K * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr.p, 0, sizeof(int));
+  if (e == cudaSuccess) e = gemm_bf16(da.p, db.p, dc.as<float>(), M, N, K, 0, derr.as<int>(), 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && reps > 0 && ms) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, 0);
+    for (int i = 0; i < reps && e == cudaSuccess; i++)
+      e = gemm_bf16(da.p, db.p, dc.as<float>(), M, N, K, 0, derr.as<int>(), 0);
+    cudaEventRecord(e1, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t / reps;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(C, dc.p, (size_t)M * N * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return SG_ERR_CUDA;
+  return herr ? SG_ERR_CUDA : SG_OK;
+}
+
+extern "C" int sg_mlp_grad_host(const float* params, const float* X, const float* T, int B,
+                                float* Y, float* loss, float* grads) {
+  if (!params || !X || !T || B <= 0 || B % 128) return SG_ERR_ARG;
+  Mlp net;
+  cudaStream_t st = 0;
+  const long long np = mlp_nparams();
+  DevBuf dx, dt;
+  cudaError_t e = net.init(B, 1, st);
+  if (e == cudaSuccess) e = dx.alloc((size_t)B * kIn * 4);
+  if (e == cudaSuccess) e = dt.alloc((size_t)B * kIn * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(net.w32, params, 4 * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = net.sync_weights(st);
+  if (e == cudaSuccess) e = cudaMemcpy(dx.p, X, (size_t)B * kIn * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dt.p, T, (size_t)B * kIn * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = f32_to_bf16(dx.as<float>(), net.x, (long long)B * kIn, st);
+  if (e == cudaSuccess) e = net.forward(B, st);
+  if (e == cudaSuccess && Y) e = cudaMemcpy(Y, net.y, (size_t)B * kIn * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = net.backward(B, dt.as<float>(), st);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, net.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && loss) e = cudaMemcpy(loss, net.loss, 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && grads) e = cudaMemcpy(grads, net.g, 4 * np, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return SG_ERR_CUDA;
+  return herr ? SG_ERR_CUDA : SG_OK;
+}
