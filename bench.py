@@ -1,22 +1,29 @@
 #!/usr/bin/env python3
-"""Benchmark: time-to-solution of the GLS map-making PCG on one GB300.
+"""Benchmark: time-to-solution of the GLS map-making PCG on one GB300,
+learned-preconditioned (flexible PCG) against plain block-Jacobi PCG.
 
 Workload (default): 64 detectors, NSIDE 256, 48 segments x 131,072 samples
 (4.03e8 samples), FP32 operator with FP64 P^T sums and CG scalars, seeded
 synthetic scan/sky/1-over-f noise (sanepic_gb300.synth).  One step = one
 solve from x0 = 0 to |r|/|b| <= 1e-6 (crit = |r|^2/|b|^2 <= 1e-12):
-  value: b = P^T N^-1 d plus the PCG, inputs already resident in HBM,
-         CUDA-event time on the library's stream (the bench's torch stream);
-  e2e:   the same through the C ABI from host buffers: pointing, noise and
+  value: b = P^T N^-1 d plus the PCG in the learned-preconditioner mode,
+         inputs already resident in HBM, CUDA-event time on the library's
+         stream (the bench's torch stream).  The network is trained and
+         judged by plain PCG before the timed region (training time is
+         reported, not timed); if it lost on its held-out validation problem
+         the learned mode runs plain block-Jacobi PCG and the line says so;
+  plain: the same steps with plain block-Jacobi PCG;
+  e2e:   a solve through the C ABI from host buffers: pointing, noise and
          TOD uploaded (host->device) every step, maps read back.
-The dominant kernel (noise filter with the fused projection P) is timed live
-with CUDA events for the roofline; its algorithmic bytes are 16 B/sample
-(int32 pixel + 2 x FP32 cos/sin in, FP32 out) plus the map and filter rows.
+The operator kernels (P, the noise filter, the per-group detector sums, P^T)
+are timed live with CUDA events for the roofline against their algorithmic
+bytes; the network's tensor-core GEMM is timed against the measured BF16 peak.
 
 --impl reference times the reference's CPU algorithm on the host cores: the
 oracle port (the FP64 restatement of sanepic.cc's operator, same operation
 order), one process per core as the reference's MPI workers, on a bounded
-sample of the workload, projected linearly in samples to the full problem.
+sample of the workload, projected linearly in samples to the full problem and
+to the iterations the reference's diagonal-preconditioned PCG needs.
 (The reference binary itself is built only where its source is available; the
 GPU host has neither the source nor an x86 CPU.)
 """
@@ -41,9 +48,11 @@ from sanepic_gb300 import synth  # noqa: E402
 METRIC = "time-to-solution at rel. residual 1e-6: learned-precond vs plain PCG, 1 GB300"
 STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
 # Iterations the reference's own preconditioner (the scalar diagonal,
-# sanepic.cc:1351-1355) needs to reach |r|/|b| = 1e-6 on this workload,
-# measured with the library's reference-diagonal mode (same algorithm).
-REFERENCE_ITERS_TO_1E6 = None
+# sanepic.cc:1351-1355) needs to reach |r|/|b| = 1e-6 on the default workload
+# (64 detectors, NSIDE 256, 48 x 131072 samples), measured on a GB300 with the
+# library's reference-diagonal mode, the same algorithm (bench.py
+# --compare-diag: 24 iterations; block-Jacobi needs 21).
+REFERENCE_ITERS_TO_1E6 = {"c2_64det_nside256": 24}
 
 
 def peaks():
@@ -53,6 +62,14 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -148,27 +165,41 @@ def run_ours(args):
         mm.rhs()
         return mm.solve(precond=precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
 
-    # ---- value: inputs resident, CUDA events on the launching stream -------
-    for _ in range(args.warmup):
-        device_step(args.precond)
-    barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps, launches = [], 0
-    with ClockSampler(local) as clk:
+    # ---- the learned preconditioner: trained and judged before timing --------
+    learn = None
+    precond = args.precond
+    if not args.no_learn:
+        tl = time.time()
+        learn = mm.learn_train(npairs=args.learn_pairs, steps=args.learn_steps)
+        learn["wall_seconds"] = time.time() - tl
+        precond = "learned"
+
+    def timed(pc, clk=None):
+        for _ in range(args.warmup):
+            device_step(pc)
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps, launches = [], 0
         ev0.record(stream)
         for _ in range(args.steps):
-            rep = device_step(args.precond)
+            rep = device_step(pc)
             reps.append(rep)
             launches += rep["kernel_launches"] + 2  # + filter and P^T of the RHS
         ev1.record(stream)
         barrier()
-    ms_step = ev0.elapsed_time(ev1) / args.steps
+        sec = ev0.elapsed_time(ev1) / args.steps / 1e3
+        if world > 1:
+            t = torch.tensor([sec], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            sec = float(t.item())
+        return sec, reps, launches
+
+    # ---- value: inputs resident, CUDA events on the launching stream -------
+    with ClockSampler(local) as clk:
+        sec, reps, launches = timed(precond)
+        if learn is not None:
+            sec_plain, reps_plain, _ = timed(args.precond)
     clocks = clk.summary()
-    sec = ms_step / 1e3
-    if world > 1:
-        t = torch.tensor([sec], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec = float(t.item())
     iters = reps[-1]["iterations"]
     # ---- roofline of the dominant kernel (same stream, live) -----------------
     prof = mm.profile_operator(reps=5)
@@ -210,7 +241,7 @@ def run_ours(args):
         barrier()
         te = time.perf_counter()
         upload(mm)
-        device_step(args.precond)
+        device_step(precond)
         maps = [mm.get_map(k) for k in ("I", "Q", "U")]
         barrier()
         e2e.append(time.perf_counter() - te)
@@ -236,15 +267,59 @@ def run_ours(args):
         "generation_s": gen_s,
     }
     line.update(extra)
+    if learn is not None:
+        line["config"]["precond"] = "learned (flexible PCG, judged by block-Jacobi PCG)"
+        line["learned"] = {
+            "plain_pcg_s": sec_plain, "plain_iterations": reps_plain[-1]["iterations"],
+            "learned_iterations": iters,
+            "network_used": bool(learn["enabled"]),
+            "fell_back_at_iteration": reps[-1]["fallback_iter"],
+            "validation": {"plain_iterations": learn["val_plain_iters"],
+                           "learned_iterations": learn["val_learned_iters"],
+                           "plain_ms": learn["val_plain_ms"],
+                           "learned_ms": learn["val_learned_ms"]},
+            "training": {"pairs": learn["pairs"], "skies": learn["skies"],
+                         "steps": learn["steps"], "loss_first": learn["loss_first"],
+                         "loss_last": learn["loss_last"],
+                         "pair_generation_s": learn["gen_seconds"],
+                         "train_s": learn["train_seconds"],
+                         "tensor_core_tflop": learn["gemm_tflop"],
+                         "loss": "-(r.z)^2/((z.Az)(r.M r)), A-cosine of the corrected direction"},
+        }
+        line["mlp_gemm"] = mlp_gemm_roofline(sg, mm)
     if not args.no_cpu_baseline and rank == 0:
         line["cpu_baseline"] = reference_cpu(
             args, spec, iters_for_projection=extra.get("diag_precond", {}).get("iterations")
-            or REFERENCE_ITERS_TO_1E6)
+            or REFERENCE_ITERS_TO_1E6.get(args.config))
     if rank == 0:
         print(json.dumps(line), flush=True)
     mm.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def mlp_gemm_roofline(sg, mm):
+    """Tensor-core throughput of the network's GEMM (tcgen05, BF16 in, FP32
+    accumulate) on the inference shape of this workload and a large training
+    shape, CUDA-event timed, against the measured BF16 peak."""
+    peak, kind = bf16_peak()
+
+    def bf16_bits(a):  # round to nearest even, upper 16 bits of FP32
+        u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+        return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+    rows = -(-mm.npix // 256)
+    rows = max(128, -(-rows // 128) * 128)
+    out = {"peak_tflops": peak, "peak_kind": kind, "shapes": []}
+    rng = np.random.default_rng(0)
+    for M, N, K in ((rows, 256, 768), (8192, 768, 8192)):
+        A = bf16_bits(rng.standard_normal((M, K)))
+        B = bf16_bits(rng.standard_normal((N, K)))
+        _, ms = sg.gemm_bf16(A, B, reps=20)
+        tf = 2.0 * M * N * K / (ms * 1e-3) / 1e12
+        out["shapes"].append({"M": M, "N": N, "K": K, "ms": ms, "tflops": tf,
+                              "frac": tf / peak})
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -301,7 +376,8 @@ def run_reference(args):
     if rank != 0:
         return
     spec = synth.spec_from_name(args.config)
-    cb = reference_cpu(args, spec, iters_for_projection=REFERENCE_ITERS_TO_1E6 or args.ref_iters)
+    cb = reference_cpu(args, spec,
+                       iters_for_projection=args.ref_iters or REFERENCE_ITERS_TO_1E6.get(args.config))
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cb["value"] * 1e3 if cb["value"] else None,
@@ -328,6 +404,9 @@ def main():
     ap.add_argument("--compare-diag", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-iters", type=int, default=None)
+    ap.add_argument("--no-learn", action="store_true")
+    ap.add_argument("--learn-pairs", type=int, default=512)
+    ap.add_argument("--learn-steps", type=int, default=1500)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
