@@ -53,6 +53,10 @@ STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
 # library's reference-diagonal mode, the same algorithm (bench.py
 # --compare-diag: 24 iterations; block-Jacobi needs 21).
 REFERENCE_ITERS_TO_1E6 = {"c2_64det_nside256": 24}
+# DRAM bytes (read + write) of one noise-filter tile of 131072 FP32 samples,
+# from the ncu capture in profiles/noise_filter_c2_8det.md (343.7 MB over
+# 384 tiles); traffic grows with the tiles, so a full launch is this x tiles.
+FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 343.67e6 / 384
 
 
 def peaks():
@@ -224,6 +228,9 @@ def run_ours(args):
                    "bytes": kbytes[k]} for k in kbytes}
     dom = max(kms, key=kms.get)
     achieved = kernels[dom]["GBps"]
+    traffic = None
+    if dom == "k_noise_filter" and spec.ns == 131072 and spec.precision == "f32":
+        traffic = FILTER_DRAM_BYTES_PER_TILE_131072_F32 * spec.ndet * spec.nseg
     # ---- plain block-Jacobi vs the reference's diagonal (same workload) -------
     extra = {}
     if args.compare_diag:
@@ -260,7 +267,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "kernel": dom,
+                     "frac": achieved / hbm, "traffic": traffic, "kernel": dom,
                      "peak_kind": peak_kind, "kernels": kernels},
         "clocks": clocks,
         "iter_per_sec": reps[-1]["iter_per_sec"],
