@@ -14,6 +14,7 @@
 #include "mpi.h"
 
 #include <errno.h>
+#include <sched.h>
 #include <signal.h>
 #include <stdio.h>
 #include <stdlib.h>

@@ -206,12 +206,37 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
 
   const int cluster_id = blockIdx.x / S;
   const int nclusters = gridDim.x / S;
+  // 16-byte global accesses: FP32, even column count per CTA, whole pairs per
+  // thread, and every timeline pointer 16-byte aligned (callers may pass
+  // offset pointers; then the 8-byte path runs)
+  const bool kVec = sizeof(T) == 4 && Cs % 2 == 0 && (E / 2) % NT == 0 &&
+                    ((reinterpret_cast<uintptr_t>(p.tod) | reinterpret_cast<uintptr_t>(p.sub) |
+                      reinterpret_cast<uintptr_t>(p.out)) & 15) == 0;
   double chi2 = 0.0;  // sum of h[k] |X[k]|^2 over this thread's bins
   for (long long tile = cluster_id; tile < p.ntiles; tile += nclusters) {
     const long long base = tile * (long long)(2 * M);
     const int det = (int)(tile / p.nseg);
     const T* h = p.filt + (long long)det * (M + 1);
     // ---- 1. load: z[C n1 + n2] = x[2n] + i x[2n+1], this CTA's columns ----
+    // FP32 timelines on 16-byte aligned buffers: two columns per 16-byte load
+    if (kVec && (p.mode == kLoadTod || p.mode == kLoadTodMinus)) {
+#pragma unroll 8
+      for (int it = 0; it < E / 2 / NT; it++) {
+        const int e2 = it * NT + tid;
+        const int c = 2 * (e2 % (Cs / 2)), n1 = e2 / (Cs / 2);
+        const long long s0 = base + 2LL * (C * n1 + j * Cs + c);
+        float4 v = *reinterpret_cast<const float4*>(p.tod + s0);
+        if (p.mode == kLoadTodMinus) {
+          const float4 w = *reinterpret_cast<const float4*>(p.sub + s0);
+          v.x -= w.x;
+          v.y -= w.y;
+          v.z -= w.z;
+          v.w -= w.w;
+        }
+        buf[n1 * PA + c] = cplx<T>{(T)v.x, (T)v.y};
+        buf[n1 * PA + c + 1] = cplx<T>{(T)v.z, (T)v.w};
+      }
+    } else
 #pragma unroll 16
     for (int it = 0; it < G::XE; it++) {
       const int e = it * NT + tid;
@@ -482,6 +507,16 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         });
     __syncthreads();
     // ---- 11. store -------------------------------------------------------------
+    if (kVec) {
+#pragma unroll 8
+      for (int it = 0; it < E / 2 / NT; it++) {
+        const int e2 = it * NT + tid;
+        const int c = 2 * (e2 % (Cs / 2)), n1 = e2 / (Cs / 2);
+        const long long s0 = base + 2LL * (C * n1 + j * Cs + c);
+        const cplx<T> a = buf[n1 * PA + c], b = buf[n1 * PA + c + 1];
+        *reinterpret_cast<float4*>(p.out + s0) = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+      }
+    } else
 #pragma unroll 16
     for (int it = 0; it < G::XE; it++) {
       const int e = it * NT + tid;
