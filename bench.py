@@ -329,6 +329,100 @@ def mlp_gemm_roofline(sg, mm):
     return out
 
 
+def run_batch(args):
+    """32 uneven independent problems (synth.batch_specs): every problem's
+    operator autotuned, then all solved together (sg_solve_batch: one CUDA
+    stream and captured iteration graphs per problem) and, for comparison,
+    one after another.  value = time until every problem reaches
+    |r|/|b| <= 1e-6; per-problem iterations and device times are reported."""
+    import torch
+
+    import sanepic_gb300 as sg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    specs = synth.batch_specs(32)
+    t0 = time.time()
+    makers = []
+    for sp in specs:
+        prob = synth.make_problem(sp)
+        mm = sg.from_problem(prob, precision="f32", device=local)
+        mm.rhs()
+        makers.append(mm)
+        del prob
+    gen_s = time.time() - t0
+    tunes = [mm.autotune() for mm in makers]
+    # the learned mode: one network trained (and judged) on the largest NSIDE-256 problem
+    learn = None
+    if not args.no_learn:
+        cand = [i for i, sp in enumerate(specs) if sp.nside == 256] or list(range(len(specs)))
+        big = max(cand, key=lambda i: specs[i].ndet * specs[i].nseg * specs[i].ns)
+        learn = makers[big].learn_train(npairs=args.learn_pairs, steps=args.learn_steps)
+        makers[big].rhs()
+        if learn["enabled"]:
+            params = makers[big].learn_params()
+            for i, mm in enumerate(makers):
+                if i != big:
+                    mm.set_learn_params(params)
+
+    def batch(precond):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        reps = sg.solve_batch(makers, precond=precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, reps
+
+    for _ in range(args.warmup):
+        batch(args.precond)
+    times, reps = [], None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, reps = batch(args.precond)
+            times.append(t)
+    clocks = clk.summary()
+    value = float(np.median(times))
+    # one after another (each solve alone on the GPU)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    seq = [mm.solve(precond=args.precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+           for mm in makers]
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t
+    learned = None
+    if learn is not None:
+        if learn["enabled"]:
+            lt, lreps = batch("learned")
+            learned = {"batch_s": lt, "iterations": [r["iterations"] for r in lreps]}
+        else:
+            learned = {"network_used": False,
+                       "reason": "plain PCG judged the network slower on its held-out problem",
+                       "validation": {"plain_iterations": learn["val_plain_iters"],
+                                      "learned_iterations": learn["val_learned_iters"]}}
+    samples = sum(sp.ndet * sp.nseg * sp.ns for sp in specs)
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scan, iid sky, 1/f noise), 32 uneven problems",
+        "config": {"workload": "batch32_uneven", "problems": len(specs), "samples": samples,
+                   "precond": args.precond, "stop": "|r|/|b| <= 1e-6",
+                   "solve": "concurrent: one stream + captured graphs per problem"},
+        "sequential_s": seq_s,
+        "problems": [{"name": sp.name, "iterations": r["iterations"],
+                      "device_s": r["device_seconds"], "converged": bool(r["converged"]),
+                      "alone_s": q["device_seconds"], "cluster_size": tu["cluster_size"]}
+                     for sp, r, q, tu in zip(specs, reps, seq, tunes)],
+        "gpu_launches": int(sum(r["kernel_launches"] for r in reps)),
+        "clocks": clocks, "generation_s": gen_s,
+    }
+    if learned is not None:
+        line["learned"] = learned
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for mm in makers:
+        mm.close()
+
+
 # ---------------------------------------------------------------------------
 def _port_worker(task):
     """One host core of the CPU baseline: the oracle port's operator (the
@@ -417,6 +511,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "batch32":
+        run_batch(args)
     else:
         run_ours(args)
 

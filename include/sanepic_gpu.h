@@ -224,6 +224,20 @@ int sg_mlp_grad_host(const float *params, const float *X, const float *T, int B,
 /* Preconditioned CG (sanepic.cc:1177-1761). */
 int sg_solve(sg_ctx *ctx, const sg_solve_opts *opts, sg_report *report);
 
+/* Solves n independent problems (contexts, each after sg_rhs) at once: every
+ * context iterates on its own CUDA stream from captured iteration graphs and
+ * the host advances each as its last iteration finishes, so problems too small
+ * to fill the GPU share it.  Same options for all (x0 must be NULL);
+ * reports[i] as sg_solve's.  No reference counterpart (one problem per run). */
+int sg_solve_batch(sg_ctx **ctxs, int n, const sg_solve_opts *opts, sg_report *reports);
+
+/* Times this context's noise filter with each compiled tile shape for its
+ * segment length (FP32 tiles of 2^14..2^17 samples: 8192 or 4096 complex
+ * points per CTA of the thread-block cluster) on its own timeline and keeps
+ * the faster; *cluster_size and *ms (may be NULL) receive the choice and its
+ * time per launch.  No reference counterpart. */
+int sg_autotune(sg_ctx *ctx, int *cluster_size, double *ms);
+
 /* A full 12*nside^2 RING map (write_reduced_map, sanepic.cc:2364-2388). */
 int sg_get_map(sg_ctx *ctx, int kind, double *out_full);
 

@@ -36,7 +36,8 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
-           "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_last_error", "sg_destroy"]
+           "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch", "sg_autotune",
+           "sg_last_error", "sg_destroy"]
 
 
 class SanepicError(RuntimeError):
@@ -137,6 +138,9 @@ def load_library(path: Optional[str] = None):
     L.sg_mlp_gemm_host.argtypes = [ctypes.POINTER(ctypes.c_ushort), ctypes.POINTER(ctypes.c_ushort),
                                    fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     L.sg_mlp_grad_host.argtypes = [fp, fp, fp, ctypes.c_int, fp, fp, fp]
+    L.sg_solve_batch.argtypes = [ctypes.POINTER(c_p), ctypes.c_int, ctypes.POINTER(SgSolveOpts),
+                                 ctypes.POINTER(SgReport)]
+    L.sg_autotune.argtypes = [c_p, ctypes.POINTER(ctypes.c_int), dp]
     L.sg_last_error.argtypes = [c_p]
     L.sg_last_error.restype = ctypes.c_char_p
     L.sg_destroy.argtypes = [c_p]
@@ -279,6 +283,13 @@ class MapMaker:
         self._check(self.L.sg_get_indpix(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
         return out
 
+    def autotune(self) -> dict:
+        """Pick the faster compiled FFT tile shape for this problem's noise filter."""
+        S = ctypes.c_int(0)
+        ms = ctypes.c_double(0.0)
+        self._check(self.L.sg_autotune(self.h, ctypes.byref(S), ctypes.byref(ms)))
+        return {"cluster_size": S.value, "filter_ms": ms.value}
+
     # ---- learned preconditioner ---------------------------------------------
     def learn_train(self, npairs: int = 512, seed: int = 5000, steps: int = 1500,
                     batch: int = 0, lr: float = 1e-3, pair_crit: float = 1e-13,
@@ -384,3 +395,19 @@ def mlp_grad(params: np.ndarray, X: np.ndarray, T: np.ndarray):
     if rc:
         raise SanepicError(rc, "sg_mlp_grad_host failed")
     return Y, float(loss.value), g
+
+
+def solve_batch(makers, precond: str = "bj3", stop_crit: float = 1e-15, maxiter: int = 2000,
+                refresh_every: int = 10, use_graph: bool = True) -> list:
+    """Solve several MapMakers (each after rhs()) concurrently, one CUDA stream
+    each; returns one report dict per problem (as MapMaker.solve)."""
+    L = load_library()
+    n = len(makers)
+    hs = (ctypes.c_void_p * n)(*[m.h.value for m in makers])
+    o = SgSolveOpts(PRECOND[precond], stop_crit, maxiter, refresh_every, 0, None,
+                    int(use_graph), ITER_CB(), None)
+    reps = (SgReport * n)()
+    rc = L.sg_solve_batch(hs, n, ctypes.byref(o), reps)
+    if rc:
+        raise SanepicError(rc, L.sg_last_error(makers[0].h).decode())
+    return [{k: getattr(r, k) for k, _ in SgReport._fields_} for r in reps]

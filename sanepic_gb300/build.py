@@ -32,6 +32,7 @@ UNITS = {
     "sg_gemm.cu": [],
     "sg_mlp.cu": [],
     "sg_learn.cu": [],
+    "sg_batch.cu": [],
     "sg_pointing.cu": ["--fmad=false"],
 }
 LIB = os.path.join(LIBDIR, "libsanepic_gpu.so")

@@ -563,7 +563,7 @@ int build_bj3(sg_ctx* c) {
 }
 
 // The reference's diagonal (also needed for the NVAR outputs).
-static int build_diag(sg_ctx* c) {
+int build_diag(sg_ctx* c) {
   if (c->have_diag) return SG_OK;
   cudaError_t e;
   const long long ns = c->ns, npix = c->npix;

@@ -1,0 +1,242 @@
+// sg_batch.cu -- many independent map-making problems at once, and the FFT
+// tile-shape autotuner (no reference counterpart: the reference solves one
+// problem per run).
+//
+// sg_solve_batch runs the PCG of every context concurrently: each context
+// iterates on its own CUDA stream, one captured graph launch per iteration,
+// and a host loop advances each problem as soon as its previous iteration has
+// finished (an event per context, no device-wide synchronisation).  Small
+// problems, whose kernels cannot fill 152 SMs, then share the GPU, and a
+// problem that converges early stops consuming it.
+//
+// sg_autotune times the noise filter of a context with each compiled tile
+// shape for its segment length (FP32: 8192 or 4096 complex points per CTA of
+// the cluster) on the context's own timeline and keeps the faster one.
+#include <cuda_runtime.h>
+
+#include <thread>
+#include <vector>
+
+#include "sg_ctx.h"
+#include "sg_kernels.h"
+
+extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
+  if (!c) return SG_ERR_ARG;
+  cudaSetDevice(c->desc.device);
+  const long long M = c->ns / 2;
+  std::vector<int> cand;
+  const long long e1 = c->f32 ? 8192 : 4096;
+  for (long long emax : {e1, e1 / 2}) {
+    const int S = (int)std::max<long long>(1, M / emax);
+    const int ncl = c->f32 ? filter_max_clusters<float>(c->logm, S)
+                           : filter_max_clusters<double>(c->logm, S);
+    if (ncl > 0 && (cand.empty() || cand.back() != S)) cand.push_back(S);
+  }
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int S0 = c->S, n0 = c->nclusters;
+  int bestS = S0;
+  double best = 1e30;
+  cudaError_t e = cudaSuccess;
+  for (int S : cand) {
+    c->S = S;
+    c->nclusters = c->f32 ? filter_max_clusters<float>(c->logm, S)
+                          : filter_max_clusters<double>(c->logm, S);
+    for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {  // first launch warms up
+      if (rep == 1) e = cudaEventRecord(a, c->st);
+      if (e == cudaSuccess) e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b, c->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float t = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&t, a, b);
+    if (e == cudaSuccess && t / 3.0 < best) {
+      best = t / 3.0;
+      bestS = S;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  c->S = bestS;
+  c->nclusters = c->f32 ? filter_max_clusters<float>(c->logm, bestS)
+                        : filter_max_clusters<double>(c->logm, bestS);
+  if (e == cudaSuccess && (bestS != S0 || c->nclusters != n0)) {
+    e = c->chi2p.alloc(sizeof(double) * c->S * c->nclusters);
+    c->drop_graphs();  // captured iterations hold the old launch shape
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "autotune");
+  if (cluster_size) *cluster_size = c->S;
+  if (ms) *ms = best;
+  return SG_OK;
+}
+
+namespace {
+
+struct Job {
+  sg_ctx* c = nullptr;
+  int pc = 1, iter = 0, fallback = -1;
+  bool started = false, pending = false, done = false;
+  double var00 = 0.0, crit = 0.0, t_done = 0.0;
+  long long launches0 = 0;
+  cudaEvent_t ready = nullptr;
+};
+
+// enqueue a solve start from x = 0 (r = 0 -> r = b) for precond pc
+cudaError_t enqueue_start(sg_ctx* c, int pc) {
+  const size_t vb = sizeof(double) * 3 * c->npix;
+  cudaError_t e = cudaMemsetAsync(c->x.p, 0, vb, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->r.p, 0, vb, c->st);
+  CgVecs v = c->vecs(pc == 2 ? 1 : pc);
+  if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v, c->st) : cg_init<double>(v, c->st);
+  c->launches += 2;
+  if (pc == 2) {
+    CgVecs v2 = c->vecs(2);
+    if (e == cudaSuccess) e = c->learned_z();
+    if (e == cudaSuccess) e = cg_dots(v2, 0, c->st);
+    if (e == cudaSuccess)
+      e = c->f32 ? cg_reinit_d<float>(v2, c->dmap.as<float>(), c->st)
+                 : cg_reinit_d<double>(v2, c->dmap.as<double>(), c->st);
+    c->launches += 2;
+  } else if (e == cudaSuccess) {
+    e = c->to_map(c->d.as<double>());
+  }
+  return e;
+}
+
+cudaError_t enqueue_scalars(Job& j) {
+  sg_ctx* c = j.c;
+  cudaError_t e =
+      cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaEventRecord(j.ready, c->st);
+  j.pending = e == cudaSuccess;
+  return e;
+}
+
+}  // namespace
+
+extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_report* reports) {
+  if (!ctxs || n <= 0 || !o) return SG_ERR_ARG;
+  if (o->x0) return SG_ERR_ARG;  // every batch solve starts from x = 0
+  std::vector<Job> jobs(n);
+  for (int i = 0; i < n; i++) {
+    sg_ctx* c = ctxs[i];
+    if (!c) return SG_ERR_ARG;
+    if (!c->have_rhs) return c->fail(SG_ERR_STATE, "call sg_rhs before sg_solve_batch");
+    if (o->precond == SG_PRECOND_LEARNED && !c->have_mlp)
+      return c->fail(SG_ERR_STATE, "no trained network");
+    cudaSetDevice(c->desc.device);
+    int rc = (o->precond == SG_PRECOND_DIAG) ? build_diag(c) : build_bj3(c);
+    if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED) rc = ensure_patches(c);
+    if (rc) return rc;
+    Job& j = jobs[i];
+    j.c = c;
+    j.pc = (o->precond == SG_PRECOND_BJ3) ? 1 : (o->precond == SG_PRECOND_DIAG ? 0 : 2);
+    if (j.pc == 2 && !c->learned_enabled) {
+      j.pc = 1;
+      j.fallback = 0;
+    }
+    cudaEventCreateWithFlags(&j.ready, cudaEventDisableTiming);
+    if (!c->ev0) cudaEventCreate(&c->ev0);
+    if (!c->ev1) cudaEventCreate(&c->ev1);
+    c->crit_hist.clear();
+    j.launches0 = c->launches;
+  }
+  const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
+  const int maxiter = o->maxiter > 0 ? o->maxiter : 2000;
+  const double t0 = now_s();
+  cudaError_t e = cudaSuccess;
+  int failed = -1;
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    sg_ctx* c = jobs[i].c;
+    cudaSetDevice(c->desc.device);
+    e = cudaEventRecord(c->ev0, c->st);
+    if (e == cudaSuccess) e = enqueue_start(c, jobs[i].pc);
+    if (e == cudaSuccess) e = enqueue_scalars(jobs[i]);
+    if (e != cudaSuccess) failed = i;
+  }
+  int active = n;
+  while (active > 0 && e == cudaSuccess) {
+    bool progressed = false;
+    for (int i = 0; i < n && e == cudaSuccess; i++) {
+      Job& j = jobs[i];
+      if (j.done || !j.pending) continue;
+      const cudaError_t q = cudaEventQuery(j.ready);
+      if (q == cudaErrorNotReady) continue;
+      if (q != cudaSuccess) {
+        e = q;
+        failed = i;
+        break;
+      }
+      progressed = true;
+      j.pending = false;
+      sg_ctx* c = j.c;
+      cudaSetDevice(c->desc.device);
+      if (!j.started) {
+        j.started = true;
+        j.var00 = c->sc_host->var00;
+        j.crit = c->sc_host->var / j.var00;
+      } else {
+        j.crit = c->sc_host->var / j.var00;
+        c->crit_hist.push_back(j.crit);
+        j.iter++;
+        const bool stop = j.crit <= o->stop_crit || j.iter >= maxiter;
+        if (!stop && c->sc_host->flag && j.pc == 2) {
+          // the network broke flexible PCG: restart with block-Jacobi
+          j.fallback = j.iter;
+          j.pc = 1;
+          CgVecs v1 = c->vecs(1);
+          e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
+          if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
+          if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
+          c->launches += 7;
+          if (e == cudaSuccess) e = enqueue_scalars(j);
+          if (e != cudaSuccess) failed = i;
+          continue;
+        }
+        if (stop || c->sc_host->flag) {
+          j.done = true;
+          j.t_done = now_s();
+          e = cudaEventRecord(c->ev1, c->st);
+          active--;
+          continue;
+        }
+      }
+      e = c->run_iteration(j.pc, (j.iter % refresh_every) == 0, o->use_graph != 0);
+      if (e == cudaSuccess) e = enqueue_scalars(j);
+      if (e != cudaSuccess) failed = i;
+    }
+    if (!progressed) std::this_thread::yield();
+  }
+  for (int i = 0; i < n; i++) {
+    Job& j = jobs[i];
+    sg_ctx* c = j.c;
+    cudaSetDevice(c->desc.device);
+    float ms = 0.f;
+    if (e == cudaSuccess && j.done) {
+      cudaEventSynchronize(c->ev1);
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    }
+    if (j.ready) cudaEventDestroy(j.ready);
+    c->have_solution = e == cudaSuccess;
+    if (reports) {
+      sg_report& r = reports[i];
+      r = sg_report{};
+      r.iterations = j.iter;
+      r.converged = j.crit <= o->stop_crit;
+      r.crit = j.crit;
+      r.var00 = j.var00;
+      r.solve_seconds = j.t_done - t0;
+      r.iter_per_sec = j.iter / (j.t_done - t0 > 0 ? j.t_done - t0 : 1e-30);
+      r.device_seconds = ms * 1e-3;
+      r.kernel_launches = (long)(c->launches - j.launches0);
+      r.breakdown = c->sc_host->flag;
+      r.fallback_iter = j.fallback;
+    }
+  }
+  if (e != cudaSuccess) {
+    sg_ctx* c = jobs[failed >= 0 ? failed : 0].c;
+    return c->cuda_fail(e, "batch solve");
+  }
+  return SG_OK;
+}

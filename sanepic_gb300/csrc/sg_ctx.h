@@ -351,3 +351,4 @@ struct sg_ctx {
 
 int build_bj3(sg_ctx* c);  // 3x3 block-Jacobi blocks for the current pointing and noise
 int ensure_patches(sg_ctx* c);  // nested patch geometry of the learned preconditioner
+int build_diag(sg_ctx* c);      // the reference's diagonal preconditioner

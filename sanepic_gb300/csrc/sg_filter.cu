@@ -596,10 +596,13 @@ static int max_clusters_one() {
 }
 
 // (LOGR, LOGC, S) per log2(M) and precision; S keeps the per-CTA share at
-// 8192 (FP32) or 4096 (FP64) complex points.
+// 8192 (FP32) or 4096 (FP64) complex points.  For FP32 tiles of 2^14..2^17
+// samples a second shape with 4096 points per CTA (twice the cluster) is
+// compiled too; sg_autotune times both on the context's data.
 #define SG_FILTER_CASES_F32(X)                                                               \
   X(float, 4, 3, 1) X(float, 4, 4, 1) X(float, 5, 4, 1) X(float, 5, 5, 1) X(float, 6, 5, 1)  \
-  X(float, 6, 6, 1) X(float, 7, 6, 1) X(float, 7, 7, 2) X(float, 8, 7, 4) X(float, 8, 8, 8)
+  X(float, 6, 6, 1) X(float, 7, 6, 1) X(float, 7, 7, 2) X(float, 8, 7, 4) X(float, 8, 8, 8)  \
+  X(float, 7, 6, 2) X(float, 7, 7, 4) X(float, 8, 7, 8) X(float, 8, 8, 16)
 #define SG_FILTER_CASES_F64(X)                                                                 \
   X(double, 4, 3, 1) X(double, 4, 4, 1) X(double, 5, 4, 1) X(double, 5, 5, 1)                  \
   X(double, 6, 5, 1) X(double, 6, 6, 1) X(double, 7, 6, 2) X(double, 7, 7, 4)                 \

@@ -78,6 +78,25 @@ def spec_from_name(name: str) -> ProblemSpec:
     return dataclasses.replace(PRESETS[name])
 
 
+def batch_specs(n: int = 32, seed: int = 500) -> List[ProblemSpec]:
+    """Uneven independent problems for batched solves: detector counts from
+    {1, 4, 16, 64}, NSIDE from {64, 128, 256}, segment lengths from {16384,
+    65536, 131072} with 8-48 segments, f_knee ~ U[0.02, 0.2] Hz (one per
+    problem), FP32 operator.  Seeded: the same list every call."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ndet = int(rng.choice([1, 4, 16, 64]))
+        nside = int(rng.choice([64, 128, 256]))
+        ns = int(rng.choice([16384, 65536, 131072]))
+        nseg = int(rng.integers(8, 49))
+        fk = float(rng.uniform(0.02, 0.2))
+        out.append(ProblemSpec(f"batch{i:02d}_{ndet}det_nside{nside}_{nseg}x{ns}", ndet, nside,
+                               nseg, ns, fknee=fk, alpha=1.0, problem=seed + i,
+                               precision="f32"))
+    return out
+
+
 # --------------------------------------------------------------------------
 # HEALPix RING ang2pix, vectorised FP64 restatement of the reference's
 # ang2pix_ring (sanepic.cc:2764-2843); used only to paint the sky into TODs.

@@ -1,0 +1,66 @@
+"""Batched solves of uneven independent problems and the FFT tile-shape
+autotuner (GPU, through the C ABI)."""
+import numpy as np
+import pytest
+
+import sanepic_gb300 as sg
+from sanepic_gb300 import build, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    build.build()
+
+
+def _makers():
+    specs = [synth.ProblemSpec("b0", ndet=2, nside=16, nseg=4, ns=4096, fknee=0.05, problem=41,
+                               precision="f32"),
+             synth.ProblemSpec("b1", ndet=4, nside=32, nseg=6, ns=16384, fknee=0.1, problem=42,
+                               precision="f32"),
+             synth.ProblemSpec("b2", ndet=2, nside=16, nseg=8, ns=2048, fknee=0.2, problem=43,
+                               precision="f32"),
+             synth.ProblemSpec("b3", ndet=3, nside=32, nseg=3, ns=32768, fknee=0.02, problem=44,
+                               precision="f32")]
+    out = []
+    for s in specs:
+        mm = sg.from_problem(synth.make_problem(s), precision="f32")
+        mm.rhs()
+        out.append(mm)
+    return out
+
+
+def test_batch_equals_individual_solves():
+    makers = _makers()
+    single = []
+    for mm in makers:
+        rep = mm.solve(precond="bj3", stop_crit=1e-10, maxiter=500)
+        single.append((rep, mm.solution()))
+    reps = sg.solve_batch(makers, precond="bj3", stop_crit=1e-10, maxiter=500)
+    for (rep1, x1), rep2, mm in zip(single, reps, makers):
+        assert rep1["converged"], rep1
+        assert rep2["converged"] and rep2["iterations"] == rep1["iterations"], (rep1, rep2)
+        # same kernels, same order, fixed-order reductions: the same bits
+        assert np.array_equal(mm.solution(), x1)
+
+
+def test_batch_rejects_missing_rhs():
+    spec = synth.ProblemSpec("nr", ndet=1, nside=16, nseg=2, ns=2048, problem=45, precision="f32")
+    mm = sg.from_problem(synth.make_problem(spec), precision="f32")
+    with pytest.raises(sg.SanepicError):
+        sg.solve_batch([mm], precond="bj3")
+
+
+def test_autotune_keeps_the_operator():
+    spec = synth.ProblemSpec("at", ndet=2, nside=32, nseg=4, ns=32768, fknee=0.1, problem=46,
+                             precision="f32")
+    mm = sg.from_problem(synth.make_problem(spec), precision="f32")
+    x = np.random.default_rng(3).standard_normal(3 * mm.npix)
+    y0 = mm.apply(x)
+    t = mm.autotune()
+    assert t["cluster_size"] in (2, 4) and t["filter_ms"] > 0
+    y1 = mm.apply(x)
+    assert np.linalg.norm(y1 - y0) <= 1e-5 * np.linalg.norm(y0)
+    mm.rhs()
+    assert mm.solve(precond="bj3", stop_crit=1e-10)["converged"]
