@@ -243,16 +243,28 @@ def run_ours(args):
     h2d = (3 * prob["ra"].size * 8 + spec.ndet * prob["ispf"][0].size * 8
            + spec.ndet * prob["tod"][0].size * 8)
     d2h = 3 * 12 * spec.nside ** 2 * 8
-    e2e = []
+    e2e, phases = [], []
     for i in range(args.e2e_steps):
         barrier()
         te = time.perf_counter()
-        upload(mm)
+        mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+        t1 = time.perf_counter()
+        for d in range(spec.ndet):
+            mm.set_noise(d, prob["ispf"][d])
+        t2 = time.perf_counter()
+        for d in range(spec.ndet):
+            mm.set_tod(d, prob["tod"][d])
+        t3 = time.perf_counter()
         device_step(precond)
+        t4 = time.perf_counter()
         maps = [mm.get_map(k) for k in ("I", "Q", "U")]
         barrier()
-        e2e.append(time.perf_counter() - te)
+        t5 = time.perf_counter()
+        e2e.append(t5 - te)
+        phases.append([t1 - te, t2 - t1, t3 - t2, t4 - t3, t5 - t4])
     e2e_s = float(np.median(e2e)) if e2e else None
+    e2e_phases = (dict(zip(("pointing", "noise", "tod", "rhs_and_solve", "maps"),
+                           np.median(np.array(phases), axis=0).tolist())) if phases else None)
     line = {
         "metric": METRIC, "value": sec, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": False,
@@ -264,7 +276,7 @@ def run_ours(args):
                    "iterations": iters, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (pointing alone %.1f GB)" % (ns_all * 12 / 1e9)},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "phases_s": e2e_phases},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "kernel": dom,

@@ -426,23 +426,38 @@ extern "C" int sg_set_tod(sg_ctx* c, long det, const double* tod, long nsamp_tot
   if (det < 0 || det >= c->ndet || !tod) return c->fail(SG_ERR_ARG, "bad detector or TOD");
   cudaSetDevice(c->desc.device);
   const long long ns = c->ns, nseg = c->nseg, nsd = ns * nseg;
-  std::vector<double> h(nsd);
-  for (long long g = 0; g < nseg; g++) {
-    const long long o = c->isampmin[g];
-    if (o + ns > nsamp_total) return c->fail(SG_ERR_ARG, "TOD shorter than the segment list");
-    memcpy(&h[g * ns], tod + o, sizeof(double) * ns);
-    for (long long i = 1; i < ns; i++) {  // sanepic.cc:784-790
-      double& v = h[g * ns + i];
-      if (!(v > 0) && !(v <= 0.0)) v = h[g * ns + i - 1];
-    }
-  }
-  cudaError_t e;
-  if (c->f32) {
-    std::vector<float> f(h.begin(), h.end());
-    e = cudaMemcpy(c->tod.as<float>() + det * nsd, f.data(), 4 * nsd, cudaMemcpyHostToDevice);
+  for (long long g = 0; g < nseg; g++)
+    if (c->isampmin[g] + ns > nsamp_total)
+      return c->fail(SG_ERR_ARG, "TOD shorter than the segment list");
+  // the segments' raw FP64 samples go to the device as they are (one copy if
+  // the segments are contiguous); conversion and the NaN rule of
+  // sanepic.cc:784-790 run there
+  cudaError_t e = cudaSuccess;
+  if (c->stage.bytes < sizeof(double) * nsd) e = c->stage.alloc(sizeof(double) * nsd);
+  if (e == cudaSuccess && !c->nanflag.p) e = c->nanflag.alloc(sizeof(int));
+  bool contiguous = true;
+  for (long long g = 1; g < nseg; g++) contiguous &= c->isampmin[g] == c->isampmin[0] + g * ns;
+  if (e == cudaSuccess && contiguous) {
+    e = cudaMemcpyAsync(c->stage.p, tod + c->isampmin[0], sizeof(double) * nsd,
+                        cudaMemcpyHostToDevice, c->st);
   } else {
-    e = cudaMemcpy(c->tod.as<double>() + det * nsd, h.data(), 8 * nsd, cudaMemcpyHostToDevice);
+    for (long long g = 0; g < nseg && e == cudaSuccess; g++)
+      e = cudaMemcpyAsync(c->stage.as<double>() + g * ns, tod + c->isampmin[g],
+                          sizeof(double) * ns, cudaMemcpyHostToDevice, c->st);
   }
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->nanflag.p, 0, sizeof(int), c->st);
+  if (e == cudaSuccess)
+    e = c->f32 ? ingest_launch<float>(c->stage.as<double>(), nsd, c->tod.as<float>() + det * nsd,
+                                      c->nanflag.as<int>(), c->st)
+               : ingest_launch<double>(c->stage.as<double>(), nsd, c->tod.as<double>() + det * nsd,
+                                       c->nanflag.as<int>(), c->st);
+  int nan = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&nan, c->nanflag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e == cudaSuccess && nan)
+    e = c->f32 ? nan_patch_launch<float>(c->tod.as<float>() + det * nsd, ns, nseg, c->st)
+               : nan_patch_launch<double>(c->tod.as<double>() + det * nsd, ns, nseg, c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "set_tod");
   c->have_tod[det] = 1;
   c->have_rhs = false;

@@ -84,6 +84,7 @@ struct sg_ctx {
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
   DevBuf chi2p;  // per-CTA chi^2 partials of the noise filter
+  DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
   std::vector<double> spn_h;  // host copy of the filter rows [ndet][M+1] (FP64)
 
   // learned preconditioner: the network, the nested patch geometry

@@ -100,6 +100,13 @@ template <typename T>
 cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
                         long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st);
 
+// timeline ingest: out = (T) in over n samples, *nan_flag |= any NaN; then, if
+// flagged, NaNs take the previous sample's value within each segment
+template <typename T>
+cudaError_t ingest_launch(const double* in, long long n, T* out, int* nan_flag, cudaStream_t st);
+template <typename T>
+cudaError_t nan_patch_launch(T* v, long long ns, long long nseg, cudaStream_t st);
+
 // ---- P, detector sums, P^T (sg_pt.cu) ------------------------------------------
 // Groups: grp_off [ngroups+1] / grp_det list the detectors of each offset group;
 // dcs [ndet] = (cos 2d', sin 2d') rotates the group base angle to the detector's.

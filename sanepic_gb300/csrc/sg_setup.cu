@@ -364,4 +364,47 @@ template cudaError_t diag_launch<float>(const long long*, const uint32_t*, long 
 template cudaError_t diag_launch<double>(const long long*, const uint32_t*, long long,
                                          long long, int, const double*, double*, cudaStream_t);
 
+// ---- timeline ingest (sg_set_tod) ---------------------------------------------
+// out = (T) in; any NaN sets *nan_flag (the patch below then runs)
+template <typename T>
+__global__ void k_ingest(const double* __restrict__ in, long long n, T* __restrict__ out,
+                         int* nan_flag) {
+  bool nan = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = in[i];
+    nan |= !(v > 0) && !(v <= 0.0);
+    out[i] = (T)v;
+  }
+  if (__any_sync(0xffffffffu, nan) && (threadIdx.x & 31) == 0) atomicOr(nan_flag, 1);
+}
+
+template <typename T>
+cudaError_t ingest_launch(const double* in, long long n, T* out, int* nan_flag, cudaStream_t st) {
+  const long long b = (n + 255) / 256;
+  k_ingest<T><<<(int)(b < 4096 ? b : 4096), 256, 0, st>>>(in, n, out, nan_flag);
+  return cudaGetLastError();
+}
+template cudaError_t ingest_launch<float>(const double*, long long, float*, int*, cudaStream_t);
+template cudaError_t ingest_launch<double>(const double*, long long, double*, int*, cudaStream_t);
+
+// a NaN sample takes the previous sample's value, within each segment, in
+// sample order (sanepic.cc:784-790): one thread walks one segment
+template <typename T>
+__global__ void k_nan_patch(T* v, long long ns, long long nseg) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= nseg) return;
+  T* s = v + g * ns;
+  for (long long i = 1; i < ns; i++)
+    if (isnan(s[i])) s[i] = s[i - 1];
+}
+
+template <typename T>
+cudaError_t nan_patch_launch(T* v, long long ns, long long nseg, cudaStream_t st) {
+  k_nan_patch<T><<<(int)((nseg + 63) / 64), 64, 0, st>>>(v, ns, nseg);
+  return cudaGetLastError();
+}
+template cudaError_t nan_patch_launch<float>(float*, long long, long long, cudaStream_t);
+template cudaError_t nan_patch_launch<double>(double*, long long, long long, cudaStream_t);
+
 }  // namespace sg

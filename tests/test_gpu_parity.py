@@ -159,3 +159,34 @@ def test_graph_and_eager_agree():
     mm.solve(precond="bj3", stop_crit=1e-8, use_graph=False)
     b = mm.solution()
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_tod_nan_rule_matches_reference(prec):
+    """NaN samples take the previous sample's value within their segment
+    (sanepic.cc:784-790); the library applies the rule on the GPU."""
+    prob = small_problem(ndet=2, nseg=4, ns=2048, precision=prec)
+    ns = prob["spec"].ns
+    tod_nan = [t.copy() for t in prob["tod"]]
+    rng = np.random.default_rng(8)
+    for t in tod_nan:
+        for i in rng.integers(1, t.size, 40):
+            if i % ns:                              # not a segment's first sample
+                t[i:i + rng.integers(1, 5)] = np.nan  # runs, some across segments
+    tod_ref = [t.copy() for t in tod_nan]
+    for t in tod_ref:                               # the reference's rule, on the host
+        for g in range(prob["spec"].nseg):
+            s = t[g * ns:(g + 1) * ns]
+            for i in range(1, ns):
+                if np.isnan(s[i]):
+                    s[i] = s[i - 1]
+    out = []
+    for tods in (tod_nan, tod_ref):
+        p = dict(prob, tod=tods)
+        mm = sg.from_problem(p, precision=prec)
+        chi2 = mm.rhs()
+        mm.solve(precond="bj3", stop_crit=1e-8)
+        out.append((chi2, mm.solution()))
+        mm.close()
+    assert np.isfinite(out[0][0]) and out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
