@@ -489,8 +489,13 @@ def run_reference(args):
     if rank != 0:
         return
     spec = synth.spec_from_name(args.config)
-    cb = reference_cpu(args, spec,
-                       iters_for_projection=args.ref_iters or REFERENCE_ITERS_TO_1E6.get(args.config))
+    iters = args.ref_iters or REFERENCE_ITERS_TO_1E6.get(args.config)
+    for _ in range(args.warmup):
+        reference_cpu(args, spec, iters_for_projection=iters)
+    samples = [reference_cpu(args, spec, iters_for_projection=iters)
+               for _ in range(max(1, args.steps))]
+    samples.sort(key=lambda c: c["value"] if c["value"] is not None else float("inf"))
+    cb = samples[len(samples) // 2]  # median sample
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cb["value"] * 1e3 if cb["value"] else None,

@@ -169,7 +169,30 @@ __global__ void __launch_bounds__(256) k_detsum_f32(const float4* __restrict__ y
     ff s0[4], sa[4], sb[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) s0[k] = sa[k] = sb[k] = ff{0.f, 0.f};
-    for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
+    const int k1 = grp_off[g + 1];
+    int k = grp_off[g];
+    // four detectors' loads in flight before their (in-order) accumulation
+    for (; k + 4 <= k1; k += 4) {
+      float4 v[4];
+      float2 r[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int d = grp_det[k + u];
+        r[u] = dcs[d];
+        v[u] = __ldcs(y + (long long)d * nsd4 + w4);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float vv[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          ff_add_f(s0[q], vv[q]);
+          ff_add_f(sa[q], r[u].x * vv[q]);
+          ff_add_f(sb[q], r[u].y * vv[q]);
+        }
+      }
+    }
+    for (; k < k1; k++) {
       const int d = grp_det[k];
       const float2 r = dcs[d];
       const float4 v = __ldcs(y + (long long)d * nsd4 + w4);
