@@ -249,14 +249,6 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       } else if (p.mode == kLoadTodMinus) {
         v = *reinterpret_cast<const cplx<T>*>(p.tod + s0) -
             *reinterpret_cast<const cplx<T>*>(p.sub + s0);
-      } else if (p.mode == kLoadProj) {
-        const int2 pp = *reinterpret_cast<const int2*>(p.pix + s0);
-        const cplx<T> cs0 = *reinterpret_cast<const cplx<T>*>(p.cs + 2 * s0);
-        const cplx<T> cs1 = *reinterpret_cast<const cplx<T>*>(p.cs + 2 * s0 + 2);
-        const map4<T> m0 = reinterpret_cast<const map4<T>*>(p.map)[pp.x];
-        const map4<T> m1 = reinterpret_cast<const map4<T>*>(p.map)[pp.y];
-        v.x = m0.I + cs0.x * m0.Q + cs0.y * m0.U;
-        v.y = m1.I + cs1.x * m1.Q + cs1.y * m1.U;
       } else {  // unit impulse at sample 0 of the tile
         v.x = (s0 == base) ? T(1) : T(0);
         v.y = T(0);

@@ -11,20 +11,17 @@
 namespace sg {
 
 // ---- noise filter (sg_filter.cu) --------------------------------------------
-enum { kLoadTod = 0, kLoadProj = 1, kLoadDelta = 2, kLoadTodMinus = 3 };
+enum { kLoadTod = 0, kLoadDelta = 2, kLoadTodMinus = 3 };
 
 template <typename T>
 struct FilterArgs {
   long long ntiles;  // (det, seg) tiles, each ns = 2M samples, tile-major
   int nseg;          // det = tile / nseg selects the filter row
-  int mode;          // kLoadTod / kLoadProj / kLoadDelta / kLoadTodMinus
+  int mode;          // kLoadTod / kLoadDelta / kLoadTodMinus
   int filt_abs;      // multiply by |h| instead of h
   const T* tod;      // kLoadTod, kLoadTodMinus: [ntiles][ns]
   const T* sub;      // kLoadTodMinus: the input is tod - sub
   double* chi2_part; // if set: per-CTA sums of h[k] |X[k]|^2, k = 0..ns/2 [gridDim]
-  const int* pix;    // kLoadProj: compact pixel per sample
-  const T* cs;       // kLoadProj: (cos 2psi, sin 2psi) per sample
-  const T* map;      // kLoadProj: [npix][4] = (I, Q, U, 0)
   const T* filt;     // [ndet][M+1]
   T* out;            // [ntiles][ns]
   const cplx<T>* tw_lo;
