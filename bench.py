@@ -2,6 +2,11 @@
 """Benchmark: time-to-solution of the GLS map-making PCG on one GB300,
 learned-preconditioned (flexible PCG) against plain block-Jacobi PCG.
 
+The learned mode applies whichever learned part plain PCG judged faster on a
+held-out problem: the coarse space (Ritz vectors of M A from the plain
+solver's own residuals, two-level balancing preconditioner) or the patch
+network; if neither gained it runs plain block-Jacobi PCG and says so.
+
 Workload (default): 64 detectors, NSIDE 256, 48 segments x 131,072 samples
 (4.03e8 samples), FP32 operator with FP64 P^T sums and CG scalars, seeded
 synthetic scan/sky/1-over-f noise (sanepic_gb300.synth).  One step = one
@@ -174,7 +179,8 @@ def run_ours(args):
     precond = args.precond
     if not args.no_learn:
         tl = time.time()
-        learn = mm.learn_train(npairs=args.learn_pairs, steps=args.learn_steps)
+        learn = mm.learn_train(npairs=args.learn_pairs, steps=args.learn_steps,
+                               coarse_k=args.coarse_k, coarse_vectors=args.coarse_vectors)
         learn["wall_seconds"] = time.time() - tl
         precond = "learned"
 
@@ -240,6 +246,15 @@ def run_ours(args):
                                  "converged": bool(rep_d["converged"])}
         device_step(args.precond)
     # ---- e2e through the C ABI with host buffers ------------------------------
+    # the step's inputs sit in pinned (page-locked) host memory, as a caller
+    # streaming observations would hold them
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        return out
+
+    host = {k: pinned(prob[k]) for k in ("ra", "dec", "psi", "ispf", "tod")}
     h2d = (3 * prob["ra"].size * 8 + spec.ndet * prob["ispf"][0].size * 8
            + spec.ndet * prob["tod"][0].size * 8)
     d2h = 3 * 12 * spec.nside ** 2 * 8
@@ -247,13 +262,13 @@ def run_ours(args):
     for i in range(args.e2e_steps):
         barrier()
         te = time.perf_counter()
-        mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+        mm.set_pointing(host["ra"], host["dec"], host["psi"], dets, prob["isampmin"])
         t1 = time.perf_counter()
         for d in range(spec.ndet):
-            mm.set_noise(d, prob["ispf"][d])
+            mm.set_noise(d, host["ispf"][d])
         t2 = time.perf_counter()
         for d in range(spec.ndet):
-            mm.set_tod(d, prob["tod"][d])
+            mm.set_tod(d, host["tod"][d])
         t3 = time.perf_counter()
         device_step(precond)
         t4 = time.perf_counter()
@@ -288,15 +303,24 @@ def run_ours(args):
     line.update(extra)
     if learn is not None:
         line["config"]["precond"] = "learned (flexible PCG, judged by block-Jacobi PCG)"
+        kind = {0: "none: plain block-Jacobi PCG", 1: "patch network",
+                2: "coarse space"}[learn["kind"]]
         line["learned"] = {
             "plain_pcg_s": sec_plain, "plain_iterations": reps_plain[-1]["iterations"],
-            "learned_iterations": iters,
-            "network_used": bool(learn["enabled"]),
+            "learned_iterations": iters, "learned_part": kind,
+            "network_used": learn["kind"] == 1,
             "fell_back_at_iteration": reps[-1]["fallback_iter"],
             "validation": {"plain_iterations": learn["val_plain_iters"],
-                           "learned_iterations": learn["val_learned_iters"],
+                           "network_iterations": learn["val_learned_iters"],
+                           "coarse_iterations": learn["val_coarse_iters"],
                            "plain_ms": learn["val_plain_ms"],
-                           "learned_ms": learn["val_learned_ms"]},
+                           "network_ms": learn["val_learned_ms"],
+                           "coarse_ms": learn["val_coarse_ms"]},
+            "coarse_space": {"vectors": learn["coarse_k"],
+                             "from_residuals": learn["coarse_vectors"],
+                             "build_s": learn["coarse_seconds"],
+                             "method": "Rayleigh-Ritz of M_bj3 A on span{M_bj3 r_k}; "
+                                       "two-level balancing preconditioner"},
             "training": {"pairs": learn["pairs"], "skies": learn["skies"],
                          "steps": learn["steps"], "loss_first": learn["loss_first"],
                          "loss_last": learn["loss_last"],
@@ -525,6 +549,8 @@ def main():
     ap.add_argument("--no-learn", action="store_true")
     ap.add_argument("--learn-pairs", type=int, default=512)
     ap.add_argument("--learn-steps", type=int, default=1500)
+    ap.add_argument("--coarse-k", type=int, default=0)
+    ap.add_argument("--coarse-vectors", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -165,21 +165,30 @@ int sg_noise_filter_noalloc(const float *in, float *out, const float *filt, long
                             long ntiles, long tiles_per_filter, void *stream);
 
 /* ---- learned preconditioner (no reference counterpart) ----------------------
- * A 4-layer MLP (768 -> 256 -> 256 -> 256 -> 768, BF16 weights on the tensor
- * cores, FP32 accumulate) maps 3 x 256-pixel nested-HEALPix patches of the
- * block-Jacobi-preconditioned residual to a correction; SG_PRECOND_LEARNED
- * uses M_bj3 r + correction inside flexible PCG and falls back to plain
- * block-Jacobi PCG if r^T z turns non-positive.  Needs nside a power of two
- * >= 16. */
+ * Two learned parts, both trained on residuals that the plain block-Jacobi
+ * solver produces on synthetic skies for this context's pointing and noise:
+ * (1) a 4-layer MLP (768 -> 256 -> 256 -> 256 -> 768, BF16 weights on the
+ * tensor cores, FP32 accumulate) that maps 3 x 256-pixel nested-HEALPix
+ * patches of the block-Jacobi-preconditioned residual to a correction
+ * (needs nside a power of two >= 16); (2) a coarse space U of kc vectors, the
+ * Ritz vectors of M_bj3 A with the smallest Ritz values on the span of the
+ * solver's preconditioned residuals, applied as the two-level balancing
+ * preconditioner z = (I - U E^-1 (AU)^T) M_bj3 (I - AU E^-1 U^T) r
+ * + U E^-1 U^T r, E = U^T A U (symmetric positive definite).
+ * SG_PRECOND_LEARNED runs flexible PCG with the part that validation chose
+ * and falls back to plain block-Jacobi PCG if r^T z turns non-positive. */
 typedef struct sg_learn_opts {
   int npairs;        /* residual/solution pairs from the plain solver (0: 512) */
   long seed;         /* first synthetic sky/noise seed (0: 5000) */
-  int steps;         /* Adam steps (0: 1500) */
+  int steps;         /* Adam steps (0: 1500; < 0: no network) */
   int batch;         /* patches per step, multiple of 128 (0: 4096) */
   float lr;          /* Adam learning rate (0: 1e-3) */
   double pair_crit;  /* plain-solver |r|^2/|b|^2 that defines each solution (0: 1e-13) */
   double val_crit;   /* stop of the validation solves (0: 1e-12) */
-  int force;         /* nonzero: use the network even if validation shows no gain */
+  int force;         /* 2: use the coarse space, other nonzero: the network, even
+                        if validation shows no gain */
+  int coarse_k;      /* coarse-space vectors, at most 32 (0: 16; < 0: no coarse space) */
+  int coarse_vectors; /* stored residuals the coarse space is built from (0: 192) */
 } sg_learn_opts;
 
 typedef struct sg_learn_report {
@@ -192,24 +201,40 @@ typedef struct sg_learn_report {
   /* validation on a held-out synthetic sky and noise realisation */
   int val_plain_iters, val_learned_iters;
   double val_plain_ms, val_learned_ms;  /* CUDA-event time of each solve */
-  int enabled;  /* 1: SG_PRECOND_LEARNED uses the network; 0: it runs plain
-                   block-Jacobi PCG because the network did not beat it */
+  int enabled;  /* 1: SG_PRECOND_LEARNED uses a learned part; 0: it runs plain
+                   block-Jacobi PCG because neither part beat it */
+  int coarse_k, coarse_vectors;  /* coarse-space vectors kept, residuals used */
+  double coarse_seconds;         /* building the coarse space */
+  int val_coarse_iters;
+  double val_coarse_ms;
+  int kind;  /* what SG_PRECOND_LEARNED applies: 0 nothing (plain PCG),
+                1 the network, 2 the coarse space */
 } sg_learn_report;
 
 /* Generates training data on this context's pointing and noise model
  * (synthetic skies and noise on the GPU; the residuals of plain block-Jacobi
- * solves run to pair_crit) and trains the network with the library's own
+ * solves run to pair_crit), builds the coarse space from the first
+ * coarse_vectors residuals (one operator application each, then a
+ * Rayleigh-Ritz step) and trains the network with the library's own
  * forward/backward kernels: each step maximises the A-cosine
  * (r^T z)^2 / ((z^T A z)(r^T M_bj3 r)) of the corrected direction z for one
  * stored residual, differentiated through one application of A.  Plain PCG
- * then judges the result on a held-out problem (report->enabled).
- * `batch` is unused (one residual's patches per step).
- * Overwrites b and the solution: call sg_rhs again before sg_solve. */
+ * then judges both on a held-out problem (report->kind, report->enabled).
+ * The coarse space belongs to this operator: a context with other pointing
+ * or noise must be trained again.  `batch` is unused (one residual's patches
+ * per step).  Overwrites b and the solution: call sg_rhs again before
+ * sg_solve. */
 int sg_learn_train(sg_ctx *ctx, const sg_learn_opts *opts, sg_learn_report *report);
 long sg_learn_nparams(void);
 /* FP32 parameters, per layer W [out x in] row-major then b [out]. */
 int sg_learn_get_params(sg_ctx *ctx, float *params);
 int sg_learn_set_params(sg_ctx *ctx, const float *params);
+/* The Rayleigh-Ritz step of the coarse space on host arrays (no GPU): from
+ * H = V^T A V and G = V^T M^-1 V [m][m] (row-major), writes C [m][k] (U = V C)
+ * for the k <= kc Ritz vectors of M A with the smallest positive Ritz values
+ * theta [k], and E^-1 [k][k] for E = C^T H C.  Returns k (0: none usable). */
+int sg_coarse_from_gram(int m, int kc, const double *H, const double *G, double *C,
+                        double *einv, double *theta);
 
 /* Tests and measurements on host arrays.  sg_mlp_gemm_host: C[M x N] =
  * A[M x K] . B[N x K]^T, BF16 bit patterns in, FP32 out (M, N multiples of

@@ -36,7 +36,8 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
-           "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch", "sg_autotune",
+           "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
+           "sg_autotune",
            "sg_last_error", "sg_destroy"]
 
 
@@ -81,7 +82,8 @@ class SgReport(ctypes.Structure):
 class SgLearnOpts(ctypes.Structure):
     _fields_ = [("npairs", ctypes.c_int), ("seed", ctypes.c_long), ("steps", ctypes.c_int),
                 ("batch", ctypes.c_int), ("lr", ctypes.c_float), ("pair_crit", ctypes.c_double),
-                ("val_crit", ctypes.c_double), ("force", ctypes.c_int)]
+                ("val_crit", ctypes.c_double), ("force", ctypes.c_int),
+                ("coarse_k", ctypes.c_int), ("coarse_vectors", ctypes.c_int)]
 
 
 class SgLearnReport(ctypes.Structure):
@@ -91,7 +93,10 @@ class SgLearnReport(ctypes.Structure):
                 ("train_seconds", ctypes.c_double), ("gemm_tflop", ctypes.c_double),
                 ("val_plain_iters", ctypes.c_int), ("val_learned_iters", ctypes.c_int),
                 ("val_plain_ms", ctypes.c_double), ("val_learned_ms", ctypes.c_double),
-                ("enabled", ctypes.c_int)]
+                ("enabled", ctypes.c_int), ("coarse_k", ctypes.c_int),
+                ("coarse_vectors", ctypes.c_int), ("coarse_seconds", ctypes.c_double),
+                ("val_coarse_iters", ctypes.c_int), ("val_coarse_ms", ctypes.c_double),
+                ("kind", ctypes.c_int)]
 
 
 _lib = None
@@ -135,6 +140,9 @@ def load_library(path: Optional[str] = None):
     L.sg_learn_nparams.restype = ctypes.c_long
     L.sg_learn_get_params.argtypes = [c_p, fp]
     L.sg_learn_set_params.argtypes = [c_p, fp]
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.sg_coarse_from_gram.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp]
+    L.sg_coarse_from_gram.restype = ctypes.c_int
     L.sg_mlp_gemm_host.argtypes = [ctypes.POINTER(ctypes.c_ushort), ctypes.POINTER(ctypes.c_ushort),
                                    fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     L.sg_mlp_grad_host.argtypes = [fp, fp, fp, ctypes.c_int, fp, fp, fp]
@@ -293,11 +301,17 @@ class MapMaker:
     # ---- learned preconditioner ---------------------------------------------
     def learn_train(self, npairs: int = 512, seed: int = 5000, steps: int = 1500,
                     batch: int = 0, lr: float = 1e-3, pair_crit: float = 1e-13,
-                    val_crit: float = 1e-12, force: bool = False) -> dict:
+                    val_crit: float = 1e-12, force=False, coarse_k: int = 0,
+                    coarse_vectors: int = 0) -> dict:
         """Make residual/solution pairs with the plain solver on synthetic skies,
-        train the network on the GPU and validate it against plain PCG on a
-        held-out problem.  Overwrites b: call rhs() again afterwards."""
-        o = SgLearnOpts(npairs, seed, steps, batch, lr, pair_crit, val_crit, int(force))
+        build the coarse space and train the network on the GPU, and validate
+        both against plain PCG on a held-out problem (steps < 0: no network;
+        coarse_k < 0: no coarse space).  force: True or "network" uses the
+        network, "coarse" the coarse space, even without a validated gain.
+        Overwrites b: call rhs() again."""
+        fcode = {False: 0, None: 0, True: 1, "network": 1, "coarse": 2}[force]
+        o = SgLearnOpts(npairs, seed, steps, batch, lr, pair_crit, val_crit, fcode,
+                        coarse_k, coarse_vectors)
         rep = SgLearnReport()
         self._check(self.L.sg_learn_train(self.h, ctypes.byref(o), ctypes.byref(rep)))
         return {k: getattr(rep, k) for k, _ in SgLearnReport._fields_}
@@ -361,6 +375,21 @@ def from_problem(prob, precision: Optional[str] = None, device: int = 0,
 
 
 # ---- tensor-core GEMM and network gradients on host arrays (tests, measurements) ----
+def coarse_from_gram(H: np.ndarray, G: np.ndarray, kc: int):
+    """The coarse space's Rayleigh-Ritz step on host arrays (no GPU): returns
+    (C [m][k], E^-1 [k][k], theta [k]) for H = V^T A V, G = V^T M^-1 V."""
+    H = np.ascontiguousarray(H, np.float64)
+    G = np.ascontiguousarray(G, np.float64)
+    m = H.shape[0]
+    C = np.zeros((m, kc))
+    einv = np.zeros((kc, kc))
+    th = np.zeros(kc)
+    k = int(load_library().sg_coarse_from_gram(m, kc, _dp(H), _dp(G), _dp(C), _dp(einv),
+                                               _dp(th)))
+    return (C.reshape(-1)[:m * k].reshape(m, k), einv.reshape(-1)[:k * k].reshape(k, k),
+            th[:k])
+
+
 def mlp_nparams() -> int:
     return int(load_library().sg_learn_nparams())
 

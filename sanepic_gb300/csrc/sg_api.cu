@@ -290,6 +290,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(cudaMemcpyAsync(hcount.data(), count.p, sizeof(int) * c->npixfull,
                          cudaMemcpyDeviceToHost, c->st));
   SG_TRY(cudaStreamSynchronize(c->st));
+  const std::vector<long long> old_int2ring = c->int2ring;
   c->indpix_host.assign(c->npixfull, -1);
   long long npix = 0;
   for (long long p = 0; p < c->npixfull; p++)
@@ -378,6 +379,18 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(cudaMemsetAsync(c->x.p, 0, vb, c->st));
   SG_TRY(cudaStreamSynchronize(c->st));
   c->drop_graphs();
+  if (c->int2ring != old_int2ring) {
+    // another pixel set: the network's patch geometry is rebuilt on demand and
+    // the coarse space (vectors over the old pixels) is dropped.  With the same
+    // pixel set a coarse space built on other pointing or noise stays a valid
+    // (symmetric positive definite) preconditioner, only a weaker one.
+    c->npatch = c->npatch_pad = 0;
+    c->coarse_k = 0;
+    if (c->learned_kind == 2) {
+      c->learned_kind = 0;
+      c->learned_enabled = false;
+    }
+  }
   c->have_pointing = true;
   c->have_rhs = c->have_solution = c->have_bj3 = c->have_diag = false;
   return SG_OK;
@@ -629,14 +642,16 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   if (o->precond != SG_PRECOND_BJ3 && o->precond != SG_PRECOND_DIAG &&
       o->precond != SG_PRECOND_LEARNED)
     return c->fail(SG_ERR_UNSUPPORTED, "preconditioner %d not available", o->precond);
-  if (o->precond == SG_PRECOND_LEARNED && !c->have_mlp)
+  if (o->precond == SG_PRECOND_LEARNED && !c->have_mlp && c->coarse_k == 0)
     return c->fail(SG_ERR_STATE, "train (sg_learn_train) or load (sg_learn_set_params) the network first");
   cudaSetDevice(c->desc.device);
   const double t0 = now_s();
   rc = (o->precond == SG_PRECOND_DIAG) ? build_diag(c) : build_bj3(c);
-  if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED) rc = ensure_patches(c);
+  if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED && c->learned_kind == 1)
+    rc = ensure_patches(c);
   if (rc) return rc;
-  // 0: reference diagonal, 1: block-Jacobi, 2: block-Jacobi + network (flexible PCG)
+  // 0: reference diagonal, 1: block-Jacobi, 2: block-Jacobi + a learned part
+  // (the network or the coarse space; flexible PCG)
   int pc = (o->precond == SG_PRECOND_BJ3) ? 1 : (o->precond == SG_PRECOND_DIAG ? 0 : 2);
   int fallback_iter = -1;
   if (pc == 2 && !c->learned_enabled) {  // plain PCG judged the network: it did not gain

@@ -123,11 +123,12 @@ extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_r
     sg_ctx* c = ctxs[i];
     if (!c) return SG_ERR_ARG;
     if (!c->have_rhs) return c->fail(SG_ERR_STATE, "call sg_rhs before sg_solve_batch");
-    if (o->precond == SG_PRECOND_LEARNED && !c->have_mlp)
-      return c->fail(SG_ERR_STATE, "no trained network");
+    if (o->precond == SG_PRECOND_LEARNED && !c->have_mlp && c->coarse_k == 0)
+      return c->fail(SG_ERR_STATE, "no trained network or coarse space");
     cudaSetDevice(c->desc.device);
     int rc = (o->precond == SG_PRECOND_DIAG) ? build_diag(c) : build_bj3(c);
-    if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED) rc = ensure_patches(c);
+    if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED && c->learned_kind == 1)
+      rc = ensure_patches(c);
     if (rc) return rc;
     Job& j = jobs[i];
     j.c = c;

@@ -398,4 +398,201 @@ cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStrea
   return cudaGetLastError();
 }
 
+// ---- two-level preconditioner with a coarse space U (kc columns) ------------
+// Balancing form (Mandel's balancing Neumann-Neumann; A-DEF2 in Tang et al.
+// 2009), with AU = A U and E = U^T A U:
+//   z = (I - U E^-1 AU^T) M (I - AU E^-1 U^T) r + U E^-1 U^T r
+// computed as  c = E^-1 U^T r,  y = M (r - AU c),  z = y + U (c - E^-1 AU^T y).
+// Symmetric positive definite for any SPD E and M, so plain (or flexible)
+// PCG applies.  U and AU are FP32 rows [kc][ld]; their products with a vector
+// run in FP32 (GB300's FP64 rate would make kc FP64 FMAs per element cost
+// more than reading U), per-thread partials and the coarse solve in FP64
+// with fixed-order reductions.  The rounding makes the preconditioner
+// slightly inexact, which the flexible (Polak-Ribiere) PCG absorbs.
+
+// part[k][block] = sum over the block's elements of U[k][i] v[i]
+__global__ void __launch_bounds__(kCgThreads)
+    k_coarse_dots(const float* __restrict__ U, long long ld, int kc, long long n3,
+                  const double* __restrict__ v, double* part) {
+  float acc[kCoarseMax];
+#pragma unroll
+  for (int k = 0; k < kCoarseMax; k++) acc[k] = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float vi = (float)v[i];
+#pragma unroll
+    for (int k = 0; k < kCoarseMax; k++)
+      if (k < kc) acc[k] = fmaf(U[k * ld + i], vi, acc[k]);
+  }
+  __shared__ double sh[kCoarseMax][kCgThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kCoarseMax; k++) {
+    if (k >= kc) break;
+    double x = (double)acc[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kc) {
+    double s = 0.0;
+    for (int w = 0; w < kCgThreads / 32; w++) s += sh[threadIdx.x][w];
+    part[threadIdx.x * kCgBlocks + blockIdx.x] = s;
+  }
+}
+
+// warp k reduces row k of the partials; then coef[k] = (E^-1 dots)[k]
+// (mode 0) or coef[kCoarseMax + k] = coef[k] - (E^-1 dots)[k] (mode 1)
+__global__ void __launch_bounds__(1024)
+    k_coarse_solve(const double* __restrict__ part, int kc, const double* __restrict__ einv,
+                   double* coef, int mode) {
+  __shared__ double dots[kCoarseMax];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (w < kc) {
+    double x = 0.0;
+    for (int b = lane; b < kCgBlocks; b += 32) x += part[w * kCgBlocks + b];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) dots[w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kc) {
+    const int k = threadIdx.x;
+    double c = 0.0;
+    for (int j = 0; j < kc; j++) c += einv[k * kc + j] * dots[j];
+    if (mode == 0)
+      coef[k] = c;
+    else
+      coef[kCoarseMax + k] = coef[k] - c;
+  }
+}
+
+// z = M (r - sum_k AU[k] coef[k])  (M: the context's block-Jacobi or diagonal)
+__global__ void __launch_bounds__(kCgThreads)
+    k_coarse_pre(CgVecs v, const float* __restrict__ AU, long long ld, int kc,
+                 const double* __restrict__ coef) {
+  __shared__ float c[kCoarseMax];
+  if (threadIdx.x < kCoarseMax) c[threadIdx.x] = threadIdx.x < kc ? (float)coef[threadIdx.x] : 0.f;
+  __syncthreads();
+  const long long n = v.npix;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+       m += (long long)gridDim.x * blockDim.x) {
+    double t[3];
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) {
+      const long long i = cc * n + m;
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < kCoarseMax; k++)
+        if (k < kc) s = fmaf(AU[k * ld + i], c[k], s);
+      t[cc] = v.r[i] - (double)s;
+    }
+    double z0, z1, z2;
+    apply_m(v, m, t[0], t[1], t[2], z0, z1, z2);
+    v.z[m] = z0;
+    v.z[n + m] = z1;
+    v.z[2 * n + m] = z2;
+  }
+}
+
+// z += sum_k U[k] coef[kCoarseMax + k]
+__global__ void __launch_bounds__(kCgThreads)
+    k_coarse_post(double* z, const float* __restrict__ U, long long ld, int kc, long long n3,
+                  const double* __restrict__ coef) {
+  __shared__ float c[kCoarseMax];
+  if (threadIdx.x < kCoarseMax)
+    c[threadIdx.x] = threadIdx.x < kc ? (float)coef[kCoarseMax + threadIdx.x] : 0.f;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kCoarseMax; k++)
+      if (k < kc) s = fmaf(U[k * ld + i], c[k], s);
+    z[i] += (double)s;
+  }
+}
+
+cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, cudaStream_t st) {
+  if (cs.kc < 1 || cs.kc > kCoarseMax) return cudaErrorInvalidValue;
+  const long long n3 = 3 * v.npix;
+  k_coarse_dots<<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, cs.ld, cs.kc, n3, v.r, cs.part);
+  k_coarse_solve<<<1, 1024, 0, st>>>(cs.part, cs.kc, cs.einv, cs.coef, 0);
+  k_coarse_pre<<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, cs.ld, cs.kc, cs.coef);
+  k_coarse_dots<<<kCgBlocks, kCgThreads, 0, st>>>(cs.au, cs.ld, cs.kc, n3, v.z, cs.part);
+  k_coarse_solve<<<1, 1024, 0, st>>>(cs.part, cs.kc, cs.einv, cs.coef, 1);
+  k_coarse_post<<<kCgBlocks, kCgThreads, 0, st>>>(v.z, cs.u, cs.ld, cs.kc, n3, cs.coef);
+  return cudaGetLastError();
+}
+
+// ---- building the coarse space ------------------------------------------------
+// part[s][i][j] = sum over split s of X[i][:] . Y[j][:]  (16 x 16 output tile
+// per block, 32-column chunks staged in shared memory)
+constexpr int kGramTile = 16, kGramChunk = 32;
+__global__ void __launch_bounds__(kGramTile* kGramTile)
+    k_gram(const double* __restrict__ X, const double* __restrict__ Y, long long ld, int m,
+           long long n, long long per_split, double* part) {
+  __shared__ double xs[kGramTile][kGramChunk + 1], ys[kGramTile][kGramChunk + 1];
+  const int tx = threadIdx.x % kGramTile, ty = threadIdx.x / kGramTile;
+  const int i0 = blockIdx.x * kGramTile, j0 = blockIdx.y * kGramTile;
+  const long long c0 = blockIdx.z * per_split;
+  const long long c1 = c0 + per_split < n ? c0 + per_split : n;
+  double acc = 0.0;
+  for (long long c = c0; c < c1; c += kGramChunk) {
+    for (int e = threadIdx.x; e < kGramTile * kGramChunk; e += kGramTile * kGramTile) {
+      const int r = e / kGramChunk, k = e % kGramChunk;
+      const long long col = c + k;
+      const bool in = col < c1;
+      xs[r][k] = (in && i0 + r < m) ? X[(i0 + r) * ld + col] : 0.0;
+      ys[r][k] = (in && j0 + r < m) ? Y[(j0 + r) * ld + col] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < kGramChunk; k++) acc += xs[ty][k] * ys[tx][k];
+    __syncthreads();
+  }
+  const int i = i0 + ty, j = j0 + tx;
+  if (i < m && j < m) part[((long long)blockIdx.z * m + i) * m + j] = acc;
+}
+
+cudaError_t gram_launch(const double* X, const double* Y, long long ld, int m, long long n,
+                        int nsplit, double* part, cudaStream_t st) {
+  const int t = (m + kGramTile - 1) / kGramTile;
+  long long per = (n + nsplit - 1) / nsplit;
+  per = (per + kGramChunk - 1) / kGramChunk * kGramChunk;
+  dim3 grid(t, t, nsplit);
+  k_gram<<<grid, kGramTile * kGramTile, 0, st>>>(X, Y, ld, m, n, per, part);
+  return cudaGetLastError();
+}
+
+// out[k][i] = (float) sum_j V[j][i] C[j][k]   (C [m][kc] FP64, m * kc <= 4096)
+__global__ void __launch_bounds__(kCgThreads)
+    k_combine(const double* __restrict__ V, long long ld, int m, const double* __restrict__ C,
+              int kc, long long n, float* out) {
+  __shared__ double cs[4096];
+  for (int e = threadIdx.x; e < m * kc; e += blockDim.x) cs[e] = C[e];
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double acc[kCoarseMax];
+#pragma unroll
+    for (int k = 0; k < kCoarseMax; k++) acc[k] = 0.0;
+    for (int j = 0; j < m; j++) {
+      const double vj = V[j * ld + i];
+#pragma unroll
+      for (int k = 0; k < kCoarseMax; k++)
+        if (k < kc) acc[k] += vj * cs[j * kc + k];
+    }
+#pragma unroll
+    for (int k = 0; k < kCoarseMax; k++)
+      if (k < kc) out[k * ld + i] = (float)acc[k];
+  }
+}
+
+cudaError_t combine_launch(const double* V, long long ld, int m, const double* C, int kc,
+                           long long n, float* out, cudaStream_t st) {
+  if (kc < 1 || kc > kCoarseMax || m * kc > 4096) return cudaErrorInvalidValue;
+  k_combine<<<kCgBlocks * 4, kCgThreads, 0, st>>>(V, ld, m, C, kc, n, out);
+  return cudaGetLastError();
+}
+
 }  // namespace sg

@@ -94,7 +94,11 @@ struct sg_ctx {
   DevBuf patch_idx, patch_sig, tod_syn, filt_noise;
   int npatch = 0, npatch_pad = 0;
   bool have_mlp = false, use_syn = false;
-  bool learned_enabled = false;  // validation: the network beat plain PCG
+  bool learned_enabled = false;  // validation: a learned component beat plain PCG
+  // learned coarse space: U, AU = A U [kc][3 npix] FP32, E^-1 [kc][kc] FP64
+  DevBuf cs_u, cs_au, cs_einv, cs_coef, cs_part;
+  int coarse_k = 0;
+  int learned_kind = 0;  // SG_PRECOND_LEARNED applies 1: the network, 2: the coarse space
   const void* tod_active() const { return use_syn ? tod_syn.p : tod.p; }
   cplx<float> wn1f{1.f, 0.f};
   cplx<double> wn1d{1.0, 0.0};
@@ -314,7 +318,18 @@ struct sg_ctx {
     launches += 2;
     return e;
   }
-  cudaError_t learned_z();  // z = M_bj3 r + correction (sg_learn.cu)
+  cudaError_t learned_z();  // z from r: the network (sg_learn.cu) or the coarse space
+  CoarseSpace coarse() const {
+    CoarseSpace c{};
+    c.kc = coarse_k;
+    c.ld = 3 * npix;
+    c.u = cs_u.as<float>();
+    c.au = cs_au.as<float>();
+    c.einv = cs_einv.as<double>();
+    c.coef = cs_coef.as<double>();
+    c.part = cs_part.as<double>();
+    return c;
+  }
 
   // captured iterations hold raw device pointers: drop them whenever a buffer
   // they use is reallocated

@@ -25,8 +25,10 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <random>
+#include <vector>
 
 #include "sg_ctx.h"
 #include "sg_healpix.h"
@@ -276,9 +278,14 @@ static int build_patches(sg_ctx* c) {
 
 }  // namespace sg
 
-// z = M_bj3 r + network correction (graph-capturable: no host sync)
+// z = M_bj3 r + network correction, or the two-level coarse-space
+// preconditioner (graph-capturable: no host sync)
 cudaError_t sg_ctx::learned_z() {
   CgVecs vb = vecs(1);
+  if (learned_kind == 2) {
+    launches += 6;
+    return coarse_apply(vb, coarse(), st);
+  }
   cudaError_t e = apply_precond(vb, r.as<double>(), z.as<double>(), st);
   if (e != cudaSuccess) return e;
   k_patch_gather<<<npatch_pad, kPatch, 0, st>>>(z.as<double>(), patch_idx.as<int>(), npatch,
@@ -417,6 +424,195 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
 
 }  // namespace
 
+namespace {
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix a (row-major,
+// overwritten): w ascending, v [n][n] with eigenvectors in its columns.
+void sym_eig(int n, std::vector<double>& a, std::vector<double>& w, std::vector<double>& v) {
+  std::vector<double> q((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) q[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = 0.0, dia = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) (i == j ? dia : off) += a[(size_t)i * n + j] * a[(size_t)i * n + j];
+    if (off <= 1e-30 * dia) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int r = p + 1; r < n; r++) {
+        const double apr = a[(size_t)p * n + r];
+        if (apr == 0.0) continue;
+        const double th = (a[(size_t)r * n + r] - a[(size_t)p * n + p]) / (2.0 * apr);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < n; k++) {  // a <- a J
+          const double x = a[(size_t)k * n + p], y = a[(size_t)k * n + r];
+          a[(size_t)k * n + p] = cs * x - sn * y;
+          a[(size_t)k * n + r] = sn * x + cs * y;
+        }
+        for (int k = 0; k < n; k++) {  // a <- J^T a
+          const double x = a[(size_t)p * n + k], y = a[(size_t)r * n + k];
+          a[(size_t)p * n + k] = cs * x - sn * y;
+          a[(size_t)r * n + k] = sn * x + cs * y;
+        }
+        for (int k = 0; k < n; k++) {  // q <- q J
+          const double x = q[(size_t)k * n + p], y = q[(size_t)k * n + r];
+          q[(size_t)k * n + p] = cs * x - sn * y;
+          q[(size_t)k * n + r] = sn * x + cs * y;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; i++) ord[i] = i;
+  std::sort(ord.begin(), ord.end(),
+            [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
+  w.resize(n);
+  v.assign((size_t)n * n, 0.0);
+  for (int j = 0; j < n; j++) {
+    w[j] = a[(size_t)ord[j] * n + ord[j]];
+    for (int i = 0; i < n; i++) v[(size_t)i * n + j] = q[(size_t)i * n + ord[j]];
+  }
+}
+
+}  // namespace
+
+// Rayleigh-Ritz for M A on span V (m vectors): H = V^T A V, G = V^T M^-1 V.
+// Writes the coefficients C [m][k] (U = V C) of the k <= kc Ritz vectors with
+// the smallest positive Ritz values theta [k], and E^-1 [k][k] for
+// E = C^T H C (= diag(theta) up to rounding).  Returns k.
+extern "C" int sg_coarse_from_gram(int m, int kc, const double* H, const double* G, double* C,
+                                   double* einv, double* theta) {
+  if (m < 1 || kc < 1 || !H || !G || !C || !einv) return 0;
+  std::vector<double> g((size_t)m * m), h((size_t)m * m), lam, Q;
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < m; j++) {
+      g[(size_t)i * m + j] = 0.5 * (G[(size_t)i * m + j] + G[(size_t)j * m + i]);
+      h[(size_t)i * m + j] = 0.5 * (H[(size_t)i * m + j] + H[(size_t)j * m + i]);
+    }
+  sym_eig(m, g, lam, Q);
+  const double lmax = lam.empty() ? 0.0 : lam.back();
+  if (!(lmax > 0.0)) return 0;
+  std::vector<int> keep;
+  for (int i = 0; i < m; i++)
+    if (lam[i] > 1e-12 * lmax) keep.push_back(i);
+  const int p = (int)keep.size();
+  std::vector<double> B((size_t)m * p);  // B = Q_keep diag(lam^-1/2): B^T G B = I
+  for (int i = 0; i < m; i++)
+    for (int j = 0; j < p; j++)
+      B[(size_t)i * p + j] = Q[(size_t)i * m + keep[j]] / std::sqrt(lam[keep[j]]);
+  std::vector<double> HB((size_t)m * p, 0.0), Hp((size_t)p * p, 0.0);
+  for (int i = 0; i < m; i++)
+    for (int k = 0; k < m; k++) {
+      const double hik = h[(size_t)i * m + k];
+      if (hik == 0.0) continue;
+      for (int j = 0; j < p; j++) HB[(size_t)i * p + j] += hik * B[(size_t)k * p + j];
+    }
+  for (int i = 0; i < p; i++)
+    for (int k = 0; k < m; k++)
+      for (int j = 0; j < p; j++) Hp[(size_t)i * p + j] += B[(size_t)k * p + i] * HB[(size_t)k * p + j];
+  for (int i = 0; i < p; i++)
+    for (int j = 0; j < i; j++)
+      Hp[(size_t)i * p + j] = Hp[(size_t)j * p + i] = 0.5 * (Hp[(size_t)i * p + j] + Hp[(size_t)j * p + i]);
+  std::vector<double> th, S;
+  sym_eig(p, Hp, th, S);
+  std::vector<int> sel;
+  for (int j = 0; j < p && (int)sel.size() < kc; j++)
+    if (th[j] > 1e-12 * th.back()) sel.push_back(j);
+  const int k = (int)sel.size();
+  if (k == 0) return 0;
+  for (int i = 0; i < m; i++)
+    for (int a = 0; a < k; a++) {
+      double x = 0.0;
+      for (int j = 0; j < p; j++) x += B[(size_t)i * p + j] * S[(size_t)j * p + sel[a]];
+      C[(size_t)i * k + a] = x;
+    }
+  // E = C^T H C, E^-1 through its eigen-decomposition
+  std::vector<double> HC((size_t)m * k, 0.0), E((size_t)k * k, 0.0);
+  for (int i = 0; i < m; i++)
+    for (int l = 0; l < m; l++)
+      for (int a = 0; a < k; a++) HC[(size_t)i * k + a] += h[(size_t)i * m + l] * C[(size_t)l * k + a];
+  for (int a = 0; a < k; a++)
+    for (int b = 0; b < k; b++) {
+      double x = 0.0;
+      for (int i = 0; i < m; i++) x += C[(size_t)i * k + a] * HC[(size_t)i * k + b];
+      E[(size_t)a * k + b] = x;
+    }
+  for (int a = 0; a < k; a++)
+    for (int b = 0; b < a; b++)
+      E[(size_t)a * k + b] = E[(size_t)b * k + a] = 0.5 * (E[(size_t)a * k + b] + E[(size_t)b * k + a]);
+  std::vector<double> mu, Y;
+  sym_eig(k, E, mu, Y);
+  if (!(mu[0] > 0.0)) return 0;
+  for (int a = 0; a < k; a++)
+    for (int b = 0; b < k; b++) {
+      double x = 0.0;
+      for (int l = 0; l < k; l++) x += Y[(size_t)a * k + l] * Y[(size_t)b * k + l] / mu[l];
+      einv[(size_t)a * k + b] = x;
+    }
+  if (theta)
+    for (int a = 0; a < k; a++) theta[a] = th[sel[a]];
+  return k;
+}
+
+namespace sg {
+
+// The coarse space from the first m stored residuals: V = M_bj3 r_j (the
+// solver's own preconditioned residuals, which span the Krylov spaces of the
+// training solves), W = A V, H = V^T W, G = V^T R (= V^T M^-1 V), then
+// sg_coarse_from_gram; U = V C and A U = W C are kept in FP32.
+int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
+  const long long n3 = 3 * c->npix;
+  if (m < 2) return SG_OK;
+  if (m * kc > 4096) m = 4096 / kc;
+  DevBuf V, W, gp, dC;
+  const int nsplit = 16;
+  cudaError_t e = V.alloc((size_t)m * n3 * 8);
+  if (e == cudaSuccess) e = W.alloc((size_t)m * n3 * 8);
+  if (e == cudaSuccess) e = gp.alloc((size_t)nsplit * m * m * 8);
+  if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space buffers");
+  CgVecs v1 = c->vecs(1);
+  for (int j = 0; j < m && e == cudaSuccess; j++) {
+    double* vj = V.as<double>() + (size_t)j * n3;
+    e = apply_precond(v1, bank + (size_t)j * n3, vj, c->st);
+    if (e == cudaSuccess) e = c->apply_dev(vj, W.as<double>() + (size_t)j * n3, true);
+  }
+  std::vector<double> part((size_t)nsplit * m * m), H((size_t)m * m, 0.0), G((size_t)m * m, 0.0);
+  for (int which = 0; which < 2 && e == cudaSuccess; which++) {
+    e = gram_launch(V.as<double>(), which == 0 ? W.as<double>() : bank, n3, m, n3, nsplit,
+                    gp.as<double>(), c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(part.data(), gp.p, 8 * part.size(), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    std::vector<double>& out = which == 0 ? H : G;
+    for (int sp = 0; sp < nsplit; sp++)
+      for (size_t i = 0; i < out.size(); i++) out[i] += part[(size_t)sp * m * m + i];
+  }
+  c->launches += 2 * (long long)m + 2;
+  if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space Gram matrices");
+  std::vector<double> C((size_t)m * kc), einv((size_t)kc * kc), th(kc);
+  const int k = sg_coarse_from_gram(m, kc, H.data(), G.data(), C.data(), einv.data(), th.data());
+  if (k == 0) return SG_OK;  // nothing usable: no coarse space
+  c->drop_graphs();
+  e = dC.alloc((size_t)m * k * 8);
+  if (e == cudaSuccess) e = cudaMemcpy(dC.p, C.data(), (size_t)m * k * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = c->cs_u.alloc((size_t)k * n3 * 4);
+  if (e == cudaSuccess) e = c->cs_au.alloc((size_t)k * n3 * 4);
+  if (e == cudaSuccess) e = c->cs_einv.alloc((size_t)k * k * 8);
+  if (e == cudaSuccess) e = c->cs_coef.alloc(2 * kCoarseMax * 8);
+  if (e == cudaSuccess) e = c->cs_part.alloc((size_t)kCoarseMax * kCgBlocks * 8);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->cs_einv.p, einv.data(), (size_t)k * k * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = combine_launch(V.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_u.as<float>(), c->st);
+  if (e == cudaSuccess)
+    e = combine_launch(W.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_au.as<float>(), c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  c->launches += 2;
+  if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space vectors");
+  c->coarse_k = k;
+  return SG_OK;
+}
+
+}  // namespace sg
+
 extern "C" long sg_learn_nparams(void) { return (long)mlp_nparams(); }
 
 extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report* rep) {
@@ -426,15 +622,20 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
     if (!c->have_noise[d]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", d);
   const int npairs = o->npairs > 0 ? o->npairs : 512;
   const uint64_t seed0 = o->seed > 0 ? (uint64_t)o->seed : 5000;
-  const int steps = o->steps > 0 ? o->steps : 1500;
+  const int steps = o->steps > 0 ? o->steps : (o->steps < 0 ? 0 : 1500);  // 0: no network
+  const int coarse_k = o->coarse_k > 0 ? std::min(o->coarse_k, kCoarseMax)
+                                       : (o->coarse_k < 0 ? 0 : 16);  // 0: no coarse space
+  const int coarse_m = o->coarse_vectors > 0 ? o->coarse_vectors : 192;
   const float lr = o->lr > 0.f ? o->lr : 1e-3f;
   const double pair_crit = o->pair_crit > 0.0 ? o->pair_crit : 1e-13;
   cudaSetDevice(c->desc.device);
   const double t0 = now_s();
   int rc = build_bj3(c);
   if (rc) return rc;
-  rc = build_patches(c);
-  if (rc) return rc;
+  if (steps > 0) {
+    rc = build_patches(c);
+    if (rc) return rc;
+  }
   rc = make_noise_table(c);
   if (rc) return rc;
   const long long npix = c->npix, n3 = 3 * npix;
@@ -482,12 +683,23 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (e != cudaSuccess) return c->cuda_fail(e, "training pairs");
   const double t1 = now_s();
 
+  // ---- the coarse space: Rayleigh-Ritz on the span of M_bj3 r_k --------------
+  c->coarse_k = 0;
+  if (coarse_k > 0) {
+    rc = build_coarse(c, bank.as<double>(), std::min(pairs, coarse_m), coarse_k);
+    if (rc) return rc;
+  }
+  const double t1c = now_s();
+
   // ---- training: maximise the A-cosine of the corrected direction ------------
   // For a residual r and z = M_bj3 r + correction, one CG step from r removes
   // (r^T z)^2 / (z^T A z) of the squared A-norm error.  The loss
   //   L = -(r^T z)^2 / ((z^T A z) (r^T M_bj3 r))
   // is differentiated through the real operator A (one application per step).
+  float loss_first = 0.f, loss_last = 0.f;
+  long long gemm_flops = 0;
   c->drop_graphs();
+  if (steps > 0) {
   c->mlp.reset(new Mlp());
   Mlp& net = *c->mlp;
   const int B = c->npatch_pad;
@@ -501,7 +713,6 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (e == cudaSuccess) e = part.alloc(8 * 3 * kCgBlocks);
   if (e == cudaSuccess) e = cudaMemsetAsync(dy.p, 0, (size_t)B * kIn * 4, c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "network init");
-  float loss_first = 0.f, loss_last = 0.f;
   for (int s = 0; s < steps && e == cudaSuccess; s++) {
     const long long k = (long long)(mix64(seed0 * 7919ULL + (uint64_t)s) % (uint64_t)pairs);
     const double* r = bank.as<double>() + (size_t)k * n3;
@@ -543,29 +754,52 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (e == cudaSuccess) e = cudaMemcpy(&gerr, net.err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return c->cuda_fail(e, "training");
   if (gerr) return c->fail(SG_ERR_CUDA, "tensor-core GEMM pipeline timed out (code %d)", gerr);
-  const double t2 = now_s();
+  gemm_flops = net.gemm_flops;
   c->have_mlp = true;
+  }
+  const double t2 = now_s();
 
-  // ---- validation: plain PCG judges the network on a held-out problem ------------
+  // ---- validation: plain PCG judges each learned part on a held-out problem --------
+  // (the fastest one that converges and beats plain PCG is used; `force` 2
+  // uses the coarse space regardless, any other nonzero `force` the network)
   const double vcrit = o->val_crit > 0.0 ? o->val_crit : 1e-12;
-  ValSolve vp, vl;
+  ValSolve vp, vl, vc;
   c->use_syn = true;
   e = synth_rhs(c, seed0 + 1000003);
   if (e == cudaSuccess) e = val_solve(c, 1, vcrit, vp);
-  if (e == cudaSuccess) e = val_solve(c, 2, vcrit, vl);
+  if (e == cudaSuccess && steps > 0) {
+    c->learned_kind = 1;
+    e = val_solve(c, 2, vcrit, vl);
+  }
+  if (e == cudaSuccess && c->coarse_k > 0) {
+    c->learned_kind = 2;
+    e = val_solve(c, 2, vcrit, vc);
+  }
   c->use_syn = false;
   c->tod_syn.release();
   c->have_solution = false;
   if (e != cudaSuccess) return c->cuda_fail(e, "validation");
-  c->learned_enabled = o->force != 0 || (vl.converged && vl.ms < vp.ms);
+  double best = vp.ms;
+  c->learned_kind = 0;
+  if (steps > 0 && vl.converged && vl.ms < best) {
+    c->learned_kind = 1;
+    best = vl.ms;
+  }
+  if (c->coarse_k > 0 && vc.converged && vc.ms < best) {
+    c->learned_kind = 2;
+    best = vc.ms;
+  }
+  if (o->force == 2 && c->coarse_k > 0)
+    c->learned_kind = 2;
+  else if (o->force != 0 && steps > 0)
+    c->learned_kind = 1;
+  c->learned_enabled = c->learned_kind != 0;
   if (rep) {
     rep->val_plain_iters = vp.iters;
     rep->val_learned_iters = vl.iters;
     rep->val_plain_ms = vp.ms;
     rep->val_learned_ms = vl.ms;
     rep->enabled = c->learned_enabled ? 1 : 0;
-  }
-  if (rep) {
     rep->pairs = pairs;
     rep->skies = skies;
     rep->rows = (long)pairs * c->npatch;
@@ -573,8 +807,14 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
     rep->loss_first = loss_first;
     rep->loss_last = loss_last;
     rep->gen_seconds = t1 - t0;
-    rep->train_seconds = t2 - t1;
-    rep->gemm_tflop = (double)net.gemm_flops * 1e-12;
+    rep->train_seconds = t2 - t1c;
+    rep->gemm_tflop = (double)gemm_flops * 1e-12;
+    rep->coarse_k = c->coarse_k;
+    rep->coarse_vectors = c->coarse_k > 0 ? std::min(pairs, coarse_m) : 0;
+    rep->coarse_seconds = t1c - t1;
+    rep->val_coarse_iters = vc.iters;
+    rep->val_coarse_ms = vc.ms;
+    rep->kind = c->learned_kind;
   }
   return SG_OK;
 }
@@ -609,12 +849,26 @@ extern "C" int sg_learn_set_params(sg_ctx* c, const float* params) {
   if (e != cudaSuccess) return c->cuda_fail(e, "set params");
   c->have_mlp = true;
   c->learned_enabled = true;  // an explicitly loaded network is used as given
+  c->learned_kind = 1;
   return SG_OK;
 }
 
 int ensure_patches(sg_ctx* c) {
   if (c->npatch_pad) return SG_OK;
-  return build_patches(c);
+  int rc = build_patches(c);
+  if (rc || !c->mlp || c->mlp->cap >= c->npatch_pad) return rc;
+  // more patches than the network's activation buffers hold: re-create them
+  // around the same weights
+  std::vector<float> w(mlp_nparams());
+  cudaError_t e = cudaMemcpy(w.data(), c->mlp->w32, 4 * w.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) {
+    c->mlp.reset(new Mlp());
+    e = c->mlp->init(c->npatch_pad, 4000, c->st);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(c->mlp->w32, w.data(), 4 * w.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = c->mlp->sync_weights(c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "network buffers");
 }
 
 // ---- host-array entry points for tests and measurements --------------------------
