@@ -147,18 +147,6 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
       return c->fail(SG_ERR_ARG, "segment %lld [%lld, %lld] outside the %ld-sample timeline",
                      g, c->isampmin[g], c->isampmin[g] + ns - 1, nsamp_total);
   }
-  // per-segment boresight, psi NaN-patched within the segment (sanepic.cc:722-727)
-  std::vector<double> hra(nsd), hdec(nsd), hpsi(nsd);
-  for (long long g = 0; g < nseg; g++) {
-    const long long o = c->isampmin[g];
-    memcpy(&hra[g * ns], ra + o, sizeof(double) * ns);
-    memcpy(&hdec[g * ns], dec + o, sizeof(double) * ns);
-    memcpy(&hpsi[g * ns], psi + o, sizeof(double) * ns);
-    for (long long i = 1; i < ns; i++) {
-      double& v = hpsi[g * ns + i];
-      if (!(v > 0) && !(v <= 0.0)) v = hpsi[g * ns + i - 1];
-    }
-  }
   cudaError_t e;
 #define SG_TRY(x)                                     \
   do {                                                \
@@ -169,10 +157,27 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(dra.alloc(sizeof(double) * nsd));
   SG_TRY(ddec.alloc(sizeof(double) * nsd));
   SG_TRY(dpsi.alloc(sizeof(double) * nsd));
-  SG_TRY(flag.alloc(sizeof(int)));
-  SG_TRY(cudaMemcpyAsync(dra.p, hra.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(ddec.p, hdec.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
-  SG_TRY(cudaMemcpyAsync(dpsi.p, hpsi.data(), sizeof(double) * nsd, cudaMemcpyHostToDevice, c->st));
+  SG_TRY(flag.alloc(2 * sizeof(int)));
+  // the segments' boresight goes to the device as it is (one copy per array if
+  // the segments are contiguous); psi's NaN samples take the previous sample's
+  // value within the segment there (sanepic.cc:722-727)
+  {
+    bool contiguous = true;
+    for (long long g = 1; g < nseg; g++) contiguous &= c->isampmin[g] == c->isampmin[0] + g * ns;
+    const double* src[3] = {ra, dec, psi};
+    DevBuf* dst[3] = {&dra, &ddec, &dpsi};
+    for (int a = 0; a < 3; a++) {
+      if (contiguous) {
+        SG_TRY(cudaMemcpyAsync(dst[a]->p, src[a] + c->isampmin[0], sizeof(double) * nsd,
+                               cudaMemcpyHostToDevice, c->st));
+      } else {
+        for (long long g = 0; g < nseg; g++)
+          SG_TRY(cudaMemcpyAsync(dst[a]->as<double>() + g * ns, src[a] + c->isampmin[g],
+                                 sizeof(double) * ns, cudaMemcpyHostToDevice, c->st));
+      }
+    }
+    SG_TRY(nan_patch_launch<double>(dpsi.as<double>(), ns, nseg, c->st));
+  }
   // offset groups: detectors with identical (offx, offy) share the pixelisation
   // (pass 1); if any pointing sample is NaN, every detector gets its own
   // stream (pass 2) so the reference's previous-pixel rule, which carries
@@ -206,7 +211,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
     SG_TRY(psio.alloc(sizeof(double) * ng));
     SG_TRY(cudaMemcpyAsync(doffx.p, offx.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
     SG_TRY(cudaMemcpyAsync(doffy.p, offy.data(), sizeof(double) * G, cudaMemcpyHostToDevice, c->st));
-    SG_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), c->st));
+    SG_TRY(cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), c->st));
     PointingArgs pa{};
     pa.ns = ns;
     pa.nseg = (int)nseg;
@@ -221,15 +226,13 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
     pa.psio = psio.as<double>();
     pa.error_flag = flag.as<int>();
     SG_TRY(pointing_launch(pa, c->st));
-    int hflag = 0;
-    SG_TRY(cudaMemcpyAsync(&hflag, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(any_negative_launch(ring.as<int>(), ng, flag.as<int>() + 1, c->st));
+    int hflag[2] = {0, 0};
+    SG_TRY(cudaMemcpyAsync(hflag, flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
     SG_TRY(cudaStreamSynchronize(c->st));
-    if (hflag)
+    if (hflag[0])
       return c->fail(SG_ERR_POINTING, "theta out of range in ang2pix (the reference exits here)");
-    hring.resize(ng);
-    SG_TRY(cudaMemcpy(hring.data(), ring.p, sizeof(int) * ng, cudaMemcpyDeviceToHost));
-    bool any_invalid = false;
-    for (long long i = 0; i < ng && !any_invalid; i++) any_invalid = hring[i] < 0;
+    const bool any_invalid = hflag[1] != 0;  // NaN pointing somewhere
     c->ngroups = G;
     c->ngsamp = ng;
     c->grp_off_h = goff;
@@ -238,6 +241,8 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
     if (pass == 1 || G == ndet) {
       // NaN pointing: reuse the previous pixel in the reference's loop order
       // (det, seg, sample; sanepic.cc:851-873), streams are per detector here
+      hring.resize(ng);
+      SG_TRY(cudaMemcpy(hring.data(), ring.p, sizeof(int) * ng, cudaMemcpyDeviceToHost));
       int prev = 0;
       for (long long i = 0; i < ng; i++) {
         if (hring[i] < 0) hring[i] = prev;
@@ -286,36 +291,37 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(hist_launch(ring.as<int>(), ng, nsd, gsz.as<int>(), count.as<int>(), c->st));
   // indpix in the reference's RING order (sanepic.cc:904-915), and the
   // library's internal numbering: observed pixels in NESTED order
-  std::vector<int> hcount(c->npixfull);
-  SG_TRY(cudaMemcpyAsync(hcount.data(), count.p, sizeof(int) * c->npixfull,
-                         cudaMemcpyDeviceToHost, c->st));
-  SG_TRY(cudaStreamSynchronize(c->st));
   const std::vector<long long> old_int2ring = c->int2ring;
-  c->indpix_host.assign(c->npixfull, -1);
   long long npix = 0;
-  for (long long p = 0; p < c->npixfull; p++)
-    if (hcount[p] != 0) c->indpix_host[p] = (int)npix++;
-  c->npix = npix;
-  c->int2ring.resize(npix);
   {
-    std::vector<std::pair<long long, long long>> key;  // (nested, ring)
-    key.reserve(npix);
-    const long long ns_ = c->desc.nside;
-    const bool pow2 = (ns_ & (ns_ - 1)) == 0;
-    for (long long p = 0; p < c->npixfull; p++)
-      if (hcount[p] != 0) key.emplace_back(pow2 ? hp_ring2nest(ns_, p) : p, p);
-    std::sort(key.begin(), key.end());
-    for (long long m = 0; m < npix; m++) c->int2ring[m] = key[m].second;
+    const long long nf = c->npixfull, nside = c->desc.nside;
+    const size_t ntb = numbering_tmp_bytes(nf);
+    DevBuf ntmp, d_i2r, d_i2rc, d_ipr, d_np;
+    SG_TRY(ntmp.alloc(ntb));
+    SG_TRY(d_i2r.alloc(sizeof(long long) * nf));
+    SG_TRY(d_i2rc.alloc(sizeof(long long) * nf));
+    SG_TRY(d_ipr.alloc(sizeof(int) * nf));
+    SG_TRY(d_np.alloc(sizeof(int)));
+    SG_TRY(c->indpix.alloc(sizeof(int) * nf));
+    SG_TRY(numbering_launch(count.as<int>(), nf, nside, (nside & (nside - 1)) == 0 ? 1 : 0,
+                            d_i2r.as<long long>(), d_i2rc.as<long long>(), c->indpix.as<int>(),
+                            d_ipr.as<int>(), d_np.as<int>(), ntmp.p, ntb, c->st));
+    int hnp = 0;
+    SG_TRY(cudaMemcpyAsync(&hnp, d_np.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaStreamSynchronize(c->st));
+    npix = hnp;
+    c->npix = npix;
+    c->int2ring.resize(npix);
+    c->int2ringc.resize(npix);
+    c->indpix_host.resize(nf);
+    SG_TRY(cudaMemcpyAsync(c->int2ring.data(), d_i2r.p, sizeof(long long) * npix,
+                           cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaMemcpyAsync(c->int2ringc.data(), d_i2rc.p, sizeof(long long) * npix,
+                           cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaMemcpyAsync(c->indpix_host.data(), d_ipr.p, sizeof(int) * nf,
+                           cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaStreamSynchronize(c->st));
   }
-  c->int2ringc.resize(npix);
-  std::vector<int> indpix_int(c->npixfull, -1);
-  for (long long m = 0; m < npix; m++) {
-    indpix_int[c->int2ring[m]] = (int)m;
-    c->int2ringc[m] = c->indpix_host[c->int2ring[m]];
-  }
-  SG_TRY(c->indpix.alloc(sizeof(int) * c->npixfull));
-  SG_TRY(cudaMemcpy(c->indpix.p, indpix_int.data(), sizeof(int) * c->npixfull,
-                    cudaMemcpyHostToDevice));
   SG_TRY(c->pix.alloc(sizeof(int) * ng));
   SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), ng, c->pix.as<int>(), c->st));
   SG_TRY(c->hits.alloc(sizeof(int) * npix));

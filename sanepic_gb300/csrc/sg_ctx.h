@@ -36,7 +36,10 @@ struct DevBuf {
     p = nullptr;
     bytes = 0;
   }
+  // contents are undefined after alloc; a buffer of the same size is kept
+  // (no cudaFree / cudaMalloc when a setter runs again on same-sized data)
   cudaError_t alloc(size_t n) {
+    if (p && bytes == n) return cudaSuccess;
     release();
     bytes = n;
     if (n == 0) return cudaSuccess;

@@ -1,5 +1,6 @@
-// sg_healpix.h -- host-side HEALPix helpers used to choose the library's
-// internal pixel numbering (plain C++, no CUDA).
+// sg_healpix.h -- HEALPix helpers used to choose the library's internal
+// pixel numbering (plain C++; the integer ring -> nested map also compiles
+// for the device).
 //
 // The reference numbers observed pixels in ascending RING order (indpix,
 // sanepic.cc:904-915).  Internally the library numbers them in NESTED order
@@ -16,6 +17,12 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+
+#ifdef __CUDACC__
+#define SG_HD __host__ __device__
+#else
+#define SG_HD
+#endif
 
 namespace sg {
 
@@ -106,6 +113,75 @@ inline long long hp_ring2nest(long long nside, long long p) {
   double z, phi;
   hp_pix2ang_ring(nside, p, &z, &phi);
   return hp_ang2pix_nest(nside, z, phi);
+}
+
+// The same map in integer arithmetic only (host and device): the ring number
+// and in-ring index of p give the pixel centre's face coordinates exactly.
+// Equatorial rings (nside <= i <= 3 nside): with f2 = 2 if i + nside is odd
+// (the ring's first centre sits at phi = pi / (2 nside)) else 1, the centre's
+// coordinates along the ascending and descending face edges are the
+// half-integers (2 iphi - f2 + i - nside) / 2 and (2 iphi - f2 + 3 nside - i) / 2.
+// Polar rings (i < nside from either pole) hold i pixels per face; the k-th
+// face's p-th pixel (1-based) sits at edge coordinates (p - 1/2, i - p + 1/2).
+SG_HD inline long long hp_isqrt_int(long long v) {
+  long long r = 0, b = 1LL << 62;
+  while (b > v) b >>= 2;
+  while (b != 0) {
+    if (v >= r + b) {
+      v -= r + b;
+      r = (r >> 1) + b;
+    } else {
+      r >>= 1;
+    }
+    b >>= 2;
+  }
+  return r;
+}
+
+SG_HD inline uint64_t hp_spread_int(uint64_t v) {
+  v &= 0xffffffffULL;
+  v = (v | (v << 16)) & 0x0000ffff0000ffffULL;
+  v = (v | (v << 8)) & 0x00ff00ff00ff00ffULL;
+  v = (v | (v << 4)) & 0x0f0f0f0f0f0f0f0fULL;
+  v = (v | (v << 2)) & 0x3333333333333333ULL;
+  v = (v | (v << 1)) & 0x5555555555555555ULL;
+  return v;
+}
+
+SG_HD inline long long hp_ring2nest_int(long long nside, long long p) {
+  const long long ncap = 2 * nside * (nside - 1), npix = 12 * nside * nside;
+  long long face, ix, iy;
+  if (p >= ncap && p < npix - ncap) {
+    const long long ip = p - ncap;
+    const long long i = ip / (4 * nside) + nside;
+    const long long iphi = ip % (4 * nside) + 1;
+    const long long f2 = ((i + nside) & 1) ? 2 : 1;
+    const long long jp = (2 * iphi - f2 + i - nside - 1) / 2;
+    const long long jm = (2 * iphi - f2 + 3 * nside - i - 1) / 2;
+    const long long ifp = jp / nside, ifm = jm / nside;
+    face = (ifp == ifm) ? (ifp | 4) : ((ifp < ifm) ? ifp : ifm + 8);
+    ix = jm & (nside - 1);
+    iy = nside - (jp & (nside - 1)) - 1;
+  } else {
+    const bool north = p < ncap;
+    const long long ip = north ? p + 1 : npix - p;  // 1-based from the pole
+    const long long i = north ? (1 + hp_isqrt_int(2 * ip - 1)) >> 1
+                              : (1 + hp_isqrt_int(2 * ip - 1)) >> 1;
+    const long long iphi = north ? ip - 2 * i * (i - 1) : 4 * i + 1 - (ip - 2 * i * (i - 1));
+    const long long k = (iphi - 1) / i, q = iphi - k * i;
+    const long long jp = q - 1, jm = i - q;
+    if (north) {
+      face = k;
+      ix = nside - jm - 1;
+      iy = nside - jp - 1;
+    } else {
+      face = k + 8;
+      ix = jp;
+      iy = jm;
+    }
+  }
+  return face * nside * nside +
+         (long long)(hp_spread_int((uint64_t)ix) | (hp_spread_int((uint64_t)iy) << 1));
 }
 
 }  // namespace sg

@@ -66,6 +66,16 @@ cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, 
 // hits_true[m] = count[ring(m)] via indpix
 cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull,
                         int* hits_true, cudaStream_t st);
+// pixel numbering from the per-RING-pixel sample counts [n = 12 nside^2]:
+// indpix_ring (reference order, -1 if unobserved), indpix_int (internal
+// index), int2ring / int2ringc [capacity n] (ring pixel and RING-order compact
+// index of each internal index), *npix (device int) the observed pixels
+size_t numbering_tmp_bytes(long long n);
+cudaError_t numbering_launch(const int* count, long long n, long long nside, int nested,
+                             long long* int2ring, long long* int2ringc, int* indpix_int,
+                             int* indpix_ring, int* npix, void* tmp, size_t tmp_bytes,
+                             cudaStream_t st);
+cudaError_t any_negative_launch(const int* v, long long n, int* flag, cudaStream_t st);
 // CSR by pixel over group samples: csr_off [npix+1], csr_idx [n]
 size_t csr_tmp_bytes(long long n, long long npix);
 cudaError_t csr_build(const int* pix, long long n, long long npix,

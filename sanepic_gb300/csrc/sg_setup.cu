@@ -8,6 +8,7 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
+#include "sg_healpix.h"
 #include "sg_kernels.h"
 
 namespace sg {
@@ -59,6 +60,94 @@ __global__ void k_hits(const int* count, const int* indpix, long long npixfull, 
 cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull, int* hits,
                         cudaStream_t st) {
   k_hits<<<grid_for(npixfull, 256), 256, 0, st>>>(count, indpix, npixfull, hits);
+  return cudaGetLastError();
+}
+
+// ---- pixel numbering -------------------------------------------------------
+// The reference's indpix (rank of each observed pixel in ascending RING order,
+// sanepic.cc:904-915) and the library's internal numbering (rank in NESTED
+// order when nside is a power of two, else RING order), by two exclusive
+// scans instead of a host sort.
+__global__ void k_obs(const int* count, long long n, int* flag) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x)
+    flag[p] = count[p] != 0;
+}
+
+__global__ void k_nest_mark(const int* count, long long n, long long nside, int nested,
+                            int* mark, int* ring_of) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (count[p] == 0) continue;
+    const long long q = nested ? hp_ring2nest_int(nside, p) : p;
+    mark[q] = 1;
+    ring_of[q] = (int)p;
+  }
+}
+
+// internal index m of the q-th marked nested pixel; indpix in both orders
+__global__ void k_number(const int* count, const int* mark, const int* mrank, const int* ring_of,
+                         const int* rrank, long long n, long long* int2ring,
+                         long long* int2ringc, int* indpix_int, int* indpix_ring) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    indpix_ring[q] = count[q] != 0 ? rrank[q] : -1;
+    if (!mark[q]) continue;
+    const int m = mrank[q], p = ring_of[q];
+    int2ring[m] = p;
+    int2ringc[m] = rrank[p];
+    indpix_int[p] = m;
+  }
+}
+
+__global__ void k_total(const int* flag, const int* rank, long long n, int* total) {
+  *total = n > 0 ? rank[n - 1] + flag[n - 1] : 0;
+}
+
+size_t numbering_tmp_bytes(long long n) {
+  size_t scan = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, scan, (const int*)nullptr, (int*)nullptr, (int)n);
+  return 5 * sizeof(int) * (size_t)n + scan + 256;
+}
+
+cudaError_t numbering_launch(const int* count, long long n, long long nside, int nested,
+                             long long* int2ring, long long* int2ringc, int* indpix_int,
+                             int* indpix_ring, int* npix, void* tmp, size_t tmp_bytes,
+                             cudaStream_t st) {
+  int* flag = reinterpret_cast<int*>(tmp);
+  int* rrank = flag + n;
+  int* mark = rrank + n;
+  int* mrank = mark + n;
+  int* ring_of = mrank + n;
+  void* scan_tmp = ring_of + n;
+  size_t scan_bytes = tmp_bytes - 5 * sizeof(int) * (size_t)n;
+  const unsigned g = grid_for(n, 256);
+  cudaError_t e = cudaMemsetAsync(mark, 0, sizeof(int) * n, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(indpix_int, 0xff, sizeof(int) * n, st);
+  if (e != cudaSuccess) return e;
+  k_obs<<<g, 256, 0, st>>>(count, n, flag);
+  k_nest_mark<<<g, 256, 0, st>>>(count, n, nside, nested, mark, ring_of);
+  e = cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, flag, rrank, (int)n, st);
+  if (e == cudaSuccess) e = cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, mark, mrank, (int)n, st);
+  if (e != cudaSuccess) return e;
+  k_number<<<g, 256, 0, st>>>(count, mark, mrank, ring_of, rrank, n, int2ring, int2ringc,
+                              indpix_int, indpix_ring);
+  k_total<<<1, 1, 0, st>>>(flag, rrank, n, npix);
+  return cudaGetLastError();
+}
+
+// *flag = 1 if any entry is negative (NaN pointing leaves -1)
+__global__ void k_any_negative(const int* v, long long n, int* flag) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    if (v[i] < 0) {
+      *flag = 1;
+      return;
+    }
+}
+
+cudaError_t any_negative_launch(const int* v, long long n, int* flag, cudaStream_t st) {
+  k_any_negative<<<grid_for(n, 256), 256, 0, st>>>(v, n, flag);
   return cudaGetLastError();
 }
 

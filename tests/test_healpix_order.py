@@ -18,6 +18,13 @@ extern "C" long long t_ring2nest(long long nside, long long p) { return sg::hp_r
 extern "C" void t_pix2ang(long long nside, long long p, double* z, double* phi) {
   sg::hp_pix2ang_ring(nside, p, z, phi);
 }
+// pixels where the integer map differs from the map through the pixel centre
+extern "C" long long t_int_mismatches(long long nside) {
+  long long bad = 0;
+  for (long long p = 0; p < 12 * nside * nside; p++)
+    bad += sg::hp_ring2nest_int(nside, p) != sg::hp_ring2nest(nside, p);
+  return bad;
+}
 """
 
 
@@ -32,6 +39,8 @@ def hp(tmp_path_factory):
     L = ctypes.CDLL(str(so))
     L.t_ring2nest.restype = ctypes.c_longlong
     L.t_ring2nest.argtypes = [ctypes.c_longlong, ctypes.c_longlong]
+    L.t_int_mismatches.restype = ctypes.c_longlong
+    L.t_int_mismatches.argtypes = [ctypes.c_longlong]
     L.t_pix2ang.argtypes = [ctypes.c_longlong, ctypes.c_longlong,
                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     return L
@@ -77,3 +86,10 @@ def test_nested_blocks_are_compact(hp):
         worst = max(worst, np.degrees(np.arccos(np.clip(blk @ c, -1, 1))).max())
     # a 16 x 16 nested block at nside 64 is ~15 deg across
     assert worst < 15.0
+
+
+@pytest.mark.parametrize("nside", [1, 2, 4, 8, 16, 32, 64, 128, 256, 512])
+def test_integer_ring2nest_matches_centre_map(hp, nside):
+    """the integer map the library runs on the GPU equals the map through
+    the pixel centres, pixel for pixel"""
+    assert hp.t_int_mismatches(nside) == 0
