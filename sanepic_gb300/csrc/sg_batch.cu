@@ -92,12 +92,11 @@ cudaError_t enqueue_start(sg_ctx* c, int pc) {
   c->launches += 2;
   if (pc == 2) {
     CgVecs v2 = c->vecs(2);
-    if (e == cudaSuccess) e = c->learned_z();
-    if (e == cudaSuccess) e = cg_dots(v2, 0, c->st);
+    if (e == cudaSuccess) e = c->learned_z(0);
     if (e == cudaSuccess)
       e = c->f32 ? cg_reinit_d<float>(v2, c->dmap.as<float>(), c->st)
                  : cg_reinit_d<double>(v2, c->dmap.as<double>(), c->st);
-    c->launches += 2;
+    c->launches += 1;
   } else if (e == cudaSuccess) {
     e = c->to_map(c->d.as<double>());
   }

@@ -404,74 +404,88 @@ cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStrea
 //   z = (I - U E^-1 AU^T) M (I - AU E^-1 U^T) r + U E^-1 U^T r
 // computed as  c = E^-1 U^T r,  y = M (r - AU c),  z = y + U (c - E^-1 AU^T y).
 // Symmetric positive definite for any SPD E and M, so plain (or flexible)
-// PCG applies.  U and AU are FP32 rows [kc][ld]; their products with a vector
-// run in FP32 (GB300's FP64 rate would make kc FP64 FMAs per element cost
-// more than reading U), per-thread partials and the coarse solve in FP64
-// with fixed-order reductions.  The rounding makes the preconditioner
-// slightly inexact, which the flexible (Polak-Ribiere) PCG absorbs.
+// PCG applies.  U and AU are stored element-major, [3 npix][kp] FP32 with
+// kp = kc rounded up to 8 (zero columns), so one thread reads an element's
+// kp values as float4s.  Their products with a vector run in FP32 (GB300's
+// FP64 rate would make kc FP64 FMAs per element cost more than reading U);
+// per-thread partials, the fixed-order reductions and the coarse solves are
+// FP64.  Every block of the kernel that needs c (or c - g) re-reduces the
+// partials itself, so the coarse solve costs no launch.  The rounding makes
+// the preconditioner slightly inexact, which flexible PCG absorbs.
 
-// part[k][block] = sum over the block's elements of U[k][i] v[i]
+// part[k][block] = sum over the block's elements of U[i][k] v[i]
+template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_dots(const float* __restrict__ U, long long ld, int kc, long long n3,
-                  const double* __restrict__ v, double* part) {
-  float acc[kCoarseMax];
+    k_coarse_dots(const float* __restrict__ U, long long n3, const double* __restrict__ v,
+                  double* part) {
+  float acc[KP];
 #pragma unroll
-  for (int k = 0; k < kCoarseMax; k++) acc[k] = 0.f;
+  for (int k = 0; k < KP; k++) acc[k] = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
     const float vi = (float)v[i];
+    const float4* row = reinterpret_cast<const float4*>(U + i * KP);
 #pragma unroll
-    for (int k = 0; k < kCoarseMax; k++)
-      if (k < kc) acc[k] = fmaf(U[k * ld + i], vi, acc[k]);
+    for (int q = 0; q < KP / 4; q++) {
+      const float4 u = row[q];
+      acc[4 * q] = fmaf(u.x, vi, acc[4 * q]);
+      acc[4 * q + 1] = fmaf(u.y, vi, acc[4 * q + 1]);
+      acc[4 * q + 2] = fmaf(u.z, vi, acc[4 * q + 2]);
+      acc[4 * q + 3] = fmaf(u.w, vi, acc[4 * q + 3]);
+    }
   }
-  __shared__ double sh[kCoarseMax][kCgThreads / 32];
+  __shared__ double sh[KP][kCgThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < kCoarseMax; k++) {
-    if (k >= kc) break;
+  for (int k = 0; k < KP; k++) {
     double x = (double)acc[k];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) sh[k][wid] = x;
   }
   __syncthreads();
-  if (threadIdx.x < kc) {
-    double s = 0.0;
-    for (int w = 0; w < kCgThreads / 32; w++) s += sh[threadIdx.x][w];
-    part[threadIdx.x * kCgBlocks + blockIdx.x] = s;
+  if (threadIdx.x < KP) {
+    double t = 0.0;
+    for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
+    part[threadIdx.x * kCgBlocks + blockIdx.x] = t;
   }
 }
 
-// warp k reduces row k of the partials; then coef[k] = (E^-1 dots)[k]
-// (mode 0) or coef[kCoarseMax + k] = coef[k] - (E^-1 dots)[k] (mode 1)
-__global__ void __launch_bounds__(1024)
-    k_coarse_solve(const double* __restrict__ part, int kc, const double* __restrict__ einv,
-                   double* coef, int mode) {
-  __shared__ double dots[kCoarseMax];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (w < kc) {
+// out[k] = (E^-1 d)[k], d[k] = sum_b part[k][b] in a fixed order (identical in
+// every block); warp w reduces rows w, w + 8, ...
+template <int KP>
+__device__ __forceinline__ void coarse_solve_block(const double* __restrict__ part,
+                                                   const double* __restrict__ einv, int kc,
+                                                   double* d, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = wid; k < KP; k += kCgThreads / 32) {
     double x = 0.0;
-    for (int b = lane; b < kCgBlocks; b += 32) x += part[w * kCgBlocks + b];
+    for (int b = lane; b < kCgBlocks; b += 32) x += part[k * kCgBlocks + b];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) dots[w] = x;
+    if (lane == 0) d[k] = x;
   }
   __syncthreads();
-  if (threadIdx.x < kc) {
+  if (threadIdx.x < KP) {
     const int k = threadIdx.x;
     double c = 0.0;
-    for (int j = 0; j < kc; j++) c += einv[k * kc + j] * dots[j];
-    if (mode == 0)
-      coef[k] = c;
-    else
-      coef[kCoarseMax + k] = coef[k] - c;
+    if (k < kc)
+      for (int j = 0; j < kc; j++) c += einv[k * kc + j] * d[j];
+    out[k] = c;
   }
+  __syncthreads();
 }
 
-// z = M (r - sum_k AU[k] coef[k])  (M: the context's block-Jacobi or diagonal)
+// c = E^-1 U^T r (from part1); z = M (r - AU c); block 0 keeps c in coef
+template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_pre(CgVecs v, const float* __restrict__ AU, long long ld, int kc,
-                 const double* __restrict__ coef) {
-  __shared__ float c[kCoarseMax];
-  if (threadIdx.x < kCoarseMax) c[threadIdx.x] = threadIdx.x < kc ? (float)coef[threadIdx.x] : 0.f;
+    k_coarse_pre(CgVecs v, const float* __restrict__ AU, const double* __restrict__ part1,
+                 const double* __restrict__ einv, int kc, double* coef) {
+  __shared__ double d[KP], cd[KP];
+  __shared__ float c[KP];
+  coarse_solve_block<KP>(part1, einv, kc, d, cd);
+  if (threadIdx.x < KP) {
+    c[threadIdx.x] = (float)cd[threadIdx.x];
+    if (blockIdx.x == 0) coef[threadIdx.x] = cd[threadIdx.x];
+  }
   __syncthreads();
   const long long n = v.npix;
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
@@ -480,10 +494,16 @@ __global__ void __launch_bounds__(kCgThreads)
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
+      const float4* row = reinterpret_cast<const float4*>(AU + i * KP);
       float s = 0.f;
 #pragma unroll
-      for (int k = 0; k < kCoarseMax; k++)
-        if (k < kc) s = fmaf(AU[k * ld + i], c[k], s);
+      for (int q = 0; q < KP / 4; q++) {
+        const float4 a = row[q];
+        s = fmaf(a.x, c[4 * q], s);
+        s = fmaf(a.y, c[4 * q + 1], s);
+        s = fmaf(a.z, c[4 * q + 2], s);
+        s = fmaf(a.w, c[4 * q + 3], s);
+      }
       t[cc] = v.r[i] - (double)s;
     }
     double z0, z1, z2;
@@ -494,34 +514,65 @@ __global__ void __launch_bounds__(kCgThreads)
   }
 }
 
-// z += sum_k U[k] coef[kCoarseMax + k]
+// g = E^-1 AU^T y (from part2); z = y + U (c - g); the CG's partial dots
+// r.z, r.r (and z.r_prev when flexible) into part + kCgBlocks..
+template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_post(double* z, const float* __restrict__ U, long long ld, int kc, long long n3,
-                  const double* __restrict__ coef) {
-  __shared__ float c[kCoarseMax];
-  if (threadIdx.x < kCoarseMax)
-    c[threadIdx.x] = threadIdx.x < kc ? (float)coef[kCoarseMax + threadIdx.x] : 0.f;
+    k_coarse_post(CgVecs v, const float* __restrict__ U, const double* __restrict__ part2,
+                  const double* __restrict__ einv, int kc, const double* __restrict__ coef,
+                  int flexible) {
+  __shared__ double d[KP], gd[KP];
+  __shared__ float w[KP];
+  coarse_solve_block<KP>(part2, einv, kc, d, gd);
+  if (threadIdx.x < KP) w[threadIdx.x] = (float)(coef[threadIdx.x] - gd[threadIdx.x]);
   __syncthreads();
+  const long long n3 = 3 * v.npix;
+  double acc[3] = {0.0, 0.0, 0.0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
+    const float4* row = reinterpret_cast<const float4*>(U + i * KP);
     float s = 0.f;
 #pragma unroll
-    for (int k = 0; k < kCoarseMax; k++)
-      if (k < kc) s = fmaf(U[k * ld + i], c[k], s);
-    z[i] += (double)s;
+    for (int q = 0; q < KP / 4; q++) {
+      const float4 u = row[q];
+      s = fmaf(u.x, w[4 * q], s);
+      s = fmaf(u.y, w[4 * q + 1], s);
+      s = fmaf(u.z, w[4 * q + 2], s);
+      s = fmaf(u.w, w[4 * q + 3], s);
+    }
+    const double z = v.z[i] + (double)s, r = v.r[i];
+    v.z[i] = z;
+    acc[0] += r * z;
+    acc[1] += r * r;
+    if (flexible) acc[2] += z * v.rprev[i];
   }
+  block_reduce_store<3>(acc, v.part + kCgBlocks, kCgBlocks);
 }
 
-cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, cudaStream_t st) {
-  if (cs.kc < 1 || cs.kc > kCoarseMax) return cudaErrorInvalidValue;
+template <int KP>
+static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int flexible,
+                                   cudaStream_t st) {
   const long long n3 = 3 * v.npix;
-  k_coarse_dots<<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, cs.ld, cs.kc, n3, v.r, cs.part);
-  k_coarse_solve<<<1, 1024, 0, st>>>(cs.part, cs.kc, cs.einv, cs.coef, 0);
-  k_coarse_pre<<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, cs.ld, cs.kc, cs.coef);
-  k_coarse_dots<<<kCgBlocks, kCgThreads, 0, st>>>(cs.au, cs.ld, cs.kc, n3, v.z, cs.part);
-  k_coarse_solve<<<1, 1024, 0, st>>>(cs.part, cs.kc, cs.einv, cs.coef, 1);
-  k_coarse_post<<<kCgBlocks, kCgThreads, 0, st>>>(v.z, cs.u, cs.ld, cs.kc, n3, cs.coef);
+  double* part1 = cs.part;
+  double* part2 = cs.part + (size_t)kCoarseMax * kCgBlocks;
+  k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
+  k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef);
+  k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.au, n3, v.z, part2);
+  k_coarse_post<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.u, part2, cs.einv, cs.kc, cs.coef,
+                                                       flexible);
   return cudaGetLastError();
+}
+
+int coarse_pad(int kc) { return (kc + 7) / 8 * 8; }
+
+cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, int flexible, cudaStream_t st) {
+  if (cs.kc < 1 || cs.kc > kCoarseMax) return cudaErrorInvalidValue;
+  switch (coarse_pad(cs.kc)) {
+    case 8: return coarse_apply_kp<8>(v, cs, flexible, st);
+    case 16: return coarse_apply_kp<16>(v, cs, flexible, st);
+    case 24: return coarse_apply_kp<24>(v, cs, flexible, st);
+    default: return coarse_apply_kp<32>(v, cs, flexible, st);
+  }
 }
 
 // ---- building the coarse space ------------------------------------------------
@@ -564,34 +615,44 @@ cudaError_t gram_launch(const double* X, const double* Y, long long ld, int m, l
   return cudaGetLastError();
 }
 
-// out[k][i] = (float) sum_j V[j][i] C[j][k]   (C [m][kc] FP64, m * kc <= 4096)
+// out[i][k] = (float) sum_j V[j][i] C[j][k] for k < kc, 0 for kc <= k < kp
+// (C [m][kc] FP64); one block per 256 elements, C staged through shared
+// memory in chunks of rows
 __global__ void __launch_bounds__(kCgThreads)
     k_combine(const double* __restrict__ V, long long ld, int m, const double* __restrict__ C,
-              int kc, long long n, float* out) {
-  __shared__ double cs[4096];
-  for (int e = threadIdx.x; e < m * kc; e += blockDim.x) cs[e] = C[e];
-  __syncthreads();
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double acc[kCoarseMax];
+              int kc, int kp, long long n, float* out) {
+  constexpr int kChunk = 4096;
+  __shared__ double cs[kChunk];
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double acc[kCoarseMax];
 #pragma unroll
-    for (int k = 0; k < kCoarseMax; k++) acc[k] = 0.0;
-    for (int j = 0; j < m; j++) {
-      const double vj = V[j * ld + i];
+  for (int k = 0; k < kCoarseMax; k++) acc[k] = 0.0;
+  const int rows = kChunk / kc;
+  for (int j0 = 0; j0 < m; j0 += rows) {
+    const int j1 = j0 + rows < m ? j0 + rows : m;
+    __syncthreads();
+    for (int e = threadIdx.x; e < (j1 - j0) * kc; e += blockDim.x) cs[e] = C[j0 * kc + e];
+    __syncthreads();
+    if (i < n)
+      for (int j = j0; j < j1; j++) {
+        const double vj = V[j * ld + i];
 #pragma unroll
-      for (int k = 0; k < kCoarseMax; k++)
-        if (k < kc) acc[k] += vj * cs[j * kc + k];
-    }
+        for (int k = 0; k < kCoarseMax; k++)
+          if (k < kc) acc[k] += vj * cs[(j - j0) * kc + k];
+      }
+  }
+  if (i < n) {
 #pragma unroll
     for (int k = 0; k < kCoarseMax; k++)
-      if (k < kc) out[k * ld + i] = (float)acc[k];
+      if (k < kp) out[i * kp + k] = k < kc ? (float)acc[k] : 0.f;
   }
 }
 
 cudaError_t combine_launch(const double* V, long long ld, int m, const double* C, int kc,
                            long long n, float* out, cudaStream_t st) {
-  if (kc < 1 || kc > kCoarseMax || m * kc > 4096) return cudaErrorInvalidValue;
-  k_combine<<<kCgBlocks * 4, kCgThreads, 0, st>>>(V, ld, m, C, kc, n, out);
+  if (kc < 1 || kc > kCoarseMax || m < 1) return cudaErrorInvalidValue;
+  const long long blocks = (n + kCgThreads - 1) / kCgThreads;
+  k_combine<<<(unsigned)blocks, kCgThreads, 0, st>>>(V, ld, m, C, kc, coarse_pad(kc), n, out);
   return cudaGetLastError();
 }
 

@@ -98,7 +98,7 @@ struct sg_ctx {
   int npatch = 0, npatch_pad = 0;
   bool have_mlp = false, use_syn = false;
   bool learned_enabled = false;  // validation: a learned component beat plain PCG
-  // learned coarse space: U, AU = A U [kc][3 npix] FP32, E^-1 [kc][kc] FP64
+  // learned coarse space: U, AU = A U [3 npix][coarse_pad(kc)] FP32, E^-1 [kc][kc] FP64
   DevBuf cs_u, cs_au, cs_einv, cs_coef, cs_part;
   int coarse_k = 0;
   int learned_kind = 0;  // SG_PRECOND_LEARNED applies 1: the network, 2: the coarse space
@@ -313,19 +313,19 @@ struct sg_ctx {
       if (e == cudaSuccess) e = cg_refresh_r(v, 1, 1, st);
       launches++;
     }
-    if (e == cudaSuccess) e = learned_z();
-    if (e == cudaSuccess) e = cg_dots(v, 1, st);
+    if (e == cudaSuccess) e = learned_z(1);
     if (e == cudaSuccess)
       e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 1, st)
               : cg_step_c<double>(v, dmap.as<double>(), 1, st);
-    launches += 2;
+    launches += 1;
     return e;
   }
-  cudaError_t learned_z();  // z from r: the network (sg_learn.cu) or the coarse space
+  // z from r by the network (sg_learn.cu) or the coarse space, then the CG's
+  // partial dots r.z, r.r (and z.r_prev when flexible)
+  cudaError_t learned_z(int flexible);
   CoarseSpace coarse() const {
     CoarseSpace c{};
     c.kc = coarse_k;
-    c.ld = 3 * npix;
     c.u = cs_u.as<float>();
     c.au = cs_au.as<float>();
     c.einv = cs_einv.as<double>();

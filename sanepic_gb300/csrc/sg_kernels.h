@@ -185,23 +185,25 @@ cudaError_t to_map4(const double* x, long long npix, T* map, cudaStream_t st);
 cudaError_t mask_qu(double* v, const int* hits_true, long long npix, cudaStream_t st);
 cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStream_t st);
 
-// two-level preconditioner: coarse space U [kc][ld] (FP32), AU = A U, E^-1 [kc][kc]
+// two-level preconditioner: coarse space U [3 npix][kp] (FP32, element-major,
+// kp = coarse_pad(kc) columns, the last kp - kc zero), AU = A U, E^-1 [kc][kc]
 constexpr int kCoarseMax = 32;
+int coarse_pad(int kc);
 struct CoarseSpace {
   int kc;             // columns (1..kCoarseMax)
-  long long ld;       // row stride of u, au (>= 3 npix)
   const float* u;
   const float* au;
   const double* einv;
-  double* coef;       // [2 * kCoarseMax] scratch
-  double* part;       // [kCoarseMax][kCgBlocks] scratch
+  double* coef;       // [kCoarseMax] scratch
+  double* part;       // [2][kCoarseMax][kCgBlocks] scratch
 };
-// v.z = z(v.r) of the balancing two-level preconditioner around v's M
-cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, cudaStream_t st);
+// v.z = z(v.r) of the balancing two-level preconditioner around v's M, and
+// the CG partial dots r.z, r.r (z.r_prev if flexible) as cg_dots leaves them
+cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, int flexible, cudaStream_t st);
 // part [nsplit][m][m]: split-K partial Gram matrices X Y^T of FP64 rows [m][ld] over n
 cudaError_t gram_launch(const double* X, const double* Y, long long ld, int m, long long n,
                         int nsplit, double* part, cudaStream_t st);
-// out [kc][ld] (FP32) = C^T V, V [m][ld] FP64, C [m][kc] FP64 (m * kc <= 4096)
+// out [n][coarse_pad(kc)] (FP32, element-major) = (C^T V)^T, V [m][ld] FP64, C [m][kc] FP64
 cudaError_t combine_launch(const double* V, long long ld, int m, const double* C, int kc,
                            long long n, float* out, cudaStream_t st);
 

@@ -279,12 +279,14 @@ static int build_patches(sg_ctx* c) {
 }  // namespace sg
 
 // z = M_bj3 r + network correction, or the two-level coarse-space
-// preconditioner (graph-capturable: no host sync)
-cudaError_t sg_ctx::learned_z() {
+// preconditioner, and the CG's partial dots (graph-capturable: no host sync)
+cudaError_t sg_ctx::learned_z(int flexible) {
   CgVecs vb = vecs(1);
   if (learned_kind == 2) {
-    launches += 6;
-    return coarse_apply(vb, coarse(), st);
+    CgVecs vf = vecs(1);
+    vf.rprev = flexible ? rprev.as<double>() : nullptr;
+    launches += 4;
+    return coarse_apply(vf, coarse(), flexible, st);
   }
   cudaError_t e = apply_precond(vb, r.as<double>(), z.as<double>(), st);
   if (e != cudaSuccess) return e;
@@ -295,8 +297,10 @@ cudaError_t sg_ctx::learned_z() {
   if (e != cudaSuccess) return e;
   k_patch_scatter<<<npatch, kPatch, 0, st>>>(mlp->y, patch_sig.as<float>(), patch_idx.as<int>(),
                                              npix, hits.as<int>(), z.as<double>());
-  launches += 3 + 8;  // precond, gather, scatter, 4 GEMMs + 4 bias/activation kernels
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cg_dots(vecs(2), flexible, st);
+  launches += 4 + 8;  // precond, gather, scatter, dots, 4 GEMMs + 4 bias/activation kernels
+  return e;
 }
 
 namespace {
@@ -382,8 +386,7 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   if (e == cudaSuccess) e = cudaEventRecord(e0, c->st);
   if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
   if (pc == 2) {
-    if (e == cudaSuccess) e = c->learned_z();
-    if (e == cudaSuccess) e = cg_dots(v2, 0, c->st);
+    if (e == cudaSuccess) e = c->learned_z(0);
     if (e == cudaSuccess)
       e = c->f32 ? cg_reinit_d<float>(v2, c->dmap.as<float>(), c->st)
                  : cg_reinit_d<double>(v2, c->dmap.as<double>(), c->st);
@@ -561,7 +564,6 @@ namespace sg {
 int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
   const long long n3 = 3 * c->npix;
   if (m < 2) return SG_OK;
-  if (m * kc > 4096) m = 4096 / kc;
   DevBuf V, W, gp, dC;
   const int nsplit = 16;
   cudaError_t e = V.alloc((size_t)m * n3 * 8);
@@ -593,11 +595,12 @@ int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
   c->drop_graphs();
   e = dC.alloc((size_t)m * k * 8);
   if (e == cudaSuccess) e = cudaMemcpy(dC.p, C.data(), (size_t)m * k * 8, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = c->cs_u.alloc((size_t)k * n3 * 4);
-  if (e == cudaSuccess) e = c->cs_au.alloc((size_t)k * n3 * 4);
+  const int kp = coarse_pad(k);
+  if (e == cudaSuccess) e = c->cs_u.alloc((size_t)kp * n3 * 4);
+  if (e == cudaSuccess) e = c->cs_au.alloc((size_t)kp * n3 * 4);
   if (e == cudaSuccess) e = c->cs_einv.alloc((size_t)k * k * 8);
-  if (e == cudaSuccess) e = c->cs_coef.alloc(2 * kCoarseMax * 8);
-  if (e == cudaSuccess) e = c->cs_part.alloc((size_t)kCoarseMax * kCgBlocks * 8);
+  if (e == cudaSuccess) e = c->cs_coef.alloc(kCoarseMax * 8);
+  if (e == cudaSuccess) e = c->cs_part.alloc((size_t)2 * kCoarseMax * kCgBlocks * 8);
   if (e == cudaSuccess)
     e = cudaMemcpy(c->cs_einv.p, einv.data(), (size_t)k * k * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -624,8 +627,8 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   const uint64_t seed0 = o->seed > 0 ? (uint64_t)o->seed : 5000;
   const int steps = o->steps > 0 ? o->steps : (o->steps < 0 ? 0 : 1500);  // 0: no network
   const int coarse_k = o->coarse_k > 0 ? std::min(o->coarse_k, kCoarseMax)
-                                       : (o->coarse_k < 0 ? 0 : 16);  // 0: no coarse space
-  const int coarse_m = o->coarse_vectors > 0 ? o->coarse_vectors : 192;
+                                       : (o->coarse_k < 0 ? 0 : 24);  // 0: no coarse space
+  const int coarse_m = o->coarse_vectors > 0 ? o->coarse_vectors : 256;
   const float lr = o->lr > 0.f ? o->lr : 1e-3f;
   const double pair_crit = o->pair_crit > 0.0 ? o->pair_crit : 1e-13;
   cudaSetDevice(c->desc.device);
