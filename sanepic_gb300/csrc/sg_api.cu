@@ -393,7 +393,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
     c->npatch = c->npatch_pad = 0;
     c->coarse_k = 0;
     if (c->learned_kind == 2) {
-      c->learned_kind = 0;
+      c->set_learned_kind(0);
       c->learned_enabled = false;
     }
   }

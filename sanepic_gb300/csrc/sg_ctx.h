@@ -102,6 +102,11 @@ struct sg_ctx {
   DevBuf cs_u, cs_au, cs_einv, cs_coef, cs_part;
   int coarse_k = 0;
   int learned_kind = 0;  // SG_PRECOND_LEARNED applies 1: the network, 2: the coarse space
+  // captured learned iterations embed the kind: change it only through here
+  void set_learned_kind(int k) {
+    if (k != learned_kind) drop_graphs();
+    learned_kind = k;
+  }
   const void* tod_active() const { return use_syn ? tod_syn.p : tod.p; }
   cplx<float> wn1f{1.f, 0.f};
   cplx<double> wn1d{1.0, 0.0};
@@ -342,8 +347,8 @@ struct sg_ctx {
     graph_launches.clear();
   }
 
-  cudaError_t run_iteration(int precond, bool refresh, bool use_graph) {
-    if (!use_graph) return enqueue_iteration(precond, refresh);
+  // the captured iteration for (precond, refresh), captured on first use
+  cudaError_t iteration_graph(int precond, bool refresh, cudaGraphExec_t* out) {
     auto key = std::make_pair(precond, refresh ? 1 : 0);
     auto it = graphs.find(key);
     if (it == graphs.end()) {
@@ -363,8 +368,17 @@ struct sg_ctx {
       if (e != cudaSuccess) return e;
       it = graphs.emplace(key, ge).first;
     }
-    launches += graph_launches[key];
-    return cudaGraphLaunch(it->second, st);
+    *out = it->second;
+    return cudaSuccess;
+  }
+
+  cudaError_t run_iteration(int precond, bool refresh, bool use_graph) {
+    if (!use_graph) return enqueue_iteration(precond, refresh);
+    cudaGraphExec_t ge;
+    cudaError_t e = iteration_graph(precond, refresh, &ge);
+    if (e != cudaSuccess) return e;
+    launches += graph_launches[std::make_pair(precond, refresh ? 1 : 0)];
+    return cudaGraphLaunch(ge, st);
   }
 };
 

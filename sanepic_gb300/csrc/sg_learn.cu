@@ -381,7 +381,12 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  cudaError_t e = cudaMemsetAsync(c->x.p, 0, 8 * n3, c->st);
+  // both iteration graphs are captured before the clock starts, so the
+  // comparison times iterations, not graph instantiation
+  cudaGraphExec_t g0, g1;
+  cudaError_t e = c->iteration_graph(pc, false, &g0);
+  if (e == cudaSuccess) e = c->iteration_graph(pc, true, &g1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->x.p, 0, 8 * n3, c->st);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->r.p, 0, 8 * n3, c->st);
   if (e == cudaSuccess) e = cudaEventRecord(e0, c->st);
   if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
@@ -399,7 +404,7 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   const double var00 = c->sc_host->var00;
   int it = 0;
   for (; it < 1000 && e == cudaSuccess; it++) {
-    e = c->run_iteration(pc, it % 10 == 0, false);
+    e = c->run_iteration(pc, it % 10 == 0, true);  // graph replay, as the solves run
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -768,34 +773,36 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   const double vcrit = o->val_crit > 0.0 ? o->val_crit : 1e-12;
   ValSolve vp, vl, vc;
   c->use_syn = true;
+  c->drop_graphs();  // refresh iterations captured earlier read the real timeline
   e = synth_rhs(c, seed0 + 1000003);
   if (e == cudaSuccess) e = val_solve(c, 1, vcrit, vp);
   if (e == cudaSuccess && steps > 0) {
-    c->learned_kind = 1;
+    c->set_learned_kind(1);
     e = val_solve(c, 2, vcrit, vl);
   }
   if (e == cudaSuccess && c->coarse_k > 0) {
-    c->learned_kind = 2;
+    c->set_learned_kind(2);
     e = val_solve(c, 2, vcrit, vc);
   }
   c->use_syn = false;
+  c->drop_graphs();  // the validation's graphs read the synthetic timeline, released here
   c->tod_syn.release();
   c->have_solution = false;
   if (e != cudaSuccess) return c->cuda_fail(e, "validation");
   double best = vp.ms;
-  c->learned_kind = 0;
+  c->set_learned_kind(0);
   if (steps > 0 && vl.converged && vl.ms < best) {
-    c->learned_kind = 1;
+    c->set_learned_kind(1);
     best = vl.ms;
   }
   if (c->coarse_k > 0 && vc.converged && vc.ms < best) {
-    c->learned_kind = 2;
+    c->set_learned_kind(2);
     best = vc.ms;
   }
   if (o->force == 2 && c->coarse_k > 0)
-    c->learned_kind = 2;
+    c->set_learned_kind(2);
   else if (o->force != 0 && steps > 0)
-    c->learned_kind = 1;
+    c->set_learned_kind(1);
   c->learned_enabled = c->learned_kind != 0;
   if (rep) {
     rep->val_plain_iters = vp.iters;
@@ -852,7 +859,7 @@ extern "C" int sg_learn_set_params(sg_ctx* c, const float* params) {
   if (e != cudaSuccess) return c->cuda_fail(e, "set params");
   c->have_mlp = true;
   c->learned_enabled = true;  // an explicitly loaded network is used as given
-  c->learned_kind = 1;
+  c->set_learned_kind(1);
   return SG_OK;
 }
 
