@@ -246,11 +246,12 @@ class MapMaker:
 
     def solve(self, precond: str = "bj3", stop_crit: float = 1e-15, maxiter: int = 2000,
               refresh_every: int = 10, verbose: bool = False, x0=None,
-              use_graph: bool = True, on_iteration=None) -> dict:
-        """Run PCG.  The report dict also holds `history`: one
-        (iter, crit, crit2, chi2) row per iteration (the reference's printed
-        line).  on_iteration(iter, crit, crit2, chi2) -> bool (True stops)
-        runs after each iteration."""
+              use_graph: bool = True, on_iteration=None, history: bool = False) -> dict:
+        """Run PCG.  on_iteration(iter, crit, crit2, chi2) -> bool (True
+        stops) runs after each iteration; with history=True the report also
+        holds `history`, one (iter, crit, crit2, chi2) row per iteration (the
+        reference's printed line).  chi^2 of the refresh iterations is computed
+        only when a callback, history or verbose asks for it."""
         x0p = None
         if x0 is not None:
             self._x0 = _f64(x0)
@@ -261,13 +262,14 @@ class MapMaker:
             hist.append((it, crit, crit2, chi2))
             return int(bool(on_iteration(it, crit, crit2, chi2))) if on_iteration else 0
 
-        cb = ITER_CB(_cb)
+        cb = ITER_CB(_cb) if (on_iteration or history) else ITER_CB()
         o = SgSolveOpts(PRECOND[precond], stop_crit, maxiter, refresh_every, int(verbose),
                         x0p, int(use_graph), cb, None)
         rep = SgReport()
         self._check(self.L.sg_solve(self.h, ctypes.byref(o), ctypes.byref(rep)))
         out = {k: getattr(rep, k) for k, _ in SgReport._fields_}
-        out["history"] = np.array(hist, dtype=np.float64).reshape(-1, 4)
+        if history:
+            out["history"] = np.array(hist, dtype=np.float64).reshape(-1, 4)
         return out
 
     # ---- outputs ------------------------------------------------------------

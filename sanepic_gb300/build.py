@@ -24,8 +24,11 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 UNITS = {
     "sg_filter.cu": [],
+    "sg_filter_spec.cu": [],
+    "sg_filter_spec64.cu": [],
     "sg_setup.cu": [],
     "sg_pt.cu": [],
+    "sg_group.cu": [],
     "sg_cg.cu": [],
     "sg_api.cu": [],
     "sg_noalloc.cu": [],

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <map>
@@ -367,6 +368,30 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
                          nsd, gsc.as<double>(), gss.as<double>(), npix, c->sumcross.as<double>(),
                          c->st));
   SG_TRY(c->ys.alloc((size_t)4 * ng * c->esize));
+  // the offset-group operator when every group is large enough (three
+  // timelines per group instead of one per detector); SANEPIC_GPU_GROUP_FILTER=0
+  // keeps the per-detector operator
+  {
+    int gmin = (int)ndet;
+    for (int g = 0; g < G; g++) gmin = std::min(gmin, c->grp_off_h[g + 1] - c->grp_off_h[g]);
+    const char* env = getenv("SANEPIC_GPU_GROUP_FILTER");
+    c->group_mode = gmin >= sg_ctx::kGroupMin && !(env && env[0] == '0');
+    c->have_hmix = false;
+    if (c->group_mode) {
+      const long long M1 = ns / 2 + 1;
+      SG_TRY(c->gtl.alloc((size_t)3 * ng * c->esize));
+      SG_TRY(c->gspec.alloc((size_t)3 * G * nseg * M1 * 2 * c->esize));
+      SG_TRY(c->hmix.alloc((size_t)G * M1 * 6 * c->esize));
+      SG_TRY(c->dspec.alloc((size_t)ndet * nseg * M1 * 2 * c->esize));
+      SG_TRY(c->rhs_part.alloc(sizeof(double) * kGroupRhsBlocks));
+    } else {
+      c->gtl.release();
+      c->gspec.release();
+      c->hmix.release();
+      c->dspec.release();
+      c->rhs_part.release();
+    }
+  }
   // CG vectors
   const size_t vb = sizeof(double) * 3 * npix;
   SG_TRY(c->x.alloc(vb));
@@ -435,7 +460,7 @@ extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) 
   std::copy(spn.begin(), spn.end(), c->spn_h.begin() + det * (M + 1));
   if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
   c->have_noise[det] = 1;
-  c->have_bj3 = c->have_diag = c->have_rhs = false;
+  c->have_bj3 = c->have_diag = c->have_rhs = c->have_hmix = false;
   return SG_OK;
 }
 
@@ -489,7 +514,13 @@ static int check_ready(sg_ctx* c, bool need_tod) {
     if (!c->have_noise[dd]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", dd);
     if (need_tod && !c->have_tod[dd]) return c->fail(SG_ERR_STATE, "TOD of detector %lld not set", dd);
   }
-  return SG_OK;
+  return prepare_operator(c);
+}
+
+int prepare_operator(sg_ctx* c) {
+  cudaSetDevice(c->desc.device);
+  const cudaError_t e = c->ensure_hmix();
+  return e == cudaSuccess ? SG_OK : c->cuda_fail(e, "group operator set-up");
 }
 
 extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
@@ -498,9 +529,7 @@ extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
   double* dchi2 = &c->sc.as<CgScalars>()->chi2;
-  cudaError_t e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0,
-                                   nullptr, dchi2);
-  if (e == cudaSuccess) e = c->pt_of_y(c->b.as<double>(), true);
+  cudaError_t e = c->rhs_of(c->tod.p, c->b.as<double>(), dchi2);
   double h = 0.0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dchi2, sizeof(double), cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -656,6 +685,8 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED && c->learned_kind == 1)
     rc = ensure_patches(c);
   if (rc) return rc;
+  // chi^2 of the refresh iterations is computed only where it is seen
+  c->refresh_chi2 = o->verbose != 0 || o->on_iteration != nullptr;
   // 0: reference diagonal, 1: block-Jacobi, 2: block-Jacobi + a learned part
   // (the network or the coarse space; flexible PCG)
   int pc = (o->precond == SG_PRECOND_BJ3) ? 1 : (o->precond == SG_PRECOND_DIAG ? 0 : 2);
@@ -868,13 +899,50 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   for (auto& x : ev) cudaEventCreate(&x);
   cudaError_t e = c->to_map(c->d.as<double>());
   float tot[4] = {0.f, 0.f, 0.f, 0.f};
+  const long long nsd = c->ns * c->nseg, M1 = c->ns / 2 + 1, gt = 3LL * c->ngroups * c->nseg;
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
     e = cudaEventRecord(ev[0], c->st);
-    if (e == cudaSuccess) e = c->launch_project();
-    if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
-    if (e == cudaSuccess) e = c->launch_filter(kLoadTod, c->y.p, c->y.p, c->ntiles, (int)c->nseg, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-    if (e == cudaSuccess) e = c->launch_detsum();
+    if (c->group_mode) {
+      // projection = (a, b1, b2); N^-1 = forward FFTs + 3 x 3 mixing + inverse
+      // FFTs; detector sums = the interleave into P^T's layout
+      if (c->f32) {
+        if (e == cudaSuccess)
+          e = group_project_launch<float>(c->pix.as<int>(), c->cs.as<float>(), c->dmap.as<float>(),
+                                          c->ngsamp, nsd, c->gtl.as<float>(), c->st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
+        if (e == cudaSuccess) e = c->launch_filter_spec(c->gtl.p, nullptr, c->gspec.p, nullptr, gt);
+        if (e == cudaSuccess)
+          e = group_mix_launch<float>(c->gspec.as<cplx<float>>(), c->hmix.as<float>(), c->ngroups,
+                                      c->nseg, M1, c->st);
+        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->gtl.p, nullptr, c->gspec.p, gt);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
+        if (e == cudaSuccess)
+          e = group_interleave_launch<float>(c->gtl.as<float>(), c->ngsamp, nsd, c->ys.as<float>(),
+                                             c->st);
+      } else {
+        if (e == cudaSuccess)
+          e = group_project_launch<double>(c->pix.as<int>(), c->cs.as<double>(),
+                                           c->dmap.as<double>(), c->ngsamp, nsd,
+                                           c->gtl.as<double>(), c->st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
+        if (e == cudaSuccess) e = c->launch_filter_spec(c->gtl.p, nullptr, c->gspec.p, nullptr, gt);
+        if (e == cudaSuccess)
+          e = group_mix_launch<double>(c->gspec.as<cplx<double>>(), c->hmix.as<double>(),
+                                       c->ngroups, c->nseg, M1, c->st);
+        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->gtl.p, nullptr, c->gspec.p, gt);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
+        if (e == cudaSuccess)
+          e = group_interleave_launch<double>(c->gtl.as<double>(), c->ngsamp, nsd,
+                                              c->ys.as<double>(), c->st);
+      }
+    } else {
+      if (e == cudaSuccess) e = c->launch_project();
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
+      if (e == cudaSuccess)
+        e = c->launch_filter(kLoadTod, c->y.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
+      if (e == cudaSuccess) e = c->launch_detsum();
+    }
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], c->st);
     if (e == cudaSuccess) e = c->launch_pt(c->q.as<double>(), true);
     if (e == cudaSuccess) e = cudaEventRecord(ev[4], c->st);

@@ -126,6 +126,7 @@ extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_r
       return c->fail(SG_ERR_STATE, "no trained network or coarse space");
     cudaSetDevice(c->desc.device);
     int rc = (o->precond == SG_PRECOND_DIAG) ? build_diag(c) : build_bj3(c);
+    if (rc == SG_OK) rc = prepare_operator(c);
     if (rc == SG_OK && o->precond == SG_PRECOND_LEARNED && c->learned_kind == 1)
       rc = ensure_patches(c);
     if (rc) return rc;
@@ -136,6 +137,7 @@ extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_r
       j.pc = 1;
       j.fallback = 0;
     }
+    c->refresh_chi2 = false;  // no printed lines in a batch
     cudaEventCreateWithFlags(&j.ready, cudaEventDisableTiming);
     if (!c->ev0) cudaEventCreate(&c->ev0);
     if (!c->ev1) cudaEventCreate(&c->ev1);

@@ -87,6 +87,12 @@ struct sg_ctx {
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
   DevBuf chi2p;  // per-CTA chi^2 partials of the noise filter
+  // offset-group operator (sg_group.cu): used when every group has at least
+  // kGroupMin detectors; gtl [G][3][nsd], gspec [G][3][nseg][M+1] complex,
+  // hmix [G][M+1][6]
+  static constexpr int kGroupMin = 4;
+  bool group_mode = false, have_hmix = false;
+  DevBuf gtl, gspec, hmix, dspec, rhs_part;  // + data spectra [ndet][nseg][M+1], chi^2 partials
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
   std::vector<double> spn_h;  // host copy of the filter rows [ndet][M+1] (FP64)
 
@@ -243,9 +249,111 @@ struct sg_ctx {
   }
 
   cudaError_t apply_map(double* out, bool masked) {
+    if (group_mode) return apply_map_group(out, masked);
     cudaError_t e = launch_project();
     if (e == cudaSuccess) e = launch_filter(kLoadTod, y.p, y.p, ntiles, (int)nseg, 0);
     if (e == cudaSuccess) e = pt_of_y(out, masked);
+    return e;
+  }
+
+  // forward FFT of tiles to spec_out, or inverse FFT of spec_in to tiles
+  cudaError_t launch_filter_spec(const void* in, void* out, void* spec_out, const void* spec_in,
+                                 long long ntiles_) {
+    const int ncl = (int)std::min<long long>(nclusters, ntiles_);
+    launches++;
+    if (f32) {
+      auto a = filter_args<float>(kLoadTod, (const float*)in, (float*)out, ntiles_, (int)nseg, 0,
+                                  nullptr, nullptr);
+      a.wn1 = wn1f;
+      a.spec_out = (cplx<float>*)spec_out;
+      a.spec_in = (const cplx<float>*)spec_in;
+      return filter_spec_launch<float>(a, logm, S, ncl, st);
+    }
+    auto a = filter_args<double>(kLoadTod, (const double*)in, (double*)out, ntiles_, (int)nseg, 0,
+                                 nullptr, nullptr);
+    a.wn1 = wn1d;
+    a.spec_out = (cplx<double>*)spec_out;
+    a.spec_in = (const cplx<double>*)spec_in;
+    return filter_spec_launch<double>(a, logm, S, ncl, st);
+  }
+
+  // the per-group mixing matrices from the filter rows (before any group apply)
+  cudaError_t ensure_hmix() {
+    if (!group_mode || have_hmix) return cudaSuccess;
+    const long long M1 = ns / 2 + 1;
+    cudaError_t e = f32 ? group_hmix_launch<float>(filt.as<float>(), dcs.as<float>(),
+                                                   grp_off.as<int>(), grp_det.as<int>(), ngroups,
+                                                   M1, hmix.as<float>(), st)
+                        : group_hmix_launch<double>(filt.as<double>(), dcs.as<double>(),
+                                                    grp_off.as<int>(), grp_det.as<int>(), ngroups,
+                                                    M1, hmix.as<double>(), st);
+    launches++;
+    if (e == cudaSuccess) have_hmix = true;
+    return e;
+  }
+
+  // b = P^T N^-1 d for the timelines d (device, one row per detector) and
+  // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
+  // their weighted sums per group and frequency, three inverse FFTs per group.
+  cudaError_t rhs_of(const void* d, double* bout, double* chi2_dev) {
+    if (!group_mode) {
+      cudaError_t e = launch_filter(kLoadTod, d, y.p, ntiles, (int)nseg, 0, nullptr, chi2_dev);
+      if (e == cudaSuccess) e = pt_of_y(bout, true);
+      return e;
+    }
+    const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
+    cudaError_t e = launch_filter_spec(d, nullptr, dspec.p, nullptr, ntiles);
+    launches += 3;  // sums, chi^2, interleave
+    if (f32) {
+      if (e == cudaSuccess)
+        e = group_rhs_launch<float>(dspec.as<cplx<float>>(), filt.as<float>(), dcs.as<float>(),
+                                    grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
+                                    gspec.as<cplx<float>>(), rhs_part.as<double>(),
+                                    kGroupRhsBlocks, st);
+    } else {
+      if (e == cudaSuccess)
+        e = group_rhs_launch<double>(dspec.as<cplx<double>>(), filt.as<double>(), dcs.as<double>(),
+                                     grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
+                                     gspec.as<cplx<double>>(), rhs_part.as<double>(),
+                                     kGroupRhsBlocks, st);
+    }
+    if (e == cudaSuccess) e = chi2_sum(rhs_part.as<double>(), kGroupRhsBlocks, chi2_dev, st);
+    if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
+    if (e == cudaSuccess)
+      e = f32 ? group_interleave_launch<float>(gtl.as<float>(), ngsamp, nsd, ys.as<float>(), st)
+              : group_interleave_launch<double>(gtl.as<double>(), ngsamp, nsd, ys.as<double>(), st);
+    if (e == cudaSuccess) e = launch_pt(bout, true);
+    return e;
+  }
+
+  // A for offset groups: (a, b1, b2) per group sample, their half spectra,
+  // the 3 x 3 mixing per frequency, the inverse FFTs, then P^T
+  cudaError_t apply_map_group(double* out, bool masked) {
+    const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
+    cudaError_t e;
+    launches += 3;
+    if (f32) {
+      e = group_project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
+                                      nsd, gtl.as<float>(), st);
+      if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
+      if (e == cudaSuccess)
+        e = group_mix_launch<float>(gspec.as<cplx<float>>(), hmix.as<float>(), ngroups, nseg, M1,
+                                    st);
+      if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
+      if (e == cudaSuccess)
+        e = group_interleave_launch<float>(gtl.as<float>(), ngsamp, nsd, ys.as<float>(), st);
+    } else {
+      e = group_project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
+                                       nsd, gtl.as<double>(), st);
+      if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
+      if (e == cudaSuccess)
+        e = group_mix_launch<double>(gspec.as<cplx<double>>(), hmix.as<double>(), ngroups, nseg,
+                                     M1, st);
+      if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
+      if (e == cudaSuccess)
+        e = group_interleave_launch<double>(gtl.as<double>(), ngsamp, nsd, ys.as<double>(), st);
+    }
+    if (e == cudaSuccess) e = launch_pt(out, masked);
     return e;
   }
 
@@ -283,21 +391,34 @@ struct sg_ctx {
     if (e == cudaSuccess) e = cg_step_a(v, st);
     if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 0, st);
     launches += 3;  // step a, b, c
-    if (refresh) {
-      // true residual r = P^T N^-1 (d - P x) in one operator pass; the filter
-      // also yields chi^2 of the residual timeline (sanepic.cc:1483-1572)
-      if (e == cudaSuccess) e = to_map(x.as<double>());
-      if (e == cudaSuccess) e = launch_project();
-      if (e == cudaSuccess)
-        e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
-                          &sc.as<CgScalars>()->chi2);
-      if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
-      if (e == cudaSuccess) e = cg_refresh_r(v, 0, 1, st);
-      launches++;
-    }
+    if (refresh && e == cudaSuccess) e = enqueue_true_residual(v, 0);
     if (e == cudaSuccess)
       e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 0, st)
               : cg_step_c<double>(v, dmap.as<double>(), 0, st);
+    return e;
+  }
+
+  // the refresh of sanepic.cc:1483-1572: r = b - A x recomputed, not updated.
+  // Exact form: r = P^T N^-1 (d - P x), one pass per detector, which also
+  // gives chi^2 of the residual timeline.  With the offset-group operator and
+  // no chi^2 wanted (no printed line, no callback) r = b - A x through the
+  // group operator instead, a few percent of the cost.
+  bool refresh_chi2 = true;
+  int refresh_kind() const { return (group_mode && !refresh_chi2) ? 2 : 1; }
+  cudaError_t enqueue_true_residual(const CgVecs& v, int flexible) {
+    cudaError_t e = to_map(x.as<double>());
+    launches++;  // cg_refresh_r
+    if (refresh_kind() == 2) {
+      if (e == cudaSuccess) e = apply_map_group(q.as<double>(), true);
+      if (e == cudaSuccess) e = cg_refresh_r(v, flexible, 0, st);
+      return e;
+    }
+    if (e == cudaSuccess) e = launch_project();
+    if (e == cudaSuccess)
+      e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
+                        &sc.as<CgScalars>()->chi2);
+    if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
+    if (e == cudaSuccess) e = cg_refresh_r(v, flexible, 1, st);
     return e;
   }
 
@@ -308,16 +429,7 @@ struct sg_ctx {
     if (e == cudaSuccess) e = cg_step_a(v, st);
     if (e == cudaSuccess) e = cg_step_b(v, refresh ? 1 : 0, 1, st);
     launches += 2;
-    if (refresh) {
-      if (e == cudaSuccess) e = to_map(x.as<double>());
-      if (e == cudaSuccess) e = launch_project();
-      if (e == cudaSuccess)
-        e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
-                          &sc.as<CgScalars>()->chi2);
-      if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
-      if (e == cudaSuccess) e = cg_refresh_r(v, 1, 1, st);
-      launches++;
-    }
+    if (refresh && e == cudaSuccess) e = enqueue_true_residual(v, 1);
     if (e == cudaSuccess) e = learned_z(1);
     if (e == cudaSuccess)
       e = f32 ? cg_step_c<float>(v, dmap.as<float>(), 1, st)
@@ -349,7 +461,7 @@ struct sg_ctx {
 
   // the captured iteration for (precond, refresh), captured on first use
   cudaError_t iteration_graph(int precond, bool refresh, cudaGraphExec_t* out) {
-    auto key = std::make_pair(precond, refresh ? 1 : 0);
+    auto key = std::make_pair(precond, refresh ? refresh_kind() : 0);
     auto it = graphs.find(key);
     if (it == graphs.end()) {
       cudaGraph_t g;
@@ -377,7 +489,7 @@ struct sg_ctx {
     cudaGraphExec_t ge;
     cudaError_t e = iteration_graph(precond, refresh, &ge);
     if (e != cudaSuccess) return e;
-    launches += graph_launches[std::make_pair(precond, refresh ? 1 : 0)];
+    launches += graph_launches[std::make_pair(precond, refresh ? refresh_kind() : 0)];
     return cudaGraphLaunch(ge, st);
   }
 };
@@ -385,3 +497,4 @@ struct sg_ctx {
 int build_bj3(sg_ctx* c);  // 3x3 block-Jacobi blocks for the current pointing and noise
 int ensure_patches(sg_ctx* c);  // nested patch geometry of the learned preconditioner
 int build_diag(sg_ctx* c);      // the reference's diagonal preconditioner
+int prepare_operator(sg_ctx* c);  // set-up the operator needs before its first application

@@ -1,0 +1,222 @@
+// sg_group.cu -- the operator A = P^T N^-1 P for an offset group (detectors
+// that share one pixel stream) at the cost of three timelines instead of one
+// per detector.
+//
+// With the group's base angle phi and detector d's rotation (c_d, s_d) =
+// (cos 2d', sin 2d'), detector d sees
+//   y_d = a + c_d b1 + s_d b2,   a = I,  b1 = Q cos 2phi + U sin 2phi,
+//                                        b2 = U cos 2phi - Q sin 2phi,
+// and P^T only needs S0 = sum_d y'_d, S1 = sum_d c_d y'_d, S2 = sum_d s_d y'_d
+// of the weighted timelines y'_d = N_d^-1 y_d (sg_pt.cu's k_pt).  Every N_d^-1
+// is diagonal in each segment's Fourier basis (h_d[k]), so per frequency
+//   (S0, S1, S2)^ = H[k] (a, b1, b2)^,   H = sum_d h_d [1 c s]^T [1 c s]
+// with a real symmetric 3 x 3 H per group and frequency.  A group of D
+// detectors then costs 3 forward and 3 inverse FFTs per segment instead of D
+// of each.  This is the same linear map as the reference's per-detector
+// deproject -> FFT -> iSpf -> inverse FFT -> scatter (sanepic.cc:2845-2873,
+// 2390-2445, 2522-2611), regrouped; only the rounding differs.
+#include <cuda_runtime.h>
+
+#include "sg_kernels.h"
+
+namespace sg {
+
+static unsigned blocks_for(long long n, long long cap = 152LL * 16) {
+  long long b = (n + 255) / 256;
+  if (b > cap) b = cap;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// gtl [G][3][nsd]: a, b1, b2 of every group sample
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_project(const int* __restrict__ gpix, const T* __restrict__ gcs,
+                    const T* __restrict__ map, long long ng, long long nsd, T* __restrict__ gtl) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i / nsd, w = i - g * nsd;
+    const int m = gpix[i];
+    const T c = gcs[2 * i], s = gcs[2 * i + 1];
+    const T I = map[4 * (long long)m], Q = map[4 * (long long)m + 1], U = map[4 * (long long)m + 2];
+    T* o = gtl + 3 * g * nsd + w;
+    o[0] = I;
+    o[nsd] = Q * c + U * s;
+    o[2 * nsd] = U * c - Q * s;
+  }
+}
+
+// in place on the half spectra [G][3][nseg][M+1]: (S0, S1, S2) = H (a, b1, b2)
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_mix(cplx<T>* __restrict__ spec, const T* __restrict__ hmix, long long G,
+                long long nseg, long long M1) {
+  const long long n = G * nseg * M1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % M1, gs = i / M1;
+    const long long seg = gs % nseg, g = gs / nseg;
+    cplx<T>* x0 = spec + ((g * 3) * nseg + seg) * M1 + k;
+    cplx<T>* x1 = x0 + nseg * M1;
+    cplx<T>* x2 = x1 + nseg * M1;
+    const T* h = hmix + (g * M1 + k) * 6;
+    const T h0 = h[0], h1 = h[1], h2 = h[2], h11 = h[3], h12 = h[4], h22 = h[5];
+    const cplx<T> a = *x0, b = *x1, c = *x2;
+    *x0 = cplx<T>{h0 * a.x + h1 * b.x + h2 * c.x, h0 * a.y + h1 * b.y + h2 * c.y};
+    *x1 = cplx<T>{h1 * a.x + h11 * b.x + h12 * c.x, h1 * a.y + h11 * b.y + h12 * c.y};
+    *x2 = cplx<T>{h2 * a.x + h12 * b.x + h22 * c.x, h2 * a.y + h12 * b.y + h22 * c.y};
+  }
+}
+
+// ys [G nsd][4] = (S0, S1, S2, 0) per group sample, the layout k_pt reads
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_interleave(const T* __restrict__ gtl, long long ng, long long nsd, T* __restrict__ ys) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i / nsd, w = i - g * nsd;
+    const T* s = gtl + 3 * g * nsd + w;
+    ys[4 * i] = s[0];
+    ys[4 * i + 1] = s[nsd];
+    ys[4 * i + 2] = s[2 * nsd];
+    ys[4 * i + 3] = T(0);
+  }
+}
+
+// hmix [G][M+1][6] = sum over the group's detectors of h_d[k] (1, c, s, cc, cs, ss)
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_hmix(const T* __restrict__ filt, const T* __restrict__ dcs, const int* __restrict__ grp_off,
+                 const int* __restrict__ grp_det, long long G, long long M1, T* __restrict__ hmix) {
+  const long long n = G * M1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i / M1, k = i - g * M1;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
+      const int d = grp_det[e];
+      const double h = (double)filt[d * M1 + k];
+      const double c = (double)dcs[2 * d], s = (double)dcs[2 * d + 1];
+      acc[0] += h;
+      acc[1] += c * h;
+      acc[2] += s * h;
+      acc[3] += c * c * h;
+      acc[4] += c * s * h;
+      acc[5] += s * s * h;
+    }
+    for (int j = 0; j < 6; j++) hmix[i * 6 + j] = (T)acc[j];
+  }
+}
+
+// FP32 sums with Neumaier compensation (FP64: plain sums)
+template <typename T>
+struct CSum {
+  T s = T(0), c = T(0);
+  __device__ __forceinline__ void add(T v) {
+    if constexpr (sizeof(T) == 4) {
+      const T t = s + v;
+      c += (fabsf(s) >= fabsf(v)) ? (s - t) + v : (v - t) + s;
+      s = t;
+    } else {
+      s += v;
+    }
+  }
+  __device__ __forceinline__ T get() const { return s + c; }
+};
+
+// right-hand side of a group from its detectors' data spectra X_d [ndet][nseg][M+1]:
+// gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c_d, s_d), detectors in list order;
+// chi2_part[block] = sum of h_d |X_d|^2 over the block's bins (k = 0..M)
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_rhs(const cplx<T>* __restrict__ dspec, const T* __restrict__ filt,
+                const T* __restrict__ dcs, const int* __restrict__ grp_off,
+                const int* __restrict__ grp_det, long long G, long long nseg, long long M1,
+                cplx<T>* __restrict__ gspec, double* chi2_part) {
+  const long long n = G * nseg * M1;
+  double chi = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % M1, gs = i / M1;
+    const long long seg = gs % nseg, g = gs / nseg;
+    CSum<T> a[6];
+    T cl = T(0);
+    for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
+      const int d = grp_det[e];
+      const cplx<T> x = dspec[((long long)d * nseg + seg) * M1 + k];
+      const T h = filt[d * M1 + k], c = dcs[2 * d], s = dcs[2 * d + 1];
+      const T hx = h * x.x, hy = h * x.y;
+      a[0].add(hx);
+      a[1].add(hy);
+      a[2].add(c * hx);
+      a[3].add(c * hy);
+      a[4].add(s * hx);
+      a[5].add(s * hy);
+      cl += h * (x.x * x.x + x.y * x.y);
+    }
+    chi += (double)cl;
+    cplx<T>* o = gspec + ((g * 3) * nseg + seg) * M1 + k;
+    o[0] = cplx<T>{a[0].get(), a[1].get()};
+    o[nseg * M1] = cplx<T>{a[2].get(), a[3].get()};
+    o[2 * nseg * M1] = cplx<T>{a[4].get(), a[5].get()};
+  }
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) chi += __shfl_xor_sync(0xffffffffu, chi, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = chi;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; w++) t += red[w];
+    chi2_part[blockIdx.x] = t;
+  }
+}
+
+template <typename T>
+cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
+                             const int* grp_det, long long G, long long nseg, long long M1,
+                             cplx<T>* gspec, double* chi2_part, int nblocks, cudaStream_t st) {
+  k_group_rhs<T><<<nblocks, 256, 0, st>>>(dspec, filt, dcs, grp_off, grp_det, G, nseg, M1, gspec,
+                                         chi2_part);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, long long ng,
+                                 long long nsd, T* gtl, cudaStream_t st) {
+  k_group_project<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, ng, nsd, gtl);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t group_mix_launch(cplx<T>* spec, const T* hmix, long long G, long long nseg,
+                             long long M1, cudaStream_t st) {
+  k_group_mix<T><<<blocks_for(G * nseg * M1), 256, 0, st>>>(spec, hmix, G, nseg, M1);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T* ys,
+                                    cudaStream_t st) {
+  k_group_interleave<T><<<blocks_for(ng), 256, 0, st>>>(gtl, ng, nsd, ys);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, const int* grp_det,
+                              long long G, long long M1, T* hmix, cudaStream_t st) {
+  k_group_hmix<T><<<blocks_for(G * M1), 256, 0, st>>>(filt, dcs, grp_off, grp_det, G, M1, hmix);
+  return cudaGetLastError();
+}
+
+#define SG_GROUP_INST(T)                                                                       \
+  template cudaError_t group_project_launch<T>(const int*, const T*, const T*, long long,        \
+                                               long long, T*, cudaStream_t);                     \
+  template cudaError_t group_mix_launch<T>(cplx<T>*, const T*, long long, long long, long long,  \
+                                           cudaStream_t);                                        \
+  template cudaError_t group_interleave_launch<T>(const T*, long long, long long, T*,            \
+                                                  cudaStream_t);                                 \
+  template cudaError_t group_hmix_launch<T>(const T*, const T*, const int*, const int*,          \
+                                            long long, long long, T*, cudaStream_t);             \
+  template cudaError_t group_rhs_launch<T>(const cplx<T>*, const T*, const T*, const int*,       \
+                                           const int*, long long, long long, long long,          \
+                                           cplx<T>*, double*, int, cudaStream_t);
+SG_GROUP_INST(float)
+SG_GROUP_INST(double)
+
+}  // namespace sg

@@ -24,6 +24,8 @@ struct FilterArgs {
   double* chi2_part; // if set: per-CTA sums of h[k] |X[k]|^2, k = 0..ns/2 [gridDim]
   const T* filt;     // [ndet][M+1]
   T* out;            // [ntiles][ns]
+  cplx<T>* spec_out;       // if set: forward FFT only, X[k] (k = 0..M) [ntiles][M+1]
+  const cplx<T>* spec_in;  // if set: inverse FFT only of Y[k] [ntiles][M+1]
   const cplx<T>* tw_lo;
   const cplx<T>* tw_hi;
   cplx<T> wn1;
@@ -34,6 +36,10 @@ cudaError_t filter_launch(const FilterArgs<T>& a, int logm, int S, int nclusters
                           cudaStream_t st);
 template <typename T>
 int filter_max_clusters(int logm, int S);
+// forward FFT to a.spec_out, or inverse FFT from a.spec_in (exactly one set)
+template <typename T>
+cudaError_t filter_spec_launch(const FilterArgs<T>& a, int logm, int S, int nclusters,
+                               cudaStream_t st);
 size_t filter_smem_bytes(int logm, int S, int esize);
 int filter_cluster_size(int logm, int esize);
 
@@ -133,6 +139,32 @@ template <typename T>
 cudaError_t pt_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                       const T* ys, long long npix, const int* hits_true, double* q,
                       cudaStream_t st);
+
+// ---- the offset-group operator (sg_group.cu) -------------------------------------
+// gtl [G][3][nsd] = (a, b1, b2) = (I, Q c + U s, U c - Q s) per group sample
+template <typename T>
+cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, long long ng,
+                                 long long nsd, T* gtl, cudaStream_t st);
+// half spectra [G][3][nseg][M+1] <- H (a, b1, b2) per frequency, hmix [G][M+1][6]
+template <typename T>
+cudaError_t group_mix_launch(cplx<T>* spec, const T* hmix, long long G, long long nseg,
+                             long long M1, cudaStream_t st);
+// ys [G nsd][4] = (S0, S1, S2, 0) from gtl
+template <typename T>
+cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T* ys,
+                                    cudaStream_t st);
+// right-hand side spectra of each group from the detectors' data spectra
+// dspec [ndet][nseg][M+1]: gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c, s);
+// chi2_part [nblocks] = partial sums of h_d |X_d|^2
+constexpr int kGroupRhsBlocks = 152 * 8;
+template <typename T>
+cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
+                             const int* grp_det, long long G, long long nseg, long long M1,
+                             cplx<T>* gspec, double* chi2_part, int nblocks, cudaStream_t st);
+// hmix [G][M+1][6] = sum_d h_d[k] (1, c, s, cc, cs, ss) over each group's detectors
+template <typename T>
+cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, const int* grp_det,
+                              long long G, long long M1, T* hmix, cudaStream_t st);
 
 // ---- CG vector algebra (sg_cg.cu) ------------------------------------------------
 struct CgScalars {

@@ -357,9 +357,7 @@ cudaError_t synth_rhs(sg_ctx* c, uint64_t seed) {
   else
     k_add<double><<<grid_for(n), kT, 0, c->st>>>(c->tod_syn.as<double>(), c->y.as<double>(), n);
   e = cudaGetLastError();
-  if (e == cudaSuccess)
-    e = c->launch_filter(kLoadTod, c->tod_syn.p, c->y.p, c->ntiles, (int)c->nseg, 0);
-  if (e == cudaSuccess) e = c->pt_of_y(c->b.as<double>(), true);
+  if (e == cudaSuccess) e = c->rhs_of(c->tod_syn.p, c->b.as<double>(), &c->sc.as<CgScalars>()->chi2);
   return e;
 }
 
@@ -639,6 +637,7 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   cudaSetDevice(c->desc.device);
   const double t0 = now_s();
   int rc = build_bj3(c);
+  if (rc == SG_OK) rc = prepare_operator(c);
   if (rc) return rc;
   if (steps > 0) {
     rc = build_patches(c);
@@ -656,6 +655,7 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   // (the residuals r_k of every iteration are kept; the solve to pair_crit
   // defines which residuals occur)
   c->use_syn = true;
+  c->refresh_chi2 = false;  // the training solves print nothing
   CgVecs v = c->vecs(1);
   int pairs = 0, skies = 0;
   while (pairs < npairs && skies < 4 * npairs && e == cudaSuccess) {

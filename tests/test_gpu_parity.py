@@ -83,11 +83,15 @@ def test_noise_filter_vs_oracle(ns, prec):
 
 
 # ---- operator ---------------------------------------------------------------------
-@pytest.mark.parametrize("prec,ns", [("f64", 2048), ("f64", 65536), ("f32", 4096),
-                                     ("f32", 131072)])
-def test_apply_vs_oracle(prec, ns):
+# ndet >= 4 on one pointing: the offset-group operator (three timelines per
+# group, 3 x 3 spectral mixing); ndet = 2: one filter per detector
+@pytest.mark.parametrize("prec,ns,ndet,hwp", [("f64", 2048, 2, False), ("f64", 65536, 2, False),
+                                              ("f32", 4096, 2, False), ("f32", 131072, 2, False),
+                                              ("f64", 4096, 4, False), ("f64", 2048, 6, True),
+                                              ("f32", 4096, 8, False), ("f32", 131072, 8, True)])
+def test_apply_vs_oracle(prec, ns, ndet, hwp):
     nseg = 2 if ns >= 65536 else 4
-    prob = small_problem(ndet=2, nseg=nseg, ns=ns, precision=prec, nside=32)
+    prob = small_problem(ndet=ndet, nseg=nseg, ns=ns, precision=prec, nside=32, hwp=hwp)
     s = oracle.Setup(prob)
     mm = sg.from_problem(prob, precision=prec, with_tod=False)
     rng = np.random.default_rng(1)
@@ -100,6 +104,28 @@ def test_apply_vs_oracle(prec, ns):
     y = rng.standard_normal(3 * s.npix)
     a, b = x @ mm.apply(y), y @ mm.apply(x)
     assert abs(a - b) <= (1e-10 if prec == "f64" else 1e-5) * max(abs(a), abs(b))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_group_operator_matches_per_detector(prec, monkeypatch):
+    """the offset-group operator and the per-detector one are the same linear
+    map: A x agrees to rounding, and so do the solves"""
+    prob = small_problem(ndet=8, nseg=4, ns=8192, precision=prec, nside=32, hwp=True)
+    x = np.random.default_rng(5).standard_normal(3 * oracle.Setup(prob).npix)
+    grouped = sg.from_problem(prob, precision=prec)
+    monkeypatch.setenv("SANEPIC_GPU_GROUP_FILTER", "0")
+    per_det = sg.from_problem(prob, precision=prec)
+    tol = 1e-12 if prec == "f64" else 2e-6
+    assert rel_rms(grouped.apply(x), per_det.apply(x)) < tol
+    for mm in (grouped, per_det):
+        mm.rhs()
+    a = grouped.solve(precond="bj3", stop_crit=1e-12)
+    xa = grouped.solution()
+    b = per_det.solve(precond="bj3", stop_crit=1e-12)
+    xb = per_det.solution()
+    assert a["converged"] and b["converged"] and abs(a["iterations"] - b["iterations"]) <= 1
+    npix = grouped.npix
+    assert rel_rms(xa[npix:], xb[npix:]) < (1e-7 if prec == "f64" else 1e-4)
 
 
 def test_apply_bitwise_deterministic():
