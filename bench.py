@@ -62,6 +62,10 @@ REFERENCE_ITERS_TO_1E6 = {"c2_64det_nside256": 24}
 # from the ncu capture in profiles/noise_filter_c2_8det.md (343.7 MB over
 # 384 tiles); traffic grows with the tiles, so a full launch is this x tiles.
 FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 343.67e6 / 384
+# DRAM bytes (read + write) of one group noise weighting (forward FFTs, 3 x 3
+# mixing, inverse FFTs) on the bench workloads with one group of 48 x 131072
+# samples, from the ncu capture in profiles/group_noise_weighting_c2_8det.md
+GROUP_NW_DRAM_BYTES = {("c2_64det_nside256", "f32"): 610.7e6, ("c2_8det_nside256", "f32"): 610.7e6}
 
 
 def peaks():
@@ -196,7 +200,9 @@ def run_ours(args):
         for _ in range(args.steps):
             rep = device_step(pc)
             reps.append(rep)
-            launches += rep["kernel_launches"] + 4  # + the RHS: filter, chi^2 sum, detector sums, P^T
+            # + the RHS: filter, chi^2 sum, detector sums, P^T; per offset group:
+            # forward FFTs, group sums, chi^2 sum, inverse FFTs, P^T
+            launches += rep["kernel_launches"] + (5 if mm.group_mode()[0] else 4)
         ev1.record(stream)
         torch.cuda.nvtx.range_pop()
         barrier()
@@ -222,16 +228,31 @@ def run_ours(args):
     # algorithmic bytes per launch (each input read once, each output written once).
     # Detectors sharing focal-plane offsets share one pixel stream: pixel index,
     # base angle and the CSR live per group sample (ng), y per detector sample.
-    ngrp = 1  # the synthetic detectors all sit on the boresight
+    group, ngrp = mm.group_mode()  # the synthetic detectors all sit on the boresight
     ng = ngrp * spec.nseg * spec.ns
-    kbytes = {
-        "k_project": ng * (4 + 2 * esz) + ns_all * esz + npix * 4 * esz,
-        "k_noise_filter": ns_all * 2 * esz + spec.ndet * (spec.ns // 2 + 1) * esz,
-        "k_detsum": ns_all * esz + ng * 4 * esz,
-        "k_pt": ng * (4 + 2 * esz + 4 * esz) + npix * (3 * 8 + 8 + 4),
-    }
-    kms = {"k_project": prof["p_ms"], "k_noise_filter": prof["filter_ms"],
-           "k_detsum": prof["detsum_ms"], "k_pt": prof["pt_ms"]}
+    m1 = spec.ns // 2 + 1
+    pt_bytes = ng * (4 + 2 * esz + 4 * esz) + npix * (3 * 8 + 8 + 4)
+    if group:
+        # per offset group: (a, b1, b2) per group sample; N^-1 = forward FFTs,
+        # 3 x 3 mixing, inverse FFTs (three launches, timed together): the
+        # three timelines read, the three weighted ones written, the mixing
+        # matrices read; the half spectra in between are not algorithmic
+        kbytes = {
+            "k_group_project": ng * (4 + 2 * esz) + npix * 4 * esz + 3 * ng * esz,
+            "group_noise_weighting": 6 * ng * esz + ngrp * m1 * 6 * esz,
+            "k_pt": pt_bytes,
+        }
+        kms = {"k_group_project": prof["p_ms"], "group_noise_weighting": prof["filter_ms"],
+               "k_pt": prof["pt_ms"]}
+    else:
+        kbytes = {
+            "k_project": ng * (4 + 2 * esz) + ns_all * esz + npix * 4 * esz,
+            "k_noise_filter": ns_all * 2 * esz + spec.ndet * m1 * esz,
+            "k_detsum": ns_all * esz + ng * 4 * esz,
+            "k_pt": pt_bytes,
+        }
+        kms = {"k_project": prof["p_ms"], "k_noise_filter": prof["filter_ms"],
+               "k_detsum": prof["detsum_ms"], "k_pt": prof["pt_ms"]}
     hbm, peak_kind = peaks()
     kernels = {k: {"ms": kms[k], "GBps": kbytes[k] / (kms[k] * 1e-3) / 1e9,
                    "bytes": kbytes[k]} for k in kbytes}
@@ -240,6 +261,8 @@ def run_ours(args):
     traffic = None
     if dom == "k_noise_filter" and spec.ns == 131072 and spec.precision == "f32":
         traffic = FILTER_DRAM_BYTES_PER_TILE_131072_F32 * spec.ndet * spec.nseg
+    if dom == "group_noise_weighting" and (args.config, spec.precision) in GROUP_NW_DRAM_BYTES:
+        traffic = GROUP_NW_DRAM_BYTES[(args.config, spec.precision)]
     # ---- plain block-Jacobi vs the reference's diagonal (same workload) -------
     extra = {}
     if args.compare_diag:

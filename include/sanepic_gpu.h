@@ -137,6 +137,11 @@ int sg_rhs(sg_ctx *ctx, double *chi2);
 
 /* Number of observed pixels (npix, sanepic.cc:915). */
 long sg_npix(const sg_ctx *ctx);
+/* 1 if the operator runs per offset group (detectors with identical
+ * focal-plane offsets, at least 4 in every group, share one pixel stream:
+ * three timelines per group instead of one per detector), else 0; *ngroups
+ * (if non-null) receives the number of groups.  No reference counterpart. */
+int sg_group_mode(const sg_ctx *ctx, long *ngroups);
 
 /* y = P^T N^-1 P x for a compact host vector [3*npix] (one operator pass,
  * sanepic.cc:1428-1448); masked != 0 applies the pol degeneracy mask

@@ -33,6 +33,7 @@ MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
 
 # every symbol include/sanepic_gpu.h declares
 EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
+           "sg_group_mode",
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
@@ -123,6 +124,8 @@ def load_library(path: Optional[str] = None):
     L.sg_rhs.argtypes = [c_p, dp]
     L.sg_npix.argtypes = [c_p]
     L.sg_npix.restype = ctypes.c_long
+    L.sg_group_mode.argtypes = [c_p, ctypes.POINTER(ctypes.c_long)]
+    L.sg_group_mode.restype = ctypes.c_int
     L.sg_apply.argtypes = [c_p, dp, dp, ctypes.c_int]
     L.sg_noise_filter.argtypes = [c_p, dp, dp]
     L.sg_noise_filter_noalloc.argtypes = [c_p, c_p, c_p, ctypes.c_long, ctypes.c_long,
@@ -292,6 +295,12 @@ class MapMaker:
         out = np.empty(12 * self.nside * self.nside, dtype=np.int64)
         self._check(self.L.sg_get_indpix(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
         return out
+
+    def group_mode(self):
+        """(True if the operator runs per offset group, number of groups)"""
+        n = ctypes.c_long(0)
+        on = bool(self.L.sg_group_mode(self.h, ctypes.byref(n)))
+        return on, int(n.value)
 
     def autotune(self) -> dict:
         """Pick the faster compiled FFT tile shape for this problem's noise filter."""

@@ -132,6 +132,12 @@ extern "C" const char* sg_last_error(const sg_ctx* c) {
 
 extern "C" long sg_npix(const sg_ctx* c) { return c ? (long)c->npix : -1; }
 
+extern "C" int sg_group_mode(const sg_ctx* c, long* ngroups) {
+  if (!c) return 0;
+  if (ngroups) *ngroups = c->ngroups;
+  return c->group_mode ? 1 : 0;
+}
+
 // ---------------------------------------------------------------------------
 extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
                                const double* psi, long nsamp_total, const long* isampmin,
@@ -904,7 +910,7 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
     e = cudaEventRecord(ev[0], c->st);
     if (c->group_mode) {
       // projection = (a, b1, b2); N^-1 = forward FFTs + 3 x 3 mixing + inverse
-      // FFTs; detector sums = the interleave into P^T's layout
+      // FFTs (written in P^T's layout); no detector sums
       if (c->f32) {
         if (e == cudaSuccess)
           e = group_project_launch<float>(c->pix.as<int>(), c->cs.as<float>(), c->dmap.as<float>(),
@@ -914,11 +920,8 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
         if (e == cudaSuccess)
           e = group_mix_launch<float>(c->gspec.as<cplx<float>>(), c->hmix.as<float>(), c->ngroups,
                                       c->nseg, M1, c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->gtl.p, nullptr, c->gspec.p, gt);
+        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->ys.p, nullptr, c->gspec.p, gt, 1);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-        if (e == cudaSuccess)
-          e = group_interleave_launch<float>(c->gtl.as<float>(), c->ngsamp, nsd, c->ys.as<float>(),
-                                             c->st);
       } else {
         if (e == cudaSuccess)
           e = group_project_launch<double>(c->pix.as<int>(), c->cs.as<double>(),
@@ -929,11 +932,8 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
         if (e == cudaSuccess)
           e = group_mix_launch<double>(c->gspec.as<cplx<double>>(), c->hmix.as<double>(),
                                        c->ngroups, c->nseg, M1, c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->gtl.p, nullptr, c->gspec.p, gt);
+        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->ys.p, nullptr, c->gspec.p, gt, 1);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-        if (e == cudaSuccess)
-          e = group_interleave_launch<double>(c->gtl.as<double>(), c->ngsamp, nsd,
-                                              c->ys.as<double>(), c->st);
       }
     } else {
       if (e == cudaSuccess) e = c->launch_project();

@@ -402,7 +402,8 @@ cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStrea
 // Balancing form (Mandel's balancing Neumann-Neumann; A-DEF2 in Tang et al.
 // 2009), with AU = A U and E = U^T A U:
 //   z = (I - U E^-1 AU^T) M (I - AU E^-1 U^T) r + U E^-1 U^T r
-// computed as  c = E^-1 U^T r,  y = M (r - AU c),  z = y + U (c - E^-1 AU^T y).
+// computed as  c = E^-1 U^T r,  y = M (r - AU c),  z = y + U (c - E^-1 AU^T y)
+// in three passes (U^T r; y and AU^T y; z and the CG's dots).
 // Symmetric positive definite for any SPD E and M, so plain (or flexible)
 // PCG applies.  U and AU are stored element-major, [3 npix][kp] FP32 with
 // kp = kc rounded up to 8 (zero columns), so one thread reads an element's
@@ -421,6 +422,7 @@ __global__ void __launch_bounds__(kCgThreads)
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
+#pragma unroll 2
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
     const float vi = (float)v[i];
@@ -474,11 +476,13 @@ __device__ __forceinline__ void coarse_solve_block(const double* __restrict__ pa
   __syncthreads();
 }
 
-// c = E^-1 U^T r (from part1); z = M (r - AU c); block 0 keeps c in coef
+// c = E^-1 U^T r (from part1); z = M (r - AU c); block 0 keeps c in coef;
+// part2[k][block] = partial sums of AU[i][k] z[i] (the rows are read once for
+// both: the second use hits L1)
 template <int KP>
-__global__ void __launch_bounds__(kCgThreads)
+__global__ void __launch_bounds__(kCgThreads, 2)
     k_coarse_pre(CgVecs v, const float* __restrict__ AU, const double* __restrict__ part1,
-                 const double* __restrict__ einv, int kc, double* coef) {
+                 const double* __restrict__ einv, int kc, double* coef, double* part2) {
   __shared__ double d[KP], cd[KP];
   __shared__ float c[KP];
   coarse_solve_block<KP>(part1, einv, kc, d, cd);
@@ -487,6 +491,9 @@ __global__ void __launch_bounds__(kCgThreads)
     if (blockIdx.x == 0) coef[threadIdx.x] = cd[threadIdx.x];
   }
   __syncthreads();
+  float acc[KP];
+#pragma unroll
+  for (int k = 0; k < KP; k++) acc[k] = 0.f;
   const long long n = v.npix;
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
        m += (long long)gridDim.x * blockDim.x) {
@@ -506,11 +513,37 @@ __global__ void __launch_bounds__(kCgThreads)
       }
       t[cc] = v.r[i] - (double)s;
     }
-    double z0, z1, z2;
-    apply_m(v, m, t[0], t[1], t[2], z0, z1, z2);
-    v.z[m] = z0;
-    v.z[n + m] = z1;
-    v.z[2 * n + m] = z2;
+    double z[3];
+    apply_m(v, m, t[0], t[1], t[2], z[0], z[1], z[2]);
+#pragma unroll
+    for (int cc = 0; cc < 3; cc++) {
+      const long long i = cc * n + m;
+      v.z[i] = z[cc];
+      const float zf = (float)z[cc];
+      const float4* row = reinterpret_cast<const float4*>(AU + i * KP);
+#pragma unroll
+      for (int q = 0; q < KP / 4; q++) {
+        const float4 a = __ldcg(row + q);  // again, from L2: keeps the rows out of registers
+        acc[4 * q] = fmaf(a.x, zf, acc[4 * q]);
+        acc[4 * q + 1] = fmaf(a.y, zf, acc[4 * q + 1]);
+        acc[4 * q + 2] = fmaf(a.z, zf, acc[4 * q + 2]);
+        acc[4 * q + 3] = fmaf(a.w, zf, acc[4 * q + 3]);
+      }
+    }
+  }
+  __shared__ double sh[KP][kCgThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KP; k++) {
+    double x = (double)acc[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < KP) {
+    double t = 0.0;
+    for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
+    part2[threadIdx.x * kCgBlocks + blockIdx.x] = t;
   }
 }
 
@@ -528,6 +561,7 @@ __global__ void __launch_bounds__(kCgThreads)
   __syncthreads();
   const long long n3 = 3 * v.npix;
   double acc[3] = {0.0, 0.0, 0.0};
+#pragma unroll 2
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
     const float4* row = reinterpret_cast<const float4*>(U + i * KP);
@@ -556,8 +590,8 @@ static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int f
   double* part1 = cs.part;
   double* part2 = cs.part + (size_t)kCoarseMax * kCgBlocks;
   k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
-  k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef);
-  k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.au, n3, v.z, part2);
+  k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef,
+                                                      part2);
   k_coarse_post<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.u, part2, cs.einv, cs.kc, cs.coef,
                                                        flexible);
   return cudaGetLastError();

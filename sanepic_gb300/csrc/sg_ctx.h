@@ -93,6 +93,8 @@ struct sg_ctx {
   static constexpr int kGroupMin = 4;
   bool group_mode = false, have_hmix = false;
   DevBuf gtl, gspec, hmix, dspec, rhs_part;  // + data spectra [ndet][nseg][M+1], chi^2 partials
+  DevBuf kslot, filt_slot;  // frequency of each spectrum slot; filter rows in slot order
+  int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
   std::vector<double> spn_h;  // host copy of the filter rows [ndet][M+1] (FP64)
 
@@ -258,7 +260,7 @@ struct sg_ctx {
 
   // forward FFT of tiles to spec_out, or inverse FFT of spec_in to tiles
   cudaError_t launch_filter_spec(const void* in, void* out, void* spec_out, const void* spec_in,
-                                 long long ntiles_) {
+                                 long long ntiles_, int ilv3 = 0) {
     const int ncl = (int)std::min<long long>(nclusters, ntiles_);
     launches++;
     if (f32) {
@@ -267,6 +269,7 @@ struct sg_ctx {
       a.wn1 = wn1f;
       a.spec_out = (cplx<float>*)spec_out;
       a.spec_in = (const cplx<float>*)spec_in;
+      a.ilv3 = ilv3;
       return filter_spec_launch<float>(a, logm, S, ncl, st);
     }
     auto a = filter_args<double>(kLoadTod, (const double*)in, (double*)out, ntiles_, (int)nseg, 0,
@@ -274,21 +277,44 @@ struct sg_ctx {
     a.wn1 = wn1d;
     a.spec_out = (cplx<double>*)spec_out;
     a.spec_in = (const cplx<double>*)spec_in;
+    a.ilv3 = ilv3;
     return filter_spec_launch<double>(a, logm, S, ncl, st);
   }
 
   // the per-group mixing matrices from the filter rows (before any group apply)
+  // (the slot order depends on the tile shape: rebuilt when the autotuner
+  // changes the cluster size)
   cudaError_t ensure_hmix() {
-    if (!group_mode || have_hmix) return cudaSuccess;
+    if (!group_mode || (have_hmix && hmix_S == S)) return cudaSuccess;
     const long long M1 = ns / 2 + 1;
-    cudaError_t e = f32 ? group_hmix_launch<float>(filt.as<float>(), dcs.as<float>(),
-                                                   grp_off.as<int>(), grp_det.as<int>(), ngroups,
-                                                   M1, hmix.as<float>(), st)
-                        : group_hmix_launch<double>(filt.as<double>(), dcs.as<double>(),
-                                                    grp_off.as<int>(), grp_det.as<int>(), ngroups,
-                                                    M1, hmix.as<double>(), st);
-    launches++;
-    if (e == cudaSuccess) have_hmix = true;
+    std::vector<int> kf;
+    spec_slot_freq(logm, S, kf);
+    cudaError_t e = kslot.alloc(sizeof(int) * M1);
+    if (e == cudaSuccess) e = filt_slot.alloc((size_t)ndet * M1 * esize);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(kslot.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
+    if (e != cudaSuccess) return e;
+    if (f32) {
+      e = group_hmix_launch<float>(filt.as<float>(), dcs.as<float>(), grp_off.as<int>(),
+                                   grp_det.as<int>(), kslot.as<int>(), ngroups, M1,
+                                   hmix.as<float>(), st);
+      if (e == cudaSuccess)
+        e = permute_rows_launch<float>(filt.as<float>(), kslot.as<int>(), ndet, M1,
+                                       filt_slot.as<float>(), st);
+    } else {
+      e = group_hmix_launch<double>(filt.as<double>(), dcs.as<double>(), grp_off.as<int>(),
+                                    grp_det.as<int>(), kslot.as<int>(), ngroups, M1,
+                                    hmix.as<double>(), st);
+      if (e == cudaSuccess)
+        e = permute_rows_launch<double>(filt.as<double>(), kslot.as<int>(), ndet, M1,
+                                        filt_slot.as<double>(), st);
+    }
+    launches += 2;
+    if (e == cudaSuccess) {
+      have_hmix = true;
+      hmix_S = S;
+    }
     return e;
   }
 
@@ -303,25 +329,23 @@ struct sg_ctx {
     }
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
     cudaError_t e = launch_filter_spec(d, nullptr, dspec.p, nullptr, ntiles);
-    launches += 3;  // sums, chi^2, interleave
+    launches += 2;  // sums, chi^2
     if (f32) {
       if (e == cudaSuccess)
-        e = group_rhs_launch<float>(dspec.as<cplx<float>>(), filt.as<float>(), dcs.as<float>(),
+        e = group_rhs_launch<float>(dspec.as<cplx<float>>(), filt_slot.as<float>(), dcs.as<float>(),
                                     grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
                                     gspec.as<cplx<float>>(), rhs_part.as<double>(),
                                     kGroupRhsBlocks, st);
     } else {
       if (e == cudaSuccess)
-        e = group_rhs_launch<double>(dspec.as<cplx<double>>(), filt.as<double>(), dcs.as<double>(),
+        e = group_rhs_launch<double>(dspec.as<cplx<double>>(), filt_slot.as<double>(),
+                                     dcs.as<double>(),
                                      grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
                                      gspec.as<cplx<double>>(), rhs_part.as<double>(),
                                      kGroupRhsBlocks, st);
     }
     if (e == cudaSuccess) e = chi2_sum(rhs_part.as<double>(), kGroupRhsBlocks, chi2_dev, st);
-    if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
-    if (e == cudaSuccess)
-      e = f32 ? group_interleave_launch<float>(gtl.as<float>(), ngsamp, nsd, ys.as<float>(), st)
-              : group_interleave_launch<double>(gtl.as<double>(), ngsamp, nsd, ys.as<double>(), st);
+    if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
     if (e == cudaSuccess) e = launch_pt(bout, true);
     return e;
   }
@@ -331,7 +355,7 @@ struct sg_ctx {
   cudaError_t apply_map_group(double* out, bool masked) {
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
     cudaError_t e;
-    launches += 3;
+    launches += 2;  // projection, mixing
     if (f32) {
       e = group_project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
                                       nsd, gtl.as<float>(), st);
@@ -339,9 +363,7 @@ struct sg_ctx {
       if (e == cudaSuccess)
         e = group_mix_launch<float>(gspec.as<cplx<float>>(), hmix.as<float>(), ngroups, nseg, M1,
                                     st);
-      if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
-      if (e == cudaSuccess)
-        e = group_interleave_launch<float>(gtl.as<float>(), ngsamp, nsd, ys.as<float>(), st);
+      if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
     } else {
       e = group_project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
                                        nsd, gtl.as<double>(), st);
@@ -349,9 +371,7 @@ struct sg_ctx {
       if (e == cudaSuccess)
         e = group_mix_launch<double>(gspec.as<cplx<double>>(), hmix.as<double>(), ngroups, nseg,
                                      M1, st);
-      if (e == cudaSuccess) e = launch_filter_spec(nullptr, gtl.p, nullptr, gspec.p, gt);
-      if (e == cudaSuccess)
-        e = group_interleave_launch<double>(gtl.as<double>(), ngsamp, nsd, ys.as<double>(), st);
+      if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
     }
     if (e == cudaSuccess) e = launch_pt(out, masked);
     return e;

@@ -1,5 +1,6 @@
 // sg_filter.cu -- the fused noise filter's launches (kernel in sg_filter.cuh)
 #include <algorithm>
+#include <vector>
 
 #include "sg_filter.cuh"
 
@@ -11,6 +12,24 @@ size_t filter_smem_bytes(int logm, int S, int esize) {
   const size_t C2 = C >> ((logc + 1) / 2);
   const size_t buf = std::max(R * (C / S + 1), C * (R / S + 1));
   return (size_t)esize * 2 * (buf + kTwLo + M / kTwLo + R + C + C2);
+}
+
+// frequency k of every spectrum slot of the spectrum-split filter variants
+// (the unit order of sg_filter.cuh), slot M the Nyquist bin
+void spec_slot_freq(int logm, int S, std::vector<int>& kfreq) {
+  const int logr = (logm + 1) / 2, logc = logm / 2;
+  const long long R = 1LL << logr, C = 1LL << logc, M = R * C;
+  const long long C1 = 1LL << ((logc + 1) / 2), Rs = R / S;
+  kfreq.assign(M + 1, 0);
+  for (long long s = 0; s < M; s++) {
+    const long long t = s % Rs, j = (s / Rs) % S, rest = s / (Rs * S);
+    const long long ka = rest % C1, i = rest / C1;
+    const long long r = j * Rs + t;  // row list index -> row k1 (rows 0, R/2, then pairs)
+    const long long p = r >> 1;
+    const long long k1 = r == 0 ? 0 : (r == 1 ? R / 2 : ((r & 1) ? R - p : p));
+    kfreq[s] = (int)(k1 + R * ka + R * C1 * i);
+  }
+  kfreq[M] = (int)M;
 }
 
 int filter_cluster_size(int logm, int esize) {

@@ -3,9 +3,13 @@
 // GB300 kernel: load (a timeline, or a timeline minus another) -> real FFT ->
 // multiply by the inverse-noise spectrum -> inverse real FFT -> store,
 // optionally accumulating chi^2 of the input.  Two more variants split it at
-// the spectrum (forward FFT to the half spectrum X[k], k = 0..M, in natural
-// order; inverse FFT from such a spectrum), for weightings that mix several
-// timelines per frequency (the offset-group operator, sg_pt.cu).
+// the spectrum (forward FFT to the half spectrum X[k], k = 0..M; inverse FFT
+// from such a spectrum), for weightings that mix several timelines per
+// frequency (the offset-group operator, sg_group.cu).  Spectra are stored in
+// the order the kernel's units hold them (slot
+// ((i C1 + ka) S + j) Rs + t for element i of unit (row t of CTA j, column
+// ka); row 0's slots equal their frequencies; slot M holds the Nyquist bin),
+// so loads and stores are coalesced; spec_slot_freq() gives each slot's k.
 //
 // Replaces the reference's write_tfAS + the first half of do_PtNd
 // (sanepic.cc:2390-2445, 2522-2582): per tile of ns samples it computes
@@ -374,7 +378,11 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
             const bool lo = k <= M - k;
             const cplx<T> wk = cmul(wb, twd[i]);
             const cplx<T> ws = lo ? wk : cplx<T>{-wk.x, wk.y};
-            const cplx<T> yo = Yin[k], yp = Yin[M - k];
+            // own slot, and the slot of frequency M - k: element C2-1-i of the
+            // partner unit (row t^1, or row R/2 itself; column C1-1-ka)
+            const int tp = (j == 0 && t == 1) ? t : (t ^ 1);
+            const cplx<T> yo = Yin[((i * C1 + ka) * S + j) * Rs + t];
+            const cplx<T> yp = Yin[(((C2 - 1 - i) * C1 + (C1 - 1 - ka)) * S + j) * Rs + tp];
             zo[i] = repack(lo ? yo : yp, lo ? yp : yo, ws, lo);
           }
           SgDft<C2, true, T>::run(zo);
@@ -409,7 +417,9 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
           zo[i] = split_filter(lo ? z[i] : zp, lo ? zp : z[i], lo ? hk[i] : hp, lo ? hp : hk[i],
                                ws, lo, x);
           if (!row0) c2 += hk[i] * (x.x * x.x + x.y * x.y);
-          if (MODE == kSpecOut && !row0) Xout[k] = x;  // X[k] at this unit's own frequency
+          // X[k] at this unit's own frequency, stored in unit order (lanes write
+          // consecutive slots); row 0's slots are its frequencies themselves
+          if (MODE == kSpecOut && !row0) Xout[((i * C1 + ka) * S + j) * Rs + t] = x;
         }
         if constexpr (MODE == kSpecOut) {
           if (row0) {
@@ -576,7 +586,23 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         });
     __syncthreads();
     // ---- 11. store -------------------------------------------------------------
-    if (kVec) {
+    if (MODE == kSpecIn && p.ilv3) {
+      // component (tile / nseg) % 3 of the interleaved [group sample][4]
+      // layout P^T reads: tile = (group * 3 + component) * nseg + segment
+      const long long nst = p.nseg;
+      const long long grp = tile / (3 * nst), comp = (tile / nst) % 3, seg = tile % nst;
+      T* dst = p.out + 4 * (grp * nst + seg) * (2LL * M) + comp;
+#pragma unroll 16
+      for (int it = 0; it < G::XE; it++) {
+        const int e = it * NT + tid;
+        if (E % NT != 0 && e >= E) break;
+        const int c = e % Cs, n1 = e / Cs;
+        const long long n = 2LL * (C * n1 + j * Cs + c);
+        const cplx<T> v = buf[n1 * PA + c];
+        dst[4 * n] = v.x;
+        dst[4 * n + 4] = v.y;
+      }
+    } else if (kVec) {
 #pragma unroll 8
       for (int it = 0; it < E / 2 / NT; it++) {
         const int e2 = it * NT + tid;

@@ -82,15 +82,17 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// hmix [G][M+1][6] = sum over the group's detectors of h_d[k] (1, c, s, cc, cs, ss)
+// hmix [G][slot][6] = sum over the group's detectors of h_d[k] (1, c, s, cc, cs, ss),
+// k = kslot[slot] (spectra are kept in the filter's slot order)
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_group_hmix(const T* __restrict__ filt, const T* __restrict__ dcs, const int* __restrict__ grp_off,
-                 const int* __restrict__ grp_det, long long G, long long M1, T* __restrict__ hmix) {
+                 const int* __restrict__ grp_det, const int* __restrict__ kslot, long long G,
+                 long long M1, T* __restrict__ hmix) {
   const long long n = G * M1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const long long g = i / M1, k = i - g * M1;
+    const long long g = i / M1, k = kslot[i - g * M1];
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
       const int d = grp_det[e];
@@ -123,7 +125,8 @@ struct CSum {
   __device__ __forceinline__ T get() const { return s + c; }
 };
 
-// right-hand side of a group from its detectors' data spectra X_d [ndet][nseg][M+1]:
+// right-hand side of a group from its detectors' data spectra X_d [ndet][nseg][M+1]
+// (slot order; filt holds the filter rows in the same order):
 // gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c_d, s_d), detectors in list order;
 // chi2_part[block] = sum of h_d |X_d|^2 over the block's bins (k = 0..M)
 template <typename T>
@@ -140,10 +143,7 @@ __global__ void __launch_bounds__(256)
     const long long seg = gs % nseg, g = gs / nseg;
     CSum<T> a[6];
     T cl = T(0);
-    for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
-      const int d = grp_det[e];
-      const cplx<T> x = dspec[((long long)d * nseg + seg) * M1 + k];
-      const T h = filt[d * M1 + k], c = dcs[2 * d], s = dcs[2 * d + 1];
+    auto acc = [&](cplx<T> x, T h, T c, T s) {
       const T hx = h * x.x, hy = h * x.y;
       a[0].add(hx);
       a[1].add(hy);
@@ -152,6 +152,26 @@ __global__ void __launch_bounds__(256)
       a[4].add(s * hx);
       a[5].add(s * hy);
       cl += h * (x.x * x.x + x.y * x.y);
+    };
+    const int e1 = grp_off[g + 1];
+    int e = grp_off[g];
+    for (; e + 4 <= e1; e += 4) {  // four detectors' loads in flight, same order
+      cplx<T> x[4];
+      T h[4], c[4], s[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int d = grp_det[e + u];
+        x[u] = dspec[((long long)d * nseg + seg) * M1 + k];
+        h[u] = filt[d * M1 + k];
+        c[u] = dcs[2 * d];
+        s[u] = dcs[2 * d + 1];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) acc(x[u], h[u], c[u], s[u]);
+    }
+    for (; e < e1; e++) {
+      const int d = grp_det[e];
+      acc(dspec[((long long)d * nseg + seg) * M1 + k], filt[d * M1 + k], dcs[2 * d], dcs[2 * d + 1]);
     }
     chi += (double)cl;
     cplx<T>* o = gspec + ((g * 3) * nseg + seg) * M1 + k;
@@ -199,8 +219,30 @@ cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T
 }
 template <typename T>
 cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, const int* grp_det,
-                              long long G, long long M1, T* hmix, cudaStream_t st) {
-  k_group_hmix<T><<<blocks_for(G * M1), 256, 0, st>>>(filt, dcs, grp_off, grp_det, G, M1, hmix);
+                              const int* kslot, long long G, long long M1, T* hmix,
+                              cudaStream_t st) {
+  k_group_hmix<T><<<blocks_for(G * M1), 256, 0, st>>>(filt, dcs, grp_off, grp_det, kslot, G, M1,
+                                                     hmix);
+  return cudaGetLastError();
+}
+
+// out [rows][slot] = in [rows][kslot[slot]]
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_permute_rows(const T* __restrict__ in, const int* __restrict__ kslot, long long rows,
+                   long long M1, T* __restrict__ out) {
+  const long long n = rows * M1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i / M1;
+    out[i] = in[r * M1 + kslot[i - r * M1]];
+  }
+}
+
+template <typename T>
+cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, long long M1, T* out,
+                                cudaStream_t st) {
+  k_permute_rows<T><<<blocks_for(rows * M1), 256, 0, st>>>(in, kslot, rows, M1, out);
   return cudaGetLastError();
 }
 
@@ -212,7 +254,9 @@ cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, c
   template cudaError_t group_interleave_launch<T>(const T*, long long, long long, T*,            \
                                                   cudaStream_t);                                 \
   template cudaError_t group_hmix_launch<T>(const T*, const T*, const int*, const int*,          \
-                                            long long, long long, T*, cudaStream_t);             \
+                                            const int*, long long, long long, T*, cudaStream_t); \
+  template cudaError_t permute_rows_launch<T>(const T*, const int*, long long, long long, T*,    \
+                                              cudaStream_t);                                     \
   template cudaError_t group_rhs_launch<T>(const cplx<T>*, const T*, const T*, const int*,       \
                                            const int*, long long, long long, long long,          \
                                            cplx<T>*, double*, int, cudaStream_t);

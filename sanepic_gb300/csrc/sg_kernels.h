@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "sg_cplx.cuh"
 
 namespace sg {
@@ -26,6 +28,7 @@ struct FilterArgs {
   T* out;            // [ntiles][ns]
   cplx<T>* spec_out;       // if set: forward FFT only, X[k] (k = 0..M) [ntiles][M+1]
   const cplx<T>* spec_in;  // if set: inverse FFT only of Y[k] [ntiles][M+1]
+  int ilv3;                // with spec_in: out is [groups][nseg * ns][4], tile = (group * 3 + component) * nseg + segment
   const cplx<T>* tw_lo;
   const cplx<T>* tw_hi;
   cplx<T> wn1;
@@ -36,6 +39,8 @@ cudaError_t filter_launch(const FilterArgs<T>& a, int logm, int S, int nclusters
                           cudaStream_t st);
 template <typename T>
 int filter_max_clusters(int logm, int S);
+// frequency of each of the M+1 slots of a split-filter spectrum (tile shape logm, S)
+void spec_slot_freq(int logm, int S, std::vector<int>& kfreq);
 // forward FFT to a.spec_out, or inverse FFT from a.spec_in (exactly one set)
 template <typename T>
 cudaError_t filter_spec_launch(const FilterArgs<T>& a, int logm, int S, int nclusters,
@@ -154,17 +159,23 @@ template <typename T>
 cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T* ys,
                                     cudaStream_t st);
 // right-hand side spectra of each group from the detectors' data spectra
-// dspec [ndet][nseg][M+1]: gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c, s);
+// dspec [ndet][nseg][M+1] (slot order, filt rows in slot order too):
+// gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c, s);
 // chi2_part [nblocks] = partial sums of h_d |X_d|^2
 constexpr int kGroupRhsBlocks = 152 * 8;
 template <typename T>
 cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
                              const int* grp_det, long long G, long long nseg, long long M1,
                              cplx<T>* gspec, double* chi2_part, int nblocks, cudaStream_t st);
-// hmix [G][M+1][6] = sum_d h_d[k] (1, c, s, cc, cs, ss) over each group's detectors
+// hmix [G][slot][6] = sum_d h_d[kslot[slot]] (1, c, s, cc, cs, ss) over each group's detectors
 template <typename T>
 cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, const int* grp_det,
-                              long long G, long long M1, T* hmix, cudaStream_t st);
+                              const int* kslot, long long G, long long M1, T* hmix,
+                              cudaStream_t st);
+// out [rows][slot] = in [rows][kslot[slot]] (filter rows into spectrum slot order)
+template <typename T>
+cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, long long M1, T* out,
+                                cudaStream_t st);
 
 // ---- CG vector algebra (sg_cg.cu) ------------------------------------------------
 struct CgScalars {

@@ -285,7 +285,7 @@ cudaError_t sg_ctx::learned_z(int flexible) {
   if (learned_kind == 2) {
     CgVecs vf = vecs(1);
     vf.rprev = flexible ? rprev.as<double>() : nullptr;
-    launches += 4;
+    launches += 3;
     return coarse_apply(vf, coarse(), flexible, st);
   }
   cudaError_t e = apply_precond(vb, r.as<double>(), z.as<double>(), st);
