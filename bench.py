@@ -287,18 +287,29 @@ def run_ours(args):
     e2e, phases = [], []
     for i in range(args.e2e_steps):
         barrier()
+        nvtx = torch.cuda.nvtx
         te = time.perf_counter()
+        nvtx.range_push("e2e_pointing")
         mm.set_pointing(host["ra"], host["dec"], host["psi"], dets, prob["isampmin"])
+        nvtx.range_pop()
         t1 = time.perf_counter()
+        nvtx.range_push("e2e_noise")
         for d in range(spec.ndet):
             mm.set_noise(d, host["ispf"][d])
+        nvtx.range_pop()
         t2 = time.perf_counter()
+        nvtx.range_push("e2e_tod")
         for d in range(spec.ndet):
             mm.set_tod(d, host["tod"][d])
+        nvtx.range_pop()
         t3 = time.perf_counter()
+        nvtx.range_push("e2e_solve")
         device_step(precond)
+        nvtx.range_pop()
         t4 = time.perf_counter()
+        nvtx.range_push("e2e_maps")
         maps = [mm.get_map(k) for k in ("I", "Q", "U")]
+        nvtx.range_pop()
         barrier()
         t5 = time.perf_counter()
         e2e.append(t5 - te)

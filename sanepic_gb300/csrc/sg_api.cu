@@ -183,7 +183,13 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
                                  sizeof(double) * ns, cudaMemcpyHostToDevice, c->st));
       }
     }
-    SG_TRY(nan_patch_launch<double>(dpsi.as<double>(), ns, nseg, c->st));
+    // the sequential rule runs only where psi has a NaN at all
+    int hnan = 0;
+    SG_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), c->st));
+    SG_TRY(any_nan_launch(dpsi.as<double>(), nsd, flag.as<int>(), c->st));
+    SG_TRY(cudaMemcpyAsync(&hnan, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    SG_TRY(cudaStreamSynchronize(c->st));
+    if (hnan) SG_TRY(nan_patch_launch<double>(dpsi.as<double>(), ns, nseg, c->st));
   }
   // offset groups: detectors with identical (offx, offy) share the pixelisation
   // (pass 1); if any pointing sample is NaN, every detector gets its own
@@ -439,32 +445,30 @@ extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) 
     return c->fail(SG_ERR_ARG, "bad detector index or noise spectrum");
   cudaSetDevice(c->desc.device);
   const long long ns = c->ns, M = ns / 2;
-  std::vector<double> spn(M + 1);
-  for (long long k = 0; k <= M; k++) {
-    const long long idx = (long long)((double)k / nssp * ns);  // sanepic.cc:535
-    if (idx < 0 || idx >= nssp)
-      return c->fail(SG_ERR_ARG, "noise spectrum of %ld values is too short for ns=%lld", nssp, ns);
-    spn[k] = ispf[idx] / (double)ns / (double)ns;
-  }
-  spn[0] = ispf[1] * 1e-6 / (double)ns / (double)ns;  // sanepic.cc:536-537
-  // diagonal of the circulant N^-1 in the time domain: c2r(spn)[0]
-  double g = spn[0];
-  for (long long k = 1; k < M; k++) g += 2.0 * spn[k];
-  g += spn[M];
-  cudaError_t e;
-  if (c->f32) {
-    std::vector<float> f(spn.begin(), spn.end());
-    e = cudaMemcpy(c->filt.as<float>() + det * (M + 1), f.data(), 4 * (M + 1), cudaMemcpyHostToDevice);
-  } else {
-    e = cudaMemcpy(c->filt.as<double>() + det * (M + 1), spn.data(), 8 * (M + 1),
-                   cudaMemcpyHostToDevice);
-  }
-  if (e == cudaSuccess) e = cudaMemcpy(c->g0.as<double>() + det, &g, 8, cudaMemcpyHostToDevice);
-  if (c->g0_h.size() != (size_t)c->ndet) c->g0_h.assign(c->ndet, 0.0);
-  c->g0_h[det] = g;
-  if (c->spn_h.size() != (size_t)(c->ndet * (M + 1))) c->spn_h.assign(c->ndet * (M + 1), 0.0);
-  std::copy(spn.begin(), spn.end(), c->spn_h.begin() + det * (M + 1));
+  // the largest index read (sanepic.cc:535; monotonic in k)
+  const long long idx_max = (long long)((double)M / nssp * ns);
+  if (idx_max < 0 || idx_max >= nssp)
+    return c->fail(SG_ERR_ARG, "noise spectrum of %ld values is too short for ns=%lld", nssp, ns);
+  // the iSpf values go to the device as they are; the row, its 1/ns^2 scale,
+  // the bin-0 override (sanepic.cc:536-537) and g0 are computed there
+  cudaError_t e = cudaSuccess;
+  if (c->noise_stage.bytes < sizeof(double) * nssp) e = c->noise_stage.alloc(sizeof(double) * nssp);
+  if (e == cudaSuccess && !c->noise_part.p) e = c->noise_part.alloc(sizeof(double) * kNoiseRowBlocks);
+  if (e == cudaSuccess && !c->ev_copy) e = cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->noise_stage.p, ispf, sizeof(double) * nssp, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_copy, c->st);
+  if (e == cudaSuccess)
+    e = c->f32 ? noise_row_launch<float>(c->noise_stage.as<double>(), nssp, ns,
+                                         c->filt.as<float>() + det * (M + 1),
+                                         c->g0.as<double>() + det, c->noise_part.as<double>(), c->st)
+               : noise_row_launch<double>(c->noise_stage.as<double>(), nssp, ns,
+                                          c->filt.as<double>() + det * (M + 1),
+                                          c->g0.as<double>() + det, c->noise_part.as<double>(),
+                                          c->st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(c->ev_copy);  // the caller's array is read
   if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
+  c->launches += 2;
   c->have_noise[det] = 1;
   c->have_bj3 = c->have_diag = c->have_rhs = c->have_hmix = false;
   return SG_OK;
@@ -483,23 +487,38 @@ extern "C" int sg_set_tod(sg_ctx* c, long det, const double* tod, long nsamp_tot
   // the segments are contiguous); conversion and the NaN rule of
   // sanepic.cc:784-790 run there
   cudaError_t e = cudaSuccess;
-  if (c->stage.bytes < sizeof(double) * nsd) e = c->stage.alloc(sizeof(double) * nsd);
-  if (e == cudaSuccess && !c->nanflag.p) e = c->nanflag.alloc(sizeof(int));
+  if (!c->nanflag.p) e = c->nanflag.alloc(sizeof(int));
   bool contiguous = true;
   for (long long g = 1; g < nseg; g++) contiguous &= c->isampmin[g] == c->isampmin[0] + g * ns;
-  if (e == cudaSuccess && contiguous) {
-    e = cudaMemcpyAsync(c->stage.p, tod + c->isampmin[0], sizeof(double) * nsd,
-                        cudaMemcpyHostToDevice, c->st);
-  } else {
-    for (long long g = 0; g < nseg && e == cudaSuccess; g++)
-      e = cudaMemcpyAsync(c->stage.as<double>() + g * ns, tod + c->isampmin[g],
-                          sizeof(double) * ns, cudaMemcpyHostToDevice, c->st);
+  // pinned (page-locked, device-mapped) caller memory is read by the ingest
+  // kernel itself over the CPU-GPU link; other memory is staged by a copy
+  const double* src = nullptr;
+  if (contiguous) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, tod + c->isampmin[0]) == cudaSuccess &&
+        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
+      src = static_cast<const double*>(pa.devicePointer);
+    else
+      (void)cudaGetLastError();
+  }
+  if (!src) {
+    if (e == cudaSuccess && c->stage.bytes < sizeof(double) * nsd)
+      e = c->stage.alloc(sizeof(double) * nsd);
+    if (e == cudaSuccess && contiguous) {
+      e = cudaMemcpyAsync(c->stage.p, tod + c->isampmin[0], sizeof(double) * nsd,
+                          cudaMemcpyHostToDevice, c->st);
+    } else {
+      for (long long g = 0; g < nseg && e == cudaSuccess; g++)
+        e = cudaMemcpyAsync(c->stage.as<double>() + g * ns, tod + c->isampmin[g],
+                            sizeof(double) * ns, cudaMemcpyHostToDevice, c->st);
+    }
+    src = c->stage.as<double>();
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(c->nanflag.p, 0, sizeof(int), c->st);
   if (e == cudaSuccess)
-    e = c->f32 ? ingest_launch<float>(c->stage.as<double>(), nsd, c->tod.as<float>() + det * nsd,
+    e = c->f32 ? ingest_launch<float>(src, nsd, c->tod.as<float>() + det * nsd,
                                       c->nanflag.as<int>(), c->st)
-               : ingest_launch<double>(c->stage.as<double>(), nsd, c->tod.as<double>() + det * nsd,
+               : ingest_launch<double>(src, nsd, c->tod.as<double>() + det * nsd,
                                        c->nanflag.as<int>(), c->st);
   int nan = 0;
   if (e == cudaSuccess)
@@ -601,6 +620,11 @@ int build_bj3(sg_ctx* c) {
   // sum g0 sin 4d') over each group's detectors, d' = the detector rotation
   const int G = c->ngroups;
   std::vector<double> gc(5 * G, 0.0);
+  c->g0_h.resize(c->ndet);
+  cudaError_t e0 = cudaMemcpyAsync(c->g0_h.data(), c->g0.p, sizeof(double) * c->ndet,
+                                   cudaMemcpyDeviceToHost, c->st);
+  if (e0 == cudaSuccess) e0 = cudaStreamSynchronize(c->st);
+  if (e0 != cudaSuccess) return c->cuda_fail(e0, "bj3 build");
   for (int g = 0; g < G; g++)
     for (int k = c->grp_off_h[g]; k < c->grp_off_h[g + 1]; k++) {
       const int dd = c->grp_det_h[k];

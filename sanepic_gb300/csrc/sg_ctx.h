@@ -96,7 +96,8 @@ struct sg_ctx {
   DevBuf kslot, filt_slot;  // frequency of each spectrum slot; filter rows in slot order
   int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
-  std::vector<double> spn_h;  // host copy of the filter rows [ndet][M+1] (FP64)
+  DevBuf noise_stage, noise_part;  // one detector's iSpf values; g0 partial sums
+  cudaEvent_t ev_copy = nullptr;   // host->device copy of a caller's array done
 
   // learned preconditioner: the network, the nested patch geometry
   // (patch_idx [npatch_pad][256] internal pixel or -1), per-patch scales, and
@@ -144,6 +145,7 @@ struct sg_ctx {
   ~sg_ctx() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     if (ev0) cudaEventDestroy(ev0);
+    if (ev_copy) cudaEventDestroy(ev_copy);
     if (ev1) cudaEventDestroy(ev1);
     if (sc_host) cudaFreeHost(sc_host);
     if (own_st) cudaStreamDestroy(own_st);
@@ -220,9 +222,9 @@ struct sg_ctx {
     launches++;
     if (f32)
       return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
-                              ys.as<float>(), npix, h, out, st);
+                              ys.as<float>(), npix, h, out, pt_lanes(ngsamp, npix), st);
     return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<double>(),
-                             ys.as<double>(), npix, h, out, st);
+                             ys.as<double>(), npix, h, out, 32, st);
   }
 
   // out = P^T y (y in time order, one row per detector)

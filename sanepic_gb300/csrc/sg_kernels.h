@@ -87,6 +87,7 @@ cudaError_t numbering_launch(const int* count, long long n, long long nside, int
                              int* indpix_ring, int* npix, void* tmp, size_t tmp_bytes,
                              cudaStream_t st);
 cudaError_t any_negative_launch(const int* v, long long n, int* flag, cudaStream_t st);
+cudaError_t any_nan_launch(const double* v, long long n, int* flag, cudaStream_t st);
 // CSR by pixel over group samples: csr_off [npix+1], csr_idx [n]
 size_t csr_tmp_bytes(long long n, long long npix);
 cudaError_t csr_build(const int* pix, long long n, long long npix,
@@ -118,6 +119,12 @@ template <typename T>
 cudaError_t diag_launch(const long long* csr_off, const uint32_t* csr_idx, long long npix,
                         long long ns, int nseg, const T* ntab, double* Mp, cudaStream_t st);
 
+// one detector's filter row from its iSpf file values, and g0 (the time-domain
+// diagonal of its N^-1) into *g0 (part: kNoiseRowBlocks doubles of scratch)
+constexpr int kNoiseRowBlocks = 64;
+template <typename T>
+cudaError_t noise_row_launch(const double* ispf, long long nssp, long long ns, T* row, double* g0,
+                             double* part, cudaStream_t st);
 // timeline ingest: out = (T) in over n samples, *nan_flag |= any NaN; then, if
 // flagged, NaNs take the previous sample's value within each segment
 template <typename T>
@@ -140,10 +147,12 @@ cudaError_t detsum_launch(const T* y, long long n, long long nsd, const int* grp
                           const int* grp_det, const T* dcs, T* ys, cudaStream_t st);
 // q[c*npix + m]: sums over the group samples of pixel m of (S0, cos2phi A - sin2phi B,
 // sin2phi A + cos2phi B); Q/U zeroed where the pol mask applies (hits_true < 2).
+// lanes per pixel (FP32: 1..32, from pt_lanes; FP64 ignores it)
 template <typename T>
 cudaError_t pt_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
-                      const T* ys, long long npix, const int* hits_true, double* q,
+                      const T* ys, long long npix, const int* hits_true, double* q, int lanes,
                       cudaStream_t st);
+int pt_lanes(long long nsamples, long long npix);
 
 // ---- the offset-group operator (sg_group.cu) -------------------------------------
 // gtl [G][3][nsd] = (a, b1, b2) = (I, Q c + U s, U c - Q s) per group sample

@@ -311,13 +311,23 @@ namespace {
 int make_noise_table(sg_ctx* c) {
   const long long M = c->ns / 2;
   const double ns2 = (double)c->ns * (double)c->ns;
-  std::vector<double> t(c->ndet * (M + 1));
+  const size_t nrow = (size_t)c->ndet * (M + 1);
+  std::vector<double> h(nrow), t(nrow);
+  cudaError_t e;
+  if (c->f32) {
+    std::vector<float> hf(nrow);
+    e = cudaMemcpy(hf.data(), c->filt.p, 4 * nrow, cudaMemcpyDeviceToHost);
+    std::copy(hf.begin(), hf.end(), h.begin());
+  } else {
+    e = cudaMemcpy(h.data(), c->filt.p, 8 * nrow, cudaMemcpyDeviceToHost);
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "noise table");
   for (long long d = 0; d < c->ndet; d++)
     for (long long k = 0; k <= M; k++) {
-      const double hk = c->spn_h[d * (M + 1) + (k == 0 ? 1 : k)];
+      const double hk = h[d * (M + 1) + (k == 0 ? 1 : k)];
       t[d * (M + 1) + k] = hk > 0.0 ? 1.0 / (ns2 * std::sqrt(hk)) : 0.0;
     }
-  cudaError_t e = c->filt_noise.alloc(t.size() * c->esize);
+  e = c->filt_noise.alloc(t.size() * c->esize);
   if (e == cudaSuccess) {
     if (c->f32) {
       std::vector<float> f(t.begin(), t.end());

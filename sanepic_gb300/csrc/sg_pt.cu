@@ -13,15 +13,15 @@
 // over the samples i that hit m.  Detectors that share a pixel stream (an
 // offset group) are first summed per group sample (k_detsum), so P^T walks
 // the group samples, read through the pixel-sorted index (CSR built once at
-// setup; the pointing never changes).  One warp per
-// pixel: the lanes stride through its samples in a fixed order (several
-// independent gathers in flight per lane) and the warp combines lanes with a
-// fixed xor tree, so the result is bitwise identical run to run.  A block
-// owns 32 consecutive pixels (warps interleaved over them); with the
+// setup; the pointing never changes).  A team of L lanes per pixel (L from
+// the mean samples per pixel: about four per lane) strides through its
+// samples in a fixed order (several independent gathers in flight per lane)
+// and combines its lanes with a fixed xor tree, so the result is bitwise
+// identical run to run.  A block owns 256 / L consecutive pixels; with the
 // nested-order pixel numbering, neighbouring pixels along the scan share the
 // block, so the 32-byte sectors of y they gather are reused from L1.  The
-// block's 32 totals are converted to FP64 and stored together.  The
-// degeneracy mask (sanepic.cc:1455-1459) is applied here.
+// block's totals are converted to FP64 and stored together.  The degeneracy
+// mask (sanepic.cc:1455-1459) is applied here.
 //
 // Precision: FP64 problems accumulate in FP64.  FP32 problems accumulate each
 // lane's FP32 products with Neumaier-compensated FP32 sums and combine lanes
@@ -263,75 +263,88 @@ cudaError_t detsum_launch<double>(const double* y, long long n, long long nsd,
 
 // ---- P^T --------------------------------------------------------------------------
 constexpr int kPtUnroll = 4;
-constexpr int kPtPix = 32;  // pixels per block (4 per warp)
 
+// L lanes per pixel (a team; 256 / L pixels per block, consecutive): the
+// lanes stride through the pixel's samples in a fixed order, four gathers in
+// flight each, and the team combines its lanes with a fixed xor tree.  L is
+// chosen from the mean samples per pixel, so a pixel's few samples do not
+// leave most of a warp idle; for a given problem the order of every sum is
+// fixed, so the result is bitwise identical run to run.
+template <int L>
 __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ off,
                                                 const uint32_t* __restrict__ idx,
                                                 const float2* __restrict__ ccs,
                                                 const float4* __restrict__ ys, long long npix,
                                                 const int* __restrict__ hits,
                                                 double* __restrict__ q) {
-  __shared__ float sh[kPtPix][6];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long m0 = (long long)blockIdx.x * kPtPix;
-  for (int k = w; k < kPtPix; k += 8) {
-    const long long m = m0 + k;
-    ff a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f};
-    if (m < npix) {
-      const long long jend = off[m + 1];
-      long long j = off[m] + lane;
-      for (; j + 32 * (kPtUnroll - 1) < jend; j += 32 * kPtUnroll) {
-        uint32_t ii[kPtUnroll];
-        float4 v[kPtUnroll];
-        float2 wv[kPtUnroll];
+  constexpr int T = 256 / L;  // pixels per block
+  __shared__ float sh[T][6];
+  const int lane = threadIdx.x % L, team = threadIdx.x / L;
+  const long long m0 = (long long)blockIdx.x * T;
+  const long long m = m0 + team;
+  ff a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f};
+  if (m < npix) {
+    const long long jend = off[m + 1];
+    long long j = off[m] + lane;
+    for (; j + L * (kPtUnroll - 1) < jend; j += L * kPtUnroll) {
+      uint32_t ii[kPtUnroll];
+      float4 v[kPtUnroll];
+      float2 wv[kPtUnroll];
 #pragma unroll
-        for (int u = 0; u < kPtUnroll; u++) ii[u] = __ldcs(idx + j + 32 * u);
+      for (int u = 0; u < kPtUnroll; u++) ii[u] = __ldcs(idx + j + L * u);
 #pragma unroll
-        for (int u = 0; u < kPtUnroll; u++) {
-          v[u] = __ldg(ys + ii[u]);
-          wv[u] = __ldcs(ccs + j + 32 * u);
-        }
-#pragma unroll
-        for (int u = 0; u < kPtUnroll; u++) {
-          ff_add_f(a0, v[u].x);
-          ff_add_f(a1, wv[u].x * v[u].y - wv[u].y * v[u].z);
-          ff_add_f(a2, wv[u].y * v[u].y + wv[u].x * v[u].z);
-        }
+      for (int u = 0; u < kPtUnroll; u++) {
+        v[u] = __ldg(ys + ii[u]);
+        wv[u] = __ldcs(ccs + j + L * u);
       }
-      for (; j < jend; j += 32) {
-        const float4 v = __ldg(ys + __ldcs(idx + j));
-        const float2 wv = __ldcs(ccs + j);
-        ff_add_f(a0, v.x);
-        ff_add_f(a1, wv.x * v.y - wv.y * v.z);
-        ff_add_f(a2, wv.y * v.y + wv.x * v.z);
+#pragma unroll
+      for (int u = 0; u < kPtUnroll; u++) {
+        ff_add_f(a0, v[u].x);
+        ff_add_f(a1, wv[u].x * v[u].y - wv[u].y * v[u].z);
+        ff_add_f(a2, wv[u].y * v[u].y + wv[u].x * v[u].z);
       }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 = ff_add(a0, ff_shfl_xor(a0, o));
-      a1 = ff_add(a1, ff_shfl_xor(a1, o));
-      a2 = ff_add(a2, ff_shfl_xor(a2, o));
+    for (; j < jend; j += L) {
+      const float4 v = __ldg(ys + __ldcs(idx + j));
+      const float2 wv = __ldcs(ccs + j);
+      ff_add_f(a0, v.x);
+      ff_add_f(a1, wv.x * v.y - wv.y * v.z);
+      ff_add_f(a2, wv.y * v.y + wv.x * v.z);
     }
-    if (lane == 0) {
-      sh[k][0] = a0.hi;
-      sh[k][1] = a0.lo;
-      sh[k][2] = a1.hi;
-      sh[k][3] = a1.lo;
-      sh[k][4] = a2.hi;
-      sh[k][5] = a2.lo;
-    }
+  }
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) {
+    a0 = ff_add(a0, ff_shfl_xor(a0, o));
+    a1 = ff_add(a1, ff_shfl_xor(a1, o));
+    a2 = ff_add(a2, ff_shfl_xor(a2, o));
+  }
+  if (lane == 0) {
+    sh[team][0] = a0.hi;
+    sh[team][1] = a0.lo;
+    sh[team][2] = a1.hi;
+    sh[team][3] = a1.lo;
+    sh[team][4] = a2.hi;
+    sh[team][5] = a2.lo;
   }
   __syncthreads();
-  // 32 lanes convert the block's 32 totals to FP64 at once
-  if (threadIdx.x < kPtPix) {
-    const long long m = m0 + threadIdx.x;
-    if (m < npix) {
+  // the block's T totals converted to FP64 and stored together
+  if (threadIdx.x < T) {
+    const long long mm = m0 + threadIdx.x;
+    if (mm < npix) {
       const float* r = sh[threadIdx.x];
-      const bool pol = hits == nullptr || hits[m] >= 2;
-      q[m] = (double)r[0] + (double)r[1];
-      q[npix + m] = pol ? (double)r[2] + (double)r[3] : 0.0;
-      q[2 * npix + m] = pol ? (double)r[4] + (double)r[5] : 0.0;
+      const bool pol = hits == nullptr || hits[mm] >= 2;
+      q[mm] = (double)r[0] + (double)r[1];
+      q[npix + mm] = pol ? (double)r[2] + (double)r[3] : 0.0;
+      q[2 * npix + mm] = pol ? (double)r[4] + (double)r[5] : 0.0;
     }
   }
+}
+
+int pt_lanes(long long nsamples, long long npix) {
+  const double mean = npix > 0 ? (double)nsamples / (double)npix : 1.0;
+  int L = 1;
+  while (L < 32 && L * 4 < mean) L *= 2;  // about four samples per lane
+  return L;
 }
 
 __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint32_t* idx,
@@ -364,22 +377,36 @@ __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint
   }
 }
 
+template <int L>
+static void pt_f32_launch(const long long* csr_off, const uint32_t* csr_idx, const float* csr_cs,
+                          const float* ys, long long npix, const int* hits_true, double* q,
+                          cudaStream_t st) {
+  const long long blocks = (npix + 256 / L - 1) / (256 / L);
+  k_pt_f32<L><<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,
+                                                reinterpret_cast<const float2*>(csr_cs),
+                                                reinterpret_cast<const float4*>(ys), npix,
+                                                hits_true, q);
+}
+
 template <>
 cudaError_t pt_launch<float>(const long long* csr_off, const uint32_t* csr_idx,
                              const float* csr_cs, const float* ys, long long npix,
-                             const int* hits_true, double* q, cudaStream_t st) {
-  const long long blocks = (npix + kPtPix - 1) / kPtPix;
-  k_pt_f32<<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,
-                                             reinterpret_cast<const float2*>(csr_cs),
-                                             reinterpret_cast<const float4*>(ys), npix,
-                                             hits_true, q);
+                             const int* hits_true, double* q, int lanes, cudaStream_t st) {
+  switch (lanes) {
+    case 1: pt_f32_launch<1>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+    case 2: pt_f32_launch<2>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+    case 4: pt_f32_launch<4>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+    case 8: pt_f32_launch<8>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+    case 16: pt_f32_launch<16>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+    default: pt_f32_launch<32>(csr_off, csr_idx, csr_cs, ys, npix, hits_true, q, st); break;
+  }
   return cudaGetLastError();
 }
 
 template <>
 cudaError_t pt_launch<double>(const long long* csr_off, const uint32_t* csr_idx,
                               const double* csr_cs, const double* ys, long long npix,
-                              const int* hits_true, double* q, cudaStream_t st) {
+                              const int* hits_true, double* q, int, cudaStream_t st) {
   long long blocks = (npix * 32 + 255) / 256;
   if (blocks > 152LL * 8 * 16) blocks = 152LL * 8 * 16;
   k_pt_f64<<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,

@@ -216,3 +216,45 @@ def test_tod_nan_rule_matches_reference(prec):
         mm.close()
     assert np.isfinite(out[0][0]) and out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_tod_from_pinned_memory(prec):
+    """timelines in pinned (page-locked) host memory are read by the ingest
+    kernel directly; the result equals the staged copy of ordinary memory,
+    NaN rule included"""
+    torch = pytest.importorskip("torch")
+    prob = small_problem(ndet=4, nseg=4, ns=2048, precision=prec)
+    tods = [t.copy() for t in prob["tod"]]
+    tods[1][100:103] = np.nan
+    out = []
+    for pinned in (False, True):
+        mm = sg.from_problem(dict(prob, tod=tods), precision=prec)
+        if pinned:
+            for d, t in enumerate(tods):
+                buf = torch.empty(t.size, dtype=torch.float64, pin_memory=True)
+                buf.numpy()[:] = t
+                mm.set_tod(d, buf.numpy())
+        out.append((mm.rhs(), mm.solve(precond="bj3", stop_crit=1e-8)["iterations"],
+                    mm.solution()))
+        mm.close()
+    assert np.isfinite(out[0][0]) and out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_psi_nan_rule_matches_oracle():
+    """NaN boresight angles take the previous sample's psi within their segment
+    (sanepic.cc:722-727, applied on the GPU): pixels and A x match the oracle"""
+    prob = small_problem(ndet=4, nseg=4, ns=2048, precision="f64")
+    ns = prob["spec"].ns
+    psi = prob["psi"].copy()
+    rng = np.random.default_rng(12)
+    for i in rng.integers(1, psi.size - 8, 30):
+        if i % ns and (i + 4) // ns == i // ns:    # inside one segment, not its first sample
+            psi[i:i + rng.integers(1, 4)] = np.nan
+    p = dict(prob, psi=psi)
+    s = oracle.Setup(p)
+    mm = sg.from_problem(p, precision="f64", with_tod=False)
+    assert np.array_equal(mm.pixels(), s.pix)
+    x = np.random.default_rng(2).standard_normal(3 * s.npix)
+    assert rel_rms(mm.apply(x), s.apply(x)) < 1e-11
