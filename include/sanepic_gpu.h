@@ -98,7 +98,9 @@ typedef struct sg_report {
   double solve_seconds; /* wall time of the iterations */
   double iter_per_sec;
   double setup_seconds; /* preconditioner build inside sg_solve */
-  double device_seconds;  /* CUDA-event time of the iterations on the GPU */
+  double device_seconds;  /* CUDA-event time of the solve on the GPU (sg_solve_batch:
+                             device clock from the batch's first iteration to this
+                             problem's last) */
   long kernel_launches;   /* kernels this library launched during the solve */
   int breakdown;          /* nonzero: stopped early because d^T A d <= 0 (bit 0) or
                              r^T M r <= 0 (bit 1) -- the residual reached rounding level */
@@ -251,14 +253,20 @@ int sg_mlp_gemm_host(const unsigned short *A, const unsigned short *B, float *C,
 int sg_mlp_grad_host(const float *params, const float *X, const float *T, int B, float *Y,
                      float *loss, float *grads);
 
-/* Preconditioned CG (sanepic.cc:1177-1761). */
+/* Preconditioned CG (sanepic.cc:1177-1761).  With use_graph and nothing to
+ * report per iteration (verbose 0, no on_iteration) the whole loop is one
+ * CUDA-graph launch: a conditional WHILE node over the captured iteration,
+ * its convergence test and iteration limit evaluated on the device
+ * (SANEPIC_GPU_DEVICE_LOOP=0 keeps the host-driven loop). */
 int sg_solve(sg_ctx *ctx, const sg_solve_opts *opts, sg_report *report);
 
-/* Solves n independent problems (contexts, each after sg_rhs) at once: every
- * context iterates on its own CUDA stream from captured iteration graphs and
- * the host advances each as its last iteration finishes, so problems too small
- * to fill the GPU share it.  Same options for all (x0 must be NULL);
- * reports[i] as sg_solve's.  No reference counterpart (one problem per run). */
+/* Solves n independent problems (contexts, each after sg_rhs) at once.  With
+ * use_graph: one CUDA graph holds every problem's solve start and WHILE loop
+ * as independent branches, so the batch is a single launch (the graph is kept
+ * for the same contexts); otherwise every context iterates on its own stream
+ * and the host advances each as its last iteration finishes.  Same options
+ * for all (x0 must be NULL); reports[i] as sg_solve's.  No reference
+ * counterpart (one problem per run). */
 int sg_solve_batch(sg_ctx **ctxs, int n, const sg_solve_opts *opts, sg_report *reports);
 
 /* Times this context's noise filter with each compiled tile shape for its

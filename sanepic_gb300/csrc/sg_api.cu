@@ -118,9 +118,7 @@ extern "C" int sg_set_stream(sg_ctx* c, void* stream) {
   cudaStream_t s = stream ? reinterpret_cast<cudaStream_t>(stream) : c->own_st;
   if (s != c->st) {
     cudaStreamSynchronize(c->st);
-    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-    c->graphs.clear();  // graphs were captured on the old stream
-    c->graph_launches.clear();
+    c->drop_graphs();  // graphs were captured on the old stream
     c->st = s;
   }
   return SG_OK;
@@ -769,7 +767,49 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   c->crit_hist.clear();
   c->have_solution = true;  // the callback may read the current map
   int iter = 0;
-  while ((iter < maxiter && crit > o->stop_crit) || iter == 0) {
+  bool loop_done = false;
+  // With nothing to report per iteration (no printed line, no callback) the
+  // whole loop runs on the device: one graph launch, the convergence test in
+  // a kernel (SANEPIC_GPU_DEVICE_LOOP=0 keeps the host-driven loop).
+  const char* dl_env = getenv("SANEPIC_GPU_DEVICE_LOOP");
+  if (o->use_graph && !o->verbose && !o->on_iteration && !(dl_env && dl_env[0] == '0')) {
+    sg_ctx::LoopGraph* lg = nullptr;
+    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0};
+    e = c->ensure_loop_buffers(maxiter);
+    if (e == cudaSuccess) e = c->solve_loop_graph(pc, &lg);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->loop_state.p, &ls, sizeof(ls), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaGraphLaunch(lg->exec, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ls, c->loop_state.p, sizeof(ls), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "device solve loop");
+    iter = ls.iter;
+    c->crit_hist.resize(iter);
+    if (iter > 0)
+      e = cudaMemcpy(c->crit_hist.data(), c->loop_hist.p, sizeof(double) * iter, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return c->cuda_fail(e, "device solve loop");
+    const long long nref = (iter + refresh_every - 1) / refresh_every;
+    c->launches += nref * lg->launches_refresh + (iter - nref) * lg->launches_plain + 2LL * iter;
+    crit = c->sc_host->var / var00;
+    // a breakdown of the learned part falls back below; any other stop is final
+    loop_done = !(ls.done == 3 && pc == 2 && crit > o->stop_crit);
+    if (ls.done == 3 && pc == 2 && crit > o->stop_crit) {
+      fallback_iter = iter;
+      pc = 1;
+      CgVecs v1 = c->vecs(1);
+      e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
+      if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
+      if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
+      c->launches += 7;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+      if (e != cudaSuccess) return c->cuda_fail(e, "fallback restart");
+    }
+  }
+  while (!loop_done && ((iter < maxiter && crit > o->stop_crit) || iter == 0)) {
     const bool refresh = (iter % refresh_every) == 0;
     e = c->run_iteration(pc, refresh, o->use_graph != 0);
     if (e == cudaSuccess)

@@ -14,6 +14,9 @@
 // the cluster) on the context's own timeline and keeps the faster one.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -112,7 +115,181 @@ cudaError_t enqueue_scalars(Job& j) {
   return e;
 }
 
+// ---- the whole batch as one graph launch ---------------------------------------
+// For every problem: [solve start, WHILE loop of its iterations], independent
+// branches of one graph, so the 32 solves are one launch.  The
+// captured graph is kept for the same contexts (same captured state, checked
+// by each context's graph generation) and dropped when a context goes away.
+struct BatchGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<unsigned long long> gens;
+  std::vector<int> pcs, rkinds;
+  std::vector<long long> nref, nplain, nstart;
+};
+std::mutex g_batch_mu;
+std::map<std::vector<const sg_ctx*>, BatchGraph> g_batch;
+
+cudaError_t build_batch_graph(std::vector<Job>& jobs, BatchGraph& bg) {
+  cudaGraph_t G;
+  cudaError_t e = cudaGraphCreate(&G, 0);
+  if (e != cudaSuccess) return e;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  for (size_t i = 0; i < jobs.size() && e == cudaSuccess; i++) {
+    sg_ctx* c = jobs[i].c;
+    cudaGraph_t cap;
+    e = cudaStreamBeginCaptureToGraph(c->st, G, nullptr, nullptr, 0, mode);
+    if (e != cudaSuccess) break;
+    const long long before = c->launches;
+    e = enqueue_start(c, jobs[i].pc);
+    bg.nstart[i] = c->launches - before;
+    c->launches = before;
+    std::vector<cudaGraphNode_t> deps;
+    if (e == cudaSuccess) {
+      cudaStreamCaptureStatus status;
+      const cudaGraphNode_t* d = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(c->st, &status, nullptr, nullptr, &d, nullptr, &nd);
+      if (e == cudaSuccess) deps.assign(d, d + nd);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(c->st, &cap);
+    if (e == cudaSuccess) e = e2;
+    cudaGraphNode_t loop;
+    if (e == cudaSuccess)
+      e = c->add_solve_loop(G, deps.data(), deps.size(), jobs[i].pc, &loop, &bg.nref[i],
+                            &bg.nplain[i]);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&bg.exec, G, 0);
+  cudaGraphDestroy(G);
+  return e;
+}
+
 }  // namespace
+
+void forget_batch_graphs(const sg_ctx* c) {
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  for (auto it = g_batch.begin(); it != g_batch.end();) {
+    bool uses = false;
+    for (const sg_ctx* x : it->first) uses |= x == c;
+    if (uses) {
+      if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
+      it = g_batch.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+// one graph launch for all problems; false if the batch cannot run this way
+static int solve_batch_device(std::vector<Job>& jobs, const sg_solve_opts* o, int maxiter,
+                              int refresh_every, sg_report* reports) {
+  const int n = (int)jobs.size();
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    sg_ctx* c = jobs[i].c;
+    e = c->ensure_loop_buffers(maxiter);  // (may drop captured graphs)
+    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0};
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->loop_state.p, &ls, sizeof(ls), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  }
+  if (e != cudaSuccess) return jobs[0].c->cuda_fail(e, "batch loop set-up");
+  std::vector<const sg_ctx*> key(n);
+  for (int i = 0; i < n; i++) key[i] = jobs[i].c;
+  std::lock_guard<std::mutex> lk(g_batch_mu);
+  BatchGraph& bg = g_batch[key];
+  bool fresh = bg.exec != nullptr;
+  for (int i = 0; i < n && fresh; i++)
+    fresh = bg.gens[i] == jobs[i].c->graph_gen && bg.pcs[i] == jobs[i].pc &&
+            bg.rkinds[i] == jobs[i].c->refresh_kind();
+  if (!fresh) {
+    if (bg.exec) cudaGraphExecDestroy(bg.exec);
+    bg = BatchGraph{};
+    bg.nref.assign(n, 0);
+    bg.nplain.assign(n, 0);
+    bg.nstart.assign(n, 0);
+    e = build_batch_graph(jobs, bg);
+    if (e != cudaSuccess) {
+      if (bg.exec) cudaGraphExecDestroy(bg.exec);
+      g_batch.erase(key);
+      return jobs[0].c->cuda_fail(e, "batch graph");
+    }
+    for (int i = 0; i < n; i++) {
+      bg.gens.push_back(jobs[i].c->graph_gen);
+      bg.pcs.push_back(jobs[i].pc);
+      bg.rkinds.push_back(jobs[i].c->refresh_kind());
+    }
+  }
+  sg_ctx* c0 = jobs[0].c;
+  const double t0 = now_s();
+  e = cudaGraphLaunch(bg.exec, c0->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c0->st);
+  const double t1 = now_s();
+  if (e != cudaSuccess) return c0->cuda_fail(e, "batch graph launch");
+  unsigned long long t_begin = ~0ULL;  // the device clock at the first problem's first iteration
+  std::vector<LoopState> states(n);
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    e = cudaMemcpy(&states[i], jobs[i].c->loop_state.p, sizeof(LoopState), cudaMemcpyDeviceToHost);
+    if (states[i].iter > 0 && states[i].t_first < t_begin) t_begin = states[i].t_first;
+  }
+  if (e != cudaSuccess) return c0->cuda_fail(e, "batch results");
+  for (int i = 0; i < n; i++) {
+    Job& j = jobs[i];
+    sg_ctx* c = j.c;
+    const LoopState& ls = states[i];
+    e = cudaMemcpy(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost);
+    c->crit_hist.resize(ls.iter);
+    if (e == cudaSuccess && ls.iter > 0)
+      e = cudaMemcpy(c->crit_hist.data(), c->loop_hist.p, sizeof(double) * ls.iter,
+                     cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return c->cuda_fail(e, "batch results");
+    j.iter = ls.iter;
+    j.var00 = c->sc_host->var00;
+    j.crit = c->sc_host->var / j.var00;
+    const long long nr = (ls.iter + refresh_every - 1) / refresh_every;
+    c->launches += bg.nstart[i] + nr * bg.nref[i] + (ls.iter - nr) * bg.nplain[i] + 2LL * ls.iter;
+    if (ls.done == 3 && j.pc == 2 && j.crit > o->stop_crit) {
+      // the learned part broke flexible PCG: finish this problem with plain
+      // block-Jacobi PCG from its current map, driven from the host
+      j.fallback = j.iter;
+      j.pc = 1;
+      CgVecs v1 = c->vecs(1);
+      e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
+      if (e == cudaSuccess) e = c->f32 ? cg_init<float>(v1, c->st) : cg_init<double>(v1, c->st);
+      if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
+      c->launches += 7;
+      while (e == cudaSuccess && j.iter < maxiter && j.crit > o->stop_crit) {
+        e = c->run_iteration(1, (j.iter % refresh_every) == 0, true);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        if (e != cudaSuccess) break;
+        j.crit = c->sc_host->var / j.var00;
+        c->crit_hist.push_back(j.crit);
+        j.iter++;
+        if (c->sc_host->flag) break;
+      }
+      if (e != cudaSuccess) return c->cuda_fail(e, "batch fallback");
+    }
+    // device time from the batch's first iteration to this problem's last one
+    const double ms = ls.iter > 0 ? (double)(ls.t_last - t_begin) * 1e-6 : 0.0;
+    c->have_solution = true;
+    if (reports) {
+      sg_report& r = reports[i];
+      r = sg_report{};
+      r.iterations = j.iter;
+      r.converged = j.crit <= o->stop_crit;
+      r.crit = j.crit;
+      r.var00 = j.var00;
+      r.solve_seconds = t1 - t0;
+      r.iter_per_sec = j.iter / (t1 - t0 > 0 ? t1 - t0 : 1e-30);
+      r.device_seconds = ms * 1e-3;
+      r.kernel_launches = (long)(c->launches - j.launches0);
+      r.breakdown = c->sc_host->flag;
+      r.fallback_iter = j.fallback;
+    }
+  }
+  return SG_OK;
+}
 
 extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_report* reports) {
   if (!ctxs || n <= 0 || !o) return SG_ERR_ARG;
@@ -146,6 +323,13 @@ extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_r
   }
   const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
   const int maxiter = o->maxiter > 0 ? o->maxiter : 2000;
+  const char* dl_env = getenv("SANEPIC_GPU_DEVICE_LOOP");
+  if (o->use_graph && !(dl_env && dl_env[0] == '0')) {
+    const int rc = solve_batch_device(jobs, o, maxiter, refresh_every, reports);
+    for (auto& j : jobs)
+      if (j.ready) cudaEventDestroy(j.ready);
+    return rc;
+  }
   const double t0 = now_s();
   cudaError_t e = cudaSuccess;
   int failed = -1;

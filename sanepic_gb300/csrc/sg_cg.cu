@@ -398,6 +398,53 @@ cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStrea
   return cudaGetLastError();
 }
 
+// ---- the PCG loop on the device ----------------------------------------------
+// One thread decides; the WHILE node repeats its body (begin, the iteration
+// under one of two IF nodes, end) while the handle is non-zero.  The limit on
+// iterations is checked on the device, so the loop always ends.
+__global__ void k_loop_begin(const LoopState* s, cudaGraphConditionalHandle refresh,
+                             cudaGraphConditionalHandle normal) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const bool r = s->refresh_every <= 1 || (s->iter % s->refresh_every) == 0;
+    cudaGraphSetConditional(refresh, r ? 1u : 0u);
+    cudaGraphSetConditional(normal, r ? 0u : 1u);
+  }
+}
+
+__global__ void k_loop_end(LoopState* s, const CgScalars* sc, double* hist,
+                           cudaGraphConditionalHandle loop) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double crit = sc->var / sc->var00;
+    if (s->iter < s->maxiter) hist[s->iter] = crit;
+    const int it = s->iter + 1;
+    s->iter = it;
+    // the host loop's test: go on while iter < maxiter and crit > stop (a NaN
+    // crit stops), and stop at a breakdown flag
+    int done = 0;
+    if (!(crit > s->stop)) done = 1;
+    else if (it >= s->maxiter) done = 2;
+    else if (sc->flag) done = 3;
+    s->done = done;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (it == 1) s->t_first = t;
+    s->t_last = t;
+    cudaGraphSetConditional(loop, done ? 0u : 1u);
+  }
+}
+
+cudaError_t loop_begin_launch(const LoopState* s, cudaGraphConditionalHandle refresh,
+                              cudaGraphConditionalHandle normal, cudaStream_t st) {
+  k_loop_begin<<<1, 32, 0, st>>>(s, refresh, normal);
+  return cudaGetLastError();
+}
+
+cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
+                            cudaGraphConditionalHandle loop, cudaStream_t st) {
+  k_loop_end<<<1, 32, 0, st>>>(s, sc, hist, loop);
+  return cudaGetLastError();
+}
+
 // ---- two-level preconditioner with a coarse space U (kc columns) ------------
 // Balancing form (Mandel's balancing Neumann-Neumann; A-DEF2 in Tang et al.
 // 2009), with AU = A U and E = U^T A U:

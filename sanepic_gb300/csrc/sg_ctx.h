@@ -22,6 +22,9 @@
 
 using namespace sg;
 
+struct sg_ctx;
+void forget_batch_graphs(const sg_ctx* c);  // sg_batch.cu: drop cached batch graphs using c
+
 namespace sg {
 
 struct DevBuf {
@@ -143,6 +146,8 @@ struct sg_ctx {
     return fail(SG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
   }
   ~sg_ctx() {
+    forget_batch_graphs(this);
+    for (auto& kv : loop_graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     if (ev0) cudaEventDestroy(ev0);
     if (ev_copy) cudaEventDestroy(ev_copy);
@@ -475,10 +480,115 @@ struct sg_ctx {
 
   // captured iterations hold raw device pointers: drop them whenever a buffer
   // they use is reallocated
+  unsigned long long graph_gen = 0;  // bumped whenever captured work is invalidated
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
     graph_launches.clear();
+    for (auto& kv : loop_graphs) cudaGraphExecDestroy(kv.second.exec);
+    loop_graphs.clear();
+    graph_gen++;
+  }
+
+  // ---- the whole PCG loop as one graph: a conditional WHILE node whose body
+  // is one iteration (the refresh or the plain variant under two IF nodes)
+  // and a decision kernel; loop_state holds the limits and the count, so one
+  // captured loop serves every solve of the same preconditioner
+  DevBuf loop_state, loop_hist;
+  struct LoopGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long launches_refresh = 0, launches_plain = 0;  // per iteration of each variant
+  };
+  std::map<std::pair<int, int>, LoopGraph> loop_graphs;
+
+  // appends [WHILE loop] to g after deps; counts the launches of each variant
+  cudaError_t add_solve_loop(cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps, int precond,
+                             cudaGraphNode_t* node_out, long long* n_refresh, long long* n_plain) {
+    cudaGraphConditionalHandle hw, hr, hn;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hr, g, 0, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hn, g, 0, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    e = cudaGraphAddNode(node_out, g, deps, nullptr, ndeps, &wp);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    LoopState* ls = loop_state.as<LoopState>();
+    // begin: pick this iteration's variant
+    cudaGraph_t cap;
+    e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, mode);
+    if (e != cudaSuccess) return e;
+    e = loop_begin_launch(ls, hr, hn, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &cap);
+    if (e != cudaSuccess) return e;
+    if (e2 != cudaSuccess) return e2;
+    cudaGraphNode_t begin;
+    size_t nn = 1;
+    e = cudaGraphGetNodes(body, &begin, &nn);
+    if (e != cudaSuccess) return e;
+    if (nn != 1) return cudaErrorInvalidValue;
+    // the two variants, each under an IF node
+    cudaGraphNode_t ifs[2];
+    for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+      cudaGraphNodeParams ip = {};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = v == 0 ? hr : hn;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      e = cudaGraphAddNode(&ifs[v], body, &begin, nullptr, 1, &ip);
+      if (e != cudaSuccess) break;
+      e = cudaStreamBeginCaptureToGraph(st, ip.conditional.phGraph_out[0], nullptr, nullptr, 0, mode);
+      if (e != cudaSuccess) break;
+      const long long before = launches;
+      e = enqueue_iteration(precond, v == 0);
+      (v == 0 ? *n_refresh : *n_plain) = launches - before;
+      launches = before;
+      e2 = cudaStreamEndCapture(st, &cap);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (e != cudaSuccess) return e;
+    // end: record crit, count, decide
+    e = cudaStreamBeginCaptureToGraph(st, body, ifs, nullptr, 2, mode);
+    if (e != cudaSuccess) return e;
+    e = loop_end_launch(ls, sc.as<CgScalars>(), loop_hist.as<double>(), hw, st);
+    e2 = cudaStreamEndCapture(st, &cap);
+    return e != cudaSuccess ? e : e2;
+  }
+
+  // the single-solve loop graph for (precond, refresh kind), captured on first use
+  cudaError_t solve_loop_graph(int precond, LoopGraph** out) {
+    auto key = std::make_pair(precond, refresh_kind());
+    auto it = loop_graphs.find(key);
+    if (it == loop_graphs.end()) {
+      cudaGraph_t g;
+      cudaError_t e = cudaGraphCreate(&g, 0);
+      if (e != cudaSuccess) return e;
+      LoopGraph lg;
+      cudaGraphNode_t node;
+      e = add_solve_loop(g, nullptr, 0, precond, &node, &lg.launches_refresh, &lg.launches_plain);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&lg.exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return e;
+      it = loop_graphs.emplace(key, lg).first;
+    }
+    *out = &it->second;
+    return cudaSuccess;
+  }
+
+  // loop_state / loop_hist for a solve of at most maxiter iterations
+  cudaError_t ensure_loop_buffers(int maxiter) {
+    cudaError_t e = cudaSuccess;
+    if (!loop_state.p) e = loop_state.alloc(sizeof(LoopState));
+    if (e == cudaSuccess && loop_hist.bytes < sizeof(double) * (size_t)maxiter) {
+      drop_graphs();  // captured loops point at the old history buffer
+      e = loop_hist.alloc(sizeof(double) * (size_t)maxiter);
+    }
+    return e;
   }
 
   // the captured iteration for (precond, refresh), captured on first use

@@ -237,6 +237,23 @@ cudaError_t to_map4(const double* x, long long npix, T* map, cudaStream_t st);
 cudaError_t mask_qu(double* v, const int* hits_true, long long npix, cudaStream_t st);
 cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStream_t st);
 
+// ---- the PCG loop on the device (a conditional WHILE node of a CUDA graph) ----
+struct LoopState {
+  int iter;           // iterations done
+  int maxiter;
+  int refresh_every;  // the true residual every refresh_every-th iteration (0, r, 2r, ...)
+  int done;           // 1: converged, 2: iteration limit, 3: breakdown flag
+  double stop;        // |r|^2 / |b|^2 at which to stop
+  unsigned long long t_first, t_last;  // device clock (ns) at the first and last iteration's end
+};
+// sets the IF handles of this iteration's variant (refresh or not)
+cudaError_t loop_begin_launch(const LoopState* s, cudaGraphConditionalHandle refresh,
+                              cudaGraphConditionalHandle normal, cudaStream_t st);
+// records crit = var / var00 in hist[iter], counts the iteration, and sets the
+// WHILE handle to continue unless converged, at the limit or broken down
+cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
+                            cudaGraphConditionalHandle loop, cudaStream_t st);
+
 // two-level preconditioner: coarse space U [3 npix][kp] (FP32, element-major,
 // kp = coarse_pad(kc) columns, the last kp - kc zero), AU = A U, E^-1 [kc][kc]
 constexpr int kCoarseMax = 32;

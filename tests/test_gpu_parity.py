@@ -258,3 +258,25 @@ def test_psi_nan_rule_matches_oracle():
     assert np.array_equal(mm.pixels(), s.pix)
     x = np.random.default_rng(2).standard_normal(3 * s.npix)
     assert rel_rms(mm.apply(x), s.apply(x)) < 1e-11
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_device_loop_matches_host_loop(prec, monkeypatch):
+    """the PCG loop as one graph launch (a conditional WHILE node) runs the same
+    kernels in the same order as the host-driven loop: identical iterations,
+    crit history and map"""
+    prob = small_problem(ndet=4, nseg=4, ns=4096, precision=prec, nside=16, fknee=0.05)
+    out = []
+    for env in ("1", "0"):
+        monkeypatch.setenv("SANEPIC_GPU_DEVICE_LOOP", env)
+        mm = sg.from_problem(prob, precision=prec)
+        mm.rhs()
+        rep = mm.solve(precond="bj3", stop_crit=1e-12, maxiter=300)
+        out.append((rep["iterations"], mm.crit_history(), mm.solution()))
+        # an iteration limit is honoured on the device as on the host
+        lim = mm.solve(precond="bj3", stop_crit=1e-30, maxiter=7)
+        assert lim["iterations"] == 7 and not lim["converged"]
+        mm.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
