@@ -8,6 +8,7 @@
 // Replaces the rank-0 vector passes of the reference's PCG
 // (sanepic.cc:1336-1411 init, 1455-1481 and 1573-1610 per iteration).
 // Vectors are compact maps [I | Q | U] of npix each (sanepic.cc:919-921).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "sg_kernels.h"
@@ -452,19 +453,31 @@ cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
 // computed as  c = E^-1 U^T r,  y = M (r - AU c),  z = y + U (c - E^-1 AU^T y)
 // in three passes (U^T r; y and AU^T y; z and the CG's dots).
 // Symmetric positive definite for any SPD E and M, so plain (or flexible)
-// PCG applies.  U and AU are stored element-major, [3 npix][kp] FP32 with
+// PCG applies.  U and AU are stored element-major, [3 npix][kp] BF16 with
 // kp = kc rounded up to 8 (zero columns), so one thread reads an element's
-// kp values as float4s.  Their products with a vector run in FP32 (GB300's
+// kp values as 16-byte loads; the preconditioner stays symmetric positive
+// definite whatever their rounding (the same U on both sides, E exact in
+// FP64).  Their products with a vector run in FP32 (GB300's
 // FP64 rate would make kc FP64 FMAs per element cost more than reading U);
 // per-thread partials, the fixed-order reductions and the coarse solves are
 // FP64.  Every block of the kernel that needs c (or c - g) re-reduces the
 // partials itself, so the coarse solve costs no launch.  The rounding makes
 // the preconditioner slightly inexact, which flexible PCG absorbs.
 
+// eight BF16 values (one 16-byte load) as floats
+__device__ __forceinline__ void bf16x8(const uint4 q, float (&f)[8]) {
+  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    f[2 * t] = __uint_as_float(w[t] << 16);
+    f[2 * t + 1] = __uint_as_float(w[t] & 0xffff0000u);
+  }
+}
+
 // part[k][block] = sum over the block's elements of U[i][k] v[i]
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_dots(const float* __restrict__ U, long long n3, const double* __restrict__ v,
+    k_coarse_dots(const uint16_t* __restrict__ U, long long n3, const double* __restrict__ v,
                   double* part) {
   float acc[KP];
 #pragma unroll
@@ -473,14 +486,13 @@ __global__ void __launch_bounds__(kCgThreads)
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
     const float vi = (float)v[i];
-    const float4* row = reinterpret_cast<const float4*>(U + i * KP);
+    const uint4* row = reinterpret_cast<const uint4*>(U + i * KP);
 #pragma unroll
-    for (int q = 0; q < KP / 4; q++) {
-      const float4 u = row[q];
-      acc[4 * q] = fmaf(u.x, vi, acc[4 * q]);
-      acc[4 * q + 1] = fmaf(u.y, vi, acc[4 * q + 1]);
-      acc[4 * q + 2] = fmaf(u.z, vi, acc[4 * q + 2]);
-      acc[4 * q + 3] = fmaf(u.w, vi, acc[4 * q + 3]);
+    for (int q = 0; q < KP / 8; q++) {
+      float u[8];
+      bf16x8(row[q], u);
+#pragma unroll
+      for (int t = 0; t < 8; t++) acc[8 * q + t] = fmaf(u[t], vi, acc[8 * q + t]);
     }
   }
   __shared__ double sh[KP][kCgThreads / 32];
@@ -528,7 +540,7 @@ __device__ __forceinline__ void coarse_solve_block(const double* __restrict__ pa
 // both: the second use hits L1)
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads, 2)
-    k_coarse_pre(CgVecs v, const float* __restrict__ AU, const double* __restrict__ part1,
+    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const double* __restrict__ part1,
                  const double* __restrict__ einv, int kc, double* coef, double* part2) {
   __shared__ double d[KP], cd[KP];
   __shared__ float c[KP];
@@ -548,15 +560,14 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
-      const float4* row = reinterpret_cast<const float4*>(AU + i * KP);
+      const uint4* row = reinterpret_cast<const uint4*>(AU + i * KP);
       float s = 0.f;
 #pragma unroll
-      for (int q = 0; q < KP / 4; q++) {
-        const float4 a = row[q];
-        s = fmaf(a.x, c[4 * q], s);
-        s = fmaf(a.y, c[4 * q + 1], s);
-        s = fmaf(a.z, c[4 * q + 2], s);
-        s = fmaf(a.w, c[4 * q + 3], s);
+      for (int q = 0; q < KP / 8; q++) {
+        float a[8];
+        bf16x8(row[q], a);
+#pragma unroll
+        for (int t2 = 0; t2 < 8; t2++) s = fmaf(a[t2], c[8 * q + t2], s);
       }
       t[cc] = v.r[i] - (double)s;
     }
@@ -567,14 +578,13 @@ __global__ void __launch_bounds__(kCgThreads, 2)
       const long long i = cc * n + m;
       v.z[i] = z[cc];
       const float zf = (float)z[cc];
-      const float4* row = reinterpret_cast<const float4*>(AU + i * KP);
+      const uint4* row = reinterpret_cast<const uint4*>(AU + i * KP);
 #pragma unroll
-      for (int q = 0; q < KP / 4; q++) {
-        const float4 a = __ldcg(row + q);  // again, from L2: keeps the rows out of registers
-        acc[4 * q] = fmaf(a.x, zf, acc[4 * q]);
-        acc[4 * q + 1] = fmaf(a.y, zf, acc[4 * q + 1]);
-        acc[4 * q + 2] = fmaf(a.z, zf, acc[4 * q + 2]);
-        acc[4 * q + 3] = fmaf(a.w, zf, acc[4 * q + 3]);
+      for (int q = 0; q < KP / 8; q++) {
+        float a[8];
+        bf16x8(__ldcg(row + q), a);  // again, from L2: keeps the rows out of registers
+#pragma unroll
+        for (int t2 = 0; t2 < 8; t2++) acc[8 * q + t2] = fmaf(a[t2], zf, acc[8 * q + t2]);
       }
     }
   }
@@ -598,7 +608,7 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 // r.z, r.r (and z.r_prev when flexible) into part + kCgBlocks..
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_post(CgVecs v, const float* __restrict__ U, const double* __restrict__ part2,
+    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const double* __restrict__ part2,
                   const double* __restrict__ einv, int kc, const double* __restrict__ coef,
                   int flexible) {
   __shared__ double d[KP], gd[KP];
@@ -611,15 +621,14 @@ __global__ void __launch_bounds__(kCgThreads)
 #pragma unroll 2
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
        i += (long long)gridDim.x * blockDim.x) {
-    const float4* row = reinterpret_cast<const float4*>(U + i * KP);
+    const uint4* row = reinterpret_cast<const uint4*>(U + i * KP);
     float s = 0.f;
 #pragma unroll
-    for (int q = 0; q < KP / 4; q++) {
-      const float4 u = row[q];
-      s = fmaf(u.x, w[4 * q], s);
-      s = fmaf(u.y, w[4 * q + 1], s);
-      s = fmaf(u.z, w[4 * q + 2], s);
-      s = fmaf(u.w, w[4 * q + 3], s);
+    for (int q = 0; q < KP / 8; q++) {
+      float u[8];
+      bf16x8(row[q], u);
+#pragma unroll
+      for (int t2 = 0; t2 < 8; t2++) s = fmaf(u[t2], w[8 * q + t2], s);
     }
     const double z = v.z[i] + (double)s, r = v.r[i];
     v.z[i] = z;
@@ -696,12 +705,12 @@ cudaError_t gram_launch(const double* X, const double* Y, long long ld, int m, l
   return cudaGetLastError();
 }
 
-// out[i][k] = (float) sum_j V[j][i] C[j][k] for k < kc, 0 for kc <= k < kp
+// out[i][k] = BF16(sum_j V[j][i] C[j][k]) for k < kc, 0 for kc <= k < kp
 // (C [m][kc] FP64); one block per 256 elements, C staged through shared
 // memory in chunks of rows
 __global__ void __launch_bounds__(kCgThreads)
     k_combine(const double* __restrict__ V, long long ld, int m, const double* __restrict__ C,
-              int kc, int kp, long long n, float* out) {
+              int kc, int kp, long long n, uint16_t* out) {
   constexpr int kChunk = 4096;
   __shared__ double cs[kChunk];
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -725,12 +734,12 @@ __global__ void __launch_bounds__(kCgThreads)
   if (i < n) {
 #pragma unroll
     for (int k = 0; k < kCoarseMax; k++)
-      if (k < kp) out[i * kp + k] = k < kc ? (float)acc[k] : 0.f;
+      if (k < kp) out[i * kp + k] = k < kc ? __bfloat16_as_ushort(__float2bfloat16_rn((float)acc[k])) : 0;
   }
 }
 
 cudaError_t combine_launch(const double* V, long long ld, int m, const double* C, int kc,
-                           long long n, float* out, cudaStream_t st) {
+                           long long n, uint16_t* out, cudaStream_t st) {
   if (kc < 1 || kc > kCoarseMax || m < 1) return cudaErrorInvalidValue;
   const long long blocks = (n + kCgThreads - 1) / kCgThreads;
   k_combine<<<(unsigned)blocks, kCgThreads, 0, st>>>(V, ld, m, C, kc, coarse_pad(kc), n, out);

@@ -110,7 +110,7 @@ struct sg_ctx {
   int npatch = 0, npatch_pad = 0;
   bool have_mlp = false, use_syn = false;
   bool learned_enabled = false;  // validation: a learned component beat plain PCG
-  // learned coarse space: U, AU = A U [3 npix][coarse_pad(kc)] FP32, E^-1 [kc][kc] FP64
+  // learned coarse space: U, AU = A U [3 npix][coarse_pad(kc)] BF16, E^-1 [kc][kc] FP64
   DevBuf cs_u, cs_au, cs_einv, cs_coef, cs_part;
   int coarse_k = 0;
   int learned_kind = 0;  // SG_PRECOND_LEARNED applies 1: the network, 2: the coarse space
@@ -470,8 +470,8 @@ struct sg_ctx {
   CoarseSpace coarse() const {
     CoarseSpace c{};
     c.kc = coarse_k;
-    c.u = cs_u.as<float>();
-    c.au = cs_au.as<float>();
+    c.u = cs_u.as<uint16_t>();
+    c.au = cs_au.as<uint16_t>();
     c.einv = cs_einv.as<double>();
     c.coef = cs_coef.as<double>();
     c.part = cs_part.as<double>();

@@ -254,14 +254,14 @@ cudaError_t loop_begin_launch(const LoopState* s, cudaGraphConditionalHandle ref
 cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
                             cudaGraphConditionalHandle loop, cudaStream_t st);
 
-// two-level preconditioner: coarse space U [3 npix][kp] (FP32, element-major,
+// two-level preconditioner: coarse space U [3 npix][kp] (BF16, element-major,
 // kp = coarse_pad(kc) columns, the last kp - kc zero), AU = A U, E^-1 [kc][kc]
 constexpr int kCoarseMax = 32;
 int coarse_pad(int kc);
 struct CoarseSpace {
   int kc;             // columns (1..kCoarseMax)
-  const float* u;
-  const float* au;
+  const uint16_t* u;   // BF16 bit patterns
+  const uint16_t* au;
   const double* einv;
   double* coef;       // [kCoarseMax] scratch
   double* part;       // [2][kCoarseMax][kCgBlocks] scratch
@@ -272,9 +272,9 @@ cudaError_t coarse_apply(const CgVecs& v, const CoarseSpace& cs, int flexible, c
 // part [nsplit][m][m]: split-K partial Gram matrices X Y^T of FP64 rows [m][ld] over n
 cudaError_t gram_launch(const double* X, const double* Y, long long ld, int m, long long n,
                         int nsplit, double* part, cudaStream_t st);
-// out [n][coarse_pad(kc)] (FP32, element-major) = (C^T V)^T, V [m][ld] FP64, C [m][kc] FP64
+// out [n][coarse_pad(kc)] (BF16, element-major) = (C^T V)^T, V [m][ld] FP64, C [m][kc] FP64
 cudaError_t combine_launch(const double* V, long long ld, int m, const double* C, int kc,
-                           long long n, float* out, cudaStream_t st);
+                           long long n, uint16_t* out, cudaStream_t st);
 
 // ---- tensor-core BF16 GEMM (sg_gemm.cu) -----------------------------------------
 // C[M x N] (FP32, row-major, ldc = N) = A[M x K] . B[N x K]^T (+ C if beta);

@@ -573,7 +573,7 @@ namespace sg {
 // The coarse space from the first m stored residuals: V = M_bj3 r_j (the
 // solver's own preconditioned residuals, which span the Krylov spaces of the
 // training solves), W = A V, H = V^T W, G = V^T R (= V^T M^-1 V), then
-// sg_coarse_from_gram; U = V C and A U = W C are kept in FP32.
+// sg_coarse_from_gram; U = V C and A U = W C are kept in BF16.
 int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
   const long long n3 = 3 * c->npix;
   if (m < 2) return SG_OK;
@@ -609,17 +609,17 @@ int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
   e = dC.alloc((size_t)m * k * 8);
   if (e == cudaSuccess) e = cudaMemcpy(dC.p, C.data(), (size_t)m * k * 8, cudaMemcpyHostToDevice);
   const int kp = coarse_pad(k);
-  if (e == cudaSuccess) e = c->cs_u.alloc((size_t)kp * n3 * 4);
-  if (e == cudaSuccess) e = c->cs_au.alloc((size_t)kp * n3 * 4);
+  if (e == cudaSuccess) e = c->cs_u.alloc((size_t)kp * n3 * 2);
+  if (e == cudaSuccess) e = c->cs_au.alloc((size_t)kp * n3 * 2);
   if (e == cudaSuccess) e = c->cs_einv.alloc((size_t)k * k * 8);
   if (e == cudaSuccess) e = c->cs_coef.alloc(kCoarseMax * 8);
   if (e == cudaSuccess) e = c->cs_part.alloc((size_t)2 * kCoarseMax * kCgBlocks * 8);
   if (e == cudaSuccess)
     e = cudaMemcpy(c->cs_einv.p, einv.data(), (size_t)k * k * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = combine_launch(V.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_u.as<float>(), c->st);
+    e = combine_launch(V.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_u.as<uint16_t>(), c->st);
   if (e == cudaSuccess)
-    e = combine_launch(W.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_au.as<float>(), c->st);
+    e = combine_launch(W.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_au.as<uint16_t>(), c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   c->launches += 2;
   if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space vectors");
