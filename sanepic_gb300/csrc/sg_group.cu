@@ -67,21 +67,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// ys [G nsd][4] = (S0, S1, S2, 0) per group sample, the layout k_pt reads
-template <typename T>
-__global__ void __launch_bounds__(256)
-    k_group_interleave(const T* __restrict__ gtl, long long ng, long long nsd, T* __restrict__ ys) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long g = i / nsd, w = i - g * nsd;
-    const T* s = gtl + 3 * g * nsd + w;
-    ys[4 * i] = s[0];
-    ys[4 * i + 1] = s[nsd];
-    ys[4 * i + 2] = s[2 * nsd];
-    ys[4 * i + 3] = T(0);
-  }
-}
-
 // hmix [G][slot][6] = sum over the group's detectors of h_d[k] (1, c, s, cc, cs, ss),
 // k = kslot[slot] (spectra are kept in the filter's slot order)
 template <typename T>
@@ -109,75 +94,69 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// FP32 sums with Neumaier compensation (FP64: plain sums)
-template <typename T>
-struct CSum {
-  T s = T(0), c = T(0);
-  __device__ __forceinline__ void add(T v) {
-    if constexpr (sizeof(T) == 4) {
-      const T t = s + v;
-      c += (fabsf(s) >= fabsf(v)) ? (s - t) + v : (v - t) + s;
-      s = t;
-    } else {
-      s += v;
-    }
-  }
-  __device__ __forceinline__ T get() const { return s + c; }
-};
-
 // right-hand side of a group from its detectors' data spectra X_d [ndet][nseg][M+1]
 // (slot order; filt holds the filter rows in the same order):
 // gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c_d, s_d), detectors in list order;
-// chi2_part[block] = sum of h_d |X_d|^2 over the block's bins (k = 0..M)
+// chi2_part[block] = sum of h_d |X_d|^2 over the block's bins (k = 0..M).
+// A thread takes four consecutive slots, so a warp reads 1 KB of every
+// detector's spectrum at once (the detectors' spectra lie 25 MB apart).
+// Plain FP32 sums over the group's detectors in a fixed order (a
+// compensated sum made the kernel issue-bound; with tens of terms of
+// similar size the plain sum keeps ~1e-6 of the largest term).
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_group_rhs(const cplx<T>* __restrict__ dspec, const T* __restrict__ filt,
                 const T* __restrict__ dcs, const int* __restrict__ grp_off,
                 const int* __restrict__ grp_det, long long G, long long nseg, long long M1,
                 cplx<T>* __restrict__ gspec, double* chi2_part) {
-  const long long n = G * nseg * M1;
+  constexpr int KV = 4;
+  const long long nq = (M1 + KV - 1) / KV;  // slot quads per (group, segment)
+  const long long n = G * nseg * nq;
   double chi = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const long long k = i % M1, gs = i / M1;
+    const long long k0 = (i % nq) * KV, gs = i / nq;
     const long long seg = gs % nseg, g = gs / nseg;
-    CSum<T> a[6];
-    T cl = T(0);
-    auto acc = [&](cplx<T> x, T h, T c, T s) {
-      const T hx = h * x.x, hy = h * x.y;
-      a[0].add(hx);
-      a[1].add(hy);
-      a[2].add(c * hx);
-      a[3].add(c * hy);
-      a[4].add(s * hx);
-      a[5].add(s * hy);
-      cl += h * (x.x * x.x + x.y * x.y);
-    };
-    const int e1 = grp_off[g + 1];
-    int e = grp_off[g];
-    for (; e + 4 <= e1; e += 4) {  // four detectors' loads in flight, same order
-      cplx<T> x[4];
-      T h[4], c[4], s[4];
+    const int kn = (int)(M1 - k0 < KV ? M1 - k0 : KV);
+    T a[KV][6];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int d = grp_det[e + u];
-        x[u] = dspec[((long long)d * nseg + seg) * M1 + k];
-        h[u] = filt[d * M1 + k];
-        c[u] = dcs[2 * d];
-        s[u] = dcs[2 * d + 1];
+    for (int u = 0; u < KV; u++)
+#pragma unroll
+      for (int q = 0; q < 6; q++) a[u][q] = T(0);
+    T cl = T(0);
+    for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
+      const int d = grp_det[e];
+      const cplx<T>* x = dspec + ((long long)d * nseg + seg) * M1 + k0;
+      const T* h = filt + d * M1 + k0;
+      const T c = dcs[2 * d], s = dcs[2 * d + 1];
+      cplx<T> xv[KV];
+      T hv[KV];
+#pragma unroll
+      for (int u = 0; u < KV; u++) {
+        xv[u] = u < kn ? x[u] : cplx<T>{T(0), T(0)};
+        hv[u] = u < kn ? h[u] : T(0);
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++) acc(x[u], h[u], c[u], s[u]);
-    }
-    for (; e < e1; e++) {
-      const int d = grp_det[e];
-      acc(dspec[((long long)d * nseg + seg) * M1 + k], filt[d * M1 + k], dcs[2 * d], dcs[2 * d + 1]);
+      for (int u = 0; u < KV; u++) {
+        const T hx = hv[u] * xv[u].x, hy = hv[u] * xv[u].y;
+        a[u][0] += hx;
+        a[u][1] += hy;
+        a[u][2] = fma(c, hx, a[u][2]);
+        a[u][3] = fma(c, hy, a[u][3]);
+        a[u][4] = fma(s, hx, a[u][4]);
+        a[u][5] = fma(s, hy, a[u][5]);
+        cl = fma(hx, xv[u].x, fma(hy, xv[u].y, cl));
+      }
     }
     chi += (double)cl;
-    cplx<T>* o = gspec + ((g * 3) * nseg + seg) * M1 + k;
-    o[0] = cplx<T>{a[0].get(), a[1].get()};
-    o[nseg * M1] = cplx<T>{a[2].get(), a[3].get()};
-    o[2 * nseg * M1] = cplx<T>{a[4].get(), a[5].get()};
+    cplx<T>* o = gspec + ((g * 3) * nseg + seg) * M1 + k0;
+#pragma unroll
+    for (int u = 0; u < KV; u++) {
+      if (u >= kn) break;
+      o[u] = cplx<T>{a[u][0], a[u][1]};
+      o[nseg * M1 + u] = cplx<T>{a[u][2], a[u][3]};
+      o[2 * nseg * M1 + u] = cplx<T>{a[u][4], a[u][5]};
+    }
   }
   __shared__ double red[8];
   for (int o = 16; o > 0; o >>= 1) chi += __shfl_xor_sync(0xffffffffu, chi, o);
@@ -209,12 +188,6 @@ template <typename T>
 cudaError_t group_mix_launch(cplx<T>* spec, const T* hmix, long long G, long long nseg,
                              long long M1, cudaStream_t st) {
   k_group_mix<T><<<blocks_for(G * nseg * M1), 256, 0, st>>>(spec, hmix, G, nseg, M1);
-  return cudaGetLastError();
-}
-template <typename T>
-cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T* ys,
-                                    cudaStream_t st) {
-  k_group_interleave<T><<<blocks_for(ng), 256, 0, st>>>(gtl, ng, nsd, ys);
   return cudaGetLastError();
 }
 template <typename T>
@@ -251,8 +224,6 @@ cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, l
                                                long long, T*, cudaStream_t);                     \
   template cudaError_t group_mix_launch<T>(cplx<T>*, const T*, long long, long long, long long,  \
                                            cudaStream_t);                                        \
-  template cudaError_t group_interleave_launch<T>(const T*, long long, long long, T*,            \
-                                                  cudaStream_t);                                 \
   template cudaError_t group_hmix_launch<T>(const T*, const T*, const int*, const int*,          \
                                             const int*, long long, long long, T*, cudaStream_t); \
   template cudaError_t permute_rows_launch<T>(const T*, const int*, long long, long long, T*,    \

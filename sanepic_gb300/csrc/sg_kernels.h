@@ -163,10 +163,6 @@ cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, lo
 template <typename T>
 cudaError_t group_mix_launch(cplx<T>* spec, const T* hmix, long long G, long long nseg,
                              long long M1, cudaStream_t st);
-// ys [G nsd][4] = (S0, S1, S2, 0) from gtl
-template <typename T>
-cudaError_t group_interleave_launch(const T* gtl, long long ng, long long nsd, T* ys,
-                                    cudaStream_t st);
 // right-hand side spectra of each group from the detectors' data spectra
 // dspec [ndet][nseg][M+1] (slot order, filt rows in slot order too):
 // gspec (S0, S1, S2)^ = sum_d h_d X_d (1, c, s);
