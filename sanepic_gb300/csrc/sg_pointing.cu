@@ -76,6 +76,45 @@ __global__ void k_pointing(PointingArgs a) {
     const double thetap = SG_D2PI / 4.0 - a.dec[w];
     const double phip = a.ra[w];
     const double psip_b = a.psi[w];
+    if (x == 0.0 && y == 0.0) {
+      // Zero offset: theta_ = phi_ = 0 exactly, so every term carrying
+      // sin(theta_) is a signed zero and adding it leaves the others
+      // unchanged; what remains is the same operations on the same values:
+      // theta_o = acos(cos thetap), phi_o = phip (atan2 of a signed zero over
+      // sin thetap > 0), dr = (-cos thetap cos psi, -sin psi, sin thetap cos psi),
+      // eph = (-0, 1, 0), so aaa = dr[1].  Poles and NaN angles take the
+      // general path below.
+      const double st = sin(thetap);
+      if (st > 0.0 && psip_b == psip_b) {
+        const double ct = cos(thetap), cp = cos(psip_b), sp = sin(psip_b);
+        const double theta_o = acos(ct);
+        const double phi_o = phip;
+        const double dr0 = (-ct) * cp, dr1 = -sp, dr2 = st * cp;
+        const double rrr = ((0.0 + dr0 * dr0) + dr1 * dr1) + dr2 * dr2;
+        double aaa = dr1 / sqrt(rrr);
+        if (aaa > 1.0) aaa = 1.0;
+        if (aaa < -1.0) aaa = -1.0;
+        double psitmp = acos(aaa);
+        if (dr2 < 0) psitmp = -psitmp;
+        const double psi_o =
+            (fmod(psitmp + SG_D2PI / 4.0 + 2.0 * SG_D2PI, SG_D2PI)) - SG_D2PI / 2.0;
+        const double theta = SG_D2PI / 4.0 - (SG_D2PI / 4.0 - theta_o);
+        const double phi = fmod(phi_o + SG_D2PI, SG_D2PI);
+        int pix;
+        if (theta != theta || phi != phi) {
+          pix = -1;
+        } else if (theta < 0. || theta > 3.14159265358979323846) {
+          pix = -2;
+          atomicExch(a.error_flag, 1);
+        } else {
+          pix = ang2pix_ring_dev(a.nside, theta, phi);
+          if (pix < 0 || pix > 12 * (int)a.nside * (int)a.nside - 1) pix = -1;
+        }
+        a.ring_pix[e] = pix;
+        a.psio[e] = psi_o;
+        continue;
+      }
+    }
     const double theta_ = asin(sqrt(x * x + y * y));
     const double phi_ = atan2(y, x);
     const double theta_o = acos(sin(thetap) * sin(theta_) * cos(phi_ + psip_b) +
