@@ -11,7 +11,8 @@
 //
 // sg_autotune times the noise filter of a context with each compiled tile
 // shape for its segment length (FP32: 8192 or 4096 complex points per CTA of
-// the cluster) on the context's own timeline and keeps the faster one.
+// the cluster) on the context's own timeline, or with the offset-group
+// operator one whole operator application, and keeps the faster one.
 #include <cuda_runtime.h>
 
 #include <cstdlib>
@@ -25,6 +26,9 @@
 
 extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
   if (!c) return SG_ERR_ARG;
+  if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
+  for (long long dd = 0; dd < c->ndet; dd++)
+    if (!c->have_noise[dd]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", dd);
   cudaSetDevice(c->desc.device);
   const long long M = c->ns / 2;
   std::vector<int> cand;
@@ -46,9 +50,15 @@ extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
     c->S = S;
     c->nclusters = c->f32 ? filter_max_clusters<float>(c->logm, S)
                           : filter_max_clusters<double>(c->logm, S);
+    // the offset-group operator runs the spectrum-split filter on its group
+    // tiles: time one whole operator application (its slot order follows S)
+    if (c->group_mode) e = c->ensure_hmix();
     for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {  // first launch warms up
       if (rep == 1) e = cudaEventRecord(a, c->st);
-      if (e == cudaSuccess) e = c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+      if (e != cudaSuccess) break;
+      e = c->group_mode
+              ? c->apply_dev(c->x.as<double>(), c->q.as<double>(), true)
+              : c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(b, c->st);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
@@ -68,6 +78,7 @@ extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
     e = c->chi2p.alloc(sizeof(double) * c->S * c->nclusters);
     c->drop_graphs();  // captured iterations hold the old launch shape
   }
+  if (e == cudaSuccess && c->group_mode) e = c->ensure_hmix();  // slot order of the chosen S
   if (e != cudaSuccess) return c->cuda_fail(e, "autotune");
   if (cluster_size) *cluster_size = c->S;
   if (ms) *ms = best;
