@@ -377,7 +377,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(sumcross_launch(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), psio.as<double>(),
                          nsd, gsc.as<double>(), gss.as<double>(), npix, c->sumcross.as<double>(),
                          c->st));
-  SG_TRY(c->ys.alloc((size_t)4 * ng * c->esize));
+  SG_TRY(c->ys.alloc((size_t)3 * ng * c->esize));  // [ng / 8][3][8]
   // the offset-group operator when every group is large enough (three
   // timelines per group instead of one per detector); SANEPIC_GPU_GROUP_FILTER=0
   // keeps the per-detector operator

@@ -231,7 +231,15 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
                     ((reinterpret_cast<uintptr_t>(p.tod) | reinterpret_cast<uintptr_t>(p.sub) |
                       reinterpret_cast<uintptr_t>(p.out)) & 15) == 0;
   double chi2 = 0.0;  // sum of h[k] |X[k]|^2 over this thread's bins
-  for (long long tile = cluster_id; tile < p.ntiles; tile += nclusters) {
+  for (long long L = cluster_id; L < p.ntiles; L += nclusters) {
+    // the inverse into P^T's layout visits the three components of a group
+    // segment side by side (L = (group * nseg + segment) * 3 + component), so
+    // that their stores into the same 96-byte blocks meet in L2
+    long long tile = L;
+    if (MODE == kSpecIn && p.ilv3) {
+      const long long q = L % (3LL * p.nseg);
+      tile = (L - q) + (q % 3) * p.nseg + q / 3;
+    }
     const long long base = tile * (long long)(2 * M);
     const int det = (int)(tile / p.nseg);
     const T* h = p.filt + (long long)det * (M + 1);
@@ -587,20 +595,19 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
     __syncthreads();
     // ---- 11. store -------------------------------------------------------------
     if (MODE == kSpecIn && p.ilv3) {
-      // component (tile / nseg) % 3 of the interleaved [group sample][4]
-      // layout P^T reads: tile = (group * 3 + component) * nseg + segment
+      // component (tile / nseg) % 3 of the [group sample / 8][3][8] layout P^T
+      // reads, tile = (group * 3 + component) * nseg + segment: a sample pair
+      // is 8 contiguous bytes (FP32), four lanes fill one 32-byte sector
       const long long nst = p.nseg;
       const long long grp = tile / (3 * nst), comp = (tile / nst) % 3, seg = tile % nst;
-      T* dst = p.out + 4 * (grp * nst + seg) * (2LL * M) + comp;
+      T* dst = p.out + 3 * (grp * nst + seg) * (2LL * M) + 8 * comp;
 #pragma unroll 16
       for (int it = 0; it < G::XE; it++) {
         const int e = it * NT + tid;
         if (E % NT != 0 && e >= E) break;
         const int c = e % Cs, n1 = e / Cs;
-        const long long n = 2LL * (C * n1 + j * Cs + c);
-        const cplx<T> v = buf[n1 * PA + c];
-        dst[4 * n] = v.x;
-        dst[4 * n + 4] = v.y;
+        const long long n = 2LL * (C * n1 + j * Cs + c);  // even: the pair stays in its block
+        *reinterpret_cast<cplx<T>*>(dst + 24 * (n >> 3) + (n & 7)) = buf[n1 * PA + c];
       }
     } else if (kVec) {
 #pragma unroll 8

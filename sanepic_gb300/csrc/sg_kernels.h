@@ -28,7 +28,7 @@ struct FilterArgs {
   T* out;            // [ntiles][ns]
   cplx<T>* spec_out;       // if set: forward FFT only, X[k] (k = 0..M) [ntiles][M+1]
   const cplx<T>* spec_in;  // if set: inverse FFT only of Y[k] [ntiles][M+1]
-  int ilv3;                // with spec_in: out is [groups][nseg * ns][4], tile = (group * 3 + component) * nseg + segment
+  int ilv3;                // with spec_in: out is [groups][nseg * ns / 8][3][8], tile = (group * 3 + component) * nseg + segment
   const cplx<T>* tw_lo;
   const cplx<T>* tw_hi;
   cplx<T> wn1;

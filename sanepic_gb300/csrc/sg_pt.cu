@@ -11,9 +11,13 @@
 // pixel m
 //   q_I[m] = sum y_i,  q_Q[m] = sum cos(2psi_i) y_i,  q_U[m] = sum sin(2psi_i) y_i
 // over the samples i that hit m.  Detectors that share a pixel stream (an
-// offset group) are first summed per group sample (k_detsum), so P^T walks
-// the group samples, read through the pixel-sorted index (CSR built once at
-// setup; the pointing never changes).  A team of L lanes per pixel (L from
+// offset group) are first summed per group sample (k_detsum, or the group
+// operator's inverse FFTs), so P^T walks the group samples, read through the
+// pixel-sorted index (CSR built once at setup; the pointing never changes).
+// The sums (S0, S1, S2) are stored in blocks of 8 group samples,
+// [i / 8][3][8]: a writer that produces one component for consecutive
+// samples fills whole 32-byte sectors, and P^T's gathers of neighbouring
+// samples share them.  A team of L lanes per pixel (L from
 // the mean samples per pixel: about four per lane) strides through its
 // samples in a fixed order (several independent gathers in flight per lane)
 // and combines its lanes with a fixed xor tree, so the result is bitwise
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(256) k_detsum_f32(const float4* __restrict__ y
                                                     const int* __restrict__ grp_off,
                                                     const int* __restrict__ grp_det,
                                                     const float2* __restrict__ dcs,
-                                                    float4* __restrict__ ys) {
+                                                    float* __restrict__ ys) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
        i += (long long)gridDim.x * blockDim.x) {
     const int g = (int)(i / nsd4);
@@ -204,10 +208,14 @@ __global__ void __launch_bounds__(256) k_detsum_f32(const float4* __restrict__ y
         ff_add_f(sb[q], r.y * vv[q]);
       }
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      ys[4 * i + q] = make_float4(s0[q].hi + s0[q].lo, sa[q].hi + sa[q].lo, sb[q].hi + sb[q].lo,
-                                  0.f);
+    // samples 4i..4i+3: half of one 8-sample block of the [block][3][8] layout
+    float* blk = ys + (i >> 1) * 24 + (i & 1) * 4;
+    *reinterpret_cast<float4*>(blk) = make_float4(s0[0].hi + s0[0].lo, s0[1].hi + s0[1].lo,
+                                                  s0[2].hi + s0[2].lo, s0[3].hi + s0[3].lo);
+    *reinterpret_cast<float4*>(blk + 8) = make_float4(sa[0].hi + sa[0].lo, sa[1].hi + sa[1].lo,
+                                                      sa[2].hi + sa[2].lo, sa[3].hi + sa[3].lo);
+    *reinterpret_cast<float4*>(blk + 16) = make_float4(sb[0].hi + sb[0].lo, sb[1].hi + sb[1].lo,
+                                                       sb[2].hi + sb[2].lo, sb[3].hi + sb[3].lo);
   }
 }
 
@@ -229,10 +237,10 @@ __global__ void __launch_bounds__(256) k_detsum_f64(const double* __restrict__ y
       sa += dcs[d].x * v;
       sb += dcs[d].y * v;
     }
-    ys[4 * i] = s0;
-    ys[4 * i + 1] = sa;
-    ys[4 * i + 2] = sb;
-    ys[4 * i + 3] = 0.0;
+    double* blk = ys + (i >> 3) * 24 + (i & 7);
+    blk[0] = s0;
+    blk[8] = sa;
+    blk[16] = sb;
   }
 }
 
@@ -245,8 +253,7 @@ cudaError_t detsum_launch<float>(const float* y, long long n, long long nsd, con
   if (blocks > 152LL * 16) blocks = 152LL * 16;
   k_detsum_f32<<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<const float4*>(y), n4, nsd / 4,
                                                  grp_off, grp_det,
-                                                 reinterpret_cast<const float2*>(dcs),
-                                                 reinterpret_cast<float4*>(ys));
+                                                 reinterpret_cast<const float2*>(dcs), ys);
   return cudaGetLastError();
 }
 
@@ -264,6 +271,12 @@ cudaError_t detsum_launch<double>(const double* y, long long n, long long nsd,
 // ---- P^T --------------------------------------------------------------------------
 constexpr int kPtUnroll = 4;
 
+// (S0, S1, S2) of group sample i in the [i / 8][3][8] layout
+__device__ __forceinline__ float3 ys_at(const float* __restrict__ ys, uint32_t i) {
+  const float* b = ys + (size_t)(i >> 3) * 24 + (i & 7);
+  return make_float3(__ldg(b), __ldg(b + 8), __ldg(b + 16));
+}
+
 // L lanes per pixel (a team; 256 / L pixels per block, consecutive): the
 // lanes stride through the pixel's samples in a fixed order, four gathers in
 // flight each, and the team combines its lanes with a fixed xor tree.  L is
@@ -274,7 +287,7 @@ template <int L>
 __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ off,
                                                 const uint32_t* __restrict__ idx,
                                                 const float2* __restrict__ ccs,
-                                                const float4* __restrict__ ys, long long npix,
+                                                const float* __restrict__ ys, long long npix,
                                                 const int* __restrict__ hits,
                                                 double* __restrict__ q) {
   constexpr int T = 256 / L;  // pixels per block
@@ -288,13 +301,13 @@ __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ of
     long long j = off[m] + lane;
     for (; j + L * (kPtUnroll - 1) < jend; j += L * kPtUnroll) {
       uint32_t ii[kPtUnroll];
-      float4 v[kPtUnroll];
+      float3 v[kPtUnroll];
       float2 wv[kPtUnroll];
 #pragma unroll
       for (int u = 0; u < kPtUnroll; u++) ii[u] = __ldcs(idx + j + L * u);
 #pragma unroll
       for (int u = 0; u < kPtUnroll; u++) {
-        v[u] = __ldg(ys + ii[u]);
+        v[u] = ys_at(ys, ii[u]);
         wv[u] = __ldcs(ccs + j + L * u);
       }
 #pragma unroll
@@ -305,7 +318,7 @@ __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ of
       }
     }
     for (; j < jend; j += L) {
-      const float4 v = __ldg(ys + __ldcs(idx + j));
+      const float3 v = ys_at(ys, __ldcs(idx + j));
       const float2 wv = __ldcs(ccs + j);
       ff_add_f(a0, v.x);
       ff_add_f(a1, wv.x * v.y - wv.y * v.z);
@@ -357,11 +370,12 @@ __global__ void __launch_bounds__(256) k_pt_f64(const long long* off, const uint
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     const long long j1 = off[m + 1];
     for (long long j = off[m] + lane; j < j1; j += 32) {
-      const double* v = ys + 4 * (long long)idx[j];
+      const uint32_t i = idx[j];
+      const double* v = ys + (size_t)(i >> 3) * 24 + (i & 7);
       const double2 w = ccs[j];
       a0 += v[0];
-      a1 += w.x * v[1] - w.y * v[2];
-      a2 += w.y * v[1] + w.x * v[2];
+      a1 += w.x * v[8] - w.y * v[16];
+      a2 += w.y * v[8] + w.x * v[16];
     }
     for (int o = 16; o > 0; o >>= 1) {
       a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -384,8 +398,7 @@ static void pt_f32_launch(const long long* csr_off, const uint32_t* csr_idx, con
   const long long blocks = (npix + 256 / L - 1) / (256 / L);
   k_pt_f32<L><<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx,
                                                 reinterpret_cast<const float2*>(csr_cs),
-                                                reinterpret_cast<const float4*>(ys), npix,
-                                                hits_true, q);
+                                                ys, npix, hits_true, q);
 }
 
 template <>
