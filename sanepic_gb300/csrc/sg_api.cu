@@ -879,17 +879,24 @@ extern "C" int sg_get_map(sg_ctx* c, int kind, double* out) {
   if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
   cudaSetDevice(c->desc.device);
   const long long npix = c->npix;
-  std::vector<double> v(3 * npix);
+  std::vector<double> v;
+  if (kind < SG_MAP_I || kind > SG_MAP_U) v.resize(3 * npix);
   cudaError_t e = cudaSuccess;
   const double* blk = nullptr;
   switch (kind) {
     case SG_MAP_I:
     case SG_MAP_Q:
-    case SG_MAP_U:
+    case SG_MAP_U: {
+      // only the requested component, through page-locked memory
       if (!c->have_solution) return c->fail(SG_ERR_STATE, "no solution yet");
-      e = cudaMemcpy(v.data(), c->x.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost);
-      blk = v.data() + (kind - SG_MAP_I) * npix;
+      e = c->map_stage.reserve(sizeof(double) * npix);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->map_stage.p, c->x.as<double>() + (kind - SG_MAP_I) * npix,
+                            sizeof(double) * npix, cudaMemcpyDeviceToHost, c->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+      blk = static_cast<const double*>(c->map_stage.p);
       break;
+    }
     case SG_MAP_NVAR:
     case SG_MAP_Q_NVAR:
     case SG_MAP_U_NVAR: {

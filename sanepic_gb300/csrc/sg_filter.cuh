@@ -125,7 +125,13 @@ struct Geo {
   static constexpr int Cs = C / S, Rs = R / S;   // columns / rows per CTA
   static constexpr int PA = Cs + 1, PC = Rs + 1; // padded strides
   static constexpr int E = M / S;                // complex points per CTA
-  static constexpr int BUF = (R * PA > C * PC) ? R * PA : C * PC;
+  // column-pass (A) layout: element (row, column) at row PA + row / 16 +
+  // column.  The extra element per 16 rows spreads the transpose back from the
+  // row passes, whose lanes write rows k1 -> R2 (k1 % R1) + k1 / R1 (16 apart
+  // for consecutive k1), over all bank pairs.
+  static __device__ __forceinline__ int pa(int row, int c) { return row * PA + (row >> 4) + c; }
+  static constexpr int ABUF = R * PA + R / 16;
+  static constexpr int BUF = (ABUF > C * PC) ? ABUF : C * PC;
   static constexpr int XE = (E + kFilterThreads - 1) / kFilterThreads;  // per thread
   // shared twiddle tables: lo, hi, W_R, W_C, W_N^{R C1 i} (i < C2)
   static constexpr int TWN = kTwLo + M / kTwLo + R + C + C2;
@@ -198,7 +204,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
     k_noise_filter(FilterArgs<T> p) {
   using G = Geo<LOGR, LOGC, S>;
   constexpr int R = G::R, C = G::C, M = G::M, R1 = G::R1, R2 = G::R2, C1 = G::C1, C2 = G::C2;
-  constexpr int Cs = G::Cs, Rs = G::Rs, PA = G::PA, PC = G::PC, E = G::E;
+  constexpr int Cs = G::Cs, Rs = G::Rs, PC = G::PC, E = G::E;
   constexpr int NT = kFilterThreads;
   constexpr bool PAIR = sizeof(T) == 4;
   cg::cluster_group cl = cg::this_cluster();
@@ -265,8 +271,8 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
           v.z -= w.z;
           v.w -= w.w;
         }
-        buf[n1 * PA + c] = cplx<T>{(T)v.x, (T)v.y};
-        buf[n1 * PA + c + 1] = cplx<T>{(T)v.z, (T)v.w};
+        buf[G::pa(n1, c)] = cplx<T>{(T)v.x, (T)v.y};
+        buf[G::pa(n1, c + 1)] = cplx<T>{(T)v.z, (T)v.w};
       }
     } else
 #pragma unroll 16
@@ -285,7 +291,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         v.x = (s0 == base) ? T(1) : T(0);
         v.y = T(0);
       }
-      buf[n1 * PA + c] = v;
+      buf[G::pa(n1, c)] = v;
     }
     __syncthreads();
     // ---- 2. forward column pass 1: DFT_R1 over n1, twiddle W_R^{n2 k} ------
@@ -294,13 +300,13 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         [&](int u, auto& a) {
           const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-          for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
+          for (int i = 0; i < R1; i++) a[i] = buf[G::pa(R2 * i + n2, c)];
         },
         [&](int u, auto& a) {
           const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
           for (int k = 0; k < R1; k++)
-            buf[(R2 * k + n2) * PA + c] =
+            buf[G::pa(R2 * k + n2, c)] =
                 (k == 0 || n2 == 0) ? a[k] : cmul(a[k], twr[(n2 * k) & (R - 1)]);
         });
     __syncthreads();
@@ -310,14 +316,14 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         [&](int u, auto& b) {
           const int c = u % Cs, ka = u / Cs;
 #pragma unroll
-          for (int i = 0; i < R2; i++) b[i] = buf[(R2 * ka + i) * PA + c];
+          for (int i = 0; i < R2; i++) b[i] = buf[G::pa(R2 * ka + i, c)];
         },
         [&](int u, auto& b) {
           const int c = u % Cs, ka = u / Cs;
           const int n2g = j * Cs + c;
 #pragma unroll
           for (int kb = 0; kb < R2; kb++)
-            buf[(R2 * ka + kb) * PA + c] = cmul(b[kb], tw((n2g * (ka + R1 * kb)) & (M - 1)));
+            buf[G::pa(R2 * ka + kb, c)] = cmul(b[kb], tw((n2g * (ka + R1 * kb)) & (M - 1)));
         });
     cluster_arrive();
     cluster_wait();
@@ -331,7 +337,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         const int c = e % Cs, r = e / Cs, q = r % S, t = r / S;
         const int k1 = row_of<R>(j * Rs + t);
         const int posr = R2 * (k1 % R1) + k1 / R1;
-        v[it] = ld_cluster(cluster_map(buf + posr * PA + c, q), (cplx<T>*)nullptr);
+        v[it] = ld_cluster(cluster_map(buf + G::pa(posr, c), q), (cplx<T>*)nullptr);
       }
       cluster_arrive();
       cluster_wait();
@@ -361,6 +367,19 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         });
     __syncthreads();
     }  // MODE != kSpecIn
+    if constexpr (MODE == kSpecIn) {
+      // stage this CTA's spectrum slots, coalesced: slot ((i C1 + ka) S + j)
+      // Rs + t (a run of Rs per (i, ka)) goes where unit (t, ka) keeps its
+      // element i, (C2 ka + i) PC + t
+#pragma unroll 16
+      for (int it = 0; it < G::XE; it++) {
+        const int e = it * NT + tid;
+        if (E % NT != 0 && e >= E) break;
+        const int t = e % Rs, r = e / Rs;  // r = i C1 + ka
+        buf[(C2 * (r % C1) + r / C1) * PC + t] = Yin[((long long)r * S + j) * Rs + t];
+      }
+      __syncthreads();
+    }
     // ---- 6. forward row pass 2 + spectrum + inverse row pass 1, in registers --
     // unit (t, ka): lanes l < 16 take ka = q, lanes l >= 16 take C1-1-q, so
     // the partner unit (t^1, C1-1-ka) is lane l^17 (row R/2: (t, C1-1-ka),
@@ -374,25 +393,27 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         const int q = g / TB;
         const int ka = (l < 16) ? q : C1 - 1 - q;
         const int k1 = row_of<R>(j * Rs + t);
-        if constexpr (MODE == kSpecIn) {  // re-pack the stored spectrum (no lane exchange)
-          if (j == 0 && t == 0) continue;  // row 0: below
+        if constexpr (MODE == kSpecIn) {
+          // re-pack the staged spectrum: own slots from shared memory, the
+          // partner's (frequencies M - k) by lane exchange
+          cplx<T> y[C2];
+#pragma unroll
+          for (int i = 0; i < C2; i++) y[i] = buf[(C2 * ka + i) * PC + t];
+          const int src = (j == 0 && t == 1) ? (l ^ 16) : (l ^ 17);
           const int kb0 = k1 + R * ka;
           cplx<T> wb = tw(kb0 >> 1);
           if (kb0 & 1) wb = cmul(wb, wn1);
           cplx<T> zo[C2];
 #pragma unroll
           for (int i = 0; i < C2; i++) {
+            const cplx<T> yp{shfl(y[C2 - 1 - i].x, src), shfl(y[C2 - 1 - i].y, src)};
             const int k = kb0 + R * C1 * i;
             const bool lo = k <= M - k;
             const cplx<T> wk = cmul(wb, twd[i]);
             const cplx<T> ws = lo ? wk : cplx<T>{-wk.x, wk.y};
-            // own slot, and the slot of frequency M - k: element C2-1-i of the
-            // partner unit (row t^1, or row R/2 itself; column C1-1-ka)
-            const int tp = (j == 0 && t == 1) ? t : (t ^ 1);
-            const cplx<T> yo = Yin[((i * C1 + ka) * S + j) * Rs + t];
-            const cplx<T> yp = Yin[(((C2 - 1 - i) * C1 + (C1 - 1 - ka)) * S + j) * Rs + tp];
-            zo[i] = repack(lo ? yo : yp, lo ? yp : yo, ws, lo);
+            zo[i] = repack(lo ? y[i] : yp, lo ? yp : y[i], ws, lo);
           }
+          if (j == 0 && t == 0) continue;  // row 0: below (its lanes only lent values)
           SgDft<C2, true, T>::run(zo);
 #pragma unroll
           for (int n2 = 0; n2 < C2; n2++)
@@ -559,7 +580,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         const int t = e % Rs, r = e / Rs, c = r % Cs, q = r / Cs;
         const int k1 = row_of<R>(q * Rs + t);
         const int posr = R2 * (k1 % R1) + k1 / R1;
-        buf[posr * PA + c] = v[it];
+        buf[G::pa(posr, c)] = v[it];
       }
     }
     __syncthreads();
@@ -569,13 +590,13 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         [&](int u, auto& b) {
           const int c = u % Cs, a1 = u / Cs;
 #pragma unroll
-          for (int i = 0; i < R2; i++) b[i] = buf[(R2 * a1 + i) * PA + c];
+          for (int i = 0; i < R2; i++) b[i] = buf[G::pa(R2 * a1 + i, c)];
         },
         [&](int u, auto& b) {
           const int c = u % Cs, a1 = u / Cs;
 #pragma unroll
           for (int n2 = 0; n2 < R2; n2++)
-            buf[(R2 * a1 + n2) * PA + c] =
+            buf[G::pa(R2 * a1 + n2, c)] =
                 (a1 == 0 || n2 == 0) ? b[n2] : cmulc(b[n2], twr[(n2 * a1) & (R - 1)]);
         });
     __syncthreads();
@@ -585,12 +606,12 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         [&](int u, auto& a) {
           const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-          for (int i = 0; i < R1; i++) a[i] = buf[(R2 * i + n2) * PA + c];
+          for (int i = 0; i < R1; i++) a[i] = buf[G::pa(R2 * i + n2, c)];
         },
         [&](int u, auto& a) {
           const int c = u % Cs, n2 = u / Cs;
 #pragma unroll
-          for (int n1 = 0; n1 < R1; n1++) buf[(R2 * n1 + n2) * PA + c] = a[n1];
+          for (int n1 = 0; n1 < R1; n1++) buf[G::pa(R2 * n1 + n2, c)] = a[n1];
         });
     __syncthreads();
     // ---- 11. store -------------------------------------------------------------
@@ -607,7 +628,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         if (E % NT != 0 && e >= E) break;
         const int c = e % Cs, n1 = e / Cs;
         const long long n = 2LL * (C * n1 + j * Cs + c);  // even: the pair stays in its block
-        *reinterpret_cast<cplx<T>*>(dst + 24 * (n >> 3) + (n & 7)) = buf[n1 * PA + c];
+        *reinterpret_cast<cplx<T>*>(dst + 24 * (n >> 3) + (n & 7)) = buf[G::pa(n1, c)];
       }
     } else if (kVec) {
 #pragma unroll 8
@@ -615,7 +636,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         const int e2 = it * NT + tid;
         const int c = 2 * (e2 % (Cs / 2)), n1 = e2 / (Cs / 2);
         const long long s0 = base + 2LL * (C * n1 + j * Cs + c);
-        const cplx<T> a = buf[n1 * PA + c], b = buf[n1 * PA + c + 1];
+        const cplx<T> a = buf[G::pa(n1, c)], b = buf[G::pa(n1, c + 1)];
         *reinterpret_cast<float4*>(p.out + s0) = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
       }
     } else
@@ -625,7 +646,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
       if (E % NT != 0 && e >= E) break;
       const int c = e % Cs, n1 = e / Cs;
       const long long s0 = base + 2LL * (C * n1 + j * Cs + c);
-      *reinterpret_cast<cplx<T>*>(p.out + s0) = buf[n1 * PA + c];
+      *reinterpret_cast<cplx<T>*>(p.out + s0) = buf[G::pa(n1, c)];
     }
     __syncthreads();
   }
