@@ -65,7 +65,7 @@ FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 343.67e6 / 384
 # DRAM bytes (read + write) of one group noise weighting (forward FFTs, 3 x 3
 # mixing, inverse FFTs) on the bench workloads with one group of 48 x 131072
 # samples, from the ncu capture in profiles/group_noise_weighting_c2_8det.md
-GROUP_NW_DRAM_BYTES = {("c2_64det_nside256", "f32"): 610.7e6, ("c2_8det_nside256", "f32"): 610.7e6}
+GROUP_NW_DRAM_BYTES = {("c2_64det_nside256", "f32"): 284.7e6, ("c2_8det_nside256", "f32"): 284.7e6}
 
 
 def peaks():

@@ -298,31 +298,31 @@ __global__ void __launch_bounds__(256) k_pt_f32(const long long* __restrict__ of
   ff a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f};
   if (m < npix) {
     const long long jend = off[m + 1];
-    long long j = off[m] + lane;
-    for (; j + L * (kPtUnroll - 1) < jend; j += L * kPtUnroll) {
+    // kPtUnroll samples per lane per round, the ones past the pixel's end
+    // masked: a pixel's few samples (about four per lane) take one round of
+    // dependent loads, not one per sample; each lane still adds its samples
+    // j, j + L, j + 2L, ... in that order
+    for (long long j = off[m] + lane; j < jend; j += L * kPtUnroll) {
       uint32_t ii[kPtUnroll];
       float3 v[kPtUnroll];
       float2 wv[kPtUnroll];
 #pragma unroll
-      for (int u = 0; u < kPtUnroll; u++) ii[u] = __ldcs(idx + j + L * u);
+      for (int u = 0; u < kPtUnroll; u++) ii[u] = j + L * u < jend ? __ldcs(idx + j + L * u) : 0u;
 #pragma unroll
       for (int u = 0; u < kPtUnroll; u++) {
-        v[u] = ys_at(ys, ii[u]);
-        wv[u] = __ldcs(ccs + j + L * u);
+        if (j + L * u < jend) {
+          v[u] = ys_at(ys, ii[u]);
+          wv[u] = __ldcs(ccs + j + L * u);
+        }
       }
 #pragma unroll
       for (int u = 0; u < kPtUnroll; u++) {
-        ff_add_f(a0, v[u].x);
-        ff_add_f(a1, wv[u].x * v[u].y - wv[u].y * v[u].z);
-        ff_add_f(a2, wv[u].y * v[u].y + wv[u].x * v[u].z);
+        if (j + L * u < jend) {
+          ff_add_f(a0, v[u].x);
+          ff_add_f(a1, wv[u].x * v[u].y - wv[u].y * v[u].z);
+          ff_add_f(a2, wv[u].y * v[u].y + wv[u].x * v[u].z);
+        }
       }
-    }
-    for (; j < jend; j += L) {
-      const float3 v = ys_at(ys, __ldcs(idx + j));
-      const float2 wv = __ldcs(ccs + j);
-      ff_add_f(a0, v.x);
-      ff_add_f(a1, wv.x * v.y - wv.y * v.z);
-      ff_add_f(a2, wv.y * v.y + wv.x * v.z);
     }
   }
 #pragma unroll
