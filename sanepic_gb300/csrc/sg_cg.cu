@@ -143,10 +143,21 @@ template cudaError_t cg_init<double>(const CgVecs&, cudaStream_t);
 // (a) rtq = q . d  (q is already masked by P^T)
 __global__ void __launch_bounds__(kCgThreads) k_step_a(CgVecs v) {
   const long long n3 = 3 * v.npix;
+  const long long stride = (long long)gridDim.x * blockDim.x;
   double acc[1] = {0.0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x)
-    acc[0] += v.q[i] * v.d[i];
+  // four elements' loads in flight per round, added in the same order
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += 4 * stride) {
+    double qv[4], dv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const long long k = i + u * stride;
+      qv[u] = k < n3 ? v.q[k] : 0.0;
+      dv[u] = k < n3 ? v.d[k] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (i + u * stride < n3) acc[0] += qv[u] * dv[u];
+  }
   block_reduce_store<1>(acc, v.part, kCgBlocks);
 }
 
@@ -162,34 +173,54 @@ __global__ void __launch_bounds__(kCgThreads) k_step_b(CgVecs v, int refresh, in
   const double delta = v.sc->delta;
   const double alpha = delta / rtq;
   const long long n = v.npix;
+  const long long stride = (long long)gridDim.x * blockDim.x;
   double acc[3] = {0.0, 0.0, 0.0};
-  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
-       m += (long long)gridDim.x * blockDim.x) {
-    double r[3];
+  // two pixels per round: every load of both before any store
+  for (long long m0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; m0 < n; m0 += 2 * stride) {
+    double xv[2][3], dv[2][3], rv[2][3], qv[2][3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long i = c * n + m;
-      v.x[i] += alpha * v.d[i];
-      r[c] = v.r[i];
-    }
-    if (refresh) continue;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long i = c * n + m;
-      if (flexible) v.rprev[i] = r[c];
-      r[c] -= alpha * v.q[i];
-      v.r[i] = r[c];
-    }
-    if (v.precond != 2) {
-      double z[3];
-      apply_m(v, m, r[0], r[1], r[2], z[0], z[1], z[2]);
+    for (int p = 0; p < 2; p++) {
+      const long long m = m0 + p * stride;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const long long i = c * n + m;
-        v.z[i] = z[c];
-        acc[0] += r[c] * z[c];
-        acc[1] += r[c] * r[c];
-        if (flexible) acc[2] += z[c] * v.rprev[i];
+        const bool in = m < n;
+        xv[p][c] = in ? v.x[i] : 0.0;
+        dv[p][c] = in ? v.d[i] : 0.0;
+        rv[p][c] = in ? v.r[i] : 0.0;
+        qv[p][c] = (in && !refresh) ? v.q[i] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+      const long long m = m0 + p * stride;
+      if (m >= n) break;
+      double r[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const long long i = c * n + m;
+        v.x[i] = xv[p][c] + alpha * dv[p][c];
+        r[c] = rv[p][c];
+      }
+      if (refresh) continue;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const long long i = c * n + m;
+        if (flexible) v.rprev[i] = r[c];
+        r[c] -= alpha * qv[p][c];
+        v.r[i] = r[c];
+      }
+      if (v.precond != 2) {
+        double z[3];
+        apply_m(v, m, r[0], r[1], r[2], z[0], z[1], z[2]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const long long i = c * n + m;
+          v.z[i] = z[c];
+          acc[0] += r[c] * z[c];
+          acc[1] += r[c] * r[c];
+          if (flexible) acc[2] += z[c] * rv[p][c];
+        }
       }
     }
   }
@@ -293,16 +324,30 @@ __global__ void __launch_bounds__(kCgThreads) k_step_c(CgVecs v, T* dmap, int fl
   const double dold = v.sc->delta_old;
   double beta = flexible ? (rz - zrp) / dold : rz / dold;
   const long long n = v.npix;
-  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
-       m += (long long)gridDim.x * blockDim.x) {
-    double d[3];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long m0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; m0 < n; m0 += 2 * stride) {
+    double zv[2][3], dv[2][3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long i = c * n + m;
-      d[c] = v.z[i] + beta * v.d[i];
-      v.d[i] = d[c];
+    for (int p = 0; p < 2; p++) {
+      const long long m = m0 + p * stride;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        zv[p][c] = m < n ? v.z[c * n + m] : 0.0;
+        dv[p][c] = m < n ? v.d[c * n + m] : 0.0;
+      }
     }
-    store_map<T>(dmap, m, d[0], d[1], d[2]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+      const long long m = m0 + p * stride;
+      if (m >= n) break;
+      double d[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        d[c] = zv[p][c] + beta * dv[p][c];
+        v.d[c * n + m] = d[c];
+      }
+      store_map<T>(dmap, m, d[0], d[1], d[2]);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     v.sc->delta = rz;
@@ -482,17 +527,29 @@ __global__ void __launch_bounds__(kCgThreads)
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
-#pragma unroll 2
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x) {
-    const float vi = (float)v[i];
-    const uint4* row = reinterpret_cast<const uint4*>(U + i * KP);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // two elements' rows in flight per round, added in the same order
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += 2 * stride) {
+    uint4 rows[2][KP / 8];
+    float vi[2];
 #pragma unroll
-    for (int q = 0; q < KP / 8; q++) {
-      float u[8];
-      bf16x8(row[q], u);
+    for (int p = 0; p < 2; p++) {
+      const long long k = i + p * stride;
+      const uint4* row = reinterpret_cast<const uint4*>(U + k * KP);
+      vi[p] = k < n3 ? (float)v[k] : 0.f;
 #pragma unroll
-      for (int t = 0; t < 8; t++) acc[8 * q + t] = fmaf(u[t], vi, acc[8 * q + t]);
+      for (int q = 0; q < KP / 8; q++) rows[p][q] = k < n3 ? row[q] : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+      if (i + p * stride >= n3) break;
+#pragma unroll
+      for (int q = 0; q < KP / 8; q++) {
+        float u[8];
+        bf16x8(rows[p][q], u);
+#pragma unroll
+        for (int t = 0; t < 8; t++) acc[8 * q + t] = fmaf(u[t], vi[p], acc[8 * q + t]);
+      }
     }
   }
   __shared__ double sh[KP][kCgThreads / 32];
@@ -617,24 +674,41 @@ __global__ void __launch_bounds__(kCgThreads)
   if (threadIdx.x < KP) w[threadIdx.x] = (float)(coef[threadIdx.x] - gd[threadIdx.x]);
   __syncthreads();
   const long long n3 = 3 * v.npix;
+  const long long stride = (long long)gridDim.x * blockDim.x;
   double acc[3] = {0.0, 0.0, 0.0};
-#pragma unroll 2
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
-       i += (long long)gridDim.x * blockDim.x) {
-    const uint4* row = reinterpret_cast<const uint4*>(U + i * KP);
-    float s = 0.f;
+  // two elements per round: every load of both before any store
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += 2 * stride) {
+    uint4 rows[2][KP / 8];
+    double zv[2], rv[2], pv[2];
 #pragma unroll
-    for (int q = 0; q < KP / 8; q++) {
-      float u[8];
-      bf16x8(row[q], u);
+    for (int p = 0; p < 2; p++) {
+      const long long k = i + p * stride;
+      const bool in = k < n3;
+      const uint4* row = reinterpret_cast<const uint4*>(U + k * KP);
 #pragma unroll
-      for (int t2 = 0; t2 < 8; t2++) s = fmaf(u[t2], w[8 * q + t2], s);
+      for (int q = 0; q < KP / 8; q++) rows[p][q] = in ? row[q] : make_uint4(0, 0, 0, 0);
+      zv[p] = in ? v.z[k] : 0.0;
+      rv[p] = in ? v.r[k] : 0.0;
+      pv[p] = (in && flexible) ? v.rprev[k] : 0.0;
     }
-    const double z = v.z[i] + (double)s, r = v.r[i];
-    v.z[i] = z;
-    acc[0] += r * z;
-    acc[1] += r * r;
-    if (flexible) acc[2] += z * v.rprev[i];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+      const long long k = i + p * stride;
+      if (k >= n3) break;
+      float s = 0.f;
+#pragma unroll
+      for (int q = 0; q < KP / 8; q++) {
+        float u[8];
+        bf16x8(rows[p][q], u);
+#pragma unroll
+        for (int t2 = 0; t2 < 8; t2++) s = fmaf(u[t2], w[8 * q + t2], s);
+      }
+      const double z = zv[p] + (double)s, r = rv[p];
+      v.z[k] = z;
+      acc[0] += r * z;
+      acc[1] += r * r;
+      if (flexible) acc[2] += z * pv[p];
+    }
   }
   block_reduce_store<3>(acc, v.part + kCgBlocks, kCgBlocks);
 }
