@@ -349,14 +349,16 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   // base angles (cos 2phi, sin 2phi) in time order and in CSR order
   SG_TRY(c->cs.alloc((size_t)2 * ng * c->esize));
   SG_TRY(c->csr_cs.alloc((size_t)2 * ng * c->esize));
+  DevBuf cs64;  // FP64 (cos, sin) 2 psi_o for the cross-link sums (no half-wave plate)
+  if (!hwp) SG_TRY(cs64.alloc(sizeof(double) * 2 * ng));
   if (c->f32) {
     SG_TRY(base_angles_launch<float>(psio.as<double>(), ng, ns, nsd, hwp ? 1 : 0, c->desc.omega,
-                                     c->cs.as<float>(), c->st));
+                                     c->cs.as<float>(), cs64.as<double>(), c->st));
     SG_TRY(gather_cs_launch<float>(c->cs.as<float>(), c->csr_idx.as<uint32_t>(), ng,
                                    c->csr_cs.as<float>(), c->st));
   } else {
     SG_TRY(base_angles_launch<double>(psio.as<double>(), ng, ns, nsd, hwp ? 1 : 0, c->desc.omega,
-                                      c->cs.as<double>(), c->st));
+                                      c->cs.as<double>(), cs64.as<double>(), c->st));
     SG_TRY(gather_cs_launch<double>(c->cs.as<double>(), c->csr_idx.as<uint32_t>(), ng,
                                     c->csr_cs.as<double>(), c->st));
   }
@@ -375,8 +377,8 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   }
   SG_TRY(c->sumcross.alloc(sizeof(double) * 3 * npix));
   SG_TRY(sumcross_launch(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(), psio.as<double>(),
-                         nsd, gsc.as<double>(), gss.as<double>(), npix, c->sumcross.as<double>(),
-                         c->st));
+                         cs64.as<double>(), nsd, gsc.as<double>(), gss.as<double>(), npix,
+                         c->sumcross.as<double>(), c->st));
   SG_TRY(c->ys.alloc((size_t)3 * ng * c->esize));  // [ng / 8][3][8]
   // the offset-group operator when every group is large enough (three
   // timelines per group instead of one per detector); SANEPIC_GPU_GROUP_FILTER=0

@@ -96,14 +96,16 @@ cudaError_t csr_build(const int* pix, long long n, long long npix,
 template <typename T>
 cudaError_t gather_cs_launch(const T* cs, const uint32_t* csr_idx, long long n, T* csr_cs,
                              cudaStream_t st);
-// (cos 2phi, sin 2phi) of the group base angle per group sample
+// (cos 2phi, sin 2phi) of the group base angle per group sample; cs64
+// (optional, no half-wave plate): FP64 (cos, sin) of 2 psi_o for sumcross
 template <typename T>
 cudaError_t base_angles_launch(const double* psio, long long n, long long ns, long long nsd,
-                               int hwp, double omega, T* cs, cudaStream_t st);
-// COS2P/SIN2P sums over the CSR; gsc/gss [ngroups] = group sums of cos/sin 2psi_det
+                               int hwp, double omega, T* cs, double* cs64, cudaStream_t st);
+// COS2P/SIN2P sums over the CSR; gsc/gss [ngroups] = group sums of cos/sin 2psi_det;
+// tab (optional): the cs64 table of base_angles_launch instead of sincos of psio
 cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, const double* psio,
-                            long long nsd, const double* gsc, const double* gss, long long npix,
-                            double* sumcross, cudaStream_t st);
+                            const double* tab, long long nsd, const double* gsc, const double* gss,
+                            long long npix, double* sumcross, cudaStream_t st);
 // 3x3 block-Jacobi build+invert; gconst [5][ngroups]; minv [6][npix] (00 01 02 11 12 22)
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,

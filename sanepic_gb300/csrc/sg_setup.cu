@@ -249,17 +249,31 @@ template cudaError_t gather_cs_launch<double>(const double*, const uint32_t*, lo
 // (sanepic.cc:757-766); the detector's own angle is applied as a rotation.
 // For FP32 storage the FP64 angle is first reduced modulo 2pi (exact fmod)
 // so that HWP angles of ~1e6 rad stay on the fast path.
+// Without a half-wave plate the cross-link sums below need cos/sin of the
+// same 2 psi_o in FP64: with cs64 set they are stored there too (one FP64
+// sincos per sample serves both where the arguments agree bit for bit).
 template <typename T>
 __global__ void k_base_angles(const double* psio, long long n, long long ns, long long nsd,
-                              int hwp, double omega, T* cs) {
+                              int hwp, double omega, T* cs, double2* cs64) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     double phi = psio[i];
+    double s0 = 0.0, c0 = 0.0, araw = 0.0;
+    if (cs64) {  // the cross-link argument, 2 (psi_o + 0)
+      araw = 2.0 * (phi + 0.0);
+      sincos(araw, &s0, &c0);
+      cs64[i] = make_double2(c0, s0);
+    }
     if (hwp) phi = -phi + 2.0 * omega * (double)(i % nsd);  // i % nsd = ii + ns * iseg
     double a = 2.0 * phi;
     if (sizeof(T) == 4) a = fmod(a, 6.2831853071795864769252867665590057683943387987502);
     double s, c;
-    sincos(a, &s, &c);
+    if (cs64 && __double_as_longlong(a) == __double_as_longlong(araw)) {
+      s = s0;
+      c = c0;
+    } else {
+      sincos(a, &s, &c);
+    }
     cs[2 * i] = (T)c;
     cs[2 * i + 1] = (T)s;
   }
@@ -267,24 +281,27 @@ __global__ void k_base_angles(const double* psio, long long n, long long ns, lon
 
 template <typename T>
 cudaError_t base_angles_launch(const double* psio, long long n, long long ns, long long nsd,
-                               int hwp, double omega, T* cs, cudaStream_t st) {
+                               int hwp, double omega, T* cs, double* cs64, cudaStream_t st) {
   (void)ns;
-  k_base_angles<T><<<grid_for(n, 256), 256, 0, st>>>(psio, n, ns, nsd, hwp, omega, cs);
+  k_base_angles<T><<<grid_for(n, 256), 256, 0, st>>>(psio, n, ns, nsd, hwp, omega, cs,
+                                                     reinterpret_cast<double2*>(cs64));
   return cudaGetLastError();
 }
 template cudaError_t base_angles_launch<float>(const double*, long long, long long, long long,
-                                               int, double, float*, cudaStream_t);
+                                               int, double, float*, double*, cudaStream_t);
 template cudaError_t base_angles_launch<double>(const double*, long long, long long, long long,
-                                                int, double, double*, cudaStream_t);
+                                                int, double, double*, double*, cudaStream_t);
 
 // ---- per-pixel reductions over the CSR (one warp per pixel) -----------------
 // COS2P/SIN2P (sanepic.cc:2594-2597): per pixel, the sum over detector
 // samples of cos/sin(2 (psi_o + psi_det)).  Per group sample that is
 // cos 2psi_o SC - sin 2psi_o SS (and sin 2psi_o SC + cos 2psi_o SS) with
 // SC, SS the group's sums of cos/sin(2 psi_det).  FP64, warp per pixel.
+// With tab set, cos/sin of 2 psi_o come from the table the base-angle pass
+// filled (the same FP64 values) instead of one sincos per sample here.
 __global__ void k_sumcross(const long long* off, const uint32_t* idx, const double* psio,
-                           long long nsd, const double* gsc, const double* gss, long long npix,
-                           double* out) {
+                           const double2* tab, long long nsd, const double* gsc,
+                           const double* gss, long long npix, double* out) {
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -294,7 +311,13 @@ __global__ void k_sumcross(const long long* off, const uint32_t* idx, const doub
       const long long gs = idx[j];
       const int g = (int)(gs / nsd);
       double sn, cs;
-      sincos(2.0 * (psio[gs] + 0.0), &sn, &cs);
+      if (tab) {
+        const double2 t = tab[gs];
+        cs = t.x;
+        sn = t.y;
+      } else {
+        sincos(2.0 * (psio[gs] + 0.0), &sn, &cs);
+      }
       c += cs * gsc[g] - sn * gss[g];
       s += sn * gsc[g] + cs * gss[g];
     }
@@ -311,10 +334,11 @@ __global__ void k_sumcross(const long long* off, const uint32_t* idx, const doub
 }
 
 cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, const double* psio,
-                            long long nsd, const double* gsc, const double* gss, long long npix,
-                            double* sumcross, cudaStream_t st) {
-  k_sumcross<<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(csr_off, csr_idx, psio, nsd,
-                                                                   gsc, gss, npix, sumcross);
+                            const double* tab, long long nsd, const double* gsc, const double* gss,
+                            long long npix, double* sumcross, cudaStream_t st) {
+  k_sumcross<<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(
+      csr_off, csr_idx, psio, reinterpret_cast<const double2*>(tab), nsd, gsc, gss, npix,
+      sumcross);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,16 @@ def test_reference_hits_and_weights(name):
         assert rel_rms(mm.get_map(k), ref[k]) < 1e-10, k
 
 
+def test_cross_link_maps_same_in_both_precisions():
+    """COS2P/SIN2P are FP64 sums whatever the operator precision (without a
+    half-wave plate their cos/sin come from the base-angle pass's FP64 table)"""
+    prob = small_problem(ndet=4, nseg=2, ns=4096, nside=32)
+    m64 = sg.from_problem(prob, precision="f64", with_tod=False)
+    m32 = sg.from_problem(prob, precision="f32", with_tod=False)
+    for k in ("COS2P", "SIN2P"):
+        assert np.array_equal(m64.get_map(k), m32.get_map(k)), k
+
+
 # ---- noise filter (FFT) ---------------------------------------------------------
 @pytest.mark.parametrize("ns,prec", [(256, "f64"), (2048, "f64"), (16384, "f64"),
                                      (65536, "f64"), (1024, "f32"), (32768, "f32"),
