@@ -119,6 +119,7 @@ struct sg_ctx {
   bool group_mode = false, have_hmix = false;
   DevBuf gtl, gspec, hmix, dspec, rhs_part;  // + data spectra [ndet][nseg][M+1], chi^2 partials
   DevBuf kslot, filt_slot;  // frequency of each spectrum slot; filter rows in slot order
+  int kslot_S = -1;         // the tile shape kslot was made for
   int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
   DevBuf noise_stage, noise_part;  // one detector's iSpf values; g0 partial sums
@@ -316,13 +317,16 @@ struct sg_ctx {
   cudaError_t ensure_hmix() {
     if (!group_mode || (have_hmix && hmix_S == S)) return cudaSuccess;
     const long long M1 = ns / 2 + 1;
-    std::vector<int> kf;
-    spec_slot_freq(logm, S, kf);
-    cudaError_t e = kslot.alloc(sizeof(int) * M1);
-    if (e == cudaSuccess) e = filt_slot.alloc((size_t)ndet * M1 * esize);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(kslot.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
+    cudaError_t e = filt_slot.alloc((size_t)ndet * M1 * esize);
+    if (e == cudaSuccess && kslot_S != S) {  // the slot order depends on the tile shape only
+      std::vector<int> kf;
+      spec_slot_freq(logm, S, kf);
+      e = kslot.alloc(sizeof(int) * M1);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(kslot.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
+      if (e == cudaSuccess) kslot_S = S;
+    }
     if (e != cudaSuccess) return e;
     if (f32) {
       e = group_hmix_launch<float>(filt.as<float>(), dcs.as<float>(), grp_off.as<int>(),

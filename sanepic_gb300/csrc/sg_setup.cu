@@ -348,68 +348,117 @@ cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, c
 //   gc = (sum g0, sum g0 cos 2d, sum g0 sin 2d, sum g0 cos 4d, sum g0 sin 4d)
 // with cos^2 = (1 + cos 4a)/2, cos sin = sin 4a / 2.  Inverse in FP64.
 template <typename T>
-__global__ void k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix,
-                      long long nsd, int ngroups, const double* gc, const int* hits,
-                      double* minv) {
-  const int lane = threadIdx.x & 31;
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long m = warp; m < npix; m += nwarps) {
-    double a[6] = {0, 0, 0, 0, 0, 0};
-    for (long long j = off[m] + lane; j < off[m + 1]; j += 32) {
-      const int g = (int)(idx[j] / nsd);
-      const double G0 = gc[g], G2c = gc[ngroups + g], G2s = gc[2 * ngroups + g];
-      const double G4c = gc[3 * ngroups + g], G4s = gc[4 * ngroups + g];
-      const double c2 = (double)ccs[2 * j], s2 = (double)ccs[2 * j + 1];
-      const double c4 = c2 * c2 - s2 * s2, s4 = 2.0 * c2 * s2;
-      const double C4 = c4 * G4c - s4 * G4s, S4 = s4 * G4c + c4 * G4s;
-      a[0] += G0;
-      a[1] += c2 * G2c - s2 * G2s;
-      a[2] += s2 * G2c + c2 * G2s;
-      a[3] += 0.5 * (G0 + C4);
-      a[4] += 0.5 * S4;
-      a[5] += 0.5 * (G0 - C4);
-    }
-    for (int o = 16; o > 0; o >>= 1)
-      for (int k = 0; k < 6; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
-    if (lane == 0) {
-      double o6[6] = {0, 0, 0, 0, 0, 0};
-      if (hits[m] < 2) {
-        o6[0] = a[0] != 0.0 ? 1.0 / a[0] : 0.0;
-      } else {
-        const double c00 = a[3] * a[5] - a[4] * a[4];
-        const double c01 = a[2] * a[4] - a[1] * a[5];
-        const double c02 = a[1] * a[4] - a[2] * a[3];
-        const double c11 = a[0] * a[5] - a[2] * a[2];
-        const double c12 = a[1] * a[2] - a[0] * a[4];
-        const double c22 = a[0] * a[3] - a[1] * a[1];
-        const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
-        const double scale = a[0] * a[0] * a[0];
-        if (!(det > 1e-12 * scale)) {
-          o6[0] = 1.0 / a[0];
-          o6[3] = a[3] > 0.0 ? 1.0 / a[3] : 0.0;
-          o6[5] = a[5] > 0.0 ? 1.0 / a[5] : 0.0;
-        } else {
-          const double id = 1.0 / det;
-          o6[0] = c00 * id;
-          o6[1] = c01 * id;
-          o6[2] = c02 * id;
-          o6[3] = c11 * id;
-          o6[4] = c12 * id;
-          o6[5] = c22 * id;
-        }
+struct pair_of;
+template <>
+struct pair_of<float> {
+  using type = float2;
+};
+template <>
+struct pair_of<double> {
+  using type = double2;
+};
+
+// A team of L lanes per pixel (256 / L pixels per block), each lane taking
+// its samples j, j + L, ... four at a time with the loads of all four in
+// flight; FP64 sums, combined over the team with a fixed xor tree.
+template <typename T, int L>
+__global__ void __launch_bounds__(256)
+    k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix, uint32_t nsd,
+          int ngroups, const double* gc, const int* hits, double* minv) {
+  using P2 = typename pair_of<T>::type;
+  constexpr int U = 4;
+  const int lane = threadIdx.x % L;
+  const long long m = (long long)blockIdx.x * (256 / L) + threadIdx.x / L;
+  const P2* cs2 = reinterpret_cast<const P2*>(ccs);
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  if (m < npix) {
+    const long long jend = off[m + 1];
+    for (long long j = off[m] + lane; j < jend; j += L * U) {
+      int g[U];
+      P2 w[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const long long k = j + L * u;
+        const bool in = k < jend;
+        g[u] = (in && ngroups > 1) ? (int)(idx[k] / nsd) : 0;
+        w[u] = in ? cs2[k] : P2{};
       }
-      for (int k = 0; k < 6; k++) minv[k * npix + m] = o6[k];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (j + L * u >= jend) break;
+        const int gg = g[u];
+        const double G0 = gc[gg], G2c = gc[ngroups + gg], G2s = gc[2 * ngroups + gg];
+        const double G4c = gc[3 * ngroups + gg], G4s = gc[4 * ngroups + gg];
+        const double c2 = (double)w[u].x, s2 = (double)w[u].y;
+        const double c4 = c2 * c2 - s2 * s2, s4 = 2.0 * c2 * s2;
+        const double C4 = c4 * G4c - s4 * G4s, S4 = s4 * G4c + c4 * G4s;
+        a[0] += G0;
+        a[1] += c2 * G2c - s2 * G2s;
+        a[2] += s2 * G2c + c2 * G2s;
+        a[3] += 0.5 * (G0 + C4);
+        a[4] += 0.5 * S4;
+        a[5] += 0.5 * (G0 - C4);
+      }
     }
   }
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 6; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+  if (lane == 0 && m < npix) {
+    double o6[6] = {0, 0, 0, 0, 0, 0};
+    if (hits[m] < 2) {
+      o6[0] = a[0] != 0.0 ? 1.0 / a[0] : 0.0;
+    } else {
+      const double c00 = a[3] * a[5] - a[4] * a[4];
+      const double c01 = a[2] * a[4] - a[1] * a[5];
+      const double c02 = a[1] * a[4] - a[2] * a[3];
+      const double c11 = a[0] * a[5] - a[2] * a[2];
+      const double c12 = a[1] * a[2] - a[0] * a[4];
+      const double c22 = a[0] * a[3] - a[1] * a[1];
+      const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+      const double scale = a[0] * a[0] * a[0];
+      if (!(det > 1e-12 * scale)) {
+        o6[0] = 1.0 / a[0];
+        o6[3] = a[3] > 0.0 ? 1.0 / a[3] : 0.0;
+        o6[5] = a[5] > 0.0 ? 1.0 / a[5] : 0.0;
+      } else {
+        const double id = 1.0 / det;
+        o6[0] = c00 * id;
+        o6[1] = c01 * id;
+        o6[2] = c02 * id;
+        o6[3] = c11 * id;
+        o6[4] = c12 * id;
+        o6[5] = c22 * id;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) minv[k * npix + m] = o6[k];
+  }
+}
+
+template <typename T, int L>
+static void bj3_team(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
+                     long long npix, long long nsd, int ngroups, const double* gconst,
+                     const int* hits_true, double* minv, cudaStream_t st) {
+  const long long blocks = (npix + 256 / L - 1) / (256 / L);
+  k_bj3<T, L><<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx, csr_cs, npix, (uint32_t)nsd,
+                                                 ngroups, gconst, hits_true, minv);
 }
 
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                        long long npix, long long nsd, int ngroups, const double* gconst,
                        const int* hits_true, double* minv, cudaStream_t st) {
-  k_bj3<T><<<grid_for(npix * 32, 256, 152LL * 64), 256, 0, st>>>(
-      csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv);
+  if (npix <= 0) return cudaSuccess;
+  switch (pt_lanes((long long)ngroups * nsd, npix)) {  // every group sample is in the CSR
+    case 1: bj3_team<T, 1>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 2: bj3_team<T, 2>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 4: bj3_team<T, 4>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 8: bj3_team<T, 8>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 16: bj3_team<T, 16>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    default: bj3_team<T, 32>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+  }
   return cudaGetLastError();
 }
 template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*, long long,
