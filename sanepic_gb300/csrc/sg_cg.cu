@@ -15,41 +15,37 @@
 
 namespace sg {
 
+// GB300 issues FP64 at ~1/64 of the FP32 rate, so a block's FP64 sums go
+// through shared memory and one warp finishes them (8 values per lane, then
+// a 5-level xor tree) rather than every warp running its own shuffle tree.
 template <int N>
 __device__ __forceinline__ void block_reduce_store(double (&v)[N], double* part, int stride) {
-  __shared__ double sh[N][kCgThreads / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ double sh[N][kCgThreads];
 #pragma unroll
-  for (int k = 0; k < N; k++) {
-    double x = v[k];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[k][wid] = x;
-  }
+  for (int k = 0; k < N; k++) sh[k][threadIdx.x] = v[k];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
 #pragma unroll
     for (int k = 0; k < N; k++) {
-      double s = 0.0;
-      for (int w = 0; w < kCgThreads / 32; w++) s += sh[k][w];
-      part[k * stride + blockIdx.x] = s;
+      double x = sh[k][lane];
+#pragma unroll
+      for (int w = 1; w < kCgThreads / 32; w++) x += sh[k][w * 32 + lane];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) part[k * stride + blockIdx.x] = x;
     }
   }
 }
 
-// Every block computes the same total from the per-block partials.
+// Every block computes the same total from the per-block partials (warp 0
+// adds them in a fixed order; the others wait).
 __device__ __forceinline__ double reduce_partials(const double* part) {
-  __shared__ double sh[kCgThreads / 32];
   __shared__ double tot;
-  double x = 0.0;
-  for (int i = threadIdx.x; i < kCgBlocks; i += kCgThreads) x += part[i];
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = x;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < kCgThreads / 32; w++) s += sh[w];
-    tot = s;
+  if (threadIdx.x < 32) {
+    double x = 0.0;
+    for (int i = threadIdx.x; i < kCgBlocks; i += 32) x += part[i];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (threadIdx.x == 0) tot = x;
   }
   __syncthreads();
   const double r = tot;
@@ -503,11 +499,12 @@ cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
 // kp values as 16-byte loads; the preconditioner stays symmetric positive
 // definite whatever their rounding (the same U on both sides, E exact in
 // FP64).  Their products with a vector run in FP32 (GB300's
-// FP64 rate would make kc FP64 FMAs per element cost more than reading U);
-// per-thread partials, the fixed-order reductions and the coarse solves are
-// FP64.  Every block of the kernel that needs c (or c - g) re-reduces the
-// partials itself, so the coarse solve costs no launch.  The rounding makes
-// the preconditioner slightly inexact, which flexible PCG absorbs.
+// FP64 rate would make kc FP64 FMAs per element cost more than reading U),
+// and so do the fixed-order block and partial sums; the coarse solves with
+// E^-1 are FP64.  Every block of the kernel that needs c (or c - g)
+// re-reduces the partials itself, so the coarse solve costs no launch.  The
+// rounding makes the preconditioner slightly inexact, which flexible PCG
+// absorbs.
 
 // eight BF16 values (one 16-byte load) as floats
 __device__ __forceinline__ void bf16x8(const uint4 q, float (&f)[8]) {
@@ -519,11 +516,35 @@ __device__ __forceinline__ void bf16x8(const uint4 q, float (&f)[8]) {
   }
 }
 
+// part[k][block] = the block's FP32 sums of acc[k] (a fixed xor tree per
+// warp, then the warps in order).  The coarse products are FP32 with BF16
+// vectors; FP32 partials lose nothing that matters there, and FP64 tree
+// reductions of KP values per warp would cost GB300 more than the loop.
+template <int KP>
+__device__ __forceinline__ void coarse_block_store(float (&acc)[KP], float* part) {
+  __shared__ float sh[KP][kCgThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < KP; k++) {
+    float x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < KP) {
+    float t = 0.f;
+#pragma unroll
+    for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
+    part[threadIdx.x * kCgBlocks + blockIdx.x] = t;
+  }
+}
+
 // part[k][block] = sum over the block's elements of U[i][k] v[i]
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
     k_coarse_dots(const uint16_t* __restrict__ U, long long n3, const double* __restrict__ v,
-                  double* part) {
+                  float* part) {
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
@@ -552,34 +573,22 @@ __global__ void __launch_bounds__(kCgThreads)
       }
     }
   }
-  __shared__ double sh[KP][kCgThreads / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < KP; k++) {
-    double x = (double)acc[k];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[k][wid] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < KP) {
-    double t = 0.0;
-    for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
-    part[threadIdx.x * kCgBlocks + blockIdx.x] = t;
-  }
+  coarse_block_store<KP>(acc, part);
 }
 
 // out[k] = (E^-1 d)[k], d[k] = sum_b part[k][b] in a fixed order (identical in
-// every block); warp w reduces rows w, w + 8, ...
+// every block; FP32 sums, warp w reduces rows w, w + 8, ...), E^-1 d in FP64
 template <int KP>
-__device__ __forceinline__ void coarse_solve_block(const double* __restrict__ part,
+__device__ __forceinline__ void coarse_solve_block(const float* __restrict__ part,
                                                    const double* __restrict__ einv, int kc,
                                                    double* d, double* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = wid; k < KP; k += kCgThreads / 32) {
-    double x = 0.0;
+    float x = 0.f;
     for (int b = lane; b < kCgBlocks; b += 32) x += part[k * kCgBlocks + b];
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) d[k] = x;
+    if (lane == 0) d[k] = (double)x;
   }
   __syncthreads();
   if (threadIdx.x < KP) {
@@ -597,8 +606,8 @@ __device__ __forceinline__ void coarse_solve_block(const double* __restrict__ pa
 // both: the second use hits L1)
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads, 2)
-    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const double* __restrict__ part1,
-                 const double* __restrict__ einv, int kc, double* coef, double* part2) {
+    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const float* __restrict__ part1,
+                 const double* __restrict__ einv, int kc, double* coef, float* part2) {
   __shared__ double d[KP], cd[KP];
   __shared__ float c[KP];
   coarse_solve_block<KP>(part1, einv, kc, d, cd);
@@ -645,27 +654,14 @@ __global__ void __launch_bounds__(kCgThreads, 2)
       }
     }
   }
-  __shared__ double sh[KP][kCgThreads / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < KP; k++) {
-    double x = (double)acc[k];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[k][wid] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < KP) {
-    double t = 0.0;
-    for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
-    part2[threadIdx.x * kCgBlocks + blockIdx.x] = t;
-  }
+  coarse_block_store<KP>(acc, part2);
 }
 
 // g = E^-1 AU^T y (from part2); z = y + U (c - g); the CG's partial dots
 // r.z, r.r (and z.r_prev when flexible) into part + kCgBlocks..
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const double* __restrict__ part2,
+    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const float* __restrict__ part2,
                   const double* __restrict__ einv, int kc, const double* __restrict__ coef,
                   int flexible) {
   __shared__ double d[KP], gd[KP];
@@ -717,8 +713,8 @@ template <int KP>
 static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int flexible,
                                    cudaStream_t st) {
   const long long n3 = 3 * v.npix;
-  double* part1 = cs.part;
-  double* part2 = cs.part + (size_t)kCoarseMax * kCgBlocks;
+  float* part1 = reinterpret_cast<float*>(cs.part);  // FP32 partials in the FP64 scratch
+  float* part2 = part1 + (size_t)kCoarseMax * kCgBlocks;
   k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
   k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef,
                                                       part2);
