@@ -414,7 +414,6 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(c->rprev.alloc(vb));
   SG_TRY(c->b.alloc(vb));
   SG_TRY(c->minv.alloc(sizeof(double) * 6 * npix));
-  SG_TRY(c->minv32.alloc(sizeof(float) * 6 * npix));
   SG_TRY(c->mdiag.alloc(vb));
   SG_TRY(c->mp_raw.alloc(vb));
   SG_TRY(c->part.alloc(sizeof(double) * 4 * kCgBlocks));
@@ -644,13 +643,12 @@ int build_bj3(sg_ctx* c) {
     if (c->f32)
       e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
                             c->csr_cs.as<float>(), c->npix, c->ns * c->nseg, G,
-                            c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(),
-                            c->minv32.as<float>(), c->st);
+                            c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
     else
       e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
                              c->csr_cs.as<double>(), c->npix, c->ns * c->nseg, G,
                              c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(),
-                             c->minv32.as<float>(), c->st);
+                             c->st);
   }
   if (e != cudaSuccess) return c->cuda_fail(e, "bj3 build");
   c->have_bj3 = true;

@@ -619,15 +619,10 @@ __global__ void __launch_bounds__(kCgThreads, 2)
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
-  // t = r - AU c and z = M t in FP32 (the block inverses' FP32 copy): inside
-  // the coarse correction an FP32 M is one more rounding flexible PCG
-  // absorbs, and GB300's FP64 rate would make it the kernel's bottleneck;
-  // z is stored in FP64 for the CG.
   const long long n = v.npix;
-  const float* o = v.minv32;
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
        m += (long long)gridDim.x * blockDim.x) {
-    float t[3];
+    double t[3];
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
@@ -640,25 +635,22 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 #pragma unroll
         for (int t2 = 0; t2 < 8; t2++) s = fmaf(a[t2], c[8 * q + t2], s);
       }
-      t[cc] = (float)v.r[i] - s;
+      t[cc] = v.r[i] - (double)s;
     }
-    const float o00 = o[m], o01 = o[n + m], o02 = o[2 * n + m];
-    const float o11 = o[3 * n + m], o12 = o[4 * n + m], o22 = o[5 * n + m];
-    float z[3];
-    z[0] = o00 * t[0] + o01 * t[1] + o02 * t[2];
-    z[1] = o01 * t[0] + o11 * t[1] + o12 * t[2];
-    z[2] = o02 * t[0] + o12 * t[1] + o22 * t[2];
+    double z[3];
+    apply_m(v, m, t[0], t[1], t[2], z[0], z[1], z[2]);
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
-      v.z[i] = (double)z[cc];
+      v.z[i] = z[cc];
+      const float zf = (float)z[cc];
       const uint4* row = reinterpret_cast<const uint4*>(AU + i * KP);
 #pragma unroll
       for (int q = 0; q < KP / 8; q++) {
         float a[8];
         bf16x8(__ldcg(row + q), a);  // again, from L2: keeps the rows out of registers
 #pragma unroll
-        for (int t2 = 0; t2 < 8; t2++) acc[8 * q + t2] = fmaf(a[t2], z[cc], acc[8 * q + t2]);
+        for (int t2 = 0; t2 < 8; t2++) acc[8 * q + t2] = fmaf(a[t2], zf, acc[8 * q + t2]);
       }
     }
   }

@@ -110,7 +110,7 @@ cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, c
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                        long long npix, long long nsd, int ngroups, const double* gconst,
-                       const int* hits_true, double* minv, float* minv32, cudaStream_t st);
+                       const int* hits_true, double* minv, cudaStream_t st);
 // per-group sum of the detectors' N_ tables: out [ngroups][ns]
 template <typename T>
 cudaError_t group_ntab_launch(const T* ntab, long long ns, int ngroups, const int* grp_off,
@@ -209,7 +209,6 @@ struct CgVecs {
   double* rprev;        // flexible PCG: previous residual (or nullptr)
   const double* b;
   const double* minv;   // bj3 [6][npix] (00 01 02 11 12 22)
-  const float* minv32;  // the same blocks rounded to FP32 (the coarse-space path)
   const double* mdiag;  // reference diagonal, inverted [3][npix]
   const int* hits_true;
   int precond;          // 0 diag, 1 bj3, 2 z supplied externally

@@ -364,7 +364,7 @@ struct pair_of<double> {
 template <typename T, int L>
 __global__ void __launch_bounds__(256)
     k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix, uint32_t nsd,
-          int ngroups, const double* gc, const int* hits, double* minv, float* minv32) {
+          int ngroups, const double* gc, const int* hits, double* minv) {
   using P2 = typename pair_of<T>::type;
   constexpr int U = 4;
   const int lane = threadIdx.x % L;
@@ -433,43 +433,40 @@ __global__ void __launch_bounds__(256)
       }
     }
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
-      minv[k * npix + m] = o6[k];
-      if (minv32) minv32[k * npix + m] = (float)o6[k];
-    }
+    for (int k = 0; k < 6; k++) minv[k * npix + m] = o6[k];
   }
 }
 
 template <typename T, int L>
 static void bj3_team(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                      long long npix, long long nsd, int ngroups, const double* gconst,
-                     const int* hits_true, double* minv, float* minv32, cudaStream_t st) {
+                     const int* hits_true, double* minv, cudaStream_t st) {
   const long long blocks = (npix + 256 / L - 1) / (256 / L);
   k_bj3<T, L><<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx, csr_cs, npix, (uint32_t)nsd,
-                                                 ngroups, gconst, hits_true, minv, minv32);
+                                                 ngroups, gconst, hits_true, minv);
 }
 
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                        long long npix, long long nsd, int ngroups, const double* gconst,
-                       const int* hits_true, double* minv, float* minv32, cudaStream_t st) {
+                       const int* hits_true, double* minv, cudaStream_t st) {
   if (npix <= 0) return cudaSuccess;
   switch (pt_lanes((long long)ngroups * nsd, npix)) {  // every group sample is in the CSR
-    case 1: bj3_team<T, 1>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
-    case 2: bj3_team<T, 2>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
-    case 4: bj3_team<T, 4>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
-    case 8: bj3_team<T, 8>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
-    case 16: bj3_team<T, 16>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
-    default: bj3_team<T, 32>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, minv32, st); break;
+    case 1: bj3_team<T, 1>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 2: bj3_team<T, 2>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 4: bj3_team<T, 4>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 8: bj3_team<T, 8>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 16: bj3_team<T, 16>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    default: bj3_team<T, 32>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
   }
   return cudaGetLastError();
 }
 template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*, long long,
                                        long long, int, const double*, const int*, double*,
-                                       float*, cudaStream_t);
+                                       cudaStream_t);
 template cudaError_t bj3_launch<double>(const long long*, const uint32_t*, const double*,
                                         long long, long long, int, const double*, const int*,
-                                        double*, float*, cudaStream_t);
+                                        double*, cudaStream_t);
 
 // N_ of every detector summed over its group: the pixel stream is common to
 // the group, so the reference's per-detector pair sums add up per group.
