@@ -499,12 +499,12 @@ cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
 // kp values as 16-byte loads; the preconditioner stays symmetric positive
 // definite whatever their rounding (the same U on both sides, E exact in
 // FP64).  Their products with a vector run in FP32 (GB300's
-// FP64 rate would make kc FP64 FMAs per element cost more than reading U),
-// and so do the fixed-order block and partial sums; the coarse solves with
-// E^-1 are FP64.  Every block of the kernel that needs c (or c - g)
-// re-reduces the partials itself, so the coarse solve costs no launch.  The
-// rounding makes the preconditioner slightly inexact, which flexible PCG
-// absorbs.
+// FP64 rate would make kc FP64 FMAs per element cost more than reading U);
+// the per-thread sums are FP32, the warp sums double-FP32, the block
+// partials, their fixed-order reductions and the coarse solves FP64.  Every
+// block of the kernel that needs c (or c - g) re-reduces the partials
+// itself, so the coarse solve costs no launch.  The rounding makes the
+// preconditioner slightly inexact, which flexible PCG absorbs.
 
 // eight BF16 values (one 16-byte load) as floats
 __device__ __forceinline__ void bf16x8(const uint4 q, float (&f)[8]) {
@@ -516,24 +516,41 @@ __device__ __forceinline__ void bf16x8(const uint4 q, float (&f)[8]) {
   }
 }
 
-// part[k][block] = the block's FP32 sums of acc[k] (a fixed xor tree per
-// warp, then the warps in order).  The coarse products are FP32 with BF16
-// vectors; FP32 partials lose nothing that matters there, and FP64 tree
-// reductions of KP values per warp would cost GB300 more than the loop.
+// Double-FP32 addition (hi, lo) += (b, bl): Knuth's two-sum of the high
+// parts, the low parts added to the error term.  ~44 bits, FP32 instructions.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float b, float bl) {
+  const float s = hi + b;
+  const float bb = s - hi;
+  const float e = ((hi - (s - bb)) + (b - bb)) + (lo + bl);
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
+// part[k][block] = the block's sum of acc[k] (FP64).  A warp first adds its
+// lanes' FP32 accumulators as double-FP32 pairs through a fixed xor tree
+// (FP32 instructions only), lane k takes total k and widens it to FP64, and
+// KP threads add the warps in order: GB300's FP64 rate would make an FP64
+// shuffle tree of KP values per warp cost more than the kernel's loop.
 template <int KP>
-__device__ __forceinline__ void coarse_block_store(float (&acc)[KP], float* part) {
-  __shared__ float sh[KP][kCgThreads / 32];
+__device__ __forceinline__ void coarse_block_store(float (&acc)[KP], double* part) {
+  __shared__ double sh[KP][kCgThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float mh = 0.f, ml = 0.f;  // this lane's total: k = lane
 #pragma unroll
   for (int k = 0; k < KP; k++) {
-    float x = acc[k];
+    float hi = acc[k], lo = 0.f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[k][wid] = x;
+    for (int o = 16; o > 0; o >>= 1)
+      df_add(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+    if (lane == k) {
+      mh = hi;
+      ml = lo;
+    }
   }
+  if (lane < KP) sh[lane][wid] = (double)mh + (double)ml;
   __syncthreads();
   if (threadIdx.x < KP) {
-    float t = 0.f;
+    double t = 0.0;
 #pragma unroll
     for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
     part[threadIdx.x * kCgBlocks + blockIdx.x] = t;
@@ -544,7 +561,7 @@ __device__ __forceinline__ void coarse_block_store(float (&acc)[KP], float* part
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
     k_coarse_dots(const uint16_t* __restrict__ U, long long n3, const double* __restrict__ v,
-                  float* part) {
+                  double* part) {
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
@@ -577,18 +594,17 @@ __global__ void __launch_bounds__(kCgThreads)
 }
 
 // out[k] = (E^-1 d)[k], d[k] = sum_b part[k][b] in a fixed order (identical in
-// every block; FP32 sums, warp w reduces rows w, w + 8, ...), E^-1 d in FP64
+// every block; FP64, warp w reduces rows w, w + 8, ...)
 template <int KP>
-__device__ __forceinline__ void coarse_solve_block(const float* __restrict__ part,
+__device__ __forceinline__ void coarse_solve_block(const double* __restrict__ part,
                                                    const double* __restrict__ einv, int kc,
                                                    double* d, double* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = wid; k < KP; k += kCgThreads / 32) {
-    float x = 0.f;
+    double x = 0.0;
     for (int b = lane; b < kCgBlocks; b += 32) x += part[k * kCgBlocks + b];
-#pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) d[k] = (double)x;
+    if (lane == 0) d[k] = x;
   }
   __syncthreads();
   if (threadIdx.x < KP) {
@@ -606,8 +622,8 @@ __device__ __forceinline__ void coarse_solve_block(const float* __restrict__ par
 // both: the second use hits L1)
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads, 2)
-    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const float* __restrict__ part1,
-                 const double* __restrict__ einv, int kc, double* coef, float* part2) {
+    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const double* __restrict__ part1,
+                 const double* __restrict__ einv, int kc, double* coef, double* part2) {
   __shared__ double d[KP], cd[KP];
   __shared__ float c[KP];
   coarse_solve_block<KP>(part1, einv, kc, d, cd);
@@ -661,7 +677,7 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 // r.z, r.r (and z.r_prev when flexible) into part + kCgBlocks..
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const float* __restrict__ part2,
+    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const double* __restrict__ part2,
                   const double* __restrict__ einv, int kc, const double* __restrict__ coef,
                   int flexible) {
   __shared__ double d[KP], gd[KP];
@@ -713,8 +729,8 @@ template <int KP>
 static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int flexible,
                                    cudaStream_t st) {
   const long long n3 = 3 * v.npix;
-  float* part1 = reinterpret_cast<float*>(cs.part);  // FP32 partials in the FP64 scratch
-  float* part2 = part1 + (size_t)kCoarseMax * kCgBlocks;
+  double* part1 = cs.part;
+  double* part2 = cs.part + (size_t)kCoarseMax * kCgBlocks;
   k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
   k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef,
                                                       part2);
