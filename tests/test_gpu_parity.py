@@ -230,9 +230,9 @@ def test_tod_nan_rule_matches_reference(prec):
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_tod_from_pinned_memory(prec):
-    """timelines in pinned (page-locked) host memory are read by the ingest
-    kernel directly; the result equals the staged copy of ordinary memory,
-    NaN rule included"""
+    """timelines and noise spectra in pinned (page-locked) host memory are
+    read by the kernels directly; the result equals the staged copy of
+    ordinary memory, NaN rule included"""
     torch = pytest.importorskip("torch")
     prob = small_problem(ndet=4, nseg=4, ns=2048, precision=prec)
     tods = [t.copy() for t in prob["tod"]]
@@ -245,6 +245,9 @@ def test_tod_from_pinned_memory(prec):
                 buf = torch.empty(t.size, dtype=torch.float64, pin_memory=True)
                 buf.numpy()[:] = t
                 mm.set_tod(d, buf.numpy())
+                nb = torch.empty(prob["ispf"][d].size, dtype=torch.float64, pin_memory=True)
+                nb.numpy()[:] = prob["ispf"][d]
+                mm.set_noise(d, nb.numpy())
         out.append((mm.rhs(), mm.solve(precond="bj3", stop_crit=1e-8)["iterations"],
                     mm.solution()))
         mm.close()
