@@ -15,37 +15,41 @@
 
 namespace sg {
 
-// GB300 issues FP64 at ~1/64 of the FP32 rate, so a block's FP64 sums go
-// through shared memory and one warp finishes them (8 values per lane, then
-// a 5-level xor tree) rather than every warp running its own shuffle tree.
 template <int N>
 __device__ __forceinline__ void block_reduce_store(double (&v)[N], double* part, int stride) {
-  __shared__ double sh[N][kCgThreads];
+  __shared__ double sh[N][kCgThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < N; k++) sh[k][threadIdx.x] = v[k];
+  for (int k = 0; k < N; k++) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[k][wid] = x;
+  }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
+  if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < N; k++) {
-      double x = sh[k][lane];
-#pragma unroll
-      for (int w = 1; w < kCgThreads / 32; w++) x += sh[k][w * 32 + lane];
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      if (lane == 0) part[k * stride + blockIdx.x] = x;
+      double s = 0.0;
+      for (int w = 0; w < kCgThreads / 32; w++) s += sh[k][w];
+      part[k * stride + blockIdx.x] = s;
     }
   }
 }
 
-// Every block computes the same total from the per-block partials (warp 0
-// adds them in a fixed order; the others wait).
+// Every block computes the same total from the per-block partials.
 __device__ __forceinline__ double reduce_partials(const double* part) {
+  __shared__ double sh[kCgThreads / 32];
   __shared__ double tot;
-  if (threadIdx.x < 32) {
-    double x = 0.0;
-    for (int i = threadIdx.x; i < kCgBlocks; i += 32) x += part[i];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (threadIdx.x == 0) tot = x;
+  double x = 0.0;
+  for (int i = threadIdx.x; i < kCgBlocks; i += kCgThreads) x += part[i];
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kCgThreads / 32; w++) s += sh[w];
+    tot = s;
   }
   __syncthreads();
   const double r = tot;
