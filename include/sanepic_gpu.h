@@ -271,9 +271,11 @@ int sg_solve_batch(sg_ctx **ctxs, int n, const sg_solve_opts *opts, sg_report *r
 
 /* Times this context's noise filter with each compiled tile shape for its
  * segment length (FP32 tiles of 2^14..2^17 samples: 8192 or 4096 complex
- * points per CTA of the thread-block cluster) on its own timeline and keeps
- * the faster; *cluster_size and *ms (may be NULL) receive the choice and its
- * time per launch.  No reference counterpart. */
+ * points per CTA of the thread-block cluster) on its own timeline, or with
+ * the offset-group operator one whole operator application, and keeps the
+ * faster; *cluster_size and *ms (may be NULL) receive the choice and its
+ * time per launch.  Needs the pointing and every detector's noise
+ * (SG_ERR_STATE otherwise).  No reference counterpart. */
 int sg_autotune(sg_ctx *ctx, int *cluster_size, double *ms);
 
 /* A full 12*nside^2 RING map (write_reduced_map, sanepic.cc:2364-2388). */
