@@ -504,8 +504,9 @@ cudaError_t loop_end_launch(LoopState* s, const CgScalars* sc, double* hist,
 // definite whatever their rounding (the same U on both sides, E exact in
 // FP64).  Their products with a vector run in FP32 (GB300's
 // FP64 rate would make kc FP64 FMAs per element cost more than reading U);
-// the per-thread sums are FP32, the warp sums double-FP32, the block
-// partials, their fixed-order reductions and the coarse solves FP64.  Every
+// the per-thread sums are FP32, the warp sums double-FP32, the block sums
+// FP64 (kept as double-FP32 pairs), their fixed-order reductions
+// double-FP32 and the coarse solves FP64.  Every
 // block of the kernel that needs c (or c - g) re-reduces the partials
 // itself, so the coarse solve costs no launch.  The rounding makes the
 // preconditioner slightly inexact, which flexible PCG absorbs.
@@ -530,13 +531,15 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float b, float bl) 
   lo = e - (hi - s);
 }
 
-// part[k][block] = the block's sum of acc[k] (FP64).  A warp first adds its
+// part[k][block] = the block's sum of acc[k] (FP64, stored as a double-FP32
+// pair so that every block can re-reduce the partials with FP32
+// instructions).  A warp first adds its
 // lanes' FP32 accumulators as double-FP32 pairs through a fixed xor tree
 // (FP32 instructions only), lane k takes total k and widens it to FP64, and
 // KP threads add the warps in order: GB300's FP64 rate would make an FP64
 // shuffle tree of KP values per warp cost more than the kernel's loop.
 template <int KP>
-__device__ __forceinline__ void coarse_block_store(float (&acc)[KP], double* part) {
+__device__ __forceinline__ void coarse_block_store(float (&acc)[KP], float2* part) {
   __shared__ double sh[KP][kCgThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float mh = 0.f, ml = 0.f;  // this lane's total: k = lane
@@ -557,7 +560,8 @@ __device__ __forceinline__ void coarse_block_store(float (&acc)[KP], double* par
     double t = 0.0;
 #pragma unroll
     for (int w = 0; w < kCgThreads / 32; w++) t += sh[threadIdx.x][w];
-    part[threadIdx.x * kCgBlocks + blockIdx.x] = t;
+    const float hi = (float)t;
+    part[threadIdx.x * kCgBlocks + blockIdx.x] = make_float2(hi, (float)(t - (double)hi));
   }
 }
 
@@ -565,7 +569,7 @@ __device__ __forceinline__ void coarse_block_store(float (&acc)[KP], double* par
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
     k_coarse_dots(const uint16_t* __restrict__ U, long long n3, const double* __restrict__ v,
-                  double* part) {
+                  float2* part) {
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
@@ -598,17 +602,23 @@ __global__ void __launch_bounds__(kCgThreads)
 }
 
 // out[k] = (E^-1 d)[k], d[k] = sum_b part[k][b] in a fixed order (identical in
-// every block; FP64, warp w reduces rows w, w + 8, ...)
+// every block; double-FP32 sums, warp w reduces rows w, w + 8, ...), E^-1 d
+// in FP64
 template <int KP>
-__device__ __forceinline__ void coarse_solve_block(const double* __restrict__ part,
+__device__ __forceinline__ void coarse_solve_block(const float2* __restrict__ part,
                                                    const double* __restrict__ einv, int kc,
                                                    double* d, double* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = wid; k < KP; k += kCgThreads / 32) {
-    double x = 0.0;
-    for (int b = lane; b < kCgBlocks; b += 32) x += part[k * kCgBlocks + b];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) d[k] = x;
+    float hi = 0.f, lo = 0.f;
+    for (int b = lane; b < kCgBlocks; b += 32) {
+      const float2 q = part[k * kCgBlocks + b];
+      df_add(hi, lo, q.x, q.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      df_add(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
+    if (lane == 0) d[k] = (double)hi + (double)lo;
   }
   __syncthreads();
   if (threadIdx.x < KP) {
@@ -626,8 +636,8 @@ __device__ __forceinline__ void coarse_solve_block(const double* __restrict__ pa
 // both: the second use hits L1)
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads, 2)
-    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const double* __restrict__ part1,
-                 const double* __restrict__ einv, int kc, double* coef, double* part2) {
+    k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const float2* __restrict__ part1,
+                 const double* __restrict__ einv, int kc, double* coef, float2* part2) {
   __shared__ double d[KP], cd[KP];
   __shared__ float c[KP];
   coarse_solve_block<KP>(part1, einv, kc, d, cd);
@@ -681,7 +691,7 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 // r.z, r.r (and z.r_prev when flexible) into part + kCgBlocks..
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
-    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const double* __restrict__ part2,
+    k_coarse_post(CgVecs v, const uint16_t* __restrict__ U, const float2* __restrict__ part2,
                   const double* __restrict__ einv, int kc, const double* __restrict__ coef,
                   int flexible) {
   __shared__ double d[KP], gd[KP];
@@ -733,8 +743,8 @@ template <int KP>
 static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int flexible,
                                    cudaStream_t st) {
   const long long n3 = 3 * v.npix;
-  double* part1 = cs.part;
-  double* part2 = cs.part + (size_t)kCoarseMax * kCgBlocks;
+  float2* part1 = reinterpret_cast<float2*>(cs.part);  // same 8 bytes per partial
+  float2* part2 = part1 + (size_t)kCoarseMax * kCgBlocks;
   k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
   k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef,
                                                       part2);
