@@ -41,7 +41,9 @@
 // phase: the unit holding frequencies k and the unit holding M-k sit in
 // lanes l and l^17 of one warp (l^16 for row R/2) and swap their values with
 // shuffles.  Only row 0, whose partners are in the same row, goes through
-// shared memory.
+// shared memory.  The inverse-from-spectrum variant first stages its CTA's
+// spectrum slots in shared memory where the units keep them (one coalesced
+// pass), then exchanges partners the same way.
 //
 // Twiddles: the inner ones (W_R, W_C) come from per-length shared tables,
 // the four-step ones (W_M) from two shared tables (W_M^j = W_M^{64 jh} W_M^{jl})
