@@ -59,9 +59,9 @@ STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
 # --compare-diag: 24 iterations; block-Jacobi needs 21).
 REFERENCE_ITERS_TO_1E6 = {"c2_64det_nside256": 24}
 # DRAM bytes (read + write) of one noise-filter tile of 131072 FP32 samples,
-# from the ncu capture in profiles/noise_filter_c2_8det.md (343.7 MB over
+# from the ncu capture in profiles/noise_filter_c2_8det.md (354.5 MB over
 # 384 tiles); traffic grows with the tiles, so a full launch is this x tiles.
-FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 343.67e6 / 384
+FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 354.46e6 / 384
 # DRAM bytes (read + write) of one group noise weighting (forward FFTs, 3 x 3
 # mixing, inverse FFTs) on the bench workloads with one group of 48 x 131072
 # samples, from the ncu capture in profiles/group_noise_weighting_c2_8det.md
