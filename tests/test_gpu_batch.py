@@ -82,3 +82,18 @@ def test_autotune_keeps_the_group_operator():
     assert np.linalg.norm(y1 - y0) <= 1e-5 * np.linalg.norm(y0)
     mm.rhs()
     assert mm.solve(precond="bj3", stop_crit=1e-10)["converged"]
+
+
+def test_autotune_needs_the_noise():
+    """the autotuner times the operator, so it refuses a context without
+    every detector's noise spectrum"""
+    spec = synth.ProblemSpec("atn", ndet=2, nside=16, nseg=2, ns=2048, problem=48, precision="f32")
+    prob = synth.make_problem(spec)
+    mm = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, precision="f32")
+    mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], sg.detectors_from_angles(prob["angles"]),
+                    prob.get("isampmin"))
+    mm.set_noise(0, prob["ispf"][0])
+    with pytest.raises(sg.SanepicError):
+        mm.autotune()
+    mm.set_noise(1, prob["ispf"][1])
+    assert mm.autotune()["cluster_size"] >= 1
