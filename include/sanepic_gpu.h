@@ -12,7 +12,11 @@
  * Errors: every int-returning call returns SG_OK (0) or a negative SG_ERR_*
  * code and never exits the process (the reference calls exit()).  The last
  * error message of a context is available from sg_last_error().
- * Threading: one context per host thread; contexts share no global state.
+ * Threading: one context per host thread.  Contexts share only this
+ * process-wide state, each piece guarded by a mutex: the cache of batch
+ * graphs of sg_solve_batch (keyed by the contexts it solves, dropped when one
+ * is destroyed), the per-device shared-memory opt-in of the tensor-core GEMM,
+ * and the no-allocation entry point's device table and its address per GPU.
  * Layouts: per-sample arrays are [det][seg][sample] (sanepic.cc:749, 874);
  * compact maps are [I | Q | U], npix each, observed pixels in ascending RING
  * order (sanepic.cc:904-921); full maps are 12*nside^2 RING doubles with 0 at
@@ -167,7 +171,8 @@ int sg_noise_filter(sg_ctx *ctx, const double *in, double *out);
  * SG_ERR_UNSUPPORTED.  The FFT twiddle table lives in one 8.5 KiB
  * library-static device array per GPU, shared by every call: calls that
  * overlap on the GPU race on it.  The first call on a device looks the array
- * up (cudaGetSymbolAddress), so make it before any stream capture. */
+ * up (cudaGetSymbolAddress) and the first call for each ns prepares that
+ * kernel, so make one call per device and ns before any stream capture. */
 int sg_noise_filter_noalloc(const float *in, float *out, const float *filt, long ns,
                             long ntiles, long tiles_per_filter, void *stream);
 

@@ -24,6 +24,8 @@ LIB_PATH = os.path.join(HERE, "lib", "libsanepic_gpu.so")
 D2PI = 6.2831853071795864769252867665590057683943387987502
 
 SG_OK = 0
+SG_ERR_ARG = -1
+SG_ERR_UNSUPPORTED = -5
 ERRORS = {-1: "SG_ERR_ARG", -2: "SG_ERR_CUDA", -3: "SG_ERR_STATE", -4: "SG_ERR_POINTING",
           -5: "SG_ERR_UNSUPPORTED", -6: "SG_ERR_PRECOND", -7: "SG_ERR_NOT_CONVERGED"}
 PRECISION = {"f64": 0, "f32": 1}

@@ -19,6 +19,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <cstdint>
 
 #include "sg_kernels.h"
@@ -274,7 +276,8 @@ bool make_map(CUtensorMap* m, const void* ptr, int rows, int cols, int box_rows)
 }
 
 // the large dynamic shared-memory opt-in, once per device (before any graph
-// capture uses the kernels)
+// capture uses the kernels); contexts on several host threads share it
+std::mutex g_prepared_mu;
 bool g_prepared[64] = {};
 
 template <int BN>
@@ -294,6 +297,7 @@ cudaError_t gemm_prepare() {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_prepared_mu);
   if (dev >= 0 && dev < 64 && g_prepared[dev]) return cudaSuccess;
   e = cudaFuncSetAttribute(k_gemm_bf16<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)gemm_smem_bytes<128>());

@@ -16,12 +16,14 @@
 // holds until the process exits.  Host code never dereferences the array's
 // name (on the host it is only a stand-in symbol); the first call on each
 // device resolves its device address with cudaGetSymbolAddress, with that
-// device current, and caches it.  That first call should therefore be made
-// before any stream capture begins.  All calls share the table and rewrite it
+// device current, and caches it, and the first call for each tile length
+// sets that kernel's launch attributes (and may load it).  So make one call
+// per device and tile length before any stream capture begins.  All calls share the table and rewrite it
 // for their own tile length, so two calls that overlap on the GPU (different
 // streams, different lengths) race on it; nothing in it has to start at zero.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -57,6 +59,10 @@ extern "C" int sg_noise_filter_noalloc(const float* in, float* out, const float*
                                        long ntiles, long tiles_per_filter, void* stream) {
   if (!in || !out || !filt || ntiles < 1 || tiles_per_filter < 1) return SG_ERR_ARG;
   if (ns < 256 || (ns & (ns - 1)) != 0 || ns > kNoAllocMaxNs) return SG_ERR_UNSUPPORTED;
+  // every tile index is below ntiles, so a larger group size only ever selects
+  // row 0: clamp it before it is narrowed to the kernel's int
+  if (tiles_per_filter > ntiles) tiles_per_filter = ntiles;
+  if (tiles_per_filter > INT_MAX) return SG_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SG_ERR_CUDA;
   void* addr = nullptr;

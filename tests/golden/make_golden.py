@@ -10,7 +10,7 @@ seeded synthetic problems and stores, per problem:
 
 The inputs are stored (not regenerated) so the fixtures do not depend on the
 host's libm.  Usage (needs the reference checkout, this container only):
-    python tests/golden/make_golden.py [--ref-src /root/reference/src/sanepic.cc]
+    python tests/golden/make_golden.py --ref-src <reference checkout>/src/sanepic.cc
 """
 from __future__ import annotations
 
@@ -72,7 +72,7 @@ def run_reference(prob, exe, workdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference/src/sanepic.cc")
+    ap.add_argument("--ref-src", required=True, help="the reference's src/sanepic.cc")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref",
                            f"REFERENCE_SRC={a.ref_src}"])

@@ -46,3 +46,15 @@ def test_struct_layouts_match_header():
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(RuntimeError):
         sg.load_library(str(tmp_path / "nope.so"))
+
+
+def test_noalloc_rejects_oversized_group_before_any_cuda_call(libpath):
+    # a filter group larger than INT_MAX tiles (and not larger than ntiles)
+    # cannot be narrowed to the kernel's int: refused as an argument error,
+    # before any CUDA call (this runs without a GPU)
+    sg.load_library(libpath)
+    rc = sg.noise_filter_noalloc(16, 16, 16, 4096, 1 << 40, (1 << 31) + 5, None)
+    assert rc == sg.SG_ERR_ARG
+    # sizes outside [256, 131072] are refused before any CUDA call too
+    assert sg.noise_filter_noalloc(16, 16, 16, 1 << 18, 1, 1, None) == sg.SG_ERR_UNSUPPORTED
+    assert sg.noise_filter_noalloc(0, 16, 16, 4096, 1, 1, None) == sg.SG_ERR_ARG

@@ -3,7 +3,9 @@
 they run a real-time loop).  It must give what the regular context-based
 sg_noise_filter gives, call after call, while allocating nothing itself: the
 test owns every device buffer (torch tensors) and passes raw pointers through
-the C ABI.  This file is collected last on purpose."""
+the C ABI, checks that the device's free memory does not move across the
+calls, and replays one call captured in a CUDA graph.  This file is collected
+last on purpose."""
 import numpy as np
 import pytest
 
@@ -27,6 +29,10 @@ def filter_rows(prob, ns):
     return np.stack(rows)
 
 
+def rel_rms(got, want):
+    return np.sqrt(np.mean((got - want) ** 2)) / np.sqrt(np.mean(want ** 2))
+
+
 @pytest.mark.parametrize("ns", [4096, 131072])
 def test_noalloc_filter_matches_context_filter(ns):
     torch = pytest.importorskip("torch")
@@ -43,16 +49,37 @@ def test_noalloc_filter_matches_context_filter(ns):
     xin = torch.tensor(x, dtype=torch.float32, device="cuda")
     out = torch.empty_like(xin)
     stream = torch.cuda.current_stream().cuda_stream
+    # one call per device and tile length before anything is measured or
+    # captured: it looks up the static table and prepares the kernel
+    assert sg.noise_filter_noalloc(xin.data_ptr(), out.data_ptr(), filt.data_ptr(), ns,
+                                   ndet * nseg, nseg, stream) == sg.SG_OK
     for _ in range(2):  # two calls in a row share the static twiddle table
         out.fill_(float("nan"))
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
         rc = sg.noise_filter_noalloc(xin.data_ptr(), out.data_ptr(), filt.data_ptr(), ns,
                                      ndet * nseg, nseg, stream)
-        assert rc == sg.SG_OK
         torch.cuda.synchronize()
-        got = out.double().cpu().numpy()
-        rel = np.sqrt(np.mean((got - want) ** 2)) / np.sqrt(np.mean(want ** 2))
-        assert rel < 2e-6, rel
+        free1, _ = torch.cuda.mem_get_info()
+        assert rc == sg.SG_OK
+        assert free1 == free0, (free0, free1)  # the call allocated no device memory
+        got = out.cpu().double().numpy()  # host copy: no device allocation
+        assert rel_rms(got, want) < 2e-6
+    # the same call recorded while a CUDA graph is being captured, then replayed
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side):
+            rc = sg.noise_filter_noalloc(xin.data_ptr(), out.data_ptr(), filt.data_ptr(), ns,
+                                         ndet * nseg, nseg, side.cuda_stream)
+    torch.cuda.current_stream().wait_stream(side)
+    assert rc == sg.SG_OK
+    out.fill_(float("nan"))
+    g.replay()
+    torch.cuda.synchronize()
+    assert rel_rms(out.cpu().double().numpy(), want) < 2e-6
     # a tile longer than the stated maximum is refused, not run
     rc = sg.noise_filter_noalloc(xin.data_ptr(), out.data_ptr(), filt.data_ptr(), 2 * 131072,
                                  1, 1, stream)
-    assert rc == -5  # SG_ERR_UNSUPPORTED
+    assert rc == sg.SG_ERR_UNSUPPORTED
