@@ -263,8 +263,11 @@ def run_ours(args):
         traffic = FILTER_DRAM_BYTES_PER_TILE_131072_F32 * spec.ndet * spec.nseg
     if dom == "group_noise_weighting" and (args.config, spec.precision) in GROUP_NW_DRAM_BYTES:
         traffic = GROUP_NW_DRAM_BYTES[(args.config, spec.precision)]
-    # ---- plain block-Jacobi vs the reference's diagonal (same workload) -------
+    # ---- accuracy of the timed solves: maps against an FP64 solve -----------
     extra = {}
+    if not args.no_map_error:
+        extra["map_error"] = map_error(sg, mm, spec, prob, dets, precond, stream, args)
+    # ---- plain block-Jacobi vs the reference's diagonal (same workload) -------
     if args.compare_diag:
         rep_d = device_step("diag")
         extra["diag_precond"] = {"iterations": rep_d["iterations"],
@@ -367,6 +370,11 @@ def run_ours(args):
                          "loss": "-(r.z)^2/((z.Az)(r.M r)), A-cosine of the corrected direction"},
         }
         line["mlp_gemm"] = mlp_gemm_roofline(sg, mm)
+    if not args.no_per_detector:
+        line["per_detector"] = per_detector(sg, spec, prob, dets, stream, args)
+    if args.c3 and spec.name != C3:
+        mm.close()
+        line["c3"] = c3_block(sg, stream, args)
     if not args.no_cpu_baseline and rank == 0:
         line["cpu_baseline"] = reference_cpu(
             args, spec, iters_for_projection=extra.get("diag_precond", {}).get("iterations")
@@ -376,6 +384,193 @@ def run_ours(args):
     mm.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+C3 = "c3_256det_nside512_hwp"
+
+
+def _map_errs(x, want, npix):
+    """Per map: max and RMS error of compact x against want, relative to
+    want's max |.| and RMS, also with the mean difference removed (the bin-0
+    override of sanepic.cc:536-537 leaves the I monopole nearly free)."""
+    out = {}
+    for c, k in enumerate("IQU"):
+        w = want[c * npix:(c + 1) * npix]
+        d = x[c * npix:(c + 1) * npix] - w
+        d0 = d - d.mean()
+        rw, mw = float(np.sqrt(np.mean(w * w))), float(np.max(np.abs(w)))
+        out[k] = {"rms": float(np.sqrt(np.mean(d * d))) / rw, "max": float(np.max(np.abs(d))) / mw,
+                  "rms_monopole_removed": float(np.sqrt(np.mean(d0 * d0))) / rw,
+                  "max_monopole_removed": float(np.max(np.abs(d0))) / mw}
+    return out
+
+
+def map_error(sg, mm, spec, prob, dets, precond, stream, args):
+    """The timed FP32 solves (learned mode and plain block-Jacobi) against an
+    FP64 solve of the same problem (the library's FP64 operator, block-Jacobi
+    PCG to |r|^2/|b|^2 <= 1e-15), at the metric's stop (|r|/|b| <= 1e-6) and
+    at tighter stops: per stop the solve's device time, its iterations and the
+    largest relative RMS map error, so that the time each mode needs for maps
+    within 1e-5 of the FP64 solve is on the record too."""
+    t = time.time()
+    m64 = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                      omega=prob["omega"], precision="f64", device=mm.device)
+    m64.set_stream(stream.cuda_stream)
+    m64.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+    for d in range(spec.ndet):
+        m64.set_noise(d, prob["ispf"][d])
+        m64.set_tod(d, prob["tod"][d])
+    m64.rhs()
+    r64 = m64.solve(precond="bj3", stop_crit=1e-15, maxiter=args.maxiter)
+    x64 = m64.solution()
+    m64.close()
+    npix = mm.npix
+    res = {"against": "FP64 solve of the same problem by the library's FP64 operator "
+                      "(block-Jacobi PCG to |r|^2/|b|^2 <= 1e-15)",
+           "fp64_iterations": r64["iterations"], "fp64_crit": r64["crit"],
+           "fp64_seconds": time.time() - t, "bar": 1e-5}
+    for pc in dict.fromkeys((precond, args.precond)):
+        key = "learned" if pc == "learned" else pc
+        sweep = []
+        for stop in (STOP_CRIT, 1e-13, 1e-14):
+            mm.rhs()
+            rep = mm.solve(precond=pc, stop_crit=stop, maxiter=args.maxiter)
+            errs = _map_errs(mm.solution(), x64, npix)
+            worst = max(errs[k]["rms"] for k in "IQU")
+            worst0 = max(errs[k]["rms_monopole_removed"] for k in "IQU")
+            if stop == STOP_CRIT:
+                res[key] = errs
+            sweep.append({"stop_crit": stop, "iterations": rep["iterations"],
+                          "converged": bool(rep["converged"]),
+                          "solve_device_s": rep["device_seconds"], "max_rms": worst,
+                          "max_rms_monopole_removed": worst0})
+        res[key + "_by_stop"] = sweep
+        ok = [r for r in sweep if r["converged"] and r["max_rms"] <= 1e-5]
+        res[key + "_solve_s_to_1e-5_maps"] = ok[0]["solve_device_s"] if ok else None
+    return res
+
+
+def per_detector(sg, spec, prob, dets, stream, args):
+    """The same workload through the per-detector operator (what detectors
+    with distinct focal-plane offsets run): plain block-Jacobi solve time and
+    the operator kernels' HBM throughput."""
+    import torch
+    os.environ["SANEPIC_GPU_GROUP_FILTER"] = "0"
+    try:
+        mp = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                         omega=prob["omega"], precision=spec.precision, device=torch.cuda.current_device())
+        mp.set_stream(stream.cuda_stream)
+        mp.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+    finally:
+        os.environ.pop("SANEPIC_GPU_GROUP_FILTER", None)
+    for d in range(spec.ndet):
+        mp.set_noise(d, prob["ispf"][d])
+        mp.set_tod(d, prob["tod"][d])
+    assert not mp.group_mode()[0]
+    for _ in range(2):
+        mp.rhs()
+        mp.solve(precond=args.precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    ev0.record(stream)
+    for _ in range(reps):
+        mp.rhs()
+        rep = mp.solve(precond=args.precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sec = ev0.elapsed_time(ev1) / reps / 1e3
+    prof = mp.profile_operator(reps=5)
+    esz = 4 if spec.precision == "f32" else 8
+    ns_all = spec.ndet * spec.nseg * spec.ns
+    ng = mp.group_mode()[1] * spec.nseg * spec.ns
+    npix = mp.npix
+    m1 = spec.ns // 2 + 1
+    kbytes = {"k_project": ng * (4 + 2 * esz) + ns_all * esz + npix * 4 * esz,
+              "k_noise_filter": ns_all * 2 * esz + spec.ndet * m1 * esz,
+              "k_detsum": ns_all * esz + ng * 4 * esz,
+              "k_pt": ng * (4 + 2 * esz + 4 * esz) + npix * (3 * 8 + 8 + 4)}
+    kms = {"k_project": prof["p_ms"], "k_noise_filter": prof["filter_ms"],
+           "k_detsum": prof["detsum_ms"], "k_pt": prof["pt_ms"]}
+    hbm, _ = peaks()
+    mp.close()
+    return {"operator": "per detector (SANEPIC_GPU_GROUP_FILTER=0)", "precond": args.precond,
+            "seconds": sec, "iterations": rep["iterations"], "iter_per_sec": rep["iter_per_sec"],
+            "kernels": {k: {"ms": kms[k], "GBps": kbytes[k] / (kms[k] * 1e-3) / 1e9,
+                            "frac": kbytes[k] / (kms[k] * 1e-3) / 1e9 / hbm, "bytes": kbytes[k]}
+                        for k in kbytes}}
+
+
+def c3_block(sg, stream, args):
+    """The largest single-GPU configuration (256 detectors, NSIDE 512, HWP,
+    48 x 131,072 samples = 1.6e9 samples, FP32 operator), inputs resident:
+    plain block-Jacobi PCG and the learned mode (coarse space trained on
+    this workload and judged by plain PCG on a held-out problem), each from
+    x0 = 0 to |r|/|b| <= 1e-6, with the learned solve's map error against an
+    FP64 solve (the library's FP64 operator, block-Jacobi to 1e-15)."""
+    import torch
+    spec = synth.spec_from_name(C3)
+    t0 = time.time()
+    prob = synth.make_problem(spec)
+    gen_s = time.time() - t0
+    dets = sg.detectors_from_angles(prob["angles"])
+    mm = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                     omega=prob["omega"], precision=spec.precision, device=torch.cuda.current_device())
+    mm.set_stream(stream.cuda_stream)
+    mm.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+    for d in range(spec.ndet):
+        mm.set_noise(d, prob["ispf"][d])
+        mm.set_tod(d, prob["tod"][d])
+    tl = time.time()
+    learn = mm.learn_train(npairs=args.learn_pairs, steps=-1, coarse_k=args.coarse_k,
+                           coarse_vectors=args.coarse_vectors)
+    learn_s = time.time() - tl
+    res = {"workload": C3, "ndet": spec.ndet, "nside": spec.nside, "nseg": spec.nseg,
+           "ns": spec.ns, "hwp": True, "samples": spec.ndet * spec.nseg * spec.ns,
+           "npix_obs": mm.npix, "generation_s": gen_s, "learn_s": learn_s,
+           "learned_part": {0: "none: plain block-Jacobi PCG", 1: "patch network",
+                            2: "coarse space"}[learn["kind"]],
+           "validation": {"plain_iterations": learn["val_plain_iters"],
+                          "coarse_iterations": learn["val_coarse_iters"],
+                          "plain_ms": learn["val_plain_ms"], "coarse_ms": learn["val_coarse_ms"]}}
+    sols = {}
+    for pc in ("bj3", "learned"):
+        for _ in range(2):
+            mm.rhs()
+            mm.solve(precond=pc, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 3
+        ev0.record(stream)
+        for _ in range(reps):
+            mm.rhs()
+            rep = mm.solve(precond=pc, stop_crit=STOP_CRIT, maxiter=args.maxiter)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        res["plain" if pc == "bj3" else "learned"] = {
+            "seconds": ev0.elapsed_time(ev1) / reps / 1e3, "iterations": rep["iterations"],
+            "converged": bool(rep["converged"])}
+        sols[pc] = mm.solution()
+    prof = mm.profile_operator(reps=5)
+    res["operator_ms"] = prof
+    npix = mm.npix
+    mm.close()
+    m64 = sg.MapMaker(spec.ns, spec.nseg, spec.ndet, spec.nside, hwp=spec.hwp,
+                      omega=prob["omega"], precision="f64", device=torch.cuda.current_device())
+    m64.set_stream(stream.cuda_stream)
+    m64.set_pointing(prob["ra"], prob["dec"], prob["psi"], dets, prob["isampmin"])
+    for d in range(spec.ndet):
+        m64.set_noise(d, prob["ispf"][d])
+        m64.set_tod(d, prob["tod"][d])
+    m64.rhs()
+    r64 = m64.solve(precond="bj3", stop_crit=1e-15, maxiter=args.maxiter)
+    x64 = m64.solution()
+    m64.close()
+    res["map_error"] = {"against": "library FP64 operator, block-Jacobi PCG to 1e-15",
+                        "fp64_iterations": r64["iterations"],
+                        "plain": _map_errs(sols["bj3"], x64, npix),
+                        "learned": _map_errs(sols["learned"], x64, npix)}
+    return res
 
 
 def mlp_gemm_roofline(sg, mm):
@@ -602,6 +797,9 @@ def main():
     ap.add_argument("--learn-steps", type=int, default=1500)
     ap.add_argument("--coarse-k", type=int, default=0)
     ap.add_argument("--coarse-vectors", type=int, default=0)
+    ap.add_argument("--no-map-error", action="store_true")
+    ap.add_argument("--no-per-detector", action="store_true")
+    ap.add_argument("--c3", type=int, default=1, help="add the C3 block (1) or not (0)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -182,6 +182,7 @@ class MapMaker:
         self.L = load_library()
         self.ns, self.nseg, self.ndet, self.nside = ns, nseg, ndet, nside
         self.precision = precision
+        self.device = device
         desc = SgDesc(ns, nseg, ndet, nside, 1, int(bool(hwp)), float(omega),
                       PRECISION[precision], device)
         h = ctypes.c_void_p()

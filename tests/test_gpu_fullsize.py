@@ -1,0 +1,159 @@
+"""Map-level parity at full size, through the C ABI:
+
+* 12 x 65,536 samples per detector at NSIDE 64 against the reference's own
+  output maps (tests/golden/c1_*): the converged 4-detector problem in FP64
+  with the reference's diagonal preconditioner and in FP32 with block-Jacobi,
+  and the 1-detector workload, where the reference stops at its iteration
+  limit without converging;
+* the benchmarked workload (64 detectors, NSIDE 256, 48 x 131,072 samples,
+  FP32 operator) against an FP64 solve by an operator written independently
+  of the library (tests/fp64_gpu_oracle.py: torch float64, cuFFT, index_add_).
+
+Every comparison prints max and RMS error relative to the reference map, with
+and without the I monopole removed; the bar is 1e-5 relative RMS."""
+import numpy as np
+import pytest
+
+import oracle
+import sanepic_gb300 as sg
+from fullsize_util import map_errors, regenerate
+from sanepic_gb300 import build
+from sanepic_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+MAPS = ("I", "Q", "U")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    build.build()
+
+
+def report(tag, got, ref):
+    out = {}
+    for k in MAPS:
+        e = map_errors(got[k], ref[k])
+        e0 = map_errors(got[k], ref[k], remove_monopole=True)
+        out[k] = (e, e0)
+        print(f"{tag} {k}: rms {e['rms']:.3e} max {e['max']:.3e} "
+              f"(monopole removed: rms {e0['rms']:.3e} max {e0['max']:.3e})")
+    return out
+
+
+def solve_maps(mm, precond, stop, maxiter=2000):
+    mm.rhs()
+    rep = mm.solve(precond=precond, stop_crit=stop, maxiter=maxiter)
+    return rep, {k: mm.get_map(k) for k in MAPS}
+
+
+def test_c1_4det_maps_vs_reference():
+    spec, prob, ref, log = regenerate("c1_4det_nside64", lambda p: oracle.Setup(p).pix)
+    mm = sg.from_problem(prob, precision="f64")
+    assert np.array_equal(mm.get_map("HITS"), ref["HITS"])
+    assert np.array_equal(mm.get_map("POL_HITS"), ref["POL_HITS"])
+    for k in ("NVAR", "COS2P", "SIN2P"):
+        np.testing.assert_allclose(mm.get_map(k), ref[k], rtol=1e-10, atol=1e-300, err_msg=k)
+    # FP64, the reference's preconditioner and stop
+    rep, maps = solve_maps(mm, "diag", 1e-15)
+    assert rep["converged"] and abs(rep["iterations"] - log["iterations"]) <= 1
+    for k, (e, _) in report("c1_4det f64 diag 1e-15", maps, ref).items():
+        assert e["rms"] < 1e-7, (k, e)
+    mm.close()
+    # FP32 operator, block-Jacobi.  Stopped at |r|/|b| <= 1e-6 the maps are
+    # a few 1e-5 from the reference's (the I monopole, which the bin-0
+    # override leaves nearly free, 3e-4); run further they meet 1e-5.
+    mm = sg.from_problem(prob, precision="f32")
+    rep, maps = solve_maps(mm, "bj3", 1e-12)
+    assert rep["converged"]
+    for k, (e, e0) in report("c1_4det f32 bj3 1e-12", maps, ref).items():
+        assert e0["rms"] < 5e-5, (k, e0)
+        assert e["rms"] < 1e-3, (k, e)
+    rep, maps = solve_maps(mm, "bj3", 1e-14)
+    assert rep["converged"]
+    for k, (e, e0) in report("c1_4det f32 bj3 1e-14", maps, ref).items():
+        assert e0["rms"] < 1e-5, (k, e0)
+    mm.close()
+
+
+def test_c1_1det_maps_vs_reference_at_the_iteration_limit():
+    # One detector angle leaves most Q/U blocks nearly singular: the
+    # reference runs its 2000 iterations without converging, and two FP64
+    # implementations of the same PCG (different summation orders) end
+    # apart by a few 1e-5 (the CPU oracle: 3.7e-5 relative RMS on I).
+    spec, prob, ref, log = regenerate("c1_1det_nside64", lambda p: oracle.Setup(p).pix)
+    mm = sg.from_problem(prob, precision="f64")
+    assert np.array_equal(mm.get_map("HITS"), ref["HITS"])
+    rep, maps = solve_maps(mm, "diag", 1e-15, maxiter=2000)
+    assert rep["iterations"] == 2000 and not rep["converged"]
+    for k, (e, _) in report("c1_1det f64 diag 2000 iterations", maps, ref).items():
+        assert e["rms"] < 3e-4, (k, e)
+    mm.close()
+
+
+def test_fp64_torch_operator_matches_cpu_oracle():
+    # the independent FP64 operator itself, against the CPU restatement
+    from fp64_gpu_oracle import Fp64Operator
+    torch = pytest.importorskip("torch")
+    for hwp in (False, True):
+        spec = synth.ProblemSpec("t", ndet=3, nside=16, nseg=4, ns=2048, hwp=hwp, fknee=0.1,
+                                 problem=11)
+        prob = synth.make_problem(spec)
+        s = oracle.Setup(prob)
+        op = Fp64Operator(prob)
+        x = np.random.default_rng(1).standard_normal(3 * s.npix)
+        want = s.apply(x)
+        msk = oracle.masked(s)
+        want[msk] = 0.0
+        got = op.apply(torch.tensor(x, dtype=torch.float64, device="cuda")).cpu().numpy()
+        assert np.abs(got - want).max() < 1e-11 * np.abs(want).max()
+        b_o, _ = s.rhs(prob["tod"])
+        b_o[msk] = 0.0
+        b_t = op.rhs(prob["tod"]).cpu().numpy()
+        assert np.abs(b_t - b_o).max() < 1e-11 * np.abs(b_o).max()
+
+
+def test_c2_maps_vs_independent_fp64_operator():
+    # the benchmarked workload: FP32 operator, block-Jacobi PCG and the
+    # learned mode, both stopped at |r|/|b| <= 1e-6, against an FP64 solve
+    # with an operator that shares no code with the library
+    from fp64_gpu_oracle import Fp64Operator
+    torch = pytest.importorskip("torch")
+    spec = synth.spec_from_name("c2_64det_nside256")
+    prob = synth.make_problem(spec)
+    op = Fp64Operator(prob)
+    b = op.rhs(prob["tod"])
+    xt, it_t, crit_t = op.solve(b, stop=1e-24, maxiter=300)
+    print(f"independent FP64 solve: {it_t} iterations, crit {crit_t:.2e}")
+    assert crit_t < 1e-20
+    want = op.compact_to_ring_order(xt)
+    del op, b, xt
+    torch.cuda.empty_cache()
+    mm = sg.from_problem(prob, precision="f32")
+    assert mm.npix == want.shape[1]
+    errs = {}
+    ref = {k: want[c] for c, k in enumerate(MAPS)}
+    for mode in ("bj3", "learned"):
+        if mode == "learned":
+            mm.learn_train(npairs=512, steps=-1)
+        for stop in (1e-12, 1e-14):
+            mm.rhs()
+            rep = mm.solve(precond=mode, stop_crit=stop)
+            assert rep["converged"]
+            x = mm.solution().reshape(3, -1)
+            full = {k: x[c] for c, k in enumerate(MAPS)}
+            errs[(mode, stop)] = report(f"c2 f32 {mode} {stop:g} ({rep['iterations']} iterations) "
+                                        "vs independent FP64", full, ref)
+    mm.close()
+    for (mode, stop), e in errs.items():
+        for k, (e1, e0) in e.items():
+            # at |r|/|b| <= 1e-6 the Q/U maps are up to 1e-4 from the FP64
+            # solve (plain block-Jacobi; the learned mode's are closer); at
+            # |r|/|b| <= 1e-7 every map is within the 1e-5 bar.  The I
+            # monopole is compared apart: the bin-0 override
+            # (sanepic.cc:536-537) weights it 1e-6 times less, so a solve
+            # stopped at 1e-12..1e-14 leaves it where x0 = 0 put it, while
+            # the independent solve runs to 1e-24 and moves it (about 2e-3
+            # of the I map's RMS, printed above)
+            got = e0 if k == "I" else e1
+            assert got["rms"] < (2e-4 if stop == 1e-12 else 1e-5), (mode, stop, k, got)
