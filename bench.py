@@ -24,13 +24,12 @@ The operator kernels (P, the noise filter, the per-group detector sums, P^T)
 are timed live with CUDA events for the roofline against their algorithmic
 bytes; the network's tensor-core GEMM is timed against the measured BF16 peak.
 
---impl reference times the reference's CPU algorithm on the host cores: the
-oracle port (the FP64 restatement of sanepic.cc's operator, same operation
-order), one process per core as the reference's MPI workers, on a bounded
-sample of the workload, projected linearly in samples to the full problem and
-to the iterations the reference's diagonal-preconditioned PCG needs.
-(The reference binary itself is built only where its source is available; the
-GPU host has neither the source nor an x86 CPU.)
+--impl reference times the reference's path on the host cores for the whole
+workload: the threaded port of sanepic.cc's algorithm (oracle/cgpar.c: the
+FP64 restatement in the reference's parallel layout, its diagonal
+preconditioner and PCG), each run from scratch to |r|/|b| <= 1e-6.  The
+reference binary itself is built only where its source is (not on the GPU
+host); oracle/calibrate_port.py times it against the port on one host.
 """
 from __future__ import annotations
 
@@ -52,12 +51,6 @@ from sanepic_gb300 import synth  # noqa: E402
 
 METRIC = "time-to-solution at rel. residual 1e-6: learned-precond vs plain PCG, 1 GB300"
 STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
-# Iterations the reference's own preconditioner (the scalar diagonal,
-# sanepic.cc:1351-1355) needs to reach |r|/|b| = 1e-6 on the default workload
-# (64 detectors, NSIDE 256, 48 x 131072 samples), measured on a GB300 with the
-# library's reference-diagonal mode, the same algorithm (bench.py
-# --compare-diag: 24 iterations; block-Jacobi needs 21).
-REFERENCE_ITERS_TO_1E6 = {"c2_64det_nside256": 24}
 # DRAM bytes (read + write) of one noise-filter tile of 131072 FP32 samples,
 # from the ncu capture in profiles/noise_filter_c2_8det.md (354.5 MB over
 # 384 tiles); traffic grows with the tiles, so a full launch is this x tiles.
@@ -376,9 +369,7 @@ def run_ours(args):
         mm.close()
         line["c3"] = c3_block(sg, stream, args)
     if not args.no_cpu_baseline and rank == 0:
-        line["cpu_baseline"] = reference_cpu(
-            args, spec, iters_for_projection=extra.get("diag_precond", {}).get("iterations")
-            or REFERENCE_ITERS_TO_1E6.get(args.config))
+        line["cpu_baseline"] = reference_cpu(args, spec)
     if rank == 0:
         print(json.dumps(line), flush=True)
     mm.close()
@@ -618,6 +609,9 @@ def run_batch(args):
     for sp in specs:
         prob = synth.make_problem(sp)
         mm = sg.from_problem(prob, precision="f32", device=local)
+        # one-detector problems leave most Q/U blocks nearly singular: mask
+        # those (sg_set_pol_rcond) so that every problem is well posed
+        mm.set_pol_rcond(args.pol_rcond)
         mm.rhs()
         makers.append(mm)
         del prob
@@ -688,7 +682,8 @@ def run_batch(args):
         "config": {"workload": "batch32_uneven", "problems": len(specs), "samples": samples,
                    "precond": "learned (per-problem coarse space, judged by block-Jacobi PCG)"
                    if learn is not None else args.precond, "stop": "|r|/|b| <= 1e-6",
-                   "solve": "concurrent: one stream + captured graphs per problem"},
+                   "solve": "concurrent: one stream + captured graphs per problem",
+                   "pol_rcond": args.pol_rcond},
         "sequential_s": seq_s,
         "problems": [{"name": sp.name, "iterations": r["iterations"],
                       "device_s": r["device_seconds"], "converged": bool(r["converged"]),
@@ -706,76 +701,94 @@ def run_batch(args):
 
 
 # ---------------------------------------------------------------------------
-def _port_worker(task):
-    """One host core of the CPU baseline: the oracle port's operator (the
-    reference's deproject + FFT weighting + scatter, FP64, same operation
-    order) on one segment of the workload, timed over `reps` applications."""
-    spec_kw, seg_problem, reps = task
-    import oracle  # the CPU checker; only this leg of bench.py uses it
-    spec = synth.ProblemSpec(**spec_kw)
-    spec.problem = seg_problem
+# The threaded port of the reference's path (oracle/cgpar.c) against the
+# shimmed reference itself on the same workload and cores (x86, 8 cores; the
+# reference cannot be built on the GPU host): the port's RHS-to-1e-6 interval
+# takes PORT_OVER_REFERENCE of the reference's (oracle/calibrate_port.py,
+# profiles/cpu_port_vs_reference.md).
+PORT_OVER_REFERENCE = {"c2_64det_nside256": None, "c1_4det_nside64": 0.52}
+
+
+def port_solve(spec, nthreads, maxiter):
+    """One whole run of the reference's path on the host: the threaded port
+    (setup, RHS, the reference's diagonal preconditioner, PCG to
+    |r|/|b| <= 1e-6), its phase times in seconds."""
+    import oracle  # the CPU checker; only the CPU-baseline legs of bench.py use it
     prob = synth.make_problem(spec)
-    s = oracle.Setup(prob)
-    x = np.random.default_rng(seg_problem).standard_normal(3 * s.npix)
-    s.apply(x)
-    t = time.perf_counter()
-    for _ in range(reps):
-        s.apply(x)
-    return (time.perf_counter() - t) / reps, spec.ndet * spec.nseg * spec.ns
+    t = time.time()
+    r = oracle.cpu_solve(prob, nthreads, stop_crit=STOP_CRIT, maxiter=maxiter)
+    r["wall_s"] = time.time() - t
+    return r
 
 
-def reference_cpu(args, spec, iters_for_projection=None):
-    """CPU baseline: the oracle port on every host core (one process per core,
-    each owning whole segments, as the reference's MPI workers do,
-    sanepic.cc:623-632), timed on a bounded sample of the workload and
-    projected linearly in samples to the full problem."""
-    import multiprocessing as mp
+def reference_cpu(args, spec):
+    """CPU baseline beside the GPU line: the threaded port on every host
+    core, timed on a bounded sample of the workload -- the same scan, sizes
+    and noise model with 8 of the detectors, solved from scratch to
+    |r|/|b| <= 1e-6 -- and scaled to the workload's detector count (the
+    per-iteration work is linear in detectors; the iterations are the
+    sample's).  The whole workload is timed by --impl reference."""
+    import dataclasses
     cores = os.cpu_count() or 2
-    workers = max(1, cores - 1)  # the reference's rank 0 holds no data
-    ndet_s = 8
-    spec_kw = dict(name="sample", ndet=ndet_s, nside=spec.nside, nseg=1, ns=spec.ns,
-                   hwp=spec.hwp, fknee=spec.fknee, alpha=spec.alpha,
-                   fknee_range=spec.fknee_range, alpha_range=spec.alpha_range)
-    reps = 3
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
-        res = pool.map(_port_worker, [(spec_kw, 100 + w, reps) for w in range(workers)])
-    t_apply = max(r[0] for r in res)           # workers run concurrently
-    n_sample = sum(r[1] for r in res)
-    n_full = spec.ndet * spec.nseg * spec.ns
-    rate = n_sample / t_apply                   # sample-applies per second, all cores
-    t_iter_full = 1.1 * n_full / rate           # + one true-residual apply per 10 iterations
-    proj = iters_for_projection * t_iter_full if iters_for_projection else None
-    return {"value": proj, "unit": "s", "cores": workers, "kind": "port",
-            "sample": (f"{workers} processes x (1 segment x {ndet_s} detectors x {spec.ns} "
-                       f"samples), {reps} operator applications each; projected linearly in "
-                       f"samples to {n_full:.3g} samples x {iters_for_projection} iterations of "
-                       f"the reference's diagonal-preconditioned PCG"),
-            "sample_applies_per_second": rate, "seconds_per_iteration_full": t_iter_full}
+    nd = min(8, spec.ndet)
+    sp = dataclasses.replace(spec, ndet=nd, name=spec.name + f"_sample{nd}det")
+    r = port_solve(sp, cores, args.maxiter)
+    t = r["times"]["to_stop"]
+    scale = spec.ndet / nd
+    return {"value": t * scale if t > 0 else None, "unit": "s", "cores": cores, "kind": "port",
+            "sample": (f"{nd} of {spec.ndet} detectors, every segment ({nd * spec.nseg} x "
+                       f"{spec.ns} samples): RHS + diagonal preconditioner + PCG to |r|/|b| <= "
+                       f"1e-6 measured ({t:.2f} s, {r['iterations']} iterations), x{scale:g} "
+                       "detectors"),
+            "sample_phases_s": r["times"], "sample_iterations": r["iterations"]}
 
 
 def run_reference(args):
+    """--impl reference: the reference's path on the host cores for the whole
+    workload -- the threaded port of sanepic.cc's algorithm (oracle/cgpar.c)
+    in its parallel layout, every host thread, each run from scratch (value =
+    RHS + diagonal preconditioner + PCG until |r|/|b| <= 1e-6, the scope of
+    the GPU value plus the reference's preconditioner build).  A run takes
+    about two minutes, so `steps` reports the runs actually made within the
+    time budget, not the requested count."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     spec = synth.spec_from_name(args.config)
-    iters = args.ref_iters or REFERENCE_ITERS_TO_1E6.get(args.config)
-    for _ in range(args.warmup):
-        reference_cpu(args, spec, iters_for_projection=iters)
-    samples = [reference_cpu(args, spec, iters_for_projection=iters)
-               for _ in range(max(1, args.steps))]
-    samples.sort(key=lambda c: c["value"] if c["value"] is not None else float("inf"))
-    cb = samples[len(samples) // 2]  # median sample
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": cb["value"] * 1e3 if cb["value"] else None,
+    cores = os.cpu_count() or 2
+    runs = []
+    t0 = time.time()
+    while len(runs) < max(1, args.steps):
+        runs.append(port_solve(spec, cores, args.maxiter))
+        per = (time.time() - t0) / len(runs)
+        if time.time() - t0 + per > args.ref_budget_s:
+            break
+    vals = sorted(r["times"]["to_stop"] for r in runs if r["times"]["to_stop"] > 0)
+    value = vals[len(vals) // 2] if vals else None
+    last = runs[-1]
+    cb = {"value": value, "unit": "s", "cores": cores, "kind": "port",
+          "sample": (f"the whole workload ({spec.ndet} det x {spec.nseg} x {spec.ns} samples), "
+                     f"{len(runs)} run(s) from scratch; timed: RHS + the reference's diagonal "
+                     "preconditioner + PCG to |r|/|b| <= 1e-6"),
+          "phases_s": last["times"], "iterations": last["iterations"],
+          "run_wall_s": [r["wall_s"] for r in runs],
+          "port_over_reference": PORT_OVER_REFERENCE.get(args.config),
+          "calibration": "oracle/calibrate_port.py: the shimmed reference and this port on the "
+                         "same workload and cores (x86); the reference cannot be built here"}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s",
+            "n_gpus": world, "steps": len(runs), "warmup": 0,
+            "requested": {"steps": args.steps, "warmup": args.warmup},
+            "ms_per_step": value * 1e3 if value else None,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": {"workload": args.config},
+            "data": "synthetic (seeded spin+precession scan, iid sky, 1/f noise)",
+            "config": {"workload": args.config, "ndet": spec.ndet, "nside": spec.nside,
+                       "nseg": spec.nseg, "ns": spec.ns, "precond": "diag (the reference's)",
+                       "stop": "|r|/|b| <= 1e-6"},
             "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    if cb["value"] is None:
-        line["unavailable"] = cb["sample"]
+    if value is None:
+        line["unavailable"] = "the port did not reach |r|/|b| <= 1e-6"
     print(json.dumps(line), flush=True)
 
 
@@ -791,13 +804,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--compare-diag", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-iters", type=int, default=None)
+    ap.add_argument("--ref-budget-s", type=float, default=240.0,
+                    help="--impl reference: no new run starts past this many seconds")
     ap.add_argument("--no-learn", action="store_true")
     ap.add_argument("--learn-pairs", type=int, default=512)
     ap.add_argument("--learn-steps", type=int, default=1500)
     ap.add_argument("--coarse-k", type=int, default=0)
     ap.add_argument("--coarse-vectors", type=int, default=0)
     ap.add_argument("--no-map-error", action="store_true")
+    ap.add_argument("--pol-rcond", type=float, default=1e-3,
+                    help="batch32: mask Q/U of pixels whose 3x3 hit block is this ill-conditioned")
     ap.add_argument("--no-per-detector", action="store_true")
     ap.add_argument("--c3", type=int, default=1, help="add the C3 block (1) or not (0)")
     args = ap.parse_args()

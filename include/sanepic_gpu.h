@@ -129,6 +129,19 @@ int sg_set_stream(sg_ctx *ctx, void *cuda_stream);
 int sg_set_pointing(sg_ctx *ctx, const double *ra, const double *dec, const double *psi,
                     long nsamp_total, const long *isampmin, const sg_det *dets);
 
+/* Extends the pol degeneracy mask of every solve: besides the reference's
+ * pixels with fewer than 2 hits (sanepic.cc:1316-1330, 1455-1459), Q and U
+ * are masked (zeroed, not solved for) in pixels whose 3 x 3 block
+ * sum_i w_i w_i^T, w = (1, cos 2psi_i, sin 2psi_i) over the pixel's detector
+ * samples, has a reciprocal condition number below rcond_min.  With one
+ * detector angle most such blocks are nearly singular and the system has
+ * (near) null vectors, on which PCG stalls (the reference stops at its
+ * iteration limit); 1e-6 is a working threshold.  0 (the default) keeps the
+ * reference's rule.  Output maps (HITS, NVAR, SIN2P) keep the reference's
+ * rule either way.  Invalidates b, the preconditioners and any learned part:
+ * call before sg_rhs and sg_learn_train.  No reference counterpart. */
+int sg_set_pol_rcond(sg_ctx *ctx, double rcond_min);
+
 /* Inverse-noise spectrum of one detector (nssp values, the -u file).
  * Replaces sanepic.cc:507-539 (including the bin-0 override, 536-537). */
 int sg_set_noise(sg_ctx *ctx, long det, const double *ispf, long nssp);

@@ -40,6 +40,7 @@ def lib():
         _LIB.orc_rhs.restype = ctypes.c_double
         _LIB.orc_pcg.restype = ctypes.c_int
         _LIB.orc_expand_detector.restype = ctypes.c_int
+        _LIB.cp_run.restype = ctypes.c_int
     return _LIB
 
 
@@ -214,3 +215,39 @@ def run_pipeline(prob, precond="diag", stop_crit=1e-15, maxiter=2000, verbose=Fa
         "COS2P": s.expand(sc[:npix]), "SIN2P": s.expand(sc[npix:2 * npix]),
     }
     return out, dict(iters=iters, crit=hist, chi20=chi20, npix=npix, setup=s)
+
+
+def cpu_solve(prob, nthreads: int, stop_crit: float = 1e-12, maxiter: int = 2000):
+    """The reference's whole path (setup, RHS, diagonal preconditioner, PCG)
+    on nthreads host threads in its parallel layout (cgpar.c).  Returns the
+    compact solution, the iteration count, crit per iteration and the phase
+    times (seconds): setup, rhs, precond, solve, and to_stop = from the end of
+    setup until crit first reached stop_crit (-1 if it never did)."""
+    L = lib()
+    spec = prob["spec"]
+    ns, nseg, ndet, nside = spec.ns, spec.nseg, spec.ndet, spec.nside
+    ra = np.ascontiguousarray(prob["ra"], np.float64)
+    dec = np.ascontiguousarray(prob["dec"], np.float64)
+    psi = np.ascontiguousarray(prob["psi"], np.float64)
+    isamp = np.ascontiguousarray(prob["isampmin"], np.int64)
+    psidet = np.ascontiguousarray(np.asarray(prob["angles"], np.float64) / 180.0
+                                  * 6.2831853071795864769252867665590057683943387987502 / 2.0)
+    ispf = np.ascontiguousarray(prob["ispf"], np.float64)
+    tod = np.ascontiguousarray(prob["tod"], np.float64)
+    x = np.zeros(3 * 12 * nside * nside)
+    hist = np.zeros(maxiter + 1)
+    times = np.zeros(5)
+    npix = ctypes.c_long(0)
+    iters = ctypes.c_int(0)
+    rc = L.cp_run(ctypes.c_long(ns), ctypes.c_long(nseg), ctypes.c_long(ndet),
+                  ctypes.c_long(nside), _pd(ra), _pd(dec), _pd(psi), _pl(isamp), _pd(psidet),
+                  ctypes.c_int(int(spec.hwp)), ctypes.c_double(prob["omega"]), _pd(ispf),
+                  ctypes.c_long(ispf.shape[1]), _pd(tod), ctypes.c_int(nthreads),
+                  ctypes.c_double(stop_crit), ctypes.c_int(maxiter), _pd(x), _pd(hist),
+                  _pd(times), ctypes.byref(npix), ctypes.byref(iters))
+    if rc != 0:
+        raise ValueError(f"cp_run failed ({rc})")
+    n = npix.value
+    it = iters.value
+    return {"x": x[:3 * n].copy(), "npix": n, "iterations": it, "crit": hist[:it].copy(),
+            "times": dict(zip(("setup", "rhs", "precond", "solve", "to_stop"), times.tolist()))}

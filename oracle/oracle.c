@@ -310,8 +310,8 @@ static int orc_kv_cmp(const void *a, const void *b) {
   return (x->idx > y->idx) - (x->idx < y->idx);
 }
 
-static void orc_diag_tile(const double *Nk, const long *pix, long ns,
-                          const long *indpix, double *dPtNP) {
+void orc_diag_tile(const double *Nk, const long *pix, long ns, const long *indpix,
+                   double *dPtNP) {
   long nk = ns / 2 + 1;
   double *Nk_ = (double *)malloc(sizeof(double) * 2 * nk);
   double *N_ = (double *)malloc(sizeof(double) * ns);

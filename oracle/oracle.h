@@ -95,6 +95,20 @@ void orc_diag_precond(long ns, long nseg, long ndet, long npix,
                       const long *indpix, const long *pix, const double *spn,
                       double *Mp);
 
+/* compute_diagPtNPCorr for one tile (sanepic.cc:2680-2762): adds to
+ * dPtNP[m] (the I block) sum_{i,j at pixel m, |i-j| < ns/2} N_[|i-j|] with
+ * N_ = c2r(|Nk|). */
+void orc_diag_tile(const double *Nk, const long *pix, long ns, const long *indpix,
+                   double *dPtNP);
+
+/* The whole path on nthreads threads in the reference's parallel layout
+ * (cgpar.c): the CPU baseline's timed run. */
+int cp_run(long ns, long nseg, long ndet, long nside, const double *ra, const double *dec,
+           const double *psi, const long *isampmin, const double *psidet, int hwp,
+           double omega, const double *ispf, long nssp, const double *tod, int nthreads,
+           double stop_crit, int maxiter, double *x, double *crit_hist, double *times,
+           long *npix_out, int *iters_out);
+
 /* 3x3 block-Jacobi preconditioner (not in the reference): per pixel
  * sum_i g0_det * w w^T with w = (1, cos 2psi, sin 2psi), g0 = the diagonal of
  * N^-1 for that detector (c2r(spn)[0]); inverted in FP64.  Pixels whose pol

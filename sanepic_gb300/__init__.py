@@ -40,7 +40,7 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
            "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
-           "sg_autotune",
+           "sg_autotune", "sg_set_pol_rcond",
            "sg_last_error", "sg_destroy"]
 
 
@@ -122,6 +122,7 @@ def load_library(path: Optional[str] = None):
     L.sg_set_stream.argtypes = [c_p, c_p]
     L.sg_set_pointing.argtypes = [c_p, dp, dp, dp, ctypes.c_long, lp, ctypes.POINTER(SgDet)]
     L.sg_set_noise.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
+    L.sg_set_pol_rcond.argtypes = [c_p, ctypes.c_double]
     L.sg_set_tod.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
     L.sg_rhs.argtypes = [c_p, dp]
     L.sg_npix.argtypes = [c_p]
@@ -223,6 +224,11 @@ class MapMaker:
             isp = self._isamp.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
         self._check(self.L.sg_set_pointing(self.h, _dp(ra), _dp(dec), _dp(psi), ra.size, isp, arr))
         self.npix = int(self.L.sg_npix(self.h))
+
+    def set_pol_rcond(self, rcond_min: float):
+        """Also mask Q/U where the pixel's 3 x 3 hit block has a reciprocal
+        condition number below rcond_min (0: the reference's rule only)."""
+        self._check(self.L.sg_set_pol_rcond(self.h, float(rcond_min)))
 
     def set_noise(self, det: int, ispf):
         ispf = _f64(ispf)

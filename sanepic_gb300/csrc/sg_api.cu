@@ -436,7 +436,22 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   }
   c->have_pointing = true;
   c->have_rhs = c->have_solution = c->have_bj3 = c->have_diag = false;
-  return SG_OK;
+  return build_polmask(c);
+}
+
+extern "C" int sg_set_pol_rcond(sg_ctx* c, double rcond_min) {
+  if (!c) return SG_ERR_ARG;
+  if (!(rcond_min >= 0.0 && rcond_min < 1.0))
+    return c->fail(SG_ERR_ARG, "rcond_min %g outside [0, 1)", rcond_min);
+  cudaSetDevice(c->desc.device);
+  c->pol_rcond = rcond_min;
+  // b, the block-Jacobi blocks and any learned part were made with the old mask
+  c->have_rhs = c->have_solution = c->have_bj3 = false;
+  c->coarse_k = 0;
+  c->set_learned_kind(0);
+  c->learned_enabled = false;
+  c->drop_graphs();
+  return c->have_pointing ? build_polmask(c) : SG_OK;
 }
 
 extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) {
@@ -614,6 +629,52 @@ extern "C" int sg_noise_filter(sg_ctx* c, const double* in, double* out) {
 }
 
 // ---------------------------------------------------------------------------
+// The pol mask of the CG steps: the true hits where the pixel's Q/U are
+// solved for, min(hits, 1) where they are masked -- fewer than 2 hits (the
+// reference's rule, sanepic.cc:1316-1330) or, with pol_rcond > 0, a 3 x 3
+// block sum_i w_i w_i^T (w = (1, cos 2psi, sin 2psi), every detector sample
+// weighted 1) whose reciprocal condition number is below pol_rcond.
+int build_polmask(sg_ctx* c) {
+  const long long npix = c->npix;
+  cudaError_t e = c->polmask.alloc(sizeof(int) * npix);
+  if (e == cudaSuccess && c->pol_rcond <= 0.0)
+    e = cudaMemcpyAsync(c->polmask.p, c->hits.p, sizeof(int) * npix, cudaMemcpyDeviceToDevice,
+                        c->st);
+  if (e == cudaSuccess && c->pol_rcond > 0.0) {
+    const int G = c->ngroups;
+    std::vector<double> gc(5 * G, 0.0);
+    for (int g = 0; g < G; g++)
+      for (int k = c->grp_off_h[g]; k < c->grp_off_h[g + 1]; k++) {
+        const int dd = c->grp_det_h[k];
+        const double d2 = 2.0 * (c->desc.hwp ? -c->psidet_h[dd] : c->psidet_h[dd]);
+        gc[g] += 1.0;
+        gc[G + g] += cos(d2);
+        gc[2 * G + g] += sin(d2);
+        gc[3 * G + g] += cos(2.0 * d2);
+        gc[4 * G + g] += sin(2.0 * d2);
+      }
+    DevBuf ones;
+    e = ones.alloc(sizeof(double) * 5 * G);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ones.p, gc.data(), sizeof(double) * 5 * G, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) {
+      if (c->f32)
+        e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                              c->csr_cs.as<float>(), npix, c->ns * c->nseg, G, ones.as<double>(),
+                              c->hits.as<int>(), c->pol_rcond, c->polmask.as<int>(), nullptr,
+                              c->st);
+      else
+        e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
+                               c->csr_cs.as<double>(), npix, c->ns * c->nseg, G,
+                               ones.as<double>(), c->hits.as<int>(), c->pol_rcond,
+                               c->polmask.as<int>(), nullptr, c->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);  // before `ones` is freed
+  }
+  if (e != cudaSuccess) return c->cuda_fail(e, "pol mask");
+  return SG_OK;
+}
+
 int build_bj3(sg_ctx* c) {
   if (c->have_bj3) return SG_OK;
   // group constants (sum g0, sum g0 cos 2d', sum g0 sin 2d', sum g0 cos 4d',
@@ -643,12 +704,13 @@ int build_bj3(sg_ctx* c) {
     if (c->f32)
       e = bj3_launch<float>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
                             c->csr_cs.as<float>(), c->npix, c->ns * c->nseg, G,
-                            c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(), c->st);
+                            c->gconst.as<double>(), c->polmask.as<int>(), 0.0, nullptr,
+                            c->minv.as<double>(), c->st);
     else
       e = bj3_launch<double>(c->csr_off.as<long long>(), c->csr_idx.as<uint32_t>(),
                              c->csr_cs.as<double>(), c->npix, c->ns * c->nseg, G,
-                             c->gconst.as<double>(), c->hits.as<int>(), c->minv.as<double>(),
-                             c->st);
+                             c->gconst.as<double>(), c->polmask.as<int>(), 0.0, nullptr,
+                             c->minv.as<double>(), c->st);
   }
   if (e != cudaSuccess) return c->cuda_fail(e, "bj3 build");
   c->have_bj3 = true;
@@ -734,7 +796,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     x0i.resize(3 * npix);
     c->to_internal(o->x0, x0i.data());
     e = cudaMemcpyAsync(c->x.p, x0i.data(), vb, cudaMemcpyHostToDevice, c->st);
-    if (e == cudaSuccess) e = mask_qu(c->x.as<double>(), c->hits.as<int>(), npix, c->st);
+    if (e == cudaSuccess) e = mask_qu(c->x.as<double>(), c->polmask.as<int>(), npix, c->st);
     if (e == cudaSuccess) e = c->apply_dev(c->x.as<double>(), c->r.as<double>(), true);
   } else {
     e = cudaMemsetAsync(c->x.p, 0, vb, c->st);

@@ -13,7 +13,9 @@
 //    the other options are accepted and ignored, as the reference ignores them;
 //  * SANEPIC_GPU_PRECISION (f64 | f32), SANEPIC_GPU_PRECOND (diag | bj3),
 //    SANEPIC_GPU_DEVICE and SANEPIC_GPU_STOP select what the reference fixes:
-//    FP64 and its diagonal preconditioner by default, stop at 1e-15.
+//    FP64 and its diagonal preconditioner by default, stop at 1e-15;
+//    SANEPIC_GPU_POL_RCOND > 0 also masks Q/U of pixels whose 3 x 3 hit block
+//    is that ill-conditioned (sg_set_pol_rcond; default 0, the reference's rule).
 #include <getopt.h>
 
 #include <cerrno>
@@ -52,7 +54,8 @@ void usage(const char* prog) {
           "          -e <output id> [-h <hwp> -w <hwp rad/sample>] [-I <start map>]\n"
           "          [-i <write iteration maps> -j <every>] [-P <pointing suffix>]\n"
           "environment: SANEPIC_GPU_PRECISION=f64|f32  SANEPIC_GPU_PRECOND=diag|bj3\n"
-          "             SANEPIC_GPU_DEVICE=<ordinal>   SANEPIC_GPU_STOP=<crit>\n",
+          "             SANEPIC_GPU_DEVICE=<ordinal>   SANEPIC_GPU_STOP=<crit>\n"
+          "             SANEPIC_GPU_POL_RCOND=<min reciprocal condition of a pixel's Q/U>\n",
           prog);
 }
 
@@ -310,6 +313,12 @@ int main(int argc, char** argv) {
   run.check(sg_set_pointing(run.ctx, ra.data(), dec.data(), psi.data(), nsamp_total,
                             isampmin.data(), dets.data()),
             "sg_set_pointing");
+  if (const char* rc = getenv("SANEPIC_GPU_POL_RCOND")) {
+    char* end = nullptr;
+    const double v = strtod(rc, &end);
+    if (end == rc || *end != '\0') die("SANEPIC_GPU_POL_RCOND must be a number");
+    run.check(sg_set_pol_rcond(run.ctx, v), "sg_set_pol_rcond");
+  }
   ra = std::vector<double>();
   dec = std::vector<double>();
   psi = std::vector<double>();

@@ -108,6 +108,11 @@ struct sg_ctx {
   std::vector<int> grp_off_h, grp_det_h;
   std::vector<double> g0_h, psidet_h;
   DevBuf pix, cs, y, tod, csr_off, csr_idx, csr_cs, hits, indpix, sumcross;
+  // the pol mask every CG step uses: true hits, or min(hits, 1) where the Q/U
+  // block is masked -- the reference's rule (fewer than 2 hits) and, with
+  // pol_rcond > 0, blocks whose reciprocal condition number is below it
+  DevBuf polmask;
+  double pol_rcond = 0.0;
   DevBuf grp_off, grp_det, dcs, ys, gconst;
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
@@ -246,7 +251,7 @@ struct sg_ctx {
   }
 
   cudaError_t launch_pt(double* out, bool masked) {
-    const int* h = masked ? hits.as<int>() : nullptr;
+    const int* h = masked ? polmask.as<int>() : nullptr;
     launches++;
     if (f32)
       return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
@@ -429,7 +434,7 @@ struct sg_ctx {
     v.b = b.as<double>();
     v.minv = minv.as<double>();
     v.mdiag = mdiag.as<double>();
-    v.hits_true = hits.as<int>();
+    v.hits_true = polmask.as<int>();
     v.precond = precond;
     v.part = part.as<double>();
     v.sc = sc.as<CgScalars>();
@@ -653,6 +658,7 @@ struct sg_ctx {
 };
 
 int build_bj3(sg_ctx* c);  // 3x3 block-Jacobi blocks for the current pointing and noise
+int build_polmask(sg_ctx* c);  // the CG's pol mask for the current pointing and pol_rcond
 int ensure_patches(sg_ctx* c);  // nested patch geometry of the learned preconditioner
 int build_diag(sg_ctx* c);      // the reference's diagonal preconditioner
 int prepare_operator(sg_ctx* c);  // set-up the operator needs before its first application

@@ -107,10 +107,14 @@ cudaError_t sumcross_launch(const long long* csr_off, const uint32_t* csr_idx, c
                             const double* tab, long long nsd, const double* gsc, const double* gss,
                             long long npix, double* sumcross, cudaStream_t st);
 // 3x3 block-Jacobi build+invert; gconst [5][ngroups]; minv [6][npix] (00 01 02 11 12 22)
+// or null.  Q/U of a pixel are masked when hits_true < 2 or (rcond_min > 0)
+// its block's reciprocal condition number is below rcond_min; polmask_out
+// (optional) receives hits_true, or min(hits_true, 1) where masked.
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                        long long npix, long long nsd, int ngroups, const double* gconst,
-                       const int* hits_true, double* minv, cudaStream_t st);
+                       const int* hits_true, double rcond_min, int* polmask_out, double* minv,
+                       cudaStream_t st);
 // per-group sum of the detectors' N_ tables: out [ngroups][ns]
 template <typename T>
 cudaError_t group_ntab_launch(const T* ntab, long long ns, int ngroups, const int* grp_off,

@@ -296,7 +296,7 @@ cudaError_t sg_ctx::learned_z(int flexible) {
   if (e == cudaSuccess) e = mlp->forward(npatch_pad, st);
   if (e != cudaSuccess) return e;
   k_patch_scatter<<<npatch, kPatch, 0, st>>>(mlp->y, patch_sig.as<float>(), patch_idx.as<int>(),
-                                             npix, hits.as<int>(), z.as<double>());
+                                             npix, polmask.as<int>(), z.as<double>());
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cg_dots(vecs(2), flexible, st);
   launches += 4 + 8;  // precond, gather, scatter, dots, 4 GEMMs + 4 bias/activation kernels
@@ -745,7 +745,7 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
     if (e != cudaSuccess) break;
     k_patch_scatter<<<c->npatch, kPatch, 0, c->st>>>(net.y, c->patch_sig.as<float>(),
                                                      c->patch_idx.as<int>(), npix,
-                                                     c->hits.as<int>(), zf.as<double>());
+                                                     c->polmask.as<int>(), zf.as<double>());
     e = cudaGetLastError();
     if (e == cudaSuccess) e = c->apply_dev(zf.as<double>(), az.as<double>(), true);
     if (e != cudaSuccess) break;
@@ -755,7 +755,7 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
                                             gz.as<double>(), scal.as<double>());
     k_patch_grad<<<c->npatch, kPatch, 0, c->st>>>(gz.as<double>(), c->patch_sig.as<float>(),
                                                   c->patch_idx.as<int>(), npix,
-                                                  c->hits.as<int>(), dy.as<float>());
+                                                  c->polmask.as<int>(), dy.as<float>());
     e = cudaGetLastError();
     if (e == cudaSuccess) e = net.backward_dy(B, dy.as<float>(), c->st);
     const float frac = (float)s / (float)steps;

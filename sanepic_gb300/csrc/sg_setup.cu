@@ -358,13 +358,41 @@ struct pair_of<double> {
   using type = double2;
 };
 
+// Reciprocal condition number lambda_min / lambda_max of the symmetric 3 x 3
+// matrix (a0 a1 a2; a1 a3 a4; a2 a4 a5), its eigenvalues from the
+// trigonometric closed form for symmetric 3 x 3 matrices (O. K. Smith,
+// "Eigenvalues of a symmetric 3 x 3 matrix", CACM 4(4), 1961).
+__device__ double sym3_rcond(const double* a) {
+  const double p1 = a[1] * a[1] + a[2] * a[2] + a[4] * a[4];
+  const double q = (a[0] + a[3] + a[5]) / 3.0;
+  const double d0 = a[0] - q, d1 = a[3] - q, d2 = a[5] - q;
+  const double p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1;
+  if (!(q > 0.0)) return 0.0;
+  if (p2 <= 0.0) return 1.0;  // a multiple of the identity
+  const double p = sqrt(p2 / 6.0), ip = 1.0 / p;
+  // B = (A - q I) / p, r = det(B) / 2
+  const double b0 = d0 * ip, b1 = a[1] * ip, b2 = a[2] * ip, b3 = d1 * ip, b4 = a[4] * ip,
+               b5 = d2 * ip;
+  double r = 0.5 * (b0 * (b3 * b5 - b4 * b4) - b1 * (b1 * b5 - b4 * b2) + b2 * (b1 * b4 - b3 * b2));
+  r = fmin(1.0, fmax(-1.0, r));
+  const double phi = acos(r) / 3.0;
+  const double lmax = q + 2.0 * p * cos(phi);
+  const double lmin = q + 2.0 * p * cos(phi + 2.0943951023931954923);  // + 2 pi / 3
+  return lmax > 0.0 ? fmax(lmin, 0.0) / lmax : 0.0;
+}
+
 // A team of L lanes per pixel (256 / L pixels per block), each lane taking
 // its samples j, j + L, ... four at a time with the loads of all four in
 // flight; FP64 sums, combined over the team with a fixed xor tree.
+// A pixel's Q/U are masked when hits[m] < 2 (the reference's rule) or, with
+// rcond_min > 0, when its block's reciprocal condition number is below
+// rcond_min; polmask_out (optional) receives hits[m], or min(hits[m], 1)
+// where the block is masked; minv (optional) the inverse blocks.
 template <typename T, int L>
 __global__ void __launch_bounds__(256)
     k_bj3(const long long* off, const uint32_t* idx, const T* ccs, long long npix, uint32_t nsd,
-          int ngroups, const double* gc, const int* hits, double* minv) {
+          int ngroups, const double* gc, const int* hits, double rcond_min, int* polmask_out,
+          double* minv) {
   using P2 = typename pair_of<T>::type;
   constexpr int U = 4;
   const int lane = threadIdx.x % L;
@@ -406,8 +434,12 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int k = 0; k < 6; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
   if (lane == 0 && m < npix) {
+    bool pol = hits[m] >= 2;
+    if (pol && rcond_min > 0.0) pol = sym3_rcond(a) >= rcond_min;
+    if (polmask_out) polmask_out[m] = pol ? hits[m] : min(hits[m], 1);
+    if (!minv) return;
     double o6[6] = {0, 0, 0, 0, 0, 0};
-    if (hits[m] < 2) {
+    if (!pol) {
       o6[0] = a[0] != 0.0 ? 1.0 / a[0] : 0.0;
     } else {
       const double c00 = a[3] * a[5] - a[4] * a[4];
@@ -440,33 +472,40 @@ __global__ void __launch_bounds__(256)
 template <typename T, int L>
 static void bj3_team(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                      long long npix, long long nsd, int ngroups, const double* gconst,
-                     const int* hits_true, double* minv, cudaStream_t st) {
+                     const int* hits_true, double rcond_min, int* polmask_out, double* minv,
+                     cudaStream_t st) {
   const long long blocks = (npix + 256 / L - 1) / (256 / L);
   k_bj3<T, L><<<(unsigned)blocks, 256, 0, st>>>(csr_off, csr_idx, csr_cs, npix, (uint32_t)nsd,
-                                                 ngroups, gconst, hits_true, minv);
+                                                 ngroups, gconst, hits_true, rcond_min,
+                                                 polmask_out, minv);
 }
 
 template <typename T>
 cudaError_t bj3_launch(const long long* csr_off, const uint32_t* csr_idx, const T* csr_cs,
                        long long npix, long long nsd, int ngroups, const double* gconst,
-                       const int* hits_true, double* minv, cudaStream_t st) {
+                       const int* hits_true, double rcond_min, int* polmask_out, double* minv,
+                       cudaStream_t st) {
   if (npix <= 0) return cudaSuccess;
+#define SG_BJ3_TEAM(L)                                                                       \
+  bj3_team<T, L>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, rcond_min, \
+                 polmask_out, minv, st)
   switch (pt_lanes((long long)ngroups * nsd, npix)) {  // every group sample is in the CSR
-    case 1: bj3_team<T, 1>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
-    case 2: bj3_team<T, 2>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
-    case 4: bj3_team<T, 4>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
-    case 8: bj3_team<T, 8>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
-    case 16: bj3_team<T, 16>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
-    default: bj3_team<T, 32>(csr_off, csr_idx, csr_cs, npix, nsd, ngroups, gconst, hits_true, minv, st); break;
+    case 1: SG_BJ3_TEAM(1); break;
+    case 2: SG_BJ3_TEAM(2); break;
+    case 4: SG_BJ3_TEAM(4); break;
+    case 8: SG_BJ3_TEAM(8); break;
+    case 16: SG_BJ3_TEAM(16); break;
+    default: SG_BJ3_TEAM(32); break;
   }
+#undef SG_BJ3_TEAM
   return cudaGetLastError();
 }
 template cudaError_t bj3_launch<float>(const long long*, const uint32_t*, const float*, long long,
-                                       long long, int, const double*, const int*, double*,
-                                       cudaStream_t);
+                                       long long, int, const double*, const int*, double, int*,
+                                       double*, cudaStream_t);
 template cudaError_t bj3_launch<double>(const long long*, const uint32_t*, const double*,
                                         long long, long long, int, const double*, const int*,
-                                        double*, cudaStream_t);
+                                        double, int*, double*, cudaStream_t);
 
 // N_ of every detector summed over its group: the pixel stream is common to
 // the group, so the reference's per-detector pair sums add up per group.

@@ -59,6 +59,10 @@ PRESETS: Dict[str, ProblemSpec] = {
     # 1 detector, NSIDE 64, 12 x 65,536 samples, FP64
     "c1_1det_nside64": ProblemSpec("c1_1det_nside64", 1, 64, 12, 65536,
                                    fknee=0.1, alpha=1.0, precision="f64"),
+    # the same scan and sizes with 4 detectors at seeded orientations (well
+    # posed: one detector angle leaves most Q/U blocks nearly singular)
+    "c1_4det_nside64": ProblemSpec("c1_4det_nside64", 4, 64, 12, 65536,
+                                   fknee=0.1, alpha=1.0, problem=3, precision="f64"),
     # 64 detectors, NSIDE 256, 48 x 131,072 samples, per-detector 1/f, FP32
     "c2_64det_nside256": ProblemSpec("c2_64det_nside256", 64, 256, 48, 131072,
                                      fknee_range=(0.02, 0.2),

@@ -65,3 +65,39 @@ def test_cli_outputs_match_reference(name, tmp_path):
     for it in (0, 10):
         for c in "IQU":
             assert read_map(f"{out}_{c}{e}_{it}").size == npixfull
+
+
+def test_cli_restart_from_its_own_start_map(tmp_path):
+    # -I: a run stopped early writes its compact solution (map__A_*,
+    # sanepic.cc:1786-1788); a second run started from it (sanepic.cc:
+    # 1209-1227) converges to the maps of one uninterrupted run
+    name = NAMES[0]
+    prob = load_problem(name)
+    spec = prob["spec"]
+    runs = {}
+    for tag, stop, init in (("full", "1e-15", None), ("first", "1e-6", None),
+                            ("resumed", "1e-15", "first")):
+        d = tmp_path / tag
+        d.mkdir()
+        args = synth.write_reference_tree(prob, str(d))
+        if init:
+            args += ["-I", runs[init]["names"]["A"]]
+        env = dict(os.environ, SANEPIC_GPU_PRECOND="diag", SANEPIC_GPU_PRECISION="f64",
+                   SANEPIC_GPU_STOP=stop)
+        r = subprocess.run([build.CLI] + args, capture_output=True, text=True, timeout=600,
+                           env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        rows = np.array([[float(v) for v in m.groups()] for m in ITER.finditer(r.stdout)])
+        runs[tag] = {"rows": rows,
+                     "names": synth.output_names(spec, os.path.join(str(d), "out_dir", "map_"))}
+    first, resumed, full = runs["first"]["rows"], runs["resumed"]["rows"], runs["full"]["rows"]
+    assert first[-1, 1] <= 1e-6 and len(first) < len(full)
+    # the resumed run starts where the first stopped, not from zero
+    assert resumed[0, 1] < 1e-3 * full[0, 1]
+    assert resumed[-1, 1] <= 1e-15
+    for k in ("I", "Q", "U"):
+        a = read_map(runs["resumed"]["names"][k])
+        b = read_map(runs["full"]["names"][k])
+        assert rel_rms(a, b, remove_monopole=(k == "I")) < 1e-6, k
+    # the start map is the compact vector the first run wrote
+    assert read_map(runs["first"]["names"]["A"]).size == read_map(runs["full"]["names"]["A"]).size

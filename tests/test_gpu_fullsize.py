@@ -157,3 +157,49 @@ def test_c2_maps_vs_independent_fp64_operator():
             # of the I map's RMS, printed above)
             got = e0 if k == "I" else e1
             assert got["rms"] < (2e-4 if stop == 1e-12 else 1e-5), (mode, stop, k, got)
+
+
+def block_rcond(s):
+    """Reciprocal condition number of every observed pixel's 3 x 3 block
+    sum w w^T, w = (1, cos 2psi, sin 2psi), from the CPU oracle's angles."""
+    m = s.indpix[s.pix]
+    w = np.stack([np.ones(s.psip.size), np.cos(2 * s.psip), np.sin(2 * s.psip)], 1)
+    W = np.zeros((s.npix, 3, 3))
+    for i in range(3):
+        for j in range(3):
+            W[:, i, j] = np.bincount(m, w[:, i] * w[:, j], minlength=s.npix)
+    ev = np.linalg.eigvalsh(W)
+    return ev[:, 0] / ev[:, 2]
+
+
+def test_c1_1det_converges_with_the_conditioning_mask():
+    # With Q/U masked where the pixel's block is nearly singular
+    # (sg_set_pol_rcond), the 1-detector workload is well posed: block-Jacobi
+    # PCG reaches |r|/|b| <= 1e-6 in FP64 and FP32, and the maps match the
+    # CPU oracle's PCG on the same mask
+    spec, prob, ref, log = regenerate("c1_1det_nside64", lambda p: oracle.Setup(p).pix)
+    s = oracle.Setup(prob)
+    npix = s.npix
+    thr = 1e-6
+    bad = (s.hits[npix:] >= 4) & (block_rcond(s) < thr)
+    assert bad.sum() > 1000  # one detector angle: thousands of degenerate pixels
+    s.hits[npix:][bad] = 0  # the oracle's mask (pol hits < 4) now covers them
+    b, _ = s.rhs(prob["tod"])
+    xo, it_o, hist = s.pcg(b, precond="bj3", stop_crit=1e-15, maxiter=2000)
+    assert hist[-1] <= 1e-15
+    for prec in ("f64", "f32"):
+        mm = sg.from_problem(prob, precision=prec)
+        mm.set_pol_rcond(thr)
+        mm.rhs()
+        rep = mm.solve(precond="bj3", stop_crit=1e-12 if prec == "f32" else 1e-15, maxiter=2000)
+        assert rep["converged"], (prec, rep["iterations"], rep["crit"])
+        x = mm.solution()
+        # masked Q/U are not solved for
+        assert np.all(x[npix:2 * npix][bad] == 0) and np.all(x[2 * npix:][bad] == 0)
+        got = {k: x[c * npix:(c + 1) * npix] for c, k in enumerate(MAPS)}
+        want = {k: xo[c * npix:(c + 1) * npix] for c, k in enumerate(MAPS)}
+        errs = report(f"c1_1det {prec} bj3 + conditioning mask ({rep['iterations']} iterations) "
+                      "vs oracle", got, want)
+        for k, (e, e0) in errs.items():
+            assert e0["rms"] < (1e-9 if prec == "f64" else 1e-4), (prec, k, e0)
+        mm.close()
