@@ -565,6 +565,12 @@ __device__ __forceinline__ void coarse_block_store(float (&acc)[KP], float2* par
   }
 }
 
+// elements per thread and round in the streaming coarse kernels: four rows
+// in flight, two for the widest coarse space (two blocks of 256 threads per
+// SM leave 128 registers a thread)
+template <int KP>
+constexpr int coarse_rows() { return KP > 24 ? 2 : 4; }
+
 // part[k][block] = sum over the block's elements of U[i][k] v[i]
 template <int KP>
 __global__ void __launch_bounds__(kCgThreads)
@@ -573,13 +579,17 @@ __global__ void __launch_bounds__(kCgThreads)
   float acc[KP];
 #pragma unroll
   for (int k = 0; k < KP; k++) acc[k] = 0.f;
+  constexpr int kCoarseRows = coarse_rows<KP>();
   const long long stride = (long long)gridDim.x * blockDim.x;
-  // two elements' rows in flight per round, added in the same order
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += 2 * stride) {
-    uint4 rows[2][KP / 8];
-    float vi[2];
+  // kCoarseRows elements' rows in flight per round (the grid is fixed at two
+  // blocks per SM, so the loads in flight per thread set the bandwidth),
+  // added in element order
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+       i += kCoarseRows * stride) {
+    uint4 rows[kCoarseRows][KP / 8];
+    float vi[kCoarseRows];
 #pragma unroll
-    for (int p = 0; p < 2; p++) {
+    for (int p = 0; p < kCoarseRows; p++) {
       const long long k = i + p * stride;
       const uint4* row = reinterpret_cast<const uint4*>(U + k * KP);
       vi[p] = k < n3 ? (float)v[k] : 0.f;
@@ -587,7 +597,7 @@ __global__ void __launch_bounds__(kCgThreads)
       for (int q = 0; q < KP / 8; q++) rows[p][q] = k < n3 ? row[q] : make_uint4(0, 0, 0, 0);
     }
 #pragma unroll
-    for (int p = 0; p < 2; p++) {
+    for (int p = 0; p < kCoarseRows; p++) {
       if (i + p * stride >= n3) break;
 #pragma unroll
       for (int q = 0; q < KP / 8; q++) {
@@ -609,12 +619,18 @@ __device__ __forceinline__ void coarse_solve_block(const float2* __restrict__ pa
                                                    const double* __restrict__ einv, int kc,
                                                    double* d, double* out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int NB = (kCgBlocks + 31) / 32;
   for (int k = wid; k < KP; k += kCgThreads / 32) {
     float hi = 0.f, lo = 0.f;
-    for (int b = lane; b < kCgBlocks; b += 32) {
-      const float2 q = part[k * kCgBlocks + b];
-      df_add(hi, lo, q.x, q.y);
+    float2 q[NB];  // every load in flight before the dependent sums
+#pragma unroll
+    for (int t = 0; t < NB; t++) {
+      const int b = lane + 32 * t;
+      q[t] = b < kCgBlocks ? part[k * kCgBlocks + b] : make_float2(0.f, 0.f);
     }
+#pragma unroll
+    for (int t = 0; t < NB; t++)
+      if (lane + 32 * t < kCgBlocks) df_add(hi, lo, q[t].x, q[t].y);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
       df_add(hi, lo, __shfl_xor_sync(0xffffffffu, hi, o), __shfl_xor_sync(0xffffffffu, lo, o));
@@ -702,12 +718,14 @@ __global__ void __launch_bounds__(kCgThreads)
   const long long n3 = 3 * v.npix;
   const long long stride = (long long)gridDim.x * blockDim.x;
   double acc[3] = {0.0, 0.0, 0.0};
-  // two elements per round: every load of both before any store
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += 2 * stride) {
-    uint4 rows[2][KP / 8];
-    double zv[2], rv[2], pv[2];
+  constexpr int kCoarseRows = coarse_rows<KP>();
+  // kCoarseRows elements per round: every load of all before any store
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3;
+       i += kCoarseRows * stride) {
+    uint4 rows[kCoarseRows][KP / 8];
+    double zv[kCoarseRows], rv[kCoarseRows], pv[kCoarseRows];
 #pragma unroll
-    for (int p = 0; p < 2; p++) {
+    for (int p = 0; p < kCoarseRows; p++) {
       const long long k = i + p * stride;
       const bool in = k < n3;
       const uint4* row = reinterpret_cast<const uint4*>(U + k * KP);
@@ -718,7 +736,7 @@ __global__ void __launch_bounds__(kCgThreads)
       pv[p] = (in && flexible) ? v.rprev[k] : 0.0;
     }
 #pragma unroll
-    for (int p = 0; p < 2; p++) {
+    for (int p = 0; p < kCoarseRows; p++) {
       const long long k = i + p * stride;
       if (k >= n3) break;
       float s = 0.f;

@@ -573,40 +573,59 @@ namespace sg {
 // The coarse space from the first m stored residuals: V = M_bj3 r_j (the
 // solver's own preconditioned residuals, which span the Krylov spaces of the
 // training solves), W = A V, H = V^T W, G = V^T R (= V^T M^-1 V), then
-// sg_coarse_from_gram; U = V C and A U = W C are kept in BF16.
-int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
+// sg_coarse_from_gram; U = V C and A U = W C are kept in BF16.  coarse_gram
+// makes V, W, H and G once; coarse_combine makes U, AU and E^-1 for any kc
+// from them (the validation tries more than one).
+struct CoarseBasis {
+  DevBuf V, W;
+  std::vector<double> H, G;
+  int m = 0;
+};
+
+static int coarse_gram(sg_ctx* c, const double* bank, int m, CoarseBasis& cb) {
   const long long n3 = 3 * c->npix;
-  if (m < 2) return SG_OK;
-  DevBuf V, W, gp, dC;
+  cb.m = m;
+  DevBuf gp;
   const int nsplit = 16;
-  cudaError_t e = V.alloc((size_t)m * n3 * 8);
-  if (e == cudaSuccess) e = W.alloc((size_t)m * n3 * 8);
+  cudaError_t e = cb.V.alloc((size_t)m * n3 * 8);
+  if (e == cudaSuccess) e = cb.W.alloc((size_t)m * n3 * 8);
   if (e == cudaSuccess) e = gp.alloc((size_t)nsplit * m * m * 8);
   if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space buffers");
   CgVecs v1 = c->vecs(1);
   for (int j = 0; j < m && e == cudaSuccess; j++) {
-    double* vj = V.as<double>() + (size_t)j * n3;
+    double* vj = cb.V.as<double>() + (size_t)j * n3;
     e = apply_precond(v1, bank + (size_t)j * n3, vj, c->st);
-    if (e == cudaSuccess) e = c->apply_dev(vj, W.as<double>() + (size_t)j * n3, true);
+    if (e == cudaSuccess) e = c->apply_dev(vj, cb.W.as<double>() + (size_t)j * n3, true);
   }
-  std::vector<double> part((size_t)nsplit * m * m), H((size_t)m * m, 0.0), G((size_t)m * m, 0.0);
+  std::vector<double> part((size_t)nsplit * m * m);
+  cb.H.assign((size_t)m * m, 0.0);
+  cb.G.assign((size_t)m * m, 0.0);
   for (int which = 0; which < 2 && e == cudaSuccess; which++) {
-    e = gram_launch(V.as<double>(), which == 0 ? W.as<double>() : bank, n3, m, n3, nsplit,
+    e = gram_launch(cb.V.as<double>(), which == 0 ? cb.W.as<double>() : bank, n3, m, n3, nsplit,
                     gp.as<double>(), c->st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(part.data(), gp.p, 8 * part.size(), cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-    std::vector<double>& out = which == 0 ? H : G;
+    std::vector<double>& out = which == 0 ? cb.H : cb.G;
     for (int sp = 0; sp < nsplit; sp++)
       for (size_t i = 0; i < out.size(); i++) out[i] += part[(size_t)sp * m * m + i];
   }
   c->launches += 2 * (long long)m + 2;
   if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space Gram matrices");
+  return SG_OK;
+}
+
+static int coarse_combine(sg_ctx* c, CoarseBasis& cb, int kc) {
+  const long long n3 = 3 * c->npix;
+  const int m = cb.m;
   std::vector<double> C((size_t)m * kc), einv((size_t)kc * kc), th(kc);
-  const int k = sg_coarse_from_gram(m, kc, H.data(), G.data(), C.data(), einv.data(), th.data());
-  if (k == 0) return SG_OK;  // nothing usable: no coarse space
+  const int k = sg_coarse_from_gram(m, kc, cb.H.data(), cb.G.data(), C.data(), einv.data(),
+                                    th.data());
   c->drop_graphs();
-  e = dC.alloc((size_t)m * k * 8);
+  c->coarse_k = 0;
+  if (k == 0) return SG_OK;  // nothing usable: no coarse space
+  DevBuf dC;
+  cudaError_t e = dC.alloc((size_t)m * k * 8);
   if (e == cudaSuccess) e = cudaMemcpy(dC.p, C.data(), (size_t)m * k * 8, cudaMemcpyHostToDevice);
   const int kp = coarse_pad(k);
   if (e == cudaSuccess) e = c->cs_u.alloc((size_t)kp * n3 * 2);
@@ -617,9 +636,11 @@ int build_coarse(sg_ctx* c, const double* bank, int m, int kc) {
   if (e == cudaSuccess)
     e = cudaMemcpy(c->cs_einv.p, einv.data(), (size_t)k * k * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = combine_launch(V.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_u.as<uint16_t>(), c->st);
+    e = combine_launch(cb.V.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_u.as<uint16_t>(),
+                       c->st);
   if (e == cudaSuccess)
-    e = combine_launch(W.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_au.as<uint16_t>(), c->st);
+    e = combine_launch(cb.W.as<double>(), n3, m, dC.as<double>(), k, n3, c->cs_au.as<uint16_t>(),
+                       c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   c->launches += 2;
   if (e != cudaSuccess) return c->cuda_fail(e, "coarse-space vectors");
@@ -641,6 +662,9 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   const int steps = o->steps > 0 ? o->steps : (o->steps < 0 ? 0 : 1500);  // 0: no network
   const int coarse_k = o->coarse_k > 0 ? std::min(o->coarse_k, kCoarseMax)
                                        : (o->coarse_k < 0 ? 0 : 24);  // 0: no coarse space
+  // the default also validates the space's first 16 Ritz vectors (cheaper
+  // per iteration; faster where the maps are large) and keeps the faster
+  const bool coarse_auto = o->coarse_k == 0;
   const int coarse_m = o->coarse_vectors > 0 ? o->coarse_vectors : 256;
   const float lr = o->lr > 0.f ? o->lr : 1e-3f;
   const double pair_crit = o->pair_crit > 0.0 ? o->pair_crit : 1e-13;
@@ -703,8 +727,10 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
 
   // ---- the coarse space: Rayleigh-Ritz on the span of M_bj3 r_k --------------
   c->coarse_k = 0;
+  CoarseBasis cbasis;
   if (coarse_k > 0) {
-    rc = build_coarse(c, bank.as<double>(), std::min(pairs, coarse_m), coarse_k);
+    rc = coarse_gram(c, bank.as<double>(), std::min(pairs, coarse_m), cbasis);
+    if (rc == SG_OK) rc = coarse_combine(c, cbasis, coarse_k);
     if (rc) return rc;
   }
   const double t1c = now_s();
@@ -793,7 +819,22 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (e == cudaSuccess && c->coarse_k > 0) {
     c->set_learned_kind(2);
     e = val_solve(c, 2, vcrit, vc);
+    if (e == cudaSuccess && coarse_auto && c->coarse_k > 16) {
+      const int k_full = c->coarse_k;
+      ValSolve v16;
+      rc = coarse_combine(c, cbasis, 16);
+      if (rc) return rc;
+      if (c->coarse_k > 0) e = val_solve(c, 2, vcrit, v16);
+      if (e == cudaSuccess && v16.converged && (!vc.converged || v16.ms < vc.ms)) {
+        vc = v16;  // keep the smaller space
+      } else if (e == cudaSuccess) {
+        rc = coarse_combine(c, cbasis, k_full);
+        if (rc) return rc;
+      }
+    }
   }
+  cbasis.V.release();
+  cbasis.W.release();
   c->use_syn = false;
   c->drop_graphs();  // the validation's graphs read the synthetic timeline, released here
   c->tod_syn.release();
