@@ -687,7 +687,8 @@ def run_batch(args):
         "sequential_s": seq_s,
         "problems": [{"name": sp.name, "iterations": r["iterations"],
                       "device_s": r["device_seconds"], "converged": bool(r["converged"]),
-                      "alone_s": q["device_seconds"], "cluster_size": tu["cluster_size"]}
+                      "alone_s": q["device_seconds"], "cluster_size": tu["cluster_size"],
+                      "pt_lanes": tu["pt_lanes"]}
                      for sp, r, q, tu in zip(specs, reps, seq, tunes)],
         "gpu_launches": int(sum(r["kernel_launches"] for r in reps)),
         "clocks": clocks, "generation_s": gen_s,

@@ -293,9 +293,16 @@ int sg_solve_batch(sg_ctx **ctxs, int n, const sg_solve_opts *opts, sg_report *r
  * points per CTA of the thread-block cluster) on its own timeline, or with
  * the offset-group operator one whole operator application, and keeps the
  * faster; *cluster_size and *ms (may be NULL) receive the choice and its
- * time per launch.  Needs the pointing and every detector's noise
- * (SG_ERR_STATE otherwise).  No reference counterpart. */
+ * time per launch.  Then times the P^T reduction's team of lanes per pixel
+ * (FP32: half, the same and twice the team chosen from the mean samples per
+ * pixel) and keeps the fastest.  Needs the pointing and every detector's
+ * noise (SG_ERR_STATE otherwise).  No reference counterpart. */
 int sg_autotune(sg_ctx *ctx, int *cluster_size, double *ms);
+
+/* The tile shapes in use: cluster size of the noise filter and lanes per
+ * pixel of the P^T reduction (32 = a warp, the FP64 kernel).  No reference
+ * counterpart. */
+int sg_tile_shapes(const sg_ctx *ctx, int *cluster_size, int *pt_lanes);
 
 /* A full 12*nside^2 RING map (write_reduced_map, sanepic.cc:2364-2388). */
 int sg_get_map(sg_ctx *ctx, int kind, double *out_full);

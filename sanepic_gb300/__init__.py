@@ -40,7 +40,7 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
            "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
-           "sg_autotune", "sg_set_pol_rcond",
+           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes",
            "sg_last_error", "sg_destroy"]
 
 
@@ -123,6 +123,7 @@ def load_library(path: Optional[str] = None):
     L.sg_set_pointing.argtypes = [c_p, dp, dp, dp, ctypes.c_long, lp, ctypes.POINTER(SgDet)]
     L.sg_set_noise.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
     L.sg_set_pol_rcond.argtypes = [c_p, ctypes.c_double]
+    L.sg_tile_shapes.argtypes = [c_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.sg_set_tod.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
     L.sg_rhs.argtypes = [c_p, dp]
     L.sg_npix.argtypes = [c_p]
@@ -316,7 +317,9 @@ class MapMaker:
         S = ctypes.c_int(0)
         ms = ctypes.c_double(0.0)
         self._check(self.L.sg_autotune(self.h, ctypes.byref(S), ctypes.byref(ms)))
-        return {"cluster_size": S.value, "filter_ms": ms.value}
+        lanes = ctypes.c_int(0)
+        self._check(self.L.sg_tile_shapes(self.h, ctypes.byref(S), ctypes.byref(lanes)))
+        return {"cluster_size": S.value, "filter_ms": ms.value, "pt_lanes": lanes.value}
 
     # ---- learned preconditioner ---------------------------------------------
     def learn_train(self, npairs: int = 512, seed: int = 5000, steps: int = 1500,

@@ -12,7 +12,9 @@
 // sg_autotune times the noise filter of a context with each compiled tile
 // shape for its segment length (FP32: 8192 or 4096 complex points per CTA of
 // the cluster) on the context's own timeline, or with the offset-group
-// operator one whole operator application, and keeps the faster one.
+// operator one whole operator application, and keeps the faster one; then
+// the P^T reduction's team of lanes per pixel (half, the same and twice the
+// size chosen from the mean samples per pixel), timed on its own.
 #include <cuda_runtime.h>
 
 #include <cstdlib>
@@ -23,6 +25,14 @@
 
 #include "sg_ctx.h"
 #include "sg_kernels.h"
+
+extern "C" int sg_tile_shapes(const sg_ctx* c, int* cluster_size, int* pt_lanes_out) {
+  if (!c) return SG_ERR_ARG;
+  if (!c->have_pointing) return SG_ERR_STATE;
+  if (cluster_size) *cluster_size = c->S;
+  if (pt_lanes_out) *pt_lanes_out = c->f32 ? c->pt_team() : 32;
+  return SG_OK;
+}
 
 extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
   if (!c) return SG_ERR_ARG;
@@ -79,6 +89,36 @@ extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
     c->drop_graphs();  // captured iterations hold the old launch shape
   }
   if (e == cudaSuccess && c->group_mode) e = c->ensure_hmix();  // slot order of the chosen S
+  // the P^T reduction tile: lanes per pixel (FP32 only; the FP64 kernel uses
+  // a warp per pixel).  It reads the per-group-sample sums the filter left.
+  if (e == cudaSuccess && c->f32) {
+    const int L0 = pt_lanes(c->ngsamp, c->npix), Lk = c->pt_L;
+    int bestL = L0;
+    double bestt = 1e30;
+    for (int L : {L0 / 2, L0, 2 * L0}) {
+      if (L < 1 || L > 32) continue;
+      c->pt_L = L;
+      cudaEvent_t a2, b2;
+      cudaEventCreate(&a2);
+      cudaEventCreate(&b2);
+      for (int rep = 0; rep < 6 && e == cudaSuccess; rep++) {  // first launch warms up
+        if (rep == 1) e = cudaEventRecord(a2, c->st);
+        if (e == cudaSuccess) e = c->launch_pt(c->q.as<double>(), true);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(b2, c->st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(b2);
+      float t = 0.f;
+      if (e == cudaSuccess) cudaEventElapsedTime(&t, a2, b2);
+      cudaEventDestroy(a2);
+      cudaEventDestroy(b2);
+      if (e == cudaSuccess && t < bestt) {
+        bestt = t;
+        bestL = L;
+      }
+    }
+    c->pt_L = bestL;
+    if (bestL != (Lk > 0 ? Lk : L0)) c->drop_graphs();  // captured iterations hold the old team
+  }
   if (e != cudaSuccess) return c->cuda_fail(e, "autotune");
   if (cluster_size) *cluster_size = c->S;
   if (ms) *ms = best;

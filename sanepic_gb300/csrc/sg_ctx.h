@@ -250,12 +250,16 @@ struct sg_ctx {
                                  grp_det.as<int>(), dcs.as<double>(), ys.as<double>(), st);
   }
 
+  // lanes per pixel of the FP32 P^T (0: from the mean samples per pixel;
+  // sg_autotune may choose another)
+  int pt_L = 0;
+  int pt_team() const { return pt_L > 0 ? pt_L : pt_lanes(ngsamp, npix); }
   cudaError_t launch_pt(double* out, bool masked) {
     const int* h = masked ? polmask.as<int>() : nullptr;
     launches++;
     if (f32)
       return pt_launch<float>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<float>(),
-                              ys.as<float>(), npix, h, out, pt_lanes(ngsamp, npix), st);
+                              ys.as<float>(), npix, h, out, pt_team(), st);
     return pt_launch<double>(csr_off.as<long long>(), csr_idx.as<uint32_t>(), csr_cs.as<double>(),
                              ys.as<double>(), npix, h, out, 32, st);
   }

@@ -60,10 +60,25 @@ def test_autotune_keeps_the_operator():
     y0 = mm.apply(x)
     t = mm.autotune()
     assert t["cluster_size"] in (2, 4) and t["filter_ms"] > 0
+    assert t["pt_lanes"] in (1, 2, 4, 8, 16, 32)
     y1 = mm.apply(x)
     assert np.linalg.norm(y1 - y0) <= 1e-5 * np.linalg.norm(y0)
     mm.rhs()
     assert mm.solve(precond="bj3", stop_crit=1e-10)["converged"]
+
+
+def test_autotuned_pt_team_is_deterministic():
+    """whatever lane team the autotuner keeps for P^T, A x is the same map
+    (FP32 sums in another order) and is bitwise repeatable"""
+    spec = synth.ProblemSpec("atp", ndet=3, nside=64, nseg=4, ns=16384, fknee=0.1, problem=49,
+                             precision="f32")
+    mm = sg.from_problem(synth.make_problem(spec), precision="f32")
+    x = np.random.default_rng(5).standard_normal(3 * mm.npix)
+    y0 = mm.apply(x)
+    mm.autotune()
+    y1, y2 = mm.apply(x), mm.apply(x)
+    assert np.array_equal(y1, y2)
+    assert np.linalg.norm(y1 - y0) <= 1e-5 * np.linalg.norm(y0)
 
 
 def test_autotune_keeps_the_group_operator():
