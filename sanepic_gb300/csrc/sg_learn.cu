@@ -382,13 +382,18 @@ struct ValSolve {
 };
 
 // PCG from x = 0 on the current b (block-Jacobi, or block-Jacobi + network),
-// timed with CUDA events on the context's stream
+// timed with CUDA events on the context's stream: the start plus the sum of
+// the iterations' own device times (the host reads crit between iterations;
+// those gaps are not counted, as the solves' device-side loop has none)
 cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   const long long n3 = 3 * c->npix;
   CgVecs v1 = c->vecs(1), v2 = c->vecs(2);
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0, e1, ia, ib;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  cudaEventCreate(&ia);
+  cudaEventCreate(&ib);
+  float ms_iter = 0.f;
   // both iteration graphs are captured before the clock starts, so the
   // comparison times iterations, not graph instantiation
   cudaGraphExec_t g0, g1;
@@ -406,17 +411,23 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   } else if (e == cudaSuccess) {
     e = c->to_map(c->d.as<double>());
   }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   const double var00 = c->sc_host->var00;
   int it = 0;
   for (; it < 1000 && e == cudaSuccess; it++) {
-    e = c->run_iteration(pc, it % 10 == 0, true);  // graph replay, as the solves run
+    e = cudaEventRecord(ia, c->st);
+    if (e == cudaSuccess) e = c->run_iteration(pc, it % 10 == 0, true);  // graph replay
+    if (e == cudaSuccess) e = cudaEventRecord(ib, c->st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) break;
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ia, ib);
+    ms_iter += t;
     if (c->sc_host->var / var00 <= stop) {
       out.converged = true;
       it++;
@@ -427,14 +438,14 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
       break;
     }
   }
-  if (e == cudaSuccess) e = cudaEventRecord(e1, c->st);
-  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
   float ms = 0.f;
   if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(ia);
+  cudaEventDestroy(ib);
   out.iters = it;
-  out.ms = ms;
+  out.ms = ms + ms_iter;
   return e;
 }
 
