@@ -92,6 +92,31 @@ def test_noise_filter_vs_oracle(ns, prec):
     assert rel_rms(got, want) < tol
 
 
+@pytest.mark.parametrize("ns", [4096, 131072])
+def test_noise_filter_vs_cufft(ns):
+    # the hand-written cluster FFT filter (FP32) against cuFFT in FP64
+    # (torch.fft): y = c2r(h . r2c(x)) with FFTW's unnormalised scaling and
+    # the weights of sanepic.cc:533-537 -- cuFFT only as a cross-check
+    torch = pytest.importorskip("torch")
+    prob = small_problem(ndet=2, nseg=3, ns=ns, precision="f32")
+    mm = sg.from_problem(prob, precision="f32", with_tod=False)
+    x = np.random.default_rng(ns + 1).standard_normal(2 * 3 * ns)
+    got = mm.noise_filter(x)
+    k = np.arange(ns // 2 + 1, dtype=np.float64)
+    want = []
+    for d in range(2):
+        ispf = prob["ispf"][d]
+        h = ispf[(k / ispf.size * ns).astype(np.int64)] / ns / ns
+        h[0] = ispf[1] * 1e-6 / ns / ns
+        xt = torch.tensor(x[d * 3 * ns:(d + 1) * 3 * ns].reshape(3, ns), dtype=torch.float64,
+                          device="cuda")
+        ht = torch.tensor(h, dtype=torch.float64, device="cuda")
+        yt = torch.fft.irfft(torch.fft.rfft(xt, dim=1) * ht, n=ns, dim=1) * ns
+        want.append(yt.cpu().numpy().reshape(-1))
+    want = np.concatenate(want)
+    assert rel_rms(got, want) < 2e-6
+
+
 # ---- operator ---------------------------------------------------------------------
 # ndet >= 4 on one pointing: the offset-group operator (three timelines per
 # group, 3 x 3 spectral mixing); ndet = 2: one filter per detector
