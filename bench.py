@@ -802,7 +802,7 @@ def main():
     ap.add_argument("--config", default="c2_64det_nside256")
     ap.add_argument("--precond", default="bj3")
     ap.add_argument("--maxiter", type=int, default=2000)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--compare-diag", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget-s", type=float, default=240.0,
