@@ -159,6 +159,44 @@ def test_c2_maps_vs_independent_fp64_operator():
             assert got["rms"] < (2e-4 if stop == 1e-12 else 1e-5), (mode, stop, k, got)
 
 
+def test_c3_maps_vs_independent_fp64_operator():
+    # the largest single-GPU workload (256 detectors, NSIDE 512, half-wave
+    # plate, 1.6e9 samples): the library's FP32 solves against the
+    # independent FP64 operator's, as at C2
+    from fp64_gpu_oracle import Fp64Operator
+    torch = pytest.importorskip("torch")
+    spec = synth.spec_from_name("c3_256det_nside512_hwp")
+    prob = synth.make_problem(spec)
+    op = Fp64Operator(prob)
+    b = op.rhs(prob["tod"])
+    xt, it_t, crit_t = op.solve(b, stop=1e-22, maxiter=300)
+    print(f"independent FP64 solve: {it_t} iterations, crit {crit_t:.2e}")
+    assert crit_t < 1e-20
+    want = op.compact_to_ring_order(xt)
+    del op, b, xt
+    torch.cuda.empty_cache()
+    mm = sg.from_problem(prob, precision="f32")
+    assert mm.npix == want.shape[1]
+    ref = {k: want[c] for c, k in enumerate(MAPS)}
+    errs = {}
+    for mode in ("bj3", "learned"):
+        if mode == "learned":
+            mm.learn_train(npairs=512, steps=-1)
+        for stop in (1e-12, 1e-14):
+            mm.rhs()
+            rep = mm.solve(precond=mode, stop_crit=stop)
+            assert rep["converged"]
+            x = mm.solution().reshape(3, -1)
+            errs[(mode, stop)] = report(
+                f"c3 f32 {mode} {stop:g} ({rep['iterations']} iterations) vs independent FP64",
+                {k: x[c] for c, k in enumerate(MAPS)}, ref)
+    mm.close()
+    for (mode, stop), e in errs.items():
+        for k, (e1, e0) in e.items():
+            got = e0 if k == "I" else e1
+            assert got["rms"] < 1e-5, (mode, stop, k, got)
+
+
 def block_rcond(s):
     """Reciprocal condition number of every observed pixel's 3 x 3 block
     sum w w^T, w = (1, cos 2psi, sin 2psi), from the CPU oracle's angles."""
