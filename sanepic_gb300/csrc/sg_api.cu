@@ -827,6 +827,9 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   const double var00 = c->sc_host->var00, delta0 = c->sc_host->delta0;
   double crit = c->sc_host->var / var00;
   const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
+  // the reference's diagonal mode, and any solve that prints or reports chi2,
+  // keeps the reference's true residual at iteration 0
+  const int skip0 = (pc != 0 && !c->refresh_chi2) ? 1 : 0;
   const int maxiter = o->maxiter > 0 ? o->maxiter : 2000;
   c->crit_hist.clear();
   c->have_solution = true;  // the callback may read the current map
@@ -838,7 +841,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   const char* dl_env = getenv("SANEPIC_GPU_DEVICE_LOOP");
   if (o->use_graph && !o->verbose && !o->on_iteration && !(dl_env && dl_env[0] == '0')) {
     sg_ctx::LoopGraph* lg = nullptr;
-    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0};
+    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0, skip0};
     e = c->ensure_loop_buffers(maxiter);
     if (e == cudaSuccess) e = c->solve_loop_graph(pc, &lg);
     if (e == cudaSuccess)
@@ -854,7 +857,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     if (iter > 0)
       e = cudaMemcpy(c->crit_hist.data(), c->loop_hist.p, sizeof(double) * iter, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return c->cuda_fail(e, "device solve loop");
-    const long long nref = (iter + refresh_every - 1) / refresh_every;
+    const long long nref = refresh_count(iter, refresh_every, skip0);
     c->launches += nref * lg->launches_refresh + (iter - nref) * lg->launches_plain + 2LL * iter;
     crit = c->sc_host->var / var00;
     // a breakdown of the learned part falls back below; any other stop is final
@@ -874,7 +877,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     }
   }
   while (!loop_done && ((iter < maxiter && crit > o->stop_crit) || iter == 0)) {
-    const bool refresh = (iter % refresh_every) == 0;
+    const bool refresh = refresh_at(iter, refresh_every, skip0);
     e = c->run_iteration(pc, refresh, o->use_graph != 0);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);

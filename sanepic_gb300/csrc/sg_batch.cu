@@ -238,7 +238,7 @@ static int solve_batch_device(std::vector<Job>& jobs, const sg_solve_opts* o, in
   for (int i = 0; i < n && e == cudaSuccess; i++) {
     sg_ctx* c = jobs[i].c;
     e = c->ensure_loop_buffers(maxiter);  // (may drop captured graphs)
-    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0};
+    LoopState ls{0, maxiter, refresh_every, 0, o->stop_crit, 0, 0, jobs[i].pc != 0 ? 1 : 0};
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(c->loop_state.p, &ls, sizeof(ls), cudaMemcpyHostToDevice, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -296,7 +296,7 @@ static int solve_batch_device(std::vector<Job>& jobs, const sg_solve_opts* o, in
     j.iter = ls.iter;
     j.var00 = c->sc_host->var00;
     j.crit = c->sc_host->var / j.var00;
-    const long long nr = (ls.iter + refresh_every - 1) / refresh_every;
+    const long long nr = refresh_count(ls.iter, refresh_every, j.pc != 0 ? 1 : 0);
     c->launches += bg.nstart[i] + nr * bg.nref[i] + (ls.iter - nr) * bg.nplain[i] + 2LL * ls.iter;
     if (ls.done == 3 && j.pc == 2 && j.crit > o->stop_crit) {
       // the learned part broke flexible PCG: finish this problem with plain
@@ -309,7 +309,7 @@ static int solve_batch_device(std::vector<Job>& jobs, const sg_solve_opts* o, in
       if (e == cudaSuccess) e = c->to_map(c->d.as<double>());
       c->launches += 7;
       while (e == cudaSuccess && j.iter < maxiter && j.crit > o->stop_crit) {
-        e = c->run_iteration(1, (j.iter % refresh_every) == 0, true);
+        e = c->run_iteration(1, refresh_at(j.iter, refresh_every, 1), true);
         if (e == cudaSuccess)
           e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -439,7 +439,8 @@ extern "C" int sg_solve_batch(sg_ctx** ctxs, int n, const sg_solve_opts* o, sg_r
           continue;
         }
       }
-      e = c->run_iteration(j.pc, (j.iter % refresh_every) == 0, o->use_graph != 0);
+      e = c->run_iteration(j.pc, refresh_at(j.iter, refresh_every, j.pc != 0 ? 1 : 0),
+                           o->use_graph != 0);
       if (e == cudaSuccess) e = enqueue_scalars(j);
       if (e != cudaSuccess) failed = i;
     }

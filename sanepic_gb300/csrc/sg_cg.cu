@@ -451,7 +451,7 @@ cudaError_t apply_precond(const CgVecs& v, const double* x, double* y, cudaStrea
 __global__ void k_loop_begin(const LoopState* s, cudaGraphConditionalHandle refresh,
                              cudaGraphConditionalHandle normal) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const bool r = s->refresh_every <= 1 || (s->iter % s->refresh_every) == 0;
+    const bool r = refresh_at(s->iter, s->refresh_every, s->skip0);
     cudaGraphSetConditional(refresh, r ? 1u : 0u);
     cudaGraphSetConditional(normal, r ? 0u : 1u);
   }

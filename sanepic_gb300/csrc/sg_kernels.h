@@ -247,7 +247,25 @@ struct LoopState {
   int done;           // 1: converged, 2: iteration limit, 3: breakdown flag
   double stop;        // |r|^2 / |b|^2 at which to stop
   unsigned long long t_first, t_last;  // device clock (ns) at the first and last iteration's end
+  int skip0;          // 1: no true residual at iteration 0 (see refresh_at)
 };
+
+// Whether iteration `iter` recomputes the true residual b - A x: every
+// refresh_every-th, as the reference (sanepic.cc:1483-1572).  With skip0 the
+// first one (iteration 0) is left out: after one step from x0 = 0 the
+// recurrence's residual equals b - A x to rounding, so that pass only costs
+// an operator application.  The reference-compatible mode keeps it (its
+// printed chi2 line comes from it).
+__host__ __device__ inline bool refresh_at(int iter, int refresh_every, int skip0) {
+  if (skip0 && iter == 0) return false;
+  return refresh_every <= 1 || (iter % refresh_every) == 0;
+}
+// refresh iterations among the first `iters`
+inline long long refresh_count(int iters, int refresh_every, int skip0) {
+  if (iters <= 0) return 0;
+  long long n = refresh_every <= 1 ? iters : (iters + refresh_every - 1) / refresh_every;
+  return (skip0 && refresh_every > 1) ? n - 1 : n;
+}
 // sets the IF handles of this iteration's variant (refresh or not)
 cudaError_t loop_begin_launch(const LoopState* s, cudaGraphConditionalHandle refresh,
                               cudaGraphConditionalHandle normal, cudaStream_t st);

@@ -420,7 +420,7 @@ cudaError_t val_solve(sg_ctx* c, int pc, double stop, ValSolve& out) {
   int it = 0;
   for (; it < 1000 && e == cudaSuccess; it++) {
     e = cudaEventRecord(ia, c->st);
-    if (e == cudaSuccess) e = c->run_iteration(pc, it % 10 == 0, true);  // graph replay
+    if (e == cudaSuccess) e = c->run_iteration(pc, refresh_at(it, 10, 1), true);  // graph replay
     if (e == cudaSuccess) e = cudaEventRecord(ib, c->st);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(c->sc_host, c->sc.p, sizeof(CgScalars), cudaMemcpyDeviceToHost, c->st);
