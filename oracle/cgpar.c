@@ -35,7 +35,13 @@
 
 #define CP_MAXW 256
 
+typedef struct cp_ctx cp_ctx;
 typedef struct {
+  cp_ctx *c;
+  int w;
+} cp_arg;
+
+struct cp_ctx {
   long ns, nseg, ndet, nside, nssp, npixfull, npix;
   const double *ra, *dec, *psi, *psidet, *ispf, *tod;
   const long *isampmin;
@@ -57,12 +63,8 @@ typedef struct {
   const double *vin;               /* the map an apply reads */
   double *vout;                    /* where the reduction writes */
   pthread_barrier_t start, done, mid;
-} cp_ctx;
-
-typedef struct {
-  cp_ctx *c;
-  int w;
-} cp_arg;
+  cp_arg args[CP_MAXW];            /* the workers' arguments (live as long as c) */
+};
 
 enum { T_EXIT, T_POINTING, T_SEEN, T_RHS, T_PRECOND, T_APPLY };
 
@@ -189,7 +191,8 @@ static void run(cp_ctx *c, int task) {
  * reference's order), crit_hist (maxiter doubles), times[0..4] = setup, rhs,
  * precond, solve seconds and the seconds from the end of setup until crit
  * first reached stop_crit, *npix_out, *iters_out.  Returns 0, -1 on an
- * ang2pix range error, -2 on bad arguments.
+ * ang2pix range error, -2 on bad arguments, -3 if a worker thread could not
+ * be started.
  */
 int cp_run(long ns, long nseg, long ndet, long nside, const double *ra, const double *dec,
            const double *psi, const long *isampmin, const double *psidet, int hwp,
@@ -236,11 +239,14 @@ int cp_run(long ns, long nseg, long ndet, long nside, const double *ra, const do
   pthread_barrier_init(&c->done, NULL, nw + 1);
   pthread_barrier_init(&c->mid, NULL, nw);
   pthread_t th[CP_MAXW];
-  cp_arg args[CP_MAXW];
   for (int w = 0; w < nw; w++) {
-    args[w].c = c;
-    args[w].w = w;
-    pthread_create(&th[w], NULL, worker, &args[w]);
+    c->args[w].c = c;
+    c->args[w].w = w;
+    if (pthread_create(&th[w], NULL, worker, &c->args[w]) != 0) {
+      /* the workers already started wait on a barrier that can no longer
+       * fill: leave them (and c, which they read) and report the failure */
+      return -3;
+    }
   }
   const double t_begin = now_s();
   int rc = 0;
