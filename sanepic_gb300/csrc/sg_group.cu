@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int q = 0; q < 6; q++) a[u][q] = T(0);
     T cl = T(0);
+#pragma unroll 4
     for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
       const int d = grp_det[e];
       const cplx<T>* x = dspec + ((long long)d * nseg + seg) * M1 + k0;
