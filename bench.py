@@ -11,7 +11,9 @@ Workload (default): 64 detectors, NSIDE 256, 48 segments x 131,072 samples
 (4.03e8 samples), FP32 operator with FP64 P^T sums and CG scalars, seeded
 synthetic scan/sky/1-over-f noise (sanepic_gb300.synth).  One step = one
 solve from x0 = 0 to |r|/|b| <= 1e-6 (crit = |r|^2/|b|^2 <= 1e-12):
-  value: b = P^T N^-1 d plus the PCG in the learned-preconditioner mode,
+  value: b = P^T N^-1 d (sg_rhs without chi2_0, a diagnostic; detectors
+         sharing pointing and noise spectrum are then summed before the
+         FFTs) plus the PCG in the learned-preconditioner mode,
          inputs already resident in HBM, CUDA-event time on the library's
          stream (the bench's torch stream).  The network is trained and
          judged by plain PCG before the timed region (training time is
@@ -168,7 +170,7 @@ def run_ours(args):
     upload(mm)
 
     def device_step(precond):
-        mm.rhs()
+        mm.rhs(chi2=False)  # b only: chi2_0 is a diagnostic, not part of the solution
         return mm.solve(precond=precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
 
     # ---- the learned preconditioner: trained and judged before timing --------
@@ -411,7 +413,7 @@ def map_error(sg, mm, spec, prob, dets, precond, stream, args):
     for d in range(spec.ndet):
         m64.set_noise(d, prob["ispf"][d])
         m64.set_tod(d, prob["tod"][d])
-    m64.rhs()
+    m64.rhs(chi2=False)
     r64 = m64.solve(precond="bj3", stop_crit=1e-15, maxiter=args.maxiter)
     x64 = m64.solution()
     m64.close()
@@ -424,7 +426,7 @@ def map_error(sg, mm, spec, prob, dets, precond, stream, args):
         key = "learned" if pc == "learned" else pc
         sweep = []
         for stop in (STOP_CRIT, 1e-13, 1e-14):
-            mm.rhs()
+            mm.rhs(chi2=False)
             rep = mm.solve(precond=pc, stop_crit=stop, maxiter=args.maxiter)
             errs = _map_errs(mm.solution(), x64, npix)
             worst = max(errs[k]["rms"] for k in "IQU")
@@ -459,14 +461,14 @@ def per_detector(sg, spec, prob, dets, stream, args):
         mp.set_tod(d, prob["tod"][d])
     assert not mp.group_mode()[0]
     for _ in range(2):
-        mp.rhs()
+        mp.rhs(chi2=False)
         mp.solve(precond=args.precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 3
     ev0.record(stream)
     for _ in range(reps):
-        mp.rhs()
+        mp.rhs(chi2=False)
         rep = mp.solve(precond=args.precond, stop_crit=STOP_CRIT, maxiter=args.maxiter)
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -527,14 +529,14 @@ def c3_block(sg, stream, args):
     sols = {}
     for pc in ("bj3", "learned"):
         for _ in range(2):
-            mm.rhs()
+            mm.rhs(chi2=False)
             mm.solve(precond=pc, stop_crit=STOP_CRIT, maxiter=args.maxiter)
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         reps = 3
         ev0.record(stream)
         for _ in range(reps):
-            mm.rhs()
+            mm.rhs(chi2=False)
             rep = mm.solve(precond=pc, stop_crit=STOP_CRIT, maxiter=args.maxiter)
         ev1.record(stream)
         torch.cuda.synchronize()
@@ -553,7 +555,7 @@ def c3_block(sg, stream, args):
     for d in range(spec.ndet):
         m64.set_noise(d, prob["ispf"][d])
         m64.set_tod(d, prob["tod"][d])
-    m64.rhs()
+    m64.rhs(chi2=False)
     r64 = m64.solve(precond="bj3", stop_crit=1e-15, maxiter=args.maxiter)
     x64 = m64.solution()
     m64.close()

@@ -151,7 +151,10 @@ int sg_set_noise(sg_ctx *ctx, long det, const double *ispf, long nssp);
 int sg_set_tod(sg_ctx *ctx, long det, const double *tod, long nsamp_total);
 
 /* b = P^T N^-1 d (sanepic.cc:1069-1125).  chi2 (may be NULL) receives the
- * reference's chi2_0 = 2 sum |F d|^2 SpN (sanepic.cc:1089-1110). */
+ * reference's chi2_0 = 2 sum |F d|^2 SpN (sanepic.cc:1089-1110).  Without
+ * it, offset groups whose detectors all have the same noise spectrum sum
+ * their timelines before the FFTs (three FFT pairs per group and segment
+ * instead of one FFT per detector; the same b up to rounding). */
 int sg_rhs(sg_ctx *ctx, double *chi2);
 
 /* Number of observed pixels (npix, sanepic.cc:915). */

@@ -240,10 +240,15 @@ class MapMaker:
         self._check(self.L.sg_set_tod(self.h, det, _dp(tod), tod.size))
 
     # ---- operator -----------------------------------------------------------
-    def rhs(self) -> float:
-        chi2 = ctypes.c_double(0.0)
-        self._check(self.L.sg_rhs(self.h, ctypes.byref(chi2)))
-        return chi2.value
+    def rhs(self, chi2: bool = True) -> Optional[float]:
+        """b = P^T N^-1 d; returns chi2_0, or None with chi2=False (then groups
+        of detectors with one noise spectrum skip the per-detector FFTs)."""
+        if not chi2:
+            self._check(self.L.sg_rhs(self.h, None))
+            return None
+        c = ctypes.c_double(0.0)
+        self._check(self.L.sg_rhs(self.h, ctypes.byref(c)))
+        return c.value
 
     def apply(self, x, masked: bool = False) -> np.ndarray:
         x = _f64(x)

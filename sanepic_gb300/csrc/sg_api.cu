@@ -568,10 +568,13 @@ extern "C" int sg_rhs(sg_ctx* c, double* chi2) {
   int rc = check_ready(c, true);
   if (rc) return rc;
   cudaSetDevice(c->desc.device);
-  double* dchi2 = &c->sc.as<CgScalars>()->chi2;
+  // chi2_0 only when asked for: without it, offset groups whose detectors
+  // share one noise spectrum skip the per-detector FFTs (rhs_of)
+  double* dchi2 = chi2 ? &c->sc.as<CgScalars>()->chi2 : nullptr;
   cudaError_t e = c->rhs_of(c->tod.p, c->b.as<double>(), dchi2);
   double h = 0.0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dchi2, sizeof(double), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess && chi2)
+    e = cudaMemcpyAsync(&h, dchi2, sizeof(double), cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "rhs");
   if (chi2) *chi2 = h;  // chi2_0 (sanepic.cc:1089-1110)

@@ -353,16 +353,40 @@ struct sg_ctx {
                                         filt_slot.as<double>(), st);
     }
     launches += 2;
+    // do all detectors of each group share one noise spectrum?  Then the
+    // right-hand side needs no per-detector FFT (rhs_of)
+    DevBuf same;
+    if (e == cudaSuccess) e = same.alloc(sizeof(int) * ndet);
+    if (e == cudaSuccess) e = cudaMemsetAsync(same.p, 0, sizeof(int) * ndet, st);
+    if (e == cudaSuccess)
+      e = f32 ? rows_match_group_launch<float>(filt.as<float>(), M1, grp_off.as<int>(),
+                                               grp_det.as<int>(), ngroups, grp_off_h[ngroups],
+                                               same.as<int>(), st)
+              : rows_match_group_launch<double>(filt.as<double>(), M1, grp_off.as<int>(),
+                                                grp_det.as<int>(), ngroups, grp_off_h[ngroups],
+                                                same.as<int>(), st);
+    std::vector<int> same_h(ndet, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(same_h.data(), same.p, sizeof(int) * ndet, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    groups_uniform = e == cudaSuccess;
+    for (long long d = 0; d < ndet && groups_uniform; d++) groups_uniform = same_h[d] == 1;
+    launches += 1;
     if (e == cudaSuccess) {
       have_hmix = true;
       hmix_S = S;
     }
     return e;
   }
+  bool groups_uniform = false;  // every offset group's detectors share one noise spectrum
 
   // b = P^T N^-1 d for the timelines d (device, one row per detector) and
   // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
   // their weighted sums per group and frequency, three inverse FFTs per group.
+  // With chi2_dev null and one noise spectrum per group, the detectors'
+  // timelines are summed per group first: 3 FFT pairs per group and segment
+  // instead of one forward FFT per detector and segment (same map; only the
+  // rounding differs).
   cudaError_t rhs_of(const void* d, double* bout, double* chi2_dev) {
     if (!group_mode) {
       cudaError_t e = launch_filter(kLoadTod, d, y.p, ntiles, (int)nseg, 0, nullptr, chi2_dev);
@@ -370,6 +394,30 @@ struct sg_ctx {
       return e;
     }
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
+    if (!chi2_dev && groups_uniform) {
+      cudaError_t e;
+      launches += 2;  // sums, scaling
+      if (f32) {
+        e = group_tod_rhs_launch<float>((const float*)d, nsd, grp_off.as<int>(), grp_det.as<int>(),
+                                        dcs.as<float>(), ngroups, gtl.as<float>(), st);
+        if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
+        if (e == cudaSuccess)
+          e = group_scale_launch<float>(gspec.as<cplx<float>>(), filt_slot.as<float>(),
+                                        grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1, st);
+      } else {
+        e = group_tod_rhs_launch<double>((const double*)d, nsd, grp_off.as<int>(),
+                                         grp_det.as<int>(), dcs.as<double>(), ngroups,
+                                         gtl.as<double>(), st);
+        if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
+        if (e == cudaSuccess)
+          e = group_scale_launch<double>(gspec.as<cplx<double>>(), filt_slot.as<double>(),
+                                         grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
+                                         st);
+      }
+      if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
+      if (e == cudaSuccess) e = launch_pt(bout, true);
+      return e;
+    }
     cudaError_t e = launch_filter_spec(d, nullptr, dspec.p, nullptr, ntiles);
     launches += 2;  // sums, chi^2
     if (f32) {
@@ -386,7 +434,8 @@ struct sg_ctx {
                                      gspec.as<cplx<double>>(), rhs_part.as<double>(),
                                      kGroupRhsBlocks, st);
     }
-    if (e == cudaSuccess) e = chi2_sum(rhs_part.as<double>(), kGroupRhsBlocks, chi2_dev, st);
+    if (e == cudaSuccess && chi2_dev)
+      e = chi2_sum(rhs_part.as<double>(), kGroupRhsBlocks, chi2_dev, st);
     if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
     if (e == cudaSuccess) e = launch_pt(bout, true);
     return e;

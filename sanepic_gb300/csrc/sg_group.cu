@@ -170,6 +170,91 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// A group whose detectors all have the same noise spectrum h needs no
+// per-detector FFT for its right-hand side: sum_d h X_d (1, c_d, s_d) =
+// h FFT(sum_d d_d (1, c_d, s_d)), so the detectors' timelines are summed
+// first (gtl [G][3][nsd], detectors in list order, FP32) ...
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_tod_sums(const T* __restrict__ tod, long long nsd, const int* __restrict__ grp_off,
+                     const int* __restrict__ grp_det, const T* __restrict__ dcs, long long G,
+                     T* __restrict__ gtl) {
+  const long long n = G * nsd;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i / nsd, w = i - g * nsd;
+    T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll 4
+    for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
+      const int d = grp_det[e];
+      const T x = tod[(long long)d * nsd + w];
+      s0 += x;
+      s1 = fma(dcs[2 * d], x, s1);
+      s2 = fma(dcs[2 * d + 1], x, s2);
+    }
+    T* o = gtl + 3 * g * nsd + w;
+    o[0] = s0;
+    o[nsd] = s1;
+    o[2 * nsd] = s2;
+  }
+}
+
+// ... and their half spectra [G][3][nseg][M+1] (slot order) are scaled by the
+// group's one filter row (filt [ndet][M+1] in slot order; its first detector's)
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_scale(cplx<T>* __restrict__ spec, const T* __restrict__ filt,
+                  const int* __restrict__ grp_off, const int* __restrict__ grp_det, long long G,
+                  long long nseg, long long M1) {
+  const long long n = G * 3 * nseg * M1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % M1, g = i / (3 * nseg * M1);
+    const T h = filt[(long long)grp_det[grp_off[g]] * M1 + k];
+    spec[i] = cscale(spec[i], h);
+  }
+}
+
+// same[d] = 1 if detector d's filter row equals (bitwise) the row of its
+// group's first detector; one block per detector
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_rows_match_group(const T* __restrict__ filt, long long M1, const int* __restrict__ grp_off,
+                       const int* __restrict__ grp_det, long long G, int* __restrict__ same) {
+  const long long e = blockIdx.x;  // position in the group lists
+  int g = 0;
+  while (g + 1 < G && grp_off[g + 1] <= e) g++;
+  const int d = grp_det[e], d0 = grp_det[grp_off[g]];
+  const T* a = filt + (long long)d * M1;
+  const T* b = filt + (long long)d0 * M1;
+  int diff = 0;
+  for (long long k = threadIdx.x; k < M1 && !diff; k += blockDim.x) diff = a[k] != b[k];
+  diff = __syncthreads_or(diff);
+  if (threadIdx.x == 0) same[d] = diff ? 0 : 1;
+}
+
+template <typename T>
+cudaError_t group_tod_rhs_launch(const T* tod, long long nsd, const int* grp_off,
+                                 const int* grp_det, const T* dcs, long long G, T* gtl,
+                                 cudaStream_t st) {
+  k_group_tod_sums<T><<<blocks_for(G * nsd), 256, 0, st>>>(tod, nsd, grp_off, grp_det, dcs, G, gtl);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t group_scale_launch(cplx<T>* spec, const T* filt, const int* grp_off, const int* grp_det,
+                               long long G, long long nseg, long long M1, cudaStream_t st) {
+  k_group_scale<T><<<blocks_for(G * 3 * nseg * M1), 256, 0, st>>>(spec, filt, grp_off, grp_det, G,
+                                                                  nseg, M1);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t rows_match_group_launch(const T* filt, long long M1, const int* grp_off,
+                                    const int* grp_det, long long G, long long ndet_listed,
+                                    int* same, cudaStream_t st) {
+  k_rows_match_group<T><<<(unsigned)ndet_listed, 256, 0, st>>>(filt, M1, grp_off, grp_det, G, same);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
                              const int* grp_det, long long G, long long nseg, long long M1,
@@ -231,7 +316,13 @@ cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, l
                                               cudaStream_t);                                     \
   template cudaError_t group_rhs_launch<T>(const cplx<T>*, const T*, const T*, const int*,       \
                                            const int*, long long, long long, long long,          \
-                                           cplx<T>*, double*, int, cudaStream_t);
+                                           cplx<T>*, double*, int, cudaStream_t);                \
+  template cudaError_t group_tod_rhs_launch<T>(const T*, long long, const int*, const int*,      \
+                                               const T*, long long, T*, cudaStream_t);           \
+  template cudaError_t group_scale_launch<T>(cplx<T>*, const T*, const int*, const int*,         \
+                                             long long, long long, long long, cudaStream_t);     \
+  template cudaError_t rows_match_group_launch<T>(const T*, long long, const int*, const int*,   \
+                                                  long long, long long, int*, cudaStream_t);
 SG_GROUP_INST(float)
 SG_GROUP_INST(double)
 

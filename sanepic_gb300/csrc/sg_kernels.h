@@ -178,6 +178,22 @@ template <typename T>
 cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
                              const int* grp_det, long long G, long long nseg, long long M1,
                              cplx<T>* gspec, double* chi2_part, int nblocks, cudaStream_t st);
+// groups whose detectors share one noise spectrum: gtl [G][3][nsd] = the
+// detectors' timelines summed with weights (1, c_d, s_d); then the group's
+// half spectra [G][3][nseg][M+1] scaled by its (first detector's) filter row
+template <typename T>
+cudaError_t group_tod_rhs_launch(const T* tod, long long nsd, const int* grp_off,
+                                 const int* grp_det, const T* dcs, long long G, T* gtl,
+                                 cudaStream_t st);
+template <typename T>
+cudaError_t group_scale_launch(cplx<T>* spec, const T* filt, const int* grp_off, const int* grp_det,
+                               long long G, long long nseg, long long M1, cudaStream_t st);
+// same[d] = 1 if detector d's filter row equals its group's first detector's
+// (one block per listed detector, ndet_listed = grp_off[G])
+template <typename T>
+cudaError_t rows_match_group_launch(const T* filt, long long M1, const int* grp_off,
+                                    const int* grp_det, long long G, long long ndet_listed,
+                                    int* same, cudaStream_t st);
 // hmix [G][slot][6] = sum_d h_d[kslot[slot]] (1, c, s, cc, cs, ss) over each group's detectors
 template <typename T>
 cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, const int* grp_det,

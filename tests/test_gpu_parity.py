@@ -318,3 +318,27 @@ def test_device_loop_matches_host_loop(prec, monkeypatch):
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("hwp", [False, True])
+def test_rhs_without_chi2_sums_detectors_with_one_noise_spectrum(hwp):
+    # every detector with the same iSpf: without chi2_0 the right-hand side
+    # sums the group's timelines before the FFTs; the map is the same
+    prob = small_problem(ndet=6, nside=32, nseg=4, ns=8192, precision="f32", hwp=hwp)
+    mm = sg.from_problem(prob, precision="f32")
+    assert mm.group_mode()[0]
+    chi2 = mm.rhs()
+    assert chi2 > 0
+    mm.solve(precond="bj3", stop_crit=1e-14)
+    x1 = mm.solution()
+    assert mm.rhs(chi2=False) is None
+    mm.solve(precond="bj3", stop_crit=1e-14)
+    x2 = mm.solution()
+    npix = mm.npix
+    s = oracle.Setup(prob)
+    b, _ = s.rhs(prob["tod"])
+    xo, _, _ = s.pcg(b, precond="bj3", stop_crit=1e-15, maxiter=500)
+    for c in range(3):
+        blk = slice(c * npix, (c + 1) * npix)
+        assert rel_rms(x2[blk], x1[blk], remove_monopole=(c == 0)) < 1e-5, c
+        assert rel_rms(x2[blk], xo[blk], remove_monopole=(c == 0)) < 1e-5, c
