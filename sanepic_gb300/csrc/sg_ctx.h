@@ -217,7 +217,7 @@ struct sg_ctx {
   // chi2_out (device double) receives 2 sum h |X|^2 over all tiles when set
   cudaError_t launch_filter(int mode, const void* in, void* out, long long ntiles_, int nseg_,
                             int filt_abs, const void* sub = nullptr, double* chi2_out = nullptr,
-                            const void* table = nullptr) {
+                            const void* table = nullptr, int ilv3 = 0) {
     const int ncl = (int)std::min<long long>(nclusters, ntiles_);
     double* part = chi2_out ? chi2p.as<double>() : nullptr;
     cudaError_t e;
@@ -226,11 +226,13 @@ struct sg_ctx {
       auto a = filter_args<float>(mode, (const float*)in, (float*)out, ntiles_, nseg_, filt_abs,
                                   (const float*)sub, part, (const float*)table);
       a.wn1 = wn1f;
+      a.ilv3 = ilv3;
       e = filter_launch<float>(a, logm, S, ncl, st);
     } else {
       auto a = filter_args<double>(mode, (const double*)in, (double*)out, ntiles_, nseg_,
                                    filt_abs, (const double*)sub, part, (const double*)table);
       a.wn1 = wn1d;
+      a.ilv3 = ilv3;
       e = filter_launch<double>(a, logm, S, ncl, st);
     }
     if (e == cudaSuccess && chi2_out) {
@@ -372,6 +374,25 @@ struct sg_ctx {
     groups_uniform = e == cudaSuccess;
     for (long long d = 0; d < ndet && groups_uniform; d++) groups_uniform = same_h[d] == 1;
     launches += 1;
+    // uniform groups: W per group and the group's filter row for each of its
+    // three timelines (tile row g * 3 + component), natural frequency order
+    if (e == cudaSuccess && groups_uniform) {
+      e = wmix.alloc((size_t)6 * ngroups * esize);
+      if (e == cudaSuccess) e = gfilt.alloc((size_t)3 * ngroups * M1 * esize);
+      if (e == cudaSuccess)
+        e = f32 ? group_wmix_launch<float>(dcs.as<float>(), grp_off.as<int>(), grp_det.as<int>(),
+                                           ngroups, wmix.as<float>(), st)
+                : group_wmix_launch<double>(dcs.as<double>(), grp_off.as<int>(), grp_det.as<int>(),
+                                            ngroups, wmix.as<double>(), st);
+      for (long long g = 0; g < ngroups && e == cudaSuccess; g++) {
+        const long long d0 = grp_det_h[grp_off_h[g]];
+        for (int comp = 0; comp < 3 && e == cudaSuccess; comp++)
+          e = cudaMemcpyAsync((char*)gfilt.p + (size_t)(3 * g + comp) * M1 * esize,
+                              (const char*)filt.p + (size_t)d0 * M1 * esize, (size_t)M1 * esize,
+                              cudaMemcpyDeviceToDevice, st);
+      }
+      launches += 1;
+    }
     if (e == cudaSuccess) {
       have_hmix = true;
       hmix_S = S;
@@ -379,6 +400,7 @@ struct sg_ctx {
     return e;
   }
   bool groups_uniform = false;  // every offset group's detectors share one noise spectrum
+  DevBuf wmix, gfilt;           // uniform groups: W [G][6]; filter rows [3 G][M+1]
 
   // b = P^T N^-1 d for the timelines d (device, one row per detector) and
   // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
@@ -446,6 +468,21 @@ struct sg_ctx {
   cudaError_t apply_map_group(double* out, bool masked) {
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
     cudaError_t e;
+    if (groups_uniform) {
+      // one noise spectrum per group: mix by W in the time domain, then the
+      // fused filter (forward FFT, x h, inverse FFT in one pass) per timeline,
+      // stored straight into P^T's layout
+      launches += 1;
+      e = f32 ? group_project_w_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(),
+                                              wmix.as<float>(), ngsamp, nsd, gtl.as<float>(), st)
+              : group_project_w_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(),
+                                               wmix.as<double>(), ngsamp, nsd, gtl.as<double>(),
+                                               st);
+      if (e == cudaSuccess)
+        e = launch_filter(kLoadTod, gtl.p, ys.p, gt, (int)nseg, 0, nullptr, nullptr, gfilt.p, 1);
+      if (e == cudaSuccess) e = launch_pt(out, masked);
+      return e;
+    }
     launches += 2;  // projection, mixing
     if (f32) {
       e = group_project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
     // segment side by side (L = (group * nseg + segment) * 3 + component), so
     // that their stores into the same 96-byte blocks meet in L2
     long long tile = L;
-    if (MODE == kSpecIn && p.ilv3) {
+    if (MODE != kSpecOut && p.ilv3) {
       const long long q = L % (3LL * p.nseg);
       tile = (L - q) + (q % 3) * p.nseg + q / 3;
     }
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(kFilterThreads, sizeof(T) == 4 ? 2 : 1)
         });
     __syncthreads();
     // ---- 11. store -------------------------------------------------------------
-    if (MODE == kSpecIn && p.ilv3) {
+    if (MODE != kSpecOut && p.ilv3) {
       // component (tile / nseg) % 3 of the [group sample / 8][3][8] layout P^T
       // reads, tile = (group * 3 + component) * nseg + segment: a sample pair
       // is 8 contiguous bytes (FP32), four lanes fill one 32-byte sector

@@ -45,6 +45,63 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Uniform groups (one noise spectrum h for all the group's detectors):
+// H = h W with the constant W = sum_d [1 c s]^T [1 c s], so W mixes the three
+// timelines before the filter instead of per frequency after it:
+// gtl = W (a, b1, b2), then N^-1 on each by the fused filter kernel.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_group_project_w(const int* __restrict__ gpix, const T* __restrict__ gcs,
+                      const T* __restrict__ map, const T* __restrict__ wmix, long long ng,
+                      long long nsd, T* __restrict__ gtl) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i / nsd, w = i - g * nsd;
+    const int m = gpix[i];
+    const T c = gcs[2 * i], s = gcs[2 * i + 1];
+    const T I = map[4 * (long long)m], Q = map[4 * (long long)m + 1], U = map[4 * (long long)m + 2];
+    const T a = I, b1 = Q * c + U * s, b2 = U * c - Q * s;
+    const T* W = wmix + 6 * g;  // W00 W01 W02 W11 W12 W22
+    T* o = gtl + 3 * g * nsd + w;
+    o[0] = W[0] * a + W[1] * b1 + W[2] * b2;
+    o[nsd] = W[1] * a + W[3] * b1 + W[4] * b2;
+    o[2 * nsd] = W[2] * a + W[4] * b1 + W[5] * b2;
+  }
+}
+
+// wmix [G][6] = sum over the group's detectors of (1, c, s, cc, cs, ss), FP64 sums
+template <typename T>
+__global__ void k_group_wmix(const T* __restrict__ dcs, const int* __restrict__ grp_off,
+                             const int* __restrict__ grp_det, long long G, T* __restrict__ wmix) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int e = grp_off[g]; e < grp_off[g + 1]; e++) {
+    const int d = grp_det[e];
+    const double c = (double)dcs[2 * d], s = (double)dcs[2 * d + 1];
+    acc[0] += 1.0;
+    acc[1] += c;
+    acc[2] += s;
+    acc[3] += c * c;
+    acc[4] += c * s;
+    acc[5] += s * s;
+  }
+  for (int j = 0; j < 6; j++) wmix[6 * g + j] = (T)acc[j];
+}
+
+template <typename T>
+cudaError_t group_project_w_launch(const int* gpix, const T* gcs, const T* map, const T* wmix,
+                                   long long ng, long long nsd, T* gtl, cudaStream_t st) {
+  k_group_project_w<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, wmix, ng, nsd, gtl);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t group_wmix_launch(const T* dcs, const int* grp_off, const int* grp_det, long long G,
+                              T* wmix, cudaStream_t st) {
+  k_group_wmix<T><<<(unsigned)((G + 127) / 128), 128, 0, st>>>(dcs, grp_off, grp_det, G, wmix);
+  return cudaGetLastError();
+}
+
 // in place on the half spectra [G][3][nseg][M+1]: (S0, S1, S2) = H (a, b1, b2)
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -322,7 +379,11 @@ cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, l
   template cudaError_t group_scale_launch<T>(cplx<T>*, const T*, const int*, const int*,         \
                                              long long, long long, long long, cudaStream_t);     \
   template cudaError_t rows_match_group_launch<T>(const T*, long long, const int*, const int*,   \
-                                                  long long, long long, int*, cudaStream_t);
+                                                  long long, long long, int*, cudaStream_t);     \
+  template cudaError_t group_project_w_launch<T>(const int*, const T*, const T*, const T*,        \
+                                                 long long, long long, T*, cudaStream_t);        \
+  template cudaError_t group_wmix_launch<T>(const T*, const int*, const int*, long long, T*,     \
+                                            cudaStream_t);
 SG_GROUP_INST(float)
 SG_GROUP_INST(double)
 

@@ -28,7 +28,7 @@ struct FilterArgs {
   T* out;            // [ntiles][ns]
   cplx<T>* spec_out;       // if set: forward FFT only, X[k] (k = 0..M) [ntiles][M+1]
   const cplx<T>* spec_in;  // if set: inverse FFT only of Y[k] [ntiles][M+1]
-  int ilv3;                // with spec_in: out is [groups][nseg * ns / 8][3][8], tile = (group * 3 + component) * nseg + segment
+  int ilv3;                // with spec_in or the fused filter: out is [groups][nseg * ns / 8][3][8], tile = (group * 3 + component) * nseg + segment
   const cplx<T>* tw_lo;
   const cplx<T>* tw_hi;
   cplx<T> wn1;
@@ -178,6 +178,14 @@ template <typename T>
 cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, const int* grp_off,
                              const int* grp_det, long long G, long long nseg, long long M1,
                              cplx<T>* gspec, double* chi2_part, int nblocks, cudaStream_t st);
+// uniform groups in the operator: gtl = W (a, b1, b2) with wmix [G][6] =
+// sum_d (1, c, s, cc, cs, ss); N^-1 then filters each timeline on its own
+template <typename T>
+cudaError_t group_project_w_launch(const int* gpix, const T* gcs, const T* map, const T* wmix,
+                                   long long ng, long long nsd, T* gtl, cudaStream_t st);
+template <typename T>
+cudaError_t group_wmix_launch(const T* dcs, const int* grp_off, const int* grp_det, long long G,
+                              T* wmix, cudaStream_t st);
 // groups whose detectors share one noise spectrum: gtl [G][3][nsd] = the
 // detectors' timelines summed with weights (1, c_d, s_d); then the group's
 // half spectra [G][3][nseg][M+1] scaled by its (first detector's) filter row
