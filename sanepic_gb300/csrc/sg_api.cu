@@ -1049,7 +1049,22 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   const long long nsd = c->ns * c->nseg, M1 = c->ns / 2 + 1, gt = 3LL * c->ngroups * c->nseg;
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
     e = cudaEventRecord(ev[0], c->st);
-    if (c->group_mode) {
+    if (c->group_mode && c->groups_uniform) {
+      // one noise spectrum per group: projection mixed by W; N^-1 = the fused
+      // filter on each of the three timelines (written in P^T's layout)
+      if (e == cudaSuccess)
+        e = c->f32 ? group_project_w_launch<float>(c->pix.as<int>(), c->cs.as<float>(),
+                                                   c->dmap.as<float>(), c->wmix.as<float>(),
+                                                   c->ngsamp, nsd, c->gtl.as<float>(), c->st)
+                   : group_project_w_launch<double>(c->pix.as<int>(), c->cs.as<double>(),
+                                                    c->dmap.as<double>(), c->wmix.as<double>(),
+                                                    c->ngsamp, nsd, c->gtl.as<double>(), c->st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
+      if (e == cudaSuccess)
+        e = c->launch_filter(kLoadTod, c->gtl.p, c->ys.p, gt, (int)c->nseg, 0, nullptr, nullptr,
+                             c->gfilt.p, 1);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
+    } else if (c->group_mode) {
       // projection = (a, b1, b2); N^-1 = forward FFTs + 3 x 3 mixing + inverse
       // FFTs (written in P^T's layout); no detector sums
       if (c->f32) {
