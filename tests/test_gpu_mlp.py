@@ -38,13 +38,15 @@ def test_network_gradients_match_oracle():
     T = (rng.normal(size=(256, 768)) * 0.3).astype(np.float32)
     Y, loss, g = sg.mlp_grad(p, X, T)
     Yo, loss_o, go = mlp.forward_backward(p, X, T)
-    assert np.linalg.norm(Y - Yo) / np.linalg.norm(Yo) < 1e-2
+    # both sides follow the same BF16 rounding contract; what remains is the
+    # FP32 accumulation order (measured: Y 1.4e-4, gradients 3e-5 .. 5e-4)
+    assert np.linalg.norm(Y - Yo) / np.linalg.norm(Yo) < 1e-3
     assert abs(loss - loss_o) / loss_o < 1e-3
     offs = np.cumsum([0] + [o * i + o for i, o in zip(mlp.LAYER_IN, mlp.LAYER_OUT)])
     for l in range(4):
         a, b = g[offs[l]:offs[l + 1]], go[offs[l]:offs[l + 1]]
-        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-2, l
-        assert np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b)) > 0.999, l
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-3, l
+        assert np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b)) > 0.99999, l
 
 
 def _rel(a, b, npix):
