@@ -161,8 +161,11 @@ int sg_rhs(sg_ctx *ctx, double *chi2);
 long sg_npix(const sg_ctx *ctx);
 /* 1 if the operator runs per offset group (detectors with identical
  * focal-plane offsets, at least 4 in every group, share one pixel stream:
- * three timelines per group instead of one per detector), else 0; *ngroups
- * (if non-null) receives the number of groups.  No reference counterpart. */
+ * three timelines per group instead of one per detector), 2 if it does and
+ * weights the group timelines with the three-pass FP32 FFT (in place in the
+ * layout P^T reads; known once the operator was prepared by a first apply,
+ * right-hand side or solve), else 0; *ngroups (if non-null) receives the
+ * number of groups.  No reference counterpart. */
 int sg_group_mode(const sg_ctx *ctx, long *ngroups);
 
 /* y = P^T N^-1 P x for a compact host vector [3*npix] (one operator pass,

@@ -317,6 +317,13 @@ class MapMaker:
         on = bool(self.L.sg_group_mode(self.h, ctypes.byref(n)))
         return on, int(n.value)
 
+    def weighting(self) -> str:
+        """How the operator applies N^-1: "per-detector" (one fused filter per
+        detector timeline), "group" (cluster FFT kernels on the offset
+        groups' three timelines) or "group-3pass" (the three-pass FP32 FFT in
+        place in P^T's layout).  Known once the operator was prepared."""
+        return {0: "per-detector", 1: "group", 2: "group-3pass"}[self.L.sg_group_mode(self.h, None)]
+
     def autotune(self) -> dict:
         """Pick the faster compiled FFT tile shape for this problem's noise filter."""
         S = ctypes.c_int(0)

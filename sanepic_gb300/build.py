@@ -29,6 +29,7 @@ UNITS = {
     "sg_setup.cu": [],
     "sg_pt.cu": [],
     "sg_group.cu": [],
+    "sg_fft3.cu": [],
     "sg_cg.cu": [],
     "sg_api.cu": [],
     "sg_noalloc.cu": [],

@@ -133,7 +133,7 @@ extern "C" long sg_npix(const sg_ctx* c) { return c ? (long)c->npix : -1; }
 extern "C" int sg_group_mode(const sg_ctx* c, long* ngroups) {
   if (!c) return 0;
   if (ngroups) *ngroups = c->ngroups;
-  return c->group_mode ? 1 : 0;
+  return c->group_mode ? (c->use_f3 ? 2 : 1) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1046,51 +1046,16 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   for (auto& x : ev) cudaEventCreate(&x);
   cudaError_t e = c->to_map(c->d.as<double>());
   float tot[4] = {0.f, 0.f, 0.f, 0.f};
-  const long long nsd = c->ns * c->nseg, M1 = c->ns / 2 + 1, gt = 3LL * c->ngroups * c->nseg;
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
     e = cudaEventRecord(ev[0], c->st);
-    if (c->group_mode && c->groups_uniform) {
-      // one noise spectrum per group: projection mixed by W; N^-1 = the fused
-      // filter on each of the three timelines (written in P^T's layout)
-      if (e == cudaSuccess)
-        e = c->f32 ? group_project_w_launch<float>(c->pix.as<int>(), c->cs.as<float>(),
-                                                   c->dmap.as<float>(), c->wmix.as<float>(),
-                                                   c->ngsamp, nsd, c->gtl.as<float>(), c->st)
-                   : group_project_w_launch<double>(c->pix.as<int>(), c->cs.as<double>(),
-                                                    c->dmap.as<double>(), c->wmix.as<double>(),
-                                                    c->ngsamp, nsd, c->gtl.as<double>(), c->st);
+    if (c->group_mode) {
+      // projection = (a, b1, b2) (mixed by W for uniform groups); N^-1 into
+      // P^T's layout (the three-pass weighting, or the cluster FFT kernels);
+      // no detector sums
+      if (e == cudaSuccess) e = c->group_project_step();
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
-      if (e == cudaSuccess)
-        e = c->launch_filter(kLoadTod, c->gtl.p, c->ys.p, gt, (int)c->nseg, 0, nullptr, nullptr,
-                             c->gfilt.p, 1);
+      if (e == cudaSuccess) e = c->group_weight_step();
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-    } else if (c->group_mode) {
-      // projection = (a, b1, b2); N^-1 = forward FFTs + 3 x 3 mixing + inverse
-      // FFTs (written in P^T's layout); no detector sums
-      if (c->f32) {
-        if (e == cudaSuccess)
-          e = group_project_launch<float>(c->pix.as<int>(), c->cs.as<float>(), c->dmap.as<float>(),
-                                          c->ngsamp, nsd, c->gtl.as<float>(), c->st);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(c->gtl.p, nullptr, c->gspec.p, nullptr, gt);
-        if (e == cudaSuccess)
-          e = group_mix_launch<float>(c->gspec.as<cplx<float>>(), c->hmix.as<float>(), c->ngroups,
-                                      c->nseg, M1, c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->ys.p, nullptr, c->gspec.p, gt, 1);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-      } else {
-        if (e == cudaSuccess)
-          e = group_project_launch<double>(c->pix.as<int>(), c->cs.as<double>(),
-                                           c->dmap.as<double>(), c->ngsamp, nsd,
-                                           c->gtl.as<double>(), c->st);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(c->gtl.p, nullptr, c->gspec.p, nullptr, gt);
-        if (e == cudaSuccess)
-          e = group_mix_launch<double>(c->gspec.as<cplx<double>>(), c->hmix.as<double>(),
-                                       c->ngroups, c->nseg, M1, c->st);
-        if (e == cudaSuccess) e = c->launch_filter_spec(nullptr, c->ys.p, nullptr, c->gspec.p, gt, 1);
-        if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
-      }
     } else {
       if (e == cudaSuccess) e = c->launch_project();
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <map>
@@ -393,6 +394,29 @@ struct sg_ctx {
       }
       launches += 1;
     }
+    // the three-pass weighting: FP32, supported lengths, not switched off
+    const char* f3env = getenv("SANEPIC_GPU_FFT3");
+    use_f3 = e == cudaSuccess && f32 && fft3_supported(logm) && !(f3env && f3env[0] == '0');
+    if (use_f3) {
+      std::vector<int> kf;
+      fft3_pos_freq(logm, kf);
+      e = krow.alloc(sizeof(int) * M1);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(krow.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
+      if (e == cudaSuccess) e = hrow.alloc((size_t)ngroups * M1 * (groups_uniform ? 1 : 6) * esize);
+      if (e == cudaSuccess && groups_uniform) {
+        for (long long g = 0; g < ngroups && e == cudaSuccess; g++)
+          e = permute_rows_launch<float>(filt.as<float>() + grp_det_h[grp_off_h[g]] * M1,
+                                         krow.as<int>(), 1, M1, hrow.as<float>() + g * M1, st);
+        launches += ngroups;
+      } else if (e == cudaSuccess) {
+        e = group_hmix_launch<float>(filt.as<float>(), dcs.as<float>(), grp_off.as<int>(),
+                                     grp_det.as<int>(), krow.as<int>(), ngroups, M1,
+                                     hrow.as<float>(), st);
+        launches += 1;
+      }
+    }
     if (e == cudaSuccess) {
       have_hmix = true;
       hmix_S = S;
@@ -401,6 +425,11 @@ struct sg_ctx {
   }
   bool groups_uniform = false;  // every offset group's detectors share one noise spectrum
   DevBuf wmix, gfilt;           // uniform groups: W [G][6]; filter rows [3 G][M+1]
+  // the three-pass weighting (sg_fft3.cu, FP32): the group timelines live in
+  // P^T's layout (ys) and the weights in its row order, hrow [G][M+1][6] (H)
+  // or [G][M+1] (one spectrum per group)
+  bool use_f3 = false;
+  DevBuf krow, hrow;
 
   // b = P^T N^-1 d for the timelines d (device, one row per detector) and
   // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
@@ -416,12 +445,23 @@ struct sg_ctx {
       return e;
     }
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
+    if (!chi2_dev && groups_uniform && use_f3) {
+      // the detectors' timelines summed per group into P^T's layout, weighted
+      // there by the group's one spectrum in place
+      launches += 4;
+      cudaError_t e = group_tod_rhs_launch<float>((const float*)d, nsd, grp_off.as<int>(),
+                                                  grp_det.as<int>(), dcs.as<float>(), ngroups,
+                                                  ys.as<float>(), 1, st);
+      if (e == cudaSuccess) e = fft3_weight();
+      if (e == cudaSuccess) e = launch_pt(bout, true);
+      return e;
+    }
     if (!chi2_dev && groups_uniform) {
       cudaError_t e;
       launches += 2;  // sums, scaling
       if (f32) {
         e = group_tod_rhs_launch<float>((const float*)d, nsd, grp_off.as<int>(), grp_det.as<int>(),
-                                        dcs.as<float>(), ngroups, gtl.as<float>(), st);
+                                        dcs.as<float>(), ngroups, gtl.as<float>(), 0, st);
         if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
         if (e == cudaSuccess)
           e = group_scale_launch<float>(gspec.as<cplx<float>>(), filt_slot.as<float>(),
@@ -429,7 +469,7 @@ struct sg_ctx {
       } else {
         e = group_tod_rhs_launch<double>((const double*)d, nsd, grp_off.as<int>(),
                                          grp_det.as<int>(), dcs.as<double>(), ngroups,
-                                         gtl.as<double>(), st);
+                                         gtl.as<double>(), 0, st);
         if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
         if (e == cudaSuccess)
           e = group_scale_launch<double>(gspec.as<cplx<double>>(), filt_slot.as<double>(),
@@ -463,44 +503,54 @@ struct sg_ctx {
     return e;
   }
 
-  // A for offset groups: (a, b1, b2) per group sample, their half spectra,
-  // the 3 x 3 mixing per frequency, the inverse FFTs, then P^T
+  // the three passes of the FP32 group weighting, in place on ys
+  cudaError_t fft3_weight() {
+    launches += 3;
+    return fft3_group_weight(ys.as<float>(), hrow.as<float>(), groups_uniform ? 0 : 1, ngroups,
+                             (int)nseg, logm, tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(),
+                             wn1f, st);
+  }
+
+  // A for offset groups in three steps: the projection to the group
+  // timelines (a, b1, b2) (mixed by W for uniform groups), N^-1 on them into
+  // P^T's layout ys, then P^T.  N^-1: the three-pass weighting in place
+  // (FP32), else the cluster FFT kernels: the fused filter per timeline
+  // (uniform groups), or forward FFTs, the 3 x 3 mixing per frequency and
+  // the inverse FFTs.
+  cudaError_t group_project_step() {
+    const long long nsd = ns * nseg;
+    launches += 1;
+    void* out = use_f3 ? ys.p : gtl.p;
+    const int ilv = use_f3 ? 1 : 0;
+    if (groups_uniform)
+      return f32 ? group_project_w_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(),
+                                                 wmix.as<float>(), ngsamp, nsd, (float*)out, ilv, st)
+                 : group_project_w_launch<double>(pix.as<int>(), cs.as<double>(),
+                                                  dmap.as<double>(), wmix.as<double>(), ngsamp,
+                                                  nsd, (double*)out, ilv, st);
+    return f32 ? group_project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
+                                             nsd, (float*)out, ilv, st)
+               : group_project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(),
+                                              ngsamp, nsd, (double*)out, ilv, st);
+  }
+  cudaError_t group_weight_step() {
+    if (use_f3) return fft3_weight();
+    const long long M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
+    if (groups_uniform)
+      return launch_filter(kLoadTod, gtl.p, ys.p, gt, (int)nseg, 0, nullptr, nullptr, gfilt.p, 1);
+    launches += 1;  // mixing
+    cudaError_t e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
+    if (e == cudaSuccess)
+      e = f32 ? group_mix_launch<float>(gspec.as<cplx<float>>(), hmix.as<float>(), ngroups, nseg,
+                                        M1, st)
+              : group_mix_launch<double>(gspec.as<cplx<double>>(), hmix.as<double>(), ngroups,
+                                         nseg, M1, st);
+    if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
+    return e;
+  }
   cudaError_t apply_map_group(double* out, bool masked) {
-    const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
-    cudaError_t e;
-    if (groups_uniform) {
-      // one noise spectrum per group: mix by W in the time domain, then the
-      // fused filter (forward FFT, x h, inverse FFT in one pass) per timeline,
-      // stored straight into P^T's layout
-      launches += 1;
-      e = f32 ? group_project_w_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(),
-                                              wmix.as<float>(), ngsamp, nsd, gtl.as<float>(), st)
-              : group_project_w_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(),
-                                               wmix.as<double>(), ngsamp, nsd, gtl.as<double>(),
-                                               st);
-      if (e == cudaSuccess)
-        e = launch_filter(kLoadTod, gtl.p, ys.p, gt, (int)nseg, 0, nullptr, nullptr, gfilt.p, 1);
-      if (e == cudaSuccess) e = launch_pt(out, masked);
-      return e;
-    }
-    launches += 2;  // projection, mixing
-    if (f32) {
-      e = group_project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
-                                      nsd, gtl.as<float>(), st);
-      if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
-      if (e == cudaSuccess)
-        e = group_mix_launch<float>(gspec.as<cplx<float>>(), hmix.as<float>(), ngroups, nseg, M1,
-                                    st);
-      if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
-    } else {
-      e = group_project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
-                                       nsd, gtl.as<double>(), st);
-      if (e == cudaSuccess) e = launch_filter_spec(gtl.p, nullptr, gspec.p, nullptr, gt);
-      if (e == cudaSuccess)
-        e = group_mix_launch<double>(gspec.as<cplx<double>>(), hmix.as<double>(), ngroups, nseg,
-                                     M1, st);
-      if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
-    }
+    cudaError_t e = group_project_step();
+    if (e == cudaSuccess) e = group_weight_step();
     if (e == cudaSuccess) e = launch_pt(out, masked);
     return e;
   }

@@ -1,0 +1,492 @@
+// sg_fft3.cu -- the offset-group noise weighting (S0, S1, S2)^ = H[k] (a, b1, b2)^
+// in FP32 as three in-place passes over the group timelines, each a plain
+// grid of independent CTAs (no cluster, no distributed shared memory).
+//
+// The group timelines live in P^T's interleaved layout: per (group, segment)
+// tile of ns = 2M samples and three components, sample i of component c at
+// float offset 24 (i / 8) + 8 c + i % 8.  A sample pair (2m, 2m+1) of one
+// component is the packed complex point z_c[m] = x_c[2m] + i x_c[2m+1] at
+// float offset 24 (m / 4) + 8 c + 2 (m % 4), so the packed complex array and
+// the real timelines share the same bytes and every pass can work in place.
+//
+// The length-M complex FFT is the four-step FFT M = R x C with m = C n1 + n2:
+//   pass 1 (columns):  Y[k1][n2] = W_M^{n2 k1} sum_n1 z[C n1 + n2] W_R^{n1 k1},
+//                      stored at m = C k1 + n2;
+//   pass 2 (rows):     Z[k1 + R k2] = sum_n2 Y[k1][n2] W_C^{n2 k2}; the real
+//                      spectrum split of the pair (k, M-k), the 3 x 3 mixing
+//                      by H (or a scaling by h), the re-packing for the
+//                      inverse, and the inverse row DFT
+//                      U[k1][n2] = sum_k2 Z'[k1 + R k2] W_C^{-n2 k2};
+//   pass 3 (columns):  z'[C n1 + n2] = sum_k1 W_R^{-n1 k1} W_M^{-n2 k1} U[k1][n2],
+//                      whose real and imaginary parts are the output samples.
+// A frequency k = k1 + R k2 (k1 > 0) has its real-FFT partner M - k =
+// (R - k1) + R (C - 1 - k2), so pass 2 takes the rows k1 and R - k1 of all
+// three components together (rows 0 and R/2 pair with themselves and share
+// one CTA).  Between the passes the tile goes through L2 (74 MB for 48
+// segments of 131,072 samples, which stays resident in the 129 MB L2); each
+// pass reads and writes it once, with 16-byte accesses to contiguous 96-byte
+// blocks.
+//
+// Every sub-DFT of length R or C is two in-register radix passes (R = R1 R2,
+// sizes <= 16) through shared memory, one unit (one small DFT) per thread.
+// Conventions are FFTW's unnormalised r2c (sign -1) and c2r (sign +1), as in
+// the reference's noise weighting (sanepic.cc:2390-2445, 2522-2582): the
+// output is c2r(H r2c(x)) per group and segment, the same linear map as the
+// cluster filter kernels (sg_filter.cuh) with the group mixing (sg_group.cu).
+#include <cuda_runtime.h>
+
+#include "sg_cplx.cuh"
+#include "sg_dft.cuh"
+#include "sg_kernels.h"
+
+namespace sg {
+namespace f3 {
+
+using cf = cplx<float>;
+
+__device__ __forceinline__ cf ldg2(const cf* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return cf{v.x, v.y};
+}
+// W_M^j from the two-level table W_M^j = hi[j / 64] lo[j % 64]
+__device__ __forceinline__ cf twm(const cf* lo, const cf* hi, int j) {
+  return cmul(ldg2(hi + (j >> 6)), ldg2(lo + (j & 63)));
+}
+
+template <int LOGN>
+struct Split {
+  static constexpr int N = 1 << LOGN;
+  static constexpr int N1 = 1 << ((LOGN + 1) / 2), N2 = N / N1;  // N = N1 N2, N1 >= N2
+  static constexpr int LOGN2 = LOGN / 2;
+  // shared layout of one length-N sequence: position p at p + p / N2, so that
+  // both radix passes reach distinct bank pairs; an odd stride between
+  // sequences
+  static __device__ __forceinline__ int pad(int p) { return p + (p >> LOGN2); }
+  static constexpr int QS = (N + N / N2) | 1;
+};
+
+// ---- passes 1 and 3: the column DFTs of CB columns (x 3 components) --------
+// Sequence q = c CB + cc is column n2 = c0 + cc of component c.  A column DFT
+// of length R = R1 R2 (n1 = t + R2 j, k1 = ka + R1 kb) is two radix passes:
+// units (q, t) take DFT_R1 over j straight from the tile, units (q, ka)
+// DFT_R2 over t and write straight back; the lanes of a warp run over q, so
+// every access to the tile is a run of whole 32-byte sectors.
+template <int LOGR, int LOGC, int CB>
+struct ColGeo {
+  static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
+  using S = Split<LOGR>;
+  static constexpr int R1 = S::N1, R2 = S::N2, QS = S::QS;
+  static constexpr int NSEQ = 3 * CB;
+  static constexpr int NT = NSEQ * R1;  // threads: the units of the R2 pass
+  static constexpr int SMEM = NSEQ * QS + R + CB * R2;  // sequences, W_R, column steps
+  static_assert(CB % 4 == 0 && CB <= C, "column blocks of whole 96-byte groups");
+};
+
+// complex point (row n, sequence q) of a tile, as an offset in complex units
+template <int LOGC, int CB>
+__device__ __forceinline__ long long col_elem(int c0, int q, int n) {
+  const int c = q / CB, cc = q % CB;
+  return 3LL * (1 << LOGC) * n + 3 * c0 + 12 * (cc >> 2) + 4 * c + (cc & 3);
+}
+
+template <int LOGR, int LOGC, int CB>
+__device__ __forceinline__ void col_tables(cf* twr, cf* step, int c0, const cf* lo, const cf* hi,
+                                           int tid) {
+  using G = ColGeo<LOGR, LOGC, CB>;
+  for (int i = tid; i < G::R; i += G::NT) twr[i] = twm(lo, hi, i * G::C);  // W_R^i
+  for (int i = tid; i < CB * G::R2; i += G::NT) {  // step[kb CB + cc] = W_M^{(c0 + cc) R1 kb}
+    const int kb = i / CB, cc = i % CB;
+    step[i] = twm(lo, hi, (c0 + cc) * G::R1 * kb);
+  }
+}
+
+// pass 1: column DFTs and the four-step twiddle W_M^{n2 k1}; grid = tiles x C / CB
+template <int LOGR, int LOGC, int CB, int MINB = 1>
+__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
+    k_f3_colfwd(float* __restrict__ data, const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi) {
+  using G = ColGeo<LOGR, LOGC, CB>;
+  using S = typename G::S;
+  constexpr int R1 = G::R1, R2 = G::R2, QS = G::QS, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twr = s + NSEQ * QS;
+  cf* step = twr + G::R;
+  const int tid = threadIdx.x;
+  const long long tile = blockIdx.x / (G::C / CB);
+  const int c0 = (int)(blockIdx.x % (G::C / CB)) * CB;
+  cf* t = reinterpret_cast<cf*>(data + tile * 6LL * G::M);
+  // pass A: DFT_R1 over j of z[t + R2 j], twiddle W_R^{t ka}
+  const bool unitA = tid < NSEQ * R2;
+  const int qa = tid % NSEQ, ta = tid / NSEQ;
+  cf a[R1];
+  if (unitA) {
+#pragma unroll
+    for (int j = 0; j < R1; j++) a[j] = t[col_elem<LOGC, CB>(c0, qa, ta + R2 * j)];
+  }
+  col_tables<LOGR, LOGC, CB>(twr, step, c0, tw_lo, tw_hi, tid);
+  __syncthreads();
+  if (unitA) {
+    SgDft<R1, false, float>::run(a);
+#pragma unroll
+    for (int ka = 0; ka < R1; ka++)
+      s[qa * QS + S::pad(ta + R2 * ka)] = (ka == 0 || ta == 0) ? a[ka] : cmul(a[ka], twr[ta * ka]);
+  }
+  __syncthreads();
+  // pass B: DFT_R2 over t, Y[ka + R1 kb] times W_M^{n2 (ka + R1 kb)}, to the tile
+  {
+    const int q = tid % NSEQ, ka = tid / NSEQ, cc = q % CB, n2 = c0 + cc;
+    cf v[R2];
+#pragma unroll
+    for (int i = 0; i < R2; i++) v[i] = s[q * QS + S::pad(i + R2 * ka)];
+    SgDft<R2, false, float>::run(v);
+    const cf wa = twm(tw_lo, tw_hi, n2 * ka);
+#pragma unroll
+    for (int kb = 0; kb < R2; kb++) {
+      const cf y = n2 == 0 ? v[kb] : cmul(v[kb], cmul(wa, step[kb * CB + cc]));
+      t[col_elem<LOGC, CB>(c0, q, ka + R1 * kb)] = y;
+    }
+  }
+}
+
+// pass 3: the conjugate four-step twiddle and the inverse column DFTs
+template <int LOGR, int LOGC, int CB, int MINB = 1>
+__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
+    k_f3_colinv(float* __restrict__ data, const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi) {
+  using G = ColGeo<LOGR, LOGC, CB>;
+  using S = typename G::S;
+  constexpr int R1 = G::R1, R2 = G::R2, QS = G::QS, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twr = s + NSEQ * QS;
+  cf* step = twr + G::R;
+  const int tid = threadIdx.x;
+  const long long tile = blockIdx.x / (G::C / CB);
+  const int c0 = (int)(blockIdx.x % (G::C / CB)) * CB;
+  cf* t = reinterpret_cast<cf*>(data + tile * 6LL * G::M);
+  // pass B': conj W_M^{n2 k1}, DFT_R2 (sign +) over kb of U[ka + R1 kb], conj W_R^{t ka}
+  {
+    const int q = tid % NSEQ, ka = tid / NSEQ, cc = q % CB, n2 = c0 + cc;
+    cf v[R2];
+#pragma unroll
+    for (int kb = 0; kb < R2; kb++) v[kb] = t[col_elem<LOGC, CB>(c0, q, ka + R1 * kb)];
+    col_tables<LOGR, LOGC, CB>(twr, step, c0, tw_lo, tw_hi, tid);
+    __syncthreads();
+    if (n2 != 0) {
+      const cf wa = twm(tw_lo, tw_hi, n2 * ka);
+#pragma unroll
+      for (int kb = 0; kb < R2; kb++) v[kb] = cmulc(v[kb], cmul(wa, step[kb * CB + cc]));
+    }
+    SgDft<R2, true, float>::run(v);
+#pragma unroll
+    for (int i = 0; i < R2; i++)
+      s[q * QS + S::pad(i + R2 * ka)] = (ka == 0 || i == 0) ? v[i] : cmulc(v[i], twr[i * ka]);
+  }
+  __syncthreads();
+  // pass A': DFT_R1 (sign +) over ka, z'[t + R2 j], to the tile
+  if (tid < NSEQ * R2) {
+    const int q = tid % NSEQ, ta = tid / NSEQ;
+    cf a[R1];
+#pragma unroll
+    for (int ka = 0; ka < R1; ka++) a[ka] = s[q * QS + S::pad(ta + R2 * ka)];
+    SgDft<R1, true, float>::run(a);
+#pragma unroll
+    for (int j = 0; j < R1; j++) t[col_elem<LOGC, CB>(c0, q, ta + R2 * j)] = a[j];
+  }
+}
+
+// ---- pass 2: rows, spectrum, mixing, inverse rows ----------------------------
+// A CTA takes RP row pairs of RSEG consecutive segments of one group: pair
+// p = 0 is rows {0, R/2}, pair p > 0 rows {p, R - p}; sequence rr = (2 pp +
+// side) 3 + c.  The weights of its rows are staged in shared memory once and
+// serve all RSEG segments.  A row DFT of length C = C1 C2 (n2 = t + C2 j,
+// k2 = ka + C1 kb): units (rr, t) read the tile, units (rr, ka) work in
+// shared memory, and the inverse's units (rr, t) write the tile.
+template <int LOGR, int LOGC, int RP, int MIX>
+struct RowGeo {
+  static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
+  using S = Split<LOGC>;
+  static constexpr int C1 = S::N1, C2 = S::N2, QS = S::QS;
+  static constexpr int NSEQ = 6 * RP;
+  static constexpr int NT = NSEQ * C1;
+  static constexpr int HW = MIX ? 6 : 1;  // weights per frequency
+  // shared: sequences, W_C twice ([ka][t] and [t][ka]), split table (complex)
+  // + weights (floats, padded to 8 B)
+  static constexpr int SMEM = NSEQ * QS + 3 * C + (2 * RP * C * HW + HW + 1) / 2;
+  static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
+};
+
+__device__ __forceinline__ int row_k1(int R, int p, int side) {
+  return p == 0 ? (side ? R / 2 : 0) : (side ? R - p : p);
+}
+
+// complex point n of sequence rr's row in a tile, as an offset in complex units
+template <int LOGR, int LOGC>
+__device__ __forceinline__ long long row_elem(int p0, int rr, int n) {
+  const int row = rr / 3, c = rr % 3;
+  const int k1 = row_k1(1 << LOGR, p0 + (row >> 1), row & 1);
+  return 3LL * (1 << LOGC) * k1 + 12 * (n >> 2) + 4 * c + (n & 3);
+}
+
+// MIX: the weighting applied per frequency. 1: the group's 3 x 3 H,
+// hrow[g][pos][6] (H00 H01 H02 H11 H12 H22); 0: one spectrum h per group,
+// hrow[g][pos].  pos = C k1 + k2 for k = k1 + R k2 < M, pos = M for k = M.
+// Grid: groups x ceil(nseg / RSEG) x (R/2) / RP.
+template <int LOGR, int LOGC, int RP, int MIX, int RSEG, int MINB = 1>
+__global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
+    k_f3_rows(float* __restrict__ data, const float* __restrict__ hrow, int nseg,
+              const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi, cf wn1) {
+  using G = RowGeo<LOGR, LOGC, RP, MIX>;
+  using S = typename G::S;
+  constexpr int R = G::R, C = G::C, M = G::M, QS = S::QS, NT = G::NT, HW = G::HW;
+  constexpr int C1 = G::C1, C2 = G::C2, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twA = s + NSEQ * QS;  // twA[ka C2 + t] = W_C^{t ka}
+  cf* twB = twA + C;        // twB[t C1 + ka] = W_C^{t ka}
+  cf* wsp = twB + C;        // W_N^{R i} = W_M^{(R/2) i}
+  float* hs = reinterpret_cast<float*>(wsp + C);  // [2 RP][C][HW], then bin M
+  const int tid = threadIdx.x;
+  constexpr int CPT = (R / 2) / RP;  // CTAs per segment
+  const int nsb = (nseg + RSEG - 1) / RSEG;
+  const int p0 = (int)(blockIdx.x % CPT) * RP;
+  const long long rest = blockIdx.x / CPT;
+  const int sb = (int)(rest % nsb);
+  const long long grp = rest / nsb;
+  const float* H = hrow + grp * (long long)(M + 1) * HW;
+  for (int i = tid; i < C; i += NT) {
+    const int ka = i / C2, t = i % C2;
+    twA[i] = twm(tw_lo, tw_hi, ((t * ka) & (C - 1)) * R);
+    const int tb = i / C1, kb = i % C1;
+    twB[i] = twm(tw_lo, tw_hi, ((tb * kb) & (C - 1)) * R);
+    wsp[i] = twm(tw_lo, tw_hi, (R / 2) * i);
+  }
+  for (int i = tid; i < 2 * RP * C * HW; i += NT) {
+    const int row = i / (C * HW), e = i % (C * HW);
+    hs[i] = __ldg(H + (long long)C * HW * row_k1(R, p0 + (row >> 1), row & 1) + e);
+  }
+  if (tid < HW) hs[2 * RP * C * HW + tid] = __ldg(H + (long long)M * HW + tid);
+  const int s_end = min(nseg, (sb + 1) * RSEG);
+  const bool unitA = tid < NSEQ * C2;
+  const int rra = tid / C2, ta = tid % C2;    // units (rr, t)
+  const int rrb = tid / C1, kab = tid % C1;   // units (rr, ka)
+  for (int seg = sb * RSEG; seg < s_end; seg++) {
+    cf* t = reinterpret_cast<cf*>(data + (grp * nseg + seg) * 6LL * M);
+    // pass A: DFT_C1 over j of Y[t + C2 j], twiddle W_C^{t ka}
+    {
+      cf a[C1];
+      if (unitA) {
+#pragma unroll
+        for (int j = 0; j < C1; j++) a[j] = t[row_elem<LOGR, LOGC>(p0, rra, ta + C2 * j)];
+      }
+      __syncthreads();  // the tables (first segment); the previous segment's last reads
+      if (unitA) {
+        SgDft<C1, false, float>::run(a);
+#pragma unroll
+        for (int ka = 0; ka < C1; ka++)
+          s[rra * QS + S::pad(ta + C2 * ka)] = (ka == 0 || ta == 0) ? a[ka] : cmul(a[ka], twA[ka * C2 + ta]);
+      }
+    }
+    __syncthreads();
+    // pass B: DFT_C2 over t: Z[ka + C1 kb], to natural order
+    {
+      cf v[C2];
+#pragma unroll
+      for (int i = 0; i < C2; i++) v[i] = s[rrb * QS + S::pad(i + C2 * kab)];
+      SgDft<C2, false, float>::run(v);
+      __syncthreads();
+#pragma unroll
+      for (int kb = 0; kb < C2; kb++) s[rrb * QS + S::pad(kab + C1 * kb)] = v[kb];
+    }
+    __syncthreads();
+    // spectrum: pairs (k, M - k) of all three components
+    for (int task = tid; task < RP * (C + 1); task += NT) {
+      const int pp = task / (C + 1), tau = task % (C + 1);
+      const int p = p0 + pp;
+      if (p != 0 && tau == C) continue;
+      int rowA, colA, rowB, colB;  // (side, column) of the smaller frequency and its partner
+      bool special = false;
+      if (p != 0) {
+        if (tau < C / 2) { rowA = 0; colA = tau; rowB = 1; colB = C - 1 - tau; }
+        else { rowA = 1; colA = C - 1 - tau; rowB = 0; colB = tau; }
+      } else if (tau < C / 2) {  // row R/2: k2 <-> C-1-k2
+        rowA = 1; colA = tau; rowB = 1; colB = C - 1 - tau;
+      } else if (tau == C / 2) {  // bins 0 and M
+        rowA = rowB = 0; colA = colB = 0; special = true;
+      } else if (tau < C) {  // row 0: k2 <-> C - k2
+        rowA = 0; colA = tau - C / 2; rowB = 0; colB = C - colA;
+      } else {  // row 0, k2 = C/2: k = M/2, its own partner
+        rowA = rowB = 0; colA = colB = C / 2;
+      }
+      const int k1A = row_k1(R, p, rowA);
+      cf* qa = s + ((2 * pp + rowA) * 3) * QS + S::pad(colA);
+      cf* qb = s + ((2 * pp + rowB) * 3) * QS + S::pad(colB);
+      const float* ha = hs + ((2 * pp + rowA) * C + colA) * HW;
+      const float* hb = hs + ((2 * pp + rowB) * C + colB) * HW;
+      if (special) {
+        const float* hm = hs + 2 * RP * C * HW;
+        float x0[3], xm[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const cf z = qa[c * QS];
+          x0[c] = z.x + z.y;
+          xm[c] = z.x - z.y;
+        }
+        float y0[3], ym[3];
+        if constexpr (MIX) {
+          y0[0] = ha[0] * x0[0] + ha[1] * x0[1] + ha[2] * x0[2];
+          y0[1] = ha[1] * x0[0] + ha[3] * x0[1] + ha[4] * x0[2];
+          y0[2] = ha[2] * x0[0] + ha[4] * x0[1] + ha[5] * x0[2];
+          ym[0] = hm[0] * xm[0] + hm[1] * xm[1] + hm[2] * xm[2];
+          ym[1] = hm[1] * xm[0] + hm[3] * xm[1] + hm[4] * xm[2];
+          ym[2] = hm[2] * xm[0] + hm[4] * xm[1] + hm[5] * xm[2];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            y0[c] = ha[0] * x0[c];
+            ym[c] = hm[0] * xm[c];
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) qa[c * QS] = cf{y0[c] + ym[c], y0[c] - ym[c]};
+        continue;
+      }
+      // W_N^k, k = k1A + R colA: W_N^{k1A} W_N^{R colA}
+      cf wk = wsp[colA];
+      if (k1A != 0) {
+        cf w1 = twm(tw_lo, tw_hi, k1A >> 1);
+        if (k1A & 1) w1 = cmul(w1, wn1);
+        wk = cmul(w1, wk);
+      }
+      cf xk[3], xm[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const cf zk = qa[c * QS], zm = qb[c * QS];
+        const cf Ev{0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y)};
+        const cf Ov{0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x)};
+        const cf wO = cmul(wk, Ov);
+        xk[c] = Ev + wO;
+        xm[c] = cconj(Ev - wO);
+      }
+      cf yk[3], ym[3];
+      if constexpr (MIX) {
+#define SG_F3_MIX(Y, X, h)                                                       \
+  Y[0] = cf{h[0] * X[0].x + h[1] * X[1].x + h[2] * X[2].x,                       \
+            h[0] * X[0].y + h[1] * X[1].y + h[2] * X[2].y};                      \
+  Y[1] = cf{h[1] * X[0].x + h[3] * X[1].x + h[4] * X[2].x,                       \
+            h[1] * X[0].y + h[3] * X[1].y + h[4] * X[2].y};                      \
+  Y[2] = cf{h[2] * X[0].x + h[4] * X[1].x + h[5] * X[2].x,                       \
+            h[2] * X[0].y + h[4] * X[1].y + h[5] * X[2].y};
+        SG_F3_MIX(yk, xk, ha)
+        SG_F3_MIX(ym, xm, hb)
+#undef SG_F3_MIX
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          yk[c] = cscale(xk[c], ha[0]);
+          ym[c] = cscale(xm[c], hb[0]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const cf P = yk[c] + cconj(ym[c]), Q = yk[c] - cconj(ym[c]);
+        const cf cwQ = cmulc(Q, wk);
+        const cf iwQ{-cwQ.y, cwQ.x};
+        qa[c * QS] = P + iwQ;
+        if (qb != qa) qb[c * QS] = cconj(P - iwQ);
+      }
+    }
+    __syncthreads();
+    // pass B': DFT_C2 (sign +) over kb of Z'[ka + C1 kb], conj W_C^{t ka}
+    {
+      cf v[C2];
+#pragma unroll
+      for (int kb = 0; kb < C2; kb++) v[kb] = s[rrb * QS + S::pad(kab + C1 * kb)];
+      SgDft<C2, true, float>::run(v);
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < C2; i++)
+        s[rrb * QS + S::pad(i + C2 * kab)] = (kab == 0 || i == 0) ? v[i] : cmulc(v[i], twB[i * C1 + kab]);
+    }
+    __syncthreads();
+    // pass A': DFT_C1 (sign +) over ka, U[t + C2 j], to the tile
+    if (unitA) {
+      cf a[C1];
+#pragma unroll
+      for (int ka = 0; ka < C1; ka++) a[ka] = s[rra * QS + S::pad(ta + C2 * ka)];
+      SgDft<C1, true, float>::run(a);
+#pragma unroll
+      for (int j = 0; j < C1; j++) t[row_elem<LOGR, LOGC>(p0, rra, ta + C2 * j)] = a[j];
+    }
+  }
+}
+
+}  // namespace f3
+
+// ---- host side -----------------------------------------------------------------
+// Tile shapes per log2(M): R x C with C >= R, CB = 8 columns per column CTA,
+// RP = 2 row pairs and RSEG = 3 segments per row CTA.  At M = 65536 the
+// column kernels are capped for three CTAs per SM and the row kernel for
+// four (fewer registers, more CTAs in flight: 149 -> 107 us per application
+// of 48 tiles on a GB300).
+namespace {
+template <int LOGR, int LOGC, int MIX, int MBC, int MBR>
+cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
+                   const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1, cudaStream_t st) {
+  constexpr int CB = 8, RP = 2, RSEG = 3;
+  using CG = f3::ColGeo<LOGR, LOGC, CB>;
+  using RG = f3::RowGeo<LOGR, LOGC, RP, MIX>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, CB, MBC>;
+  auto kr = f3::k_f3_rows<LOGR, LOGC, RP, MIX, RSEG, MBR>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, CB, MBC>;
+  const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
+  cudaError_t e = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, smc);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ki, cudaFuncAttributeMaxDynamicSharedMemorySize, smc);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, smr);
+  if (e != cudaSuccess) return e;
+  const long long ntiles = ngroups * nseg;
+  const long long gc = ntiles * (CG::C / CB);
+  const long long gr = ngroups * ((nseg + RSEG - 1) / RSEG) * (RG::R / 2 / RP);
+  if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
+  kc<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  kr<<<(unsigned)gr, RG::NT, smr, st>>>(data, hrow, nseg, lo, hi, wn1);
+  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  return cudaGetLastError();
+}
+
+template <int MIX>
+cudaError_t f3_dispatch(float* data, const float* hrow, long long ngroups, int nseg, int logm,
+                        const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1,
+                        cudaStream_t st) {
+  switch (logm) {
+    case 10: return f3_run<5, 5, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 11: return f3_run<5, 6, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 12: return f3_run<6, 6, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 13: return f3_run<6, 7, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 14: return f3_run<7, 7, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 15: return f3_run<7, 8, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    case 16: return f3_run<8, 8, MIX, 3, 4>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int f3_logr(int logm) { return logm / 2; }  // R = 2^(logm/2) <= C
+}  // namespace
+
+bool fft3_supported(int logm) { return logm >= 10 && logm <= 16; }
+
+void fft3_pos_freq(int logm, std::vector<int>& kfreq) {
+  const int M = 1 << logm, R = 1 << f3_logr(logm), C = M / R;
+  kfreq.resize(M + 1);
+  for (int pos = 0; pos < M; pos++) kfreq[pos] = pos / C + R * (pos % C);
+  kfreq[M] = M;
+}
+
+cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long ngroups, int nseg,
+                              int logm, const cplx<float>* tw_lo, const cplx<float>* tw_hi,
+                              cplx<float> wn1, cudaStream_t st) {
+  if (!fft3_supported(logm) || ngroups < 1 || nseg < 1) return cudaErrorInvalidValue;
+  return mix ? f3_dispatch<1>(data, hrow, ngroups, nseg, logm, tw_lo, tw_hi, wn1, st)
+             : f3_dispatch<0>(data, hrow, ngroups, nseg, logm, tw_lo, tw_hi, wn1, st);
+}
+
+}  // namespace sg

@@ -27,21 +27,28 @@ static unsigned blocks_for(long long n, long long cap = 152LL * 16) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
-// gtl [G][3][nsd]: a, b1, b2 of every group sample
+// Where component c of group sample w of group g goes: [G][3][nsd], or with
+// ilv P^T's interleaved layout [G][nsd / 8][3][8] (the three-pass weighting of
+// sg_fft3.cu works in place there)
+__device__ __forceinline__ long long gtl_at(long long g, int c, long long w, long long nsd, int ilv) {
+  return ilv ? 3 * g * nsd + 24 * (w >> 3) + 8 * c + (w & 7) : (3 * g + c) * nsd + w;
+}
+
+// gtl: a, b1, b2 of every group sample
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_group_project(const int* __restrict__ gpix, const T* __restrict__ gcs,
-                    const T* __restrict__ map, long long ng, long long nsd, T* __restrict__ gtl) {
+                    const T* __restrict__ map, long long ng, long long nsd, int ilv,
+                    T* __restrict__ gtl) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
        i += (long long)gridDim.x * blockDim.x) {
     const long long g = i / nsd, w = i - g * nsd;
     const int m = gpix[i];
     const T c = gcs[2 * i], s = gcs[2 * i + 1];
     const T I = map[4 * (long long)m], Q = map[4 * (long long)m + 1], U = map[4 * (long long)m + 2];
-    T* o = gtl + 3 * g * nsd + w;
-    o[0] = I;
-    o[nsd] = Q * c + U * s;
-    o[2 * nsd] = U * c - Q * s;
+    gtl[gtl_at(g, 0, w, nsd, ilv)] = I;
+    gtl[gtl_at(g, 1, w, nsd, ilv)] = Q * c + U * s;
+    gtl[gtl_at(g, 2, w, nsd, ilv)] = U * c - Q * s;
   }
 }
 
@@ -53,7 +60,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_group_project_w(const int* __restrict__ gpix, const T* __restrict__ gcs,
                       const T* __restrict__ map, const T* __restrict__ wmix, long long ng,
-                      long long nsd, T* __restrict__ gtl) {
+                      long long nsd, int ilv, T* __restrict__ gtl) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ng;
        i += (long long)gridDim.x * blockDim.x) {
     const long long g = i / nsd, w = i - g * nsd;
@@ -62,10 +69,9 @@ __global__ void __launch_bounds__(256)
     const T I = map[4 * (long long)m], Q = map[4 * (long long)m + 1], U = map[4 * (long long)m + 2];
     const T a = I, b1 = Q * c + U * s, b2 = U * c - Q * s;
     const T* W = wmix + 6 * g;  // W00 W01 W02 W11 W12 W22
-    T* o = gtl + 3 * g * nsd + w;
-    o[0] = W[0] * a + W[1] * b1 + W[2] * b2;
-    o[nsd] = W[1] * a + W[3] * b1 + W[4] * b2;
-    o[2 * nsd] = W[2] * a + W[4] * b1 + W[5] * b2;
+    gtl[gtl_at(g, 0, w, nsd, ilv)] = W[0] * a + W[1] * b1 + W[2] * b2;
+    gtl[gtl_at(g, 1, w, nsd, ilv)] = W[1] * a + W[3] * b1 + W[4] * b2;
+    gtl[gtl_at(g, 2, w, nsd, ilv)] = W[2] * a + W[4] * b1 + W[5] * b2;
   }
 }
 
@@ -91,8 +97,8 @@ __global__ void k_group_wmix(const T* __restrict__ dcs, const int* __restrict__ 
 
 template <typename T>
 cudaError_t group_project_w_launch(const int* gpix, const T* gcs, const T* map, const T* wmix,
-                                   long long ng, long long nsd, T* gtl, cudaStream_t st) {
-  k_group_project_w<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, wmix, ng, nsd, gtl);
+                                   long long ng, long long nsd, T* gtl, int ilv, cudaStream_t st) {
+  k_group_project_w<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, wmix, ng, nsd, ilv, gtl);
   return cudaGetLastError();
 }
 template <typename T>
@@ -235,7 +241,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_group_tod_sums(const T* __restrict__ tod, long long nsd, const int* __restrict__ grp_off,
                      const int* __restrict__ grp_det, const T* __restrict__ dcs, long long G,
-                     T* __restrict__ gtl) {
+                     int ilv, T* __restrict__ gtl) {
   const long long n = G * nsd;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -249,10 +255,9 @@ __global__ void __launch_bounds__(256)
       s1 = fma(dcs[2 * d], x, s1);
       s2 = fma(dcs[2 * d + 1], x, s2);
     }
-    T* o = gtl + 3 * g * nsd + w;
-    o[0] = s0;
-    o[nsd] = s1;
-    o[2 * nsd] = s2;
+    gtl[gtl_at(g, 0, w, nsd, ilv)] = s0;
+    gtl[gtl_at(g, 1, w, nsd, ilv)] = s1;
+    gtl[gtl_at(g, 2, w, nsd, ilv)] = s2;
   }
 }
 
@@ -292,9 +297,10 @@ __global__ void __launch_bounds__(256)
 
 template <typename T>
 cudaError_t group_tod_rhs_launch(const T* tod, long long nsd, const int* grp_off,
-                                 const int* grp_det, const T* dcs, long long G, T* gtl,
+                                 const int* grp_det, const T* dcs, long long G, T* gtl, int ilv,
                                  cudaStream_t st) {
-  k_group_tod_sums<T><<<blocks_for(G * nsd), 256, 0, st>>>(tod, nsd, grp_off, grp_det, dcs, G, gtl);
+  k_group_tod_sums<T><<<blocks_for(G * nsd), 256, 0, st>>>(tod, nsd, grp_off, grp_det, dcs, G, ilv,
+                                                            gtl);
   return cudaGetLastError();
 }
 template <typename T>
@@ -323,8 +329,8 @@ cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, 
 
 template <typename T>
 cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, long long ng,
-                                 long long nsd, T* gtl, cudaStream_t st) {
-  k_group_project<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, ng, nsd, gtl);
+                                 long long nsd, T* gtl, int ilv, cudaStream_t st) {
+  k_group_project<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, ng, nsd, ilv, gtl);
   return cudaGetLastError();
 }
 template <typename T>
@@ -364,7 +370,7 @@ cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, l
 
 #define SG_GROUP_INST(T)                                                                       \
   template cudaError_t group_project_launch<T>(const int*, const T*, const T*, long long,        \
-                                               long long, T*, cudaStream_t);                     \
+                                               long long, T*, int, cudaStream_t);                \
   template cudaError_t group_mix_launch<T>(cplx<T>*, const T*, long long, long long, long long,  \
                                            cudaStream_t);                                        \
   template cudaError_t group_hmix_launch<T>(const T*, const T*, const int*, const int*,          \
@@ -375,13 +381,13 @@ cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, l
                                            const int*, long long, long long, long long,          \
                                            cplx<T>*, double*, int, cudaStream_t);                \
   template cudaError_t group_tod_rhs_launch<T>(const T*, long long, const int*, const int*,      \
-                                               const T*, long long, T*, cudaStream_t);           \
+                                               const T*, long long, T*, int, cudaStream_t);      \
   template cudaError_t group_scale_launch<T>(cplx<T>*, const T*, const int*, const int*,         \
                                              long long, long long, long long, cudaStream_t);     \
   template cudaError_t rows_match_group_launch<T>(const T*, long long, const int*, const int*,   \
                                                   long long, long long, int*, cudaStream_t);     \
   template cudaError_t group_project_w_launch<T>(const int*, const T*, const T*, const T*,        \
-                                                 long long, long long, T*, cudaStream_t);        \
+                                                 long long, long long, T*, int, cudaStream_t);   \
   template cudaError_t group_wmix_launch<T>(const T*, const int*, const int*, long long, T*,     \
                                             cudaStream_t);
 SG_GROUP_INST(float)

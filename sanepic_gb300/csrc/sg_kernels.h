@@ -161,10 +161,11 @@ cudaError_t pt_launch(const long long* csr_off, const uint32_t* csr_idx, const T
 int pt_lanes(long long nsamples, long long npix);
 
 // ---- the offset-group operator (sg_group.cu) -------------------------------------
-// gtl [G][3][nsd] = (a, b1, b2) = (I, Q c + U s, U c - Q s) per group sample
+// gtl = (a, b1, b2) = (I, Q c + U s, U c - Q s) per group sample, in the
+// layout [G][3][nsd], or with ilv in P^T's interleaved [G][nsd / 8][3][8]
 template <typename T>
 cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, long long ng,
-                                 long long nsd, T* gtl, cudaStream_t st);
+                                 long long nsd, T* gtl, int ilv, cudaStream_t st);
 // half spectra [G][3][nseg][M+1] <- H (a, b1, b2) per frequency, hmix [G][M+1][6]
 template <typename T>
 cudaError_t group_mix_launch(cplx<T>* spec, const T* hmix, long long G, long long nseg,
@@ -182,16 +183,17 @@ cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, 
 // sum_d (1, c, s, cc, cs, ss); N^-1 then filters each timeline on its own
 template <typename T>
 cudaError_t group_project_w_launch(const int* gpix, const T* gcs, const T* map, const T* wmix,
-                                   long long ng, long long nsd, T* gtl, cudaStream_t st);
+                                   long long ng, long long nsd, T* gtl, int ilv, cudaStream_t st);
 template <typename T>
 cudaError_t group_wmix_launch(const T* dcs, const int* grp_off, const int* grp_det, long long G,
                               T* wmix, cudaStream_t st);
-// groups whose detectors share one noise spectrum: gtl [G][3][nsd] = the
-// detectors' timelines summed with weights (1, c_d, s_d); then the group's
-// half spectra [G][3][nseg][M+1] scaled by its (first detector's) filter row
+// groups whose detectors share one noise spectrum: gtl (layout as for the
+// projection) = the detectors' timelines summed with weights (1, c_d, s_d);
+// then the group's half spectra [G][3][nseg][M+1] scaled by its (first
+// detector's) filter row
 template <typename T>
 cudaError_t group_tod_rhs_launch(const T* tod, long long nsd, const int* grp_off,
-                                 const int* grp_det, const T* dcs, long long G, T* gtl,
+                                 const int* grp_det, const T* dcs, long long G, T* gtl, int ilv,
                                  cudaStream_t st);
 template <typename T>
 cudaError_t group_scale_launch(cplx<T>* spec, const T* filt, const int* grp_off, const int* grp_det,
@@ -211,6 +213,19 @@ cudaError_t group_hmix_launch(const T* filt, const T* dcs, const int* grp_off, c
 template <typename T>
 cudaError_t permute_rows_launch(const T* in, const int* kslot, long long rows, long long M1, T* out,
                                 cudaStream_t st);
+
+// ---- the offset-group noise weighting in three passes (sg_fft3.cu, FP32) ----------
+// In place on the group timelines in P^T's interleaved layout, tile (group g,
+// segment s) at float offset (g nseg + s) 3 ns:  y = c2r(H r2c(x)) per tile,
+// with the weights in row order (hrow: [G][M+1][6] symmetric 3 x 3 H with
+// mix, else [G][M+1] one spectrum per group; position pos = C k1 + k2 holds
+// frequency k = k1 + R k2, position M the Nyquist bin; fft3_pos_freq lists
+// them).  tw_lo / tw_hi: W_M^j = hi[j / 64] lo[j % 64], wn1 = W_{2M}.
+bool fft3_supported(int logm);
+void fft3_pos_freq(int logm, std::vector<int>& kfreq);
+cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long ngroups, int nseg,
+                              int logm, const cplx<float>* tw_lo, const cplx<float>* tw_hi,
+                              cplx<float> wn1, cudaStream_t st);
 
 // ---- CG vector algebra (sg_cg.cu) ------------------------------------------------
 struct CgScalars {

@@ -163,6 +163,41 @@ def test_group_operator_matches_per_detector(prec, monkeypatch):
     assert rel_rms(xa[npix:], xb[npix:]) < (1e-7 if prec == "f64" else 1e-4)
 
 
+@pytest.mark.parametrize("ns,distinct,hwp,nseg", [(2048, True, False, 4), (16384, False, True, 5),
+                                                  (65536, True, True, 5), (131072, True, False, 3),
+                                                  (131072, False, False, 4)])
+def test_three_pass_weighting_vs_cluster_kernels_and_oracle(ns, distinct, hwp, nseg, monkeypatch):
+    """the three-pass FP32 group weighting (sg_fft3.cu, in place in P^T's
+    layout) and the cluster FFT kernels are the same operator: A x of both
+    against the oracle and against each other; segment counts that do not
+    fill the row kernel's 3-segment blocks included"""
+    spec = synth.ProblemSpec("t", ndet=6, nside=32, nseg=nseg, ns=ns, hwp=hwp,
+                             fknee_range=(0.02, 0.2) if distinct else None,
+                             alpha_range=(1.0, 2.0) if distinct else None,
+                             fknee=0.1, alpha=1.0, problem=23, precision="f32")
+    prob = synth.make_problem(spec, with_tod=False)
+    s = oracle.Setup(prob)
+    x = np.random.default_rng(4).standard_normal(3 * s.npix)
+    f3 = sg.from_problem(prob, precision="f32", with_tod=False)
+    y3 = f3.apply(x)
+    assert f3.weighting() == "group-3pass"
+    monkeypatch.setenv("SANEPIC_GPU_FFT3", "0")
+    cl = sg.from_problem(prob, precision="f32", with_tod=False)
+    yc = cl.apply(x)
+    assert cl.weighting() == "group"
+    yo = s.apply(x)
+    assert rel_rms(y3, yo) < 1e-5
+    assert rel_rms(yc, yo) < 1e-5
+    assert rel_rms(y3, yc) < 2e-6
+    # symmetric, and deterministic run to run
+    z = np.random.default_rng(5).standard_normal(3 * s.npix)
+    a, b = z @ f3.apply(x), x @ f3.apply(z)
+    assert abs(a - b) <= 1e-5 * max(abs(a), abs(b))
+    assert np.array_equal(f3.apply(x), y3)
+    f3.close()
+    cl.close()
+
+
 def test_apply_bitwise_deterministic():
     prob = small_problem(ndet=4, nseg=4, ns=4096, precision="f32", nside=32)
     mm = sg.from_problem(prob, precision="f32", with_tod=False)
