@@ -57,10 +57,13 @@ STOP_CRIT = 1e-12  # |r|^2/|b|^2, i.e. |r|/|b| = 1e-6
 # from the ncu capture in profiles/noise_filter_c2_8det.md (354.5 MB over
 # 384 tiles); traffic grows with the tiles, so a full launch is this x tiles.
 FILTER_DRAM_BYTES_PER_TILE_131072_F32 = 354.46e6 / 384
-# DRAM bytes (read + write) of one group noise weighting (forward FFTs, 3 x 3
-# mixing, inverse FFTs) on the bench workloads with one group of 48 x 131072
-# samples, from the ncu capture in profiles/group_noise_weighting_c2_8det.md
-GROUP_NW_DRAM_BYTES = {("c2_64det_nside256", "f32"): 284.7e6, ("c2_8det_nside256", "f32"): 284.7e6}
+# DRAM bytes (read + write) of one group noise weighting (the three in-place
+# passes: columns, rows with the 3 x 3 mixing, inverse columns) on the bench
+# workloads with one group of 48 x 131072 samples, L2 as the operator's
+# previous kernel left it, from the ncu capture in
+# profiles/group_noise_weighting_c2_8det.md (273.2 MB with the caches flushed
+# before each launch)
+GROUP_NW_DRAM_BYTES = {("c2_64det_nside256", "f32"): 208.1e6, ("c2_8det_nside256", "f32"): 208.1e6}
 
 
 def peaks():
@@ -228,10 +231,12 @@ def run_ours(args):
     m1 = spec.ns // 2 + 1
     pt_bytes = ng * (4 + 2 * esz + 4 * esz) + npix * (3 * 8 + 8 + 4)
     if group:
-        # per offset group: (a, b1, b2) per group sample; N^-1 = forward FFTs,
-        # 3 x 3 mixing, inverse FFTs (three launches, timed together): the
-        # three timelines read, the three weighted ones written, the mixing
-        # matrices read; the half spectra in between are not algorithmic
+        # per offset group: (a, b1, b2) per group sample; N^-1 = the three
+        # in-place passes (column FFTs, row FFTs with the 3 x 3 mixing,
+        # inverse column FFTs; three launches, timed together): the three
+        # timelines read, the three weighted ones written, the mixing
+        # matrices read; the passes' round trips through L2 are not
+        # algorithmic
         kbytes = {
             "k_group_project": ng * (4 + 2 * esz) + npix * 4 * esz + 3 * ng * esz,
             "group_noise_weighting": 6 * ng * esz + ngrp * m1 * 6 * esz,
@@ -256,7 +261,8 @@ def run_ours(args):
     traffic = None
     if dom == "k_noise_filter" and spec.ns == 131072 and spec.precision == "f32":
         traffic = FILTER_DRAM_BYTES_PER_TILE_131072_F32 * spec.ndet * spec.nseg
-    if dom == "group_noise_weighting" and (args.config, spec.precision) in GROUP_NW_DRAM_BYTES:
+    if (dom == "group_noise_weighting" and mm.weighting() == "group-3pass"
+            and (args.config, spec.precision) in GROUP_NW_DRAM_BYTES):
         traffic = GROUP_NW_DRAM_BYTES[(args.config, spec.precision)]
     # ---- accuracy of the timed solves: maps against an FP64 solve -----------
     extra = {}
