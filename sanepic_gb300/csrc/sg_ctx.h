@@ -405,6 +405,10 @@ struct sg_ctx {
         e = cudaMemcpyAsync(krow.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
       if (e == cudaSuccess) e = hrow.alloc((size_t)ngroups * M1 * (groups_uniform ? 1 : 6) * esize);
+      if (e == cudaSuccess) e = filt_pos.alloc((size_t)ndet * M1 * esize);
+      if (e == cudaSuccess)
+        e = permute_rows_launch<float>(filt.as<float>(), krow.as<int>(), ndet, M1,
+                                       filt_pos.as<float>(), st);
       if (e == cudaSuccess && groups_uniform) {
         for (long long g = 0; g < ngroups && e == cudaSuccess; g++)
           e = permute_rows_launch<float>(filt.as<float>() + grp_det_h[grp_off_h[g]] * M1,
@@ -430,6 +434,7 @@ struct sg_ctx {
   // or [G][M+1] (one spectrum per group)
   bool use_f3 = false;
   DevBuf krow, hrow;
+  DevBuf filt_pos, f3scratch;  // filter rows in position order; the forward batches' scratch
 
   // b = P^T N^-1 d for the timelines d (device, one row per detector) and
   // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
@@ -477,6 +482,32 @@ struct sg_ctx {
                                          st);
       }
       if (e == cudaSuccess) e = launch_filter_spec(nullptr, ys.p, nullptr, gspec.p, gt, 1);
+      if (e == cudaSuccess) e = launch_pt(bout, true);
+      return e;
+    }
+    if (use_f3) {
+      // every detector's half spectrum (three-pass forward in batches that
+      // stay in L2), the group sums (and chi^2) in position order, the
+      // inverse into P^T's layout
+      const long long nb = std::min<long long>(ntiles, fft3_rhs_batch(logm));
+      cudaError_t e = f3scratch.alloc((size_t)nb * ns * sizeof(float));
+      const long long nbatches = (ntiles + nb - 1) / nb;
+      launches += 2 * nbatches + 2 + (chi2_dev ? 1 : 0) + 2;
+      if (e == cudaSuccess)
+        e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(), dspec.as<cplx<float>>(),
+                                 ntiles, logm, tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(),
+                                 wn1f, st);
+      if (e == cudaSuccess)
+        e = group_rhs_launch<float>(dspec.as<cplx<float>>(), filt_pos.as<float>(), dcs.as<float>(),
+                                    grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,
+                                    gspec.as<cplx<float>>(), rhs_part.as<double>(),
+                                    kGroupRhsBlocks, st);
+      if (e == cudaSuccess && chi2_dev)
+        e = chi2_sum(rhs_part.as<double>(), kGroupRhsBlocks, chi2_dev, st);
+      if (e == cudaSuccess)
+        e = fft3_inverse_from_spectra(gspec.as<cplx<float>>(), ys.as<float>(), ngroups, (int)nseg,
+                                      logm, tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(), wn1f,
+                                      st);
       if (e == cudaSuccess) e = launch_pt(bout, true);
       return e;
     }

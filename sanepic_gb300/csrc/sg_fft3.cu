@@ -35,6 +35,8 @@
 // cluster filter kernels (sg_filter.cuh) with the group mixing (sg_group.cu).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "sg_cplx.cuh"
 #include "sg_dft.cuh"
 #include "sg_kernels.h"
@@ -65,34 +67,42 @@ struct Split {
   static constexpr int QS = (N + N / N2) | 1;
 };
 
-// ---- passes 1 and 3: the column DFTs of CB columns (x 3 components) --------
-// Sequence q = c CB + cc is column n2 = c0 + cc of component c.  A column DFT
-// of length R = R1 R2 (n1 = t + R2 j, k1 = ka + R1 kb) is two radix passes:
+// ---- passes 1 and 3: the column DFTs of CB columns -----------------------------
+// NC = 3: the three components of a group tile in P^T's interleaved layout
+// (sequence q = c CB + cc is column n2 = c0 + cc of component c; a row's CB
+// columns of the three components are 6 CB contiguous floats); NC = 1: one
+// timeline in natural order (sequence q is column c0 + q).  A column DFT of
+// length R = R1 R2 (n1 = t + R2 j, k1 = ka + R1 kb) is two radix passes:
 // units (q, t) take DFT_R1 over j straight from the tile, units (q, ka)
 // DFT_R2 over t and write straight back; the lanes of a warp run over q, so
 // every access to the tile is a run of whole 32-byte sectors.
-template <int LOGR, int LOGC, int CB>
+template <int LOGR, int LOGC, int CB, int NC>
 struct ColGeo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
   using S = Split<LOGR>;
   static constexpr int R1 = S::N1, R2 = S::N2, QS = S::QS;
-  static constexpr int NSEQ = 3 * CB;
+  static constexpr int NSEQ = NC * CB;
   static constexpr int NT = NSEQ * R1;  // threads: the units of the R2 pass
   static constexpr int SMEM = NSEQ * QS + R + CB * R2;  // sequences, W_R, column steps
-  static_assert(CB % 4 == 0 && CB <= C, "column blocks of whole 96-byte groups");
+  static_assert(CB % 4 == 0 && CB <= C, "column blocks of whole 32-byte sectors");
+  static_assert(NC == 1 || NC == 3, "one timeline or a group tile");
 };
 
 // complex point (row n, sequence q) of a tile, as an offset in complex units
-template <int LOGC, int CB>
+template <int LOGC, int CB, int NC>
 __device__ __forceinline__ long long col_elem(int c0, int q, int n) {
-  const int c = q / CB, cc = q % CB;
-  return 3LL * (1 << LOGC) * n + 3 * c0 + 12 * (cc >> 2) + 4 * c + (cc & 3);
+  if constexpr (NC == 1) {
+    return (long long)(1 << LOGC) * n + c0 + q;
+  } else {
+    const int c = q / CB, cc = q % CB;
+    return 3LL * (1 << LOGC) * n + 3 * c0 + 12 * (cc >> 2) + 4 * c + (cc & 3);
+  }
 }
 
-template <int LOGR, int LOGC, int CB>
+template <int LOGR, int LOGC, int CB, int NC>
 __device__ __forceinline__ void col_tables(cf* twr, cf* step, int c0, const cf* lo, const cf* hi,
                                            int tid) {
-  using G = ColGeo<LOGR, LOGC, CB>;
+  using G = ColGeo<LOGR, LOGC, CB, NC>;
   for (int i = tid; i < G::R; i += G::NT) twr[i] = twm(lo, hi, i * G::C);  // W_R^i
   for (int i = tid; i < CB * G::R2; i += G::NT) {  // step[kb CB + cc] = W_M^{(c0 + cc) R1 kb}
     const int kb = i / CB, cc = i % CB;
@@ -100,11 +110,14 @@ __device__ __forceinline__ void col_tables(cf* twr, cf* step, int c0, const cf* 
   }
 }
 
-// pass 1: column DFTs and the four-step twiddle W_M^{n2 k1}; grid = tiles x C / CB
-template <int LOGR, int LOGC, int CB, int MINB = 1>
-__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
-    k_f3_colfwd(float* __restrict__ data, const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi) {
-  using G = ColGeo<LOGR, LOGC, CB>;
+// pass 1: column DFTs and the four-step twiddle W_M^{n2 k1}; grid = tiles x C / CB.
+// In place for NC = 3 (in == out); NC = 1 reads timelines and writes the
+// transformed tiles elsewhere.
+template <int LOGR, int LOGC, int CB, int NC, int MINB = 1>
+__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, NC>::NT, MINB)
+    k_f3_colfwd(const float* in, float* out, const cf* __restrict__ tw_lo,
+                const cf* __restrict__ tw_hi) {
+  using G = ColGeo<LOGR, LOGC, CB, NC>;
   using S = typename G::S;
   constexpr int R1 = G::R1, R2 = G::R2, QS = G::QS, NSEQ = G::NSEQ;
   extern __shared__ __align__(16) unsigned char f3_smem[];
@@ -114,16 +127,25 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
   const int tid = threadIdx.x;
   const long long tile = blockIdx.x / (G::C / CB);
   const int c0 = (int)(blockIdx.x % (G::C / CB)) * CB;
-  cf* t = reinterpret_cast<cf*>(data + tile * 6LL * G::M);
+  const cf* ti = reinterpret_cast<const cf*>(in) + tile * NC * (long long)G::M;
+  cf* to = reinterpret_cast<cf*>(out) + tile * NC * (long long)G::M;
   // pass A: DFT_R1 over j of z[t + R2 j], twiddle W_R^{t ka}
   const bool unitA = tid < NSEQ * R2;
   const int qa = tid % NSEQ, ta = tid / NSEQ;
   cf a[R1];
   if (unitA) {
 #pragma unroll
-    for (int j = 0; j < R1; j++) a[j] = t[col_elem<LOGC, CB>(c0, qa, ta + R2 * j)];
+    for (int j = 0; j < R1; j++) {
+      const cf* p = ti + col_elem<LOGC, CB, NC>(c0, qa, ta + R2 * j);
+      if constexpr (NC == 1) {  // timelines read once: evict first, keep L2 for the batch
+        const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+        a[j] = cf{v.x, v.y};
+      } else {
+        a[j] = *p;
+      }
+    }
   }
-  col_tables<LOGR, LOGC, CB>(twr, step, c0, tw_lo, tw_hi, tid);
+  col_tables<LOGR, LOGC, CB, NC>(twr, step, c0, tw_lo, tw_hi, tid);
   __syncthreads();
   if (unitA) {
     SgDft<R1, false, float>::run(a);
@@ -143,16 +165,17 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
 #pragma unroll
     for (int kb = 0; kb < R2; kb++) {
       const cf y = n2 == 0 ? v[kb] : cmul(v[kb], cmul(wa, step[kb * CB + cc]));
-      t[col_elem<LOGC, CB>(c0, q, ka + R1 * kb)] = y;
+      to[col_elem<LOGC, CB, NC>(c0, q, ka + R1 * kb)] = y;
     }
   }
 }
 
-// pass 3: the conjugate four-step twiddle and the inverse column DFTs
+// pass 3: the conjugate four-step twiddle and the inverse column DFTs, in
+// place on group tiles
 template <int LOGR, int LOGC, int CB, int MINB = 1>
-__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
+__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, 3>::NT, MINB)
     k_f3_colinv(float* __restrict__ data, const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi) {
-  using G = ColGeo<LOGR, LOGC, CB>;
+  using G = ColGeo<LOGR, LOGC, CB, 3>;
   using S = typename G::S;
   constexpr int R1 = G::R1, R2 = G::R2, QS = G::QS, NSEQ = G::NSEQ;
   extern __shared__ __align__(16) unsigned char f3_smem[];
@@ -168,8 +191,8 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
     const int q = tid % NSEQ, ka = tid / NSEQ, cc = q % CB, n2 = c0 + cc;
     cf v[R2];
 #pragma unroll
-    for (int kb = 0; kb < R2; kb++) v[kb] = t[col_elem<LOGC, CB>(c0, q, ka + R1 * kb)];
-    col_tables<LOGR, LOGC, CB>(twr, step, c0, tw_lo, tw_hi, tid);
+    for (int kb = 0; kb < R2; kb++) v[kb] = t[col_elem<LOGC, CB, 3>(c0, q, ka + R1 * kb)];
+    col_tables<LOGR, LOGC, CB, 3>(twr, step, c0, tw_lo, tw_hi, tid);
     __syncthreads();
     if (n2 != 0) {
       const cf wa = twm(tw_lo, tw_hi, n2 * ka);
@@ -190,17 +213,173 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB>::NT, MINB)
     for (int ka = 0; ka < R1; ka++) a[ka] = s[q * QS + S::pad(ta + R2 * ka)];
     SgDft<R1, true, float>::run(a);
 #pragma unroll
-    for (int j = 0; j < R1; j++) t[col_elem<LOGC, CB>(c0, q, ta + R2 * j)] = a[j];
+    for (int j = 0; j < R1; j++) t[col_elem<LOGC, CB, 3>(c0, q, ta + R2 * j)] = a[j];
   }
 }
 
-// ---- pass 2: rows, spectrum, mixing, inverse rows ----------------------------
-// A CTA takes RP row pairs of RSEG consecutive segments of one group: pair
-// p = 0 is rows {0, R/2}, pair p > 0 rows {p, R - p}; sequence rr = (2 pp +
-// side) 3 + c.  The weights of its rows are staged in shared memory once and
-// serve all RSEG segments.  A row DFT of length C = C1 C2 (n2 = t + C2 j,
+// ---- pass 2: rows ----------------------------------------------------------------
+// A row CTA takes row pairs: pair p = 0 is rows {0, R/2}, pair p > 0 rows
+// {p, R - p}, so that every frequency k = k1 + R k2 and its real-FFT partner
+// M - k sit in the same CTA.  A row DFT of length C = C1 C2 (n2 = t + C2 j,
 // k2 = ka + C1 kb): units (rr, t) read the tile, units (rr, ka) work in
-// shared memory, and the inverse's units (rr, t) write the tile.
+// shared memory, the inverse's units (rr, t) write the tile.
+__device__ __forceinline__ int row_k1(int R, int p, int side) {
+  return p == 0 ? (side ? R / 2 : 0) : (side ? R - p : p);
+}
+
+// complex point n of row k1, component c of a group tile (complex units)
+template <int LOGC>
+__device__ __forceinline__ long long row3_elem(int k1, int c, int n) {
+  return 3LL * (1 << LOGC) * k1 + 12 * (n >> 2) + 4 * c + (n & 3);
+}
+
+// the frequency pair of spectrum task tau (0 <= tau <= C) of row pair p:
+// (side, column) of the smaller frequency k (A) and of M - k (B); special:
+// bins 0 and M (row 0, column 0).  False if the task does not exist.
+__device__ __forceinline__ bool pair_of(int C, int p, int tau, int& rowA, int& colA, int& rowB,
+                                        int& colB, bool& special) {
+  special = false;
+  if (p != 0) {
+    if (tau >= C) return false;
+    if (tau < C / 2) { rowA = 0; colA = tau; rowB = 1; colB = C - 1 - tau; }
+    else { rowA = 1; colA = C - 1 - tau; rowB = 0; colB = tau; }
+  } else if (tau < C / 2) {  // row R/2: k2 <-> C-1-k2
+    rowA = 1; colA = tau; rowB = 1; colB = C - 1 - tau;
+  } else if (tau == C / 2) {  // bins 0 and M
+    rowA = rowB = 0; colA = colB = 0; special = true;
+  } else if (tau < C) {  // row 0: k2 <-> C - k2
+    rowA = 0; colA = tau - C / 2; rowB = 0; colB = C - colA;
+  } else {  // row 0, k2 = C/2: k = M/2, its own partner
+    rowA = rowB = 0; colA = colB = C / 2;
+  }
+  return true;
+}
+
+// W_N^k for k = k1 + R col (N = 2M): W_N^{k1} W_N^{R col}, wsp[col] = W_N^{R col}
+__device__ __forceinline__ cf split_tw(int k1, int col, const cf* wsp, const cf* lo, const cf* hi,
+                                       cf wn1) {
+  cf wk = wsp[col];
+  if (k1 != 0) {
+    cf w1 = twm(lo, hi, k1 >> 1);
+    if (k1 & 1) w1 = cmul(w1, wn1);
+    wk = cmul(w1, wk);
+  }
+  return wk;
+}
+
+// r2c values X[k], X[M-k] from the packed spectrum values Z[k], Z[M-k]
+__device__ __forceinline__ void split_pair(cf zk, cf zm, cf wk, cf& xk, cf& xm) {
+  const cf Ev{0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y)};
+  const cf Ov{0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x)};
+  const cf wO = cmul(wk, Ov);
+  xk = Ev + wO;
+  xm = cconj(Ev - wO);
+}
+// the packed values at k and M-k for the inverse of the r2c values Y[k], Y[M-k]
+__device__ __forceinline__ void repack_pair(cf yk, cf ym, cf wk, cf& zk, cf& zm) {
+  const cf P = yk + cconj(ym), Q = yk - cconj(ym);
+  const cf cwQ = cmulc(Q, wk);
+  const cf iwQ{-cwQ.y, cwQ.x};
+  zk = P + iwQ;
+  zm = cconj(P - iwQ);
+}
+
+// the row tables: twA[ka C2 + t] = twB[t C1 + ka] = W_C^{t ka}, wsp[i] = W_N^{R i}
+template <int LOGR, int LOGC>
+__device__ __forceinline__ void row_tables(cf* twA, cf* twB, cf* wsp, const cf* lo, const cf* hi,
+                                           int tid, int nt) {
+  constexpr int R = 1 << LOGR, C = 1 << LOGC;
+  constexpr int C1 = Split<LOGC>::N1, C2 = Split<LOGC>::N2;
+  for (int i = tid; i < C; i += nt) {
+    const int ka = i / C2, t = i % C2;
+    twA[i] = twm(lo, hi, ((t * ka) & (C - 1)) * R);
+    const int tb = i / C1, kb = i % C1;
+    twB[i] = twm(lo, hi, ((tb * kb) & (C - 1)) * R);
+    wsp[i] = twm(lo, hi, (R / 2) * i);
+  }
+}
+
+// Forward row DFTs of NSEQ sequences into shared memory, natural order.
+// rows_load: the pass-A units' inputs (point n of sequence rr from ld(rr, n));
+// rows_forward_loaded: the rest, starting with a barrier that also orders the
+// tables and the previous use of s.
+template <int LOGC, int NSEQ, class Ld>
+__device__ __forceinline__ void rows_load(int tid, Ld ld, cf (&a)[Split<LOGC>::N1]) {
+  constexpr int C1 = Split<LOGC>::N1, C2 = Split<LOGC>::N2;
+  if (tid < NSEQ * C2) {
+    const int rra = tid / C2, ta = tid % C2;
+#pragma unroll
+    for (int j = 0; j < C1; j++) a[j] = ld(rra, ta + C2 * j);
+  }
+}
+template <int LOGC, int NSEQ>
+__device__ __forceinline__ void rows_forward_loaded(cf* s, const cf* twA, int tid,
+                                                    cf (&a)[Split<LOGC>::N1]) {
+  using S = Split<LOGC>;
+  constexpr int C1 = S::N1, C2 = S::N2, QS = S::QS;
+  const bool unitA = tid < NSEQ * C2;
+  const int rra = tid / C2, ta = tid % C2;
+  __syncthreads();
+  if (unitA) {
+    SgDft<C1, false, float>::run(a);
+#pragma unroll
+    for (int ka = 0; ka < C1; ka++)
+      s[rra * QS + S::pad(ta + C2 * ka)] = (ka == 0 || ta == 0) ? a[ka] : cmul(a[ka], twA[ka * C2 + ta]);
+  }
+  __syncthreads();
+  const int rrb = tid / C1, kab = tid % C1;
+  cf v[C2];
+#pragma unroll
+  for (int i = 0; i < C2; i++) v[i] = s[rrb * QS + S::pad(i + C2 * kab)];
+  SgDft<C2, false, float>::run(v);
+  __syncthreads();
+#pragma unroll
+  for (int kb = 0; kb < C2; kb++) s[rrb * QS + S::pad(kab + C1 * kb)] = v[kb];
+  __syncthreads();
+}
+template <int LOGC, int NSEQ, class Ld>
+__device__ __forceinline__ void rows_forward(cf* s, const cf* twA, int tid, Ld ld) {
+  cf a[Split<LOGC>::N1];
+  rows_load<LOGC, NSEQ>(tid, ld, a);
+  rows_forward_loaded<LOGC, NSEQ>(s, twA, tid, a);
+}
+
+// Inverse row DFTs of the NSEQ sequences in shared memory (natural order);
+// st(rr, n, v) stores point n of sequence rr.
+template <int LOGC, int NSEQ, class St>
+__device__ __forceinline__ void rows_inverse(cf* s, const cf* twB, int tid, St st) {
+  using S = Split<LOGC>;
+  constexpr int C1 = S::N1, C2 = S::N2, QS = S::QS;
+  const int rrb = tid / C1, kab = tid % C1;
+  {
+    cf v[C2];
+#pragma unroll
+    for (int kb = 0; kb < C2; kb++) v[kb] = s[rrb * QS + S::pad(kab + C1 * kb)];
+    SgDft<C2, true, float>::run(v);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < C2; i++)
+      s[rrb * QS + S::pad(i + C2 * kab)] = (kab == 0 || i == 0) ? v[i] : cmulc(v[i], twB[i * C1 + kab]);
+  }
+  __syncthreads();
+  if (tid < NSEQ * C2) {
+    const int rra = tid / C2, ta = tid % C2;
+    cf a[C1];
+#pragma unroll
+    for (int ka = 0; ka < C1; ka++) a[ka] = s[rra * QS + S::pad(ta + C2 * ka)];
+    SgDft<C1, true, float>::run(a);
+#pragma unroll
+    for (int j = 0; j < C1; j++) st(rra, ta + C2 * j, a[j]);
+  }
+}
+
+// The weighting pass: RP row pairs of RSEG consecutive segments of one group
+// per CTA, three components (sequence rr = (2 pp + side) 3 + c).  The weights
+// of its rows are staged in shared memory once and serve all RSEG segments.
+// MIX 1: the group's 3 x 3 H, hrow[g][pos][6] (H00 H01 H02 H11 H12 H22);
+// MIX 0: one spectrum h per group, hrow[g][pos].  pos = C k1 + k2 for
+// k = k1 + R k2 < M, pos = M for k = M.  Grid: groups x ceil(nseg / RSEG) x
+// (R/2) / RP.
 template <int LOGR, int LOGC, int RP, int MIX>
 struct RowGeo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
@@ -209,28 +388,11 @@ struct RowGeo {
   static constexpr int NSEQ = 6 * RP;
   static constexpr int NT = NSEQ * C1;
   static constexpr int HW = MIX ? 6 : 1;  // weights per frequency
-  // shared: sequences, W_C twice ([ka][t] and [t][ka]), split table (complex)
-  // + weights (floats, padded to 8 B)
+  // shared: sequences, W_C twice, split table (complex) + weights (floats, padded to 8 B)
   static constexpr int SMEM = NSEQ * QS + 3 * C + (2 * RP * C * HW + HW + 1) / 2;
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
-__device__ __forceinline__ int row_k1(int R, int p, int side) {
-  return p == 0 ? (side ? R / 2 : 0) : (side ? R - p : p);
-}
-
-// complex point n of sequence rr's row in a tile, as an offset in complex units
-template <int LOGR, int LOGC>
-__device__ __forceinline__ long long row_elem(int p0, int rr, int n) {
-  const int row = rr / 3, c = rr % 3;
-  const int k1 = row_k1(1 << LOGR, p0 + (row >> 1), row & 1);
-  return 3LL * (1 << LOGC) * k1 + 12 * (n >> 2) + 4 * c + (n & 3);
-}
-
-// MIX: the weighting applied per frequency. 1: the group's 3 x 3 H,
-// hrow[g][pos][6] (H00 H01 H02 H11 H12 H22); 0: one spectrum h per group,
-// hrow[g][pos].  pos = C k1 + k2 for k = k1 + R k2 < M, pos = M for k = M.
-// Grid: groups x ceil(nseg / RSEG) x (R/2) / RP.
 template <int LOGR, int LOGC, int RP, int MIX, int RSEG, int MINB = 1>
 __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
     k_f3_rows(float* __restrict__ data, const float* __restrict__ hrow, int nseg,
@@ -238,12 +400,12 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   using G = RowGeo<LOGR, LOGC, RP, MIX>;
   using S = typename G::S;
   constexpr int R = G::R, C = G::C, M = G::M, QS = S::QS, NT = G::NT, HW = G::HW;
-  constexpr int C1 = G::C1, C2 = G::C2, NSEQ = G::NSEQ;
+  constexpr int NSEQ = G::NSEQ;
   extern __shared__ __align__(16) unsigned char f3_smem[];
   cf* s = reinterpret_cast<cf*>(f3_smem);
-  cf* twA = s + NSEQ * QS;  // twA[ka C2 + t] = W_C^{t ka}
-  cf* twB = twA + C;        // twB[t C1 + ka] = W_C^{t ka}
-  cf* wsp = twB + C;        // W_N^{R i} = W_M^{(R/2) i}
+  cf* twA = s + NSEQ * QS;
+  cf* twB = twA + C;
+  cf* wsp = twB + C;
   float* hs = reinterpret_cast<float*>(wsp + C);  // [2 RP][C][HW], then bin M
   const int tid = threadIdx.x;
   constexpr int CPT = (R / 2) / RP;  // CTAs per segment
@@ -253,71 +415,29 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   const int sb = (int)(rest % nsb);
   const long long grp = rest / nsb;
   const float* H = hrow + grp * (long long)(M + 1) * HW;
-  for (int i = tid; i < C; i += NT) {
-    const int ka = i / C2, t = i % C2;
-    twA[i] = twm(tw_lo, tw_hi, ((t * ka) & (C - 1)) * R);
-    const int tb = i / C1, kb = i % C1;
-    twB[i] = twm(tw_lo, tw_hi, ((tb * kb) & (C - 1)) * R);
-    wsp[i] = twm(tw_lo, tw_hi, (R / 2) * i);
-  }
+  row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
   for (int i = tid; i < 2 * RP * C * HW; i += NT) {
     const int row = i / (C * HW), e = i % (C * HW);
     hs[i] = __ldg(H + (long long)C * HW * row_k1(R, p0 + (row >> 1), row & 1) + e);
   }
   if (tid < HW) hs[2 * RP * C * HW + tid] = __ldg(H + (long long)M * HW + tid);
   const int s_end = min(nseg, (sb + 1) * RSEG);
-  const bool unitA = tid < NSEQ * C2;
-  const int rra = tid / C2, ta = tid % C2;    // units (rr, t)
-  const int rrb = tid / C1, kab = tid % C1;   // units (rr, ka)
+  auto elem = [&](int rr, int n) {
+    const int row = rr / 3;
+    return row3_elem<LOGC>(row_k1(R, p0 + (row >> 1), row & 1), rr % 3, n);
+  };
+  // (loading the next segment's rows while this one is weighted was slower:
+  // 56 -> 59-66 us at 48 x 131072 samples, registers for the prefetch)
   for (int seg = sb * RSEG; seg < s_end; seg++) {
     cf* t = reinterpret_cast<cf*>(data + (grp * nseg + seg) * 6LL * M);
-    // pass A: DFT_C1 over j of Y[t + C2 j], twiddle W_C^{t ka}
-    {
-      cf a[C1];
-      if (unitA) {
-#pragma unroll
-        for (int j = 0; j < C1; j++) a[j] = t[row_elem<LOGR, LOGC>(p0, rra, ta + C2 * j)];
-      }
-      __syncthreads();  // the tables (first segment); the previous segment's last reads
-      if (unitA) {
-        SgDft<C1, false, float>::run(a);
-#pragma unroll
-        for (int ka = 0; ka < C1; ka++)
-          s[rra * QS + S::pad(ta + C2 * ka)] = (ka == 0 || ta == 0) ? a[ka] : cmul(a[ka], twA[ka * C2 + ta]);
-      }
-    }
-    __syncthreads();
-    // pass B: DFT_C2 over t: Z[ka + C1 kb], to natural order
-    {
-      cf v[C2];
-#pragma unroll
-      for (int i = 0; i < C2; i++) v[i] = s[rrb * QS + S::pad(i + C2 * kab)];
-      SgDft<C2, false, float>::run(v);
-      __syncthreads();
-#pragma unroll
-      for (int kb = 0; kb < C2; kb++) s[rrb * QS + S::pad(kab + C1 * kb)] = v[kb];
-    }
-    __syncthreads();
+    rows_forward<LOGC, NSEQ>(s, twA, tid, [&](int rr, int n) { return t[elem(rr, n)]; });
     // spectrum: pairs (k, M - k) of all three components
     for (int task = tid; task < RP * (C + 1); task += NT) {
       const int pp = task / (C + 1), tau = task % (C + 1);
       const int p = p0 + pp;
-      if (p != 0 && tau == C) continue;
-      int rowA, colA, rowB, colB;  // (side, column) of the smaller frequency and its partner
-      bool special = false;
-      if (p != 0) {
-        if (tau < C / 2) { rowA = 0; colA = tau; rowB = 1; colB = C - 1 - tau; }
-        else { rowA = 1; colA = C - 1 - tau; rowB = 0; colB = tau; }
-      } else if (tau < C / 2) {  // row R/2: k2 <-> C-1-k2
-        rowA = 1; colA = tau; rowB = 1; colB = C - 1 - tau;
-      } else if (tau == C / 2) {  // bins 0 and M
-        rowA = rowB = 0; colA = colB = 0; special = true;
-      } else if (tau < C) {  // row 0: k2 <-> C - k2
-        rowA = 0; colA = tau - C / 2; rowB = 0; colB = C - colA;
-      } else {  // row 0, k2 = C/2: k = M/2, its own partner
-        rowA = rowB = 0; colA = colB = C / 2;
-      }
-      const int k1A = row_k1(R, p, rowA);
+      int rowA, colA, rowB, colB;
+      bool special;
+      if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
       cf* qa = s + ((2 * pp + rowA) * 3) * QS + S::pad(colA);
       cf* qb = s + ((2 * pp + rowB) * 3) * QS + S::pad(colB);
       const float* ha = hs + ((2 * pp + rowA) * C + colA) * HW;
@@ -350,23 +470,10 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
         for (int c = 0; c < 3; c++) qa[c * QS] = cf{y0[c] + ym[c], y0[c] - ym[c]};
         continue;
       }
-      // W_N^k, k = k1A + R colA: W_N^{k1A} W_N^{R colA}
-      cf wk = wsp[colA];
-      if (k1A != 0) {
-        cf w1 = twm(tw_lo, tw_hi, k1A >> 1);
-        if (k1A & 1) w1 = cmul(w1, wn1);
-        wk = cmul(w1, wk);
-      }
+      const cf wk = split_tw(row_k1(R, p, rowA), colA, wsp, tw_lo, tw_hi, wn1);
       cf xk[3], xm[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const cf zk = qa[c * QS], zm = qb[c * QS];
-        const cf Ev{0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y)};
-        const cf Ov{0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x)};
-        const cf wO = cmul(wk, Ov);
-        xk[c] = Ev + wO;
-        xm[c] = cconj(Ev - wO);
-      }
+      for (int c = 0; c < 3; c++) split_pair(qa[c * QS], qb[c * QS], wk, xk[c], xm[c]);
       cf yk[3], ym[3];
       if constexpr (MIX) {
 #define SG_F3_MIX(Y, X, h)                                                       \
@@ -388,86 +495,231 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        const cf P = yk[c] + cconj(ym[c]), Q = yk[c] - cconj(ym[c]);
-        const cf cwQ = cmulc(Q, wk);
-        const cf iwQ{-cwQ.y, cwQ.x};
-        qa[c * QS] = P + iwQ;
-        if (qb != qa) qb[c * QS] = cconj(P - iwQ);
+        cf zk, zm;
+        repack_pair(yk[c], ym[c], wk, zk, zm);
+        qa[c * QS] = zk;
+        if (qb != qa) qb[c * QS] = zm;
       }
     }
     __syncthreads();
-    // pass B': DFT_C2 (sign +) over kb of Z'[ka + C1 kb], conj W_C^{t ka}
-    {
-      cf v[C2];
-#pragma unroll
-      for (int kb = 0; kb < C2; kb++) v[kb] = s[rrb * QS + S::pad(kab + C1 * kb)];
-      SgDft<C2, true, float>::run(v);
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < C2; i++)
-        s[rrb * QS + S::pad(i + C2 * kab)] = (kab == 0 || i == 0) ? v[i] : cmulc(v[i], twB[i * C1 + kab]);
+    rows_inverse<LOGC, NSEQ>(s, twB, tid, [&](int rr, int n, cf v) { t[elem(rr, n)] = v; });
+  }
+}
+
+// Forward row pass of single timelines with the half spectrum out: RP row
+// pairs of one tile per CTA (sequence rr = 2 pp + side), the r2c values X[k]
+// stored at their positions pos (as above) of spec[tile0 + tile][M+1].
+// Grid: tiles x (R/2) / RP.
+template <int LOGR, int LOGC, int RP>
+struct RowSpecGeo {
+  static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
+  using S = Split<LOGC>;
+  static constexpr int QS = S::QS, NSEQ = 2 * RP, NT = NSEQ * S::N1;
+  static constexpr int SMEM = NSEQ * QS + 3 * C;
+  static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
+};
+
+template <int LOGR, int LOGC, int RP, int MINB = 1>
+__global__ void __launch_bounds__(RowSpecGeo<LOGR, LOGC, RP>::NT, MINB)
+    k_f3_rowspec(const float* __restrict__ in, cf* __restrict__ spec, long long tile0,
+                 const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi, cf wn1) {
+  using G = RowSpecGeo<LOGR, LOGC, RP>;
+  using S = typename G::S;
+  constexpr int R = G::R, C = G::C, M = G::M, QS = G::QS, NT = G::NT, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twA = s + NSEQ * QS;
+  cf* twB = twA + C;
+  cf* wsp = twB + C;
+  const int tid = threadIdx.x;
+  constexpr int CPT = (R / 2) / RP;
+  const int p0 = (int)(blockIdx.x % CPT) * RP;
+  const long long tile = blockIdx.x / CPT;
+  const cf* t = reinterpret_cast<const cf*>(in) + tile * (long long)M;
+  cf* X = spec + (tile0 + tile) * (long long)(M + 1);
+  row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  rows_forward<LOGC, NSEQ>(s, twA, tid, [&](int rr, int n) {
+    const float2 v = __ldcs(reinterpret_cast<const float2*>(t) +
+                            (long long)C * row_k1(R, p0 + (rr >> 1), rr & 1) + n);
+    return cf{v.x, v.y};
+  });
+  for (int task = tid; task < RP * (C + 1); task += NT) {
+    const int pp = task / (C + 1), tau = task % (C + 1);
+    const int p = p0 + pp;
+    int rowA, colA, rowB, colB;
+    bool special;
+    if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
+    const cf za = s[(2 * pp + rowA) * QS + S::pad(colA)];
+    // the spectra go to DRAM and are read once: streaming stores
+    float2* Xf = reinterpret_cast<float2*>(X);
+    if (special) {
+      __stcs(Xf, make_float2(za.x + za.y, 0.f));
+      __stcs(Xf + M, make_float2(za.x - za.y, 0.f));
+      continue;
     }
-    __syncthreads();
-    // pass A': DFT_C1 (sign +) over ka, U[t + C2 j], to the tile
-    if (unitA) {
-      cf a[C1];
+    const cf zb = s[(2 * pp + rowB) * QS + S::pad(colB)];
+    const int k1A = row_k1(R, p, rowA), k1B = row_k1(R, p, rowB);
+    cf xk, xm;
+    split_pair(za, zb, split_tw(k1A, colA, wsp, tw_lo, tw_hi, wn1), xk, xm);
+    __stcs(Xf + (long long)C * k1A + colA, make_float2(xk.x, xk.y));
+    if (k1A != k1B || colA != colB) __stcs(Xf + (long long)C * k1B + colB, make_float2(xm.x, xm.y));
+  }
+}
+
+// Inverse row pass of group tiles from their weighted half spectra: gspec
+// [G][3][nseg][M+1] (positions pos), RP row pairs of one group tile per CTA;
+// the rows go into the tile in P^T's layout for k_f3_colinv.  Grid: G nseg x
+// (R/2) / RP.
+template <int LOGR, int LOGC, int RP>
+struct RowInGeo {
+  static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
+  using S = Split<LOGC>;
+  static constexpr int QS = S::QS, NSEQ = 6 * RP, NT = NSEQ * S::N1;
+  static constexpr int SMEM = NSEQ * QS + 3 * C;
+  static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
+};
+
+template <int LOGR, int LOGC, int RP, int MINB = 1>
+__global__ void __launch_bounds__(RowInGeo<LOGR, LOGC, RP>::NT, MINB)
+    k_f3_rows_specin(const cf* __restrict__ gspec, float* __restrict__ data, int nseg,
+                     const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi, cf wn1) {
+  using G = RowInGeo<LOGR, LOGC, RP>;
+  using S = typename G::S;
+  constexpr int R = G::R, C = G::C, M = G::M, QS = G::QS, NT = G::NT, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twA = s + NSEQ * QS;
+  cf* twB = twA + C;
+  cf* wsp = twB + C;
+  const int tid = threadIdx.x;
+  constexpr int CPT = (R / 2) / RP;
+  const int p0 = (int)(blockIdx.x % CPT) * RP;
+  const long long tile = blockIdx.x / CPT;  // group * nseg + segment
+  const long long grp = tile / nseg, seg = tile % nseg;
+  cf* t = reinterpret_cast<cf*>(data + tile * 6LL * M);
+  row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  __syncthreads();
+  for (int task = tid; task < RP * (C + 1); task += NT) {
+    const int pp = task / (C + 1), tau = task % (C + 1);
+    const int p = p0 + pp;
+    int rowA, colA, rowB, colB;
+    bool special;
+    if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
+    const int k1A = row_k1(R, p, rowA), k1B = row_k1(R, p, rowB);
+    cf* qa = s + ((2 * pp + rowA) * 3) * QS + S::pad(colA);
+    cf* qb = s + ((2 * pp + rowB) * 3) * QS + S::pad(colB);
 #pragma unroll
-      for (int ka = 0; ka < C1; ka++) a[ka] = s[rra * QS + S::pad(ta + C2 * ka)];
-      SgDft<C1, true, float>::run(a);
-#pragma unroll
-      for (int j = 0; j < C1; j++) t[row_elem<LOGR, LOGC>(p0, rra, ta + C2 * j)] = a[j];
+    for (int c = 0; c < 3; c++) {
+      const cf* Y = gspec + ((grp * 3 + c) * nseg + seg) * (long long)(M + 1);
+      if (special) {
+        const float y0 = Y[0].x, yM = Y[M].x;
+        qa[c * QS] = cf{y0 + yM, y0 - yM};
+        continue;
+      }
+      const cf wk = split_tw(k1A, colA, wsp, tw_lo, tw_hi, wn1);
+      const cf yk = Y[(long long)C * k1A + colA], ym = Y[(long long)C * k1B + colB];
+      cf zk, zm;
+      repack_pair(yk, ym, wk, zk, zm);
+      qa[c * QS] = zk;
+      if (qb != qa) qb[c * QS] = zm;
     }
   }
+  __syncthreads();
+  rows_inverse<LOGC, NSEQ>(s, twB, tid, [&](int rr, int n, cf v) {
+    const int row = rr / 3;
+    t[row3_elem<LOGC>(row_k1(R, p0 + (row >> 1), row & 1), rr % 3, n)] = v;
+  });
 }
 
 }  // namespace f3
 
 // ---- host side -----------------------------------------------------------------
-// Tile shapes per log2(M): R x C with C >= R, CB = 8 columns per column CTA,
-// RP = 2 row pairs and RSEG = 3 segments per row CTA.  At M = 65536 the
-// column kernels are capped for three CTAs per SM and the row kernel for
-// four (fewer registers, more CTAs in flight: 149 -> 107 us per application
-// of 48 tiles on a GB300).
+// Tile shapes per log2(M): R x C with C >= R.  Group tiles: CB = 8 columns
+// per column CTA, RP = 2 row pairs and RSEG = 3 segments per row CTA; at
+// M = 65536 the column kernels are capped for three CTAs per SM and the row
+// kernel for four (fewer registers, more CTAs in flight: 149 -> 107 us per
+// application of 48 tiles on a GB300).  Single timelines (the right-hand
+// side's detectors): 16 columns per column CTA, 8 row pairs per row CTA.
 namespace {
+constexpr int kCB = 8, kRP = 2, kRSEG = 3, kCB1 = 16, kRP1 = 8;
+
+template <class K>
+cudaError_t set_smem(K k, int bytes) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 template <int LOGR, int LOGC, int MIX, int MBC, int MBR>
 cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
                    const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1, cudaStream_t st) {
-  constexpr int CB = 8, RP = 2, RSEG = 3;
-  using CG = f3::ColGeo<LOGR, LOGC, CB>;
-  using RG = f3::RowGeo<LOGR, LOGC, RP, MIX>;
-  auto kc = f3::k_f3_colfwd<LOGR, LOGC, CB, MBC>;
-  auto kr = f3::k_f3_rows<LOGR, LOGC, RP, MIX, RSEG, MBR>;
-  auto ki = f3::k_f3_colinv<LOGR, LOGC, CB, MBC>;
+  using CG = f3::ColGeo<LOGR, LOGC, kCB, 3>;
+  using RG = f3::RowGeo<LOGR, LOGC, kRP, MIX>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB, 3, MBC>;
+  auto kr = f3::k_f3_rows<LOGR, LOGC, kRP, MIX, kRSEG, MBR>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, MBC>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
-  cudaError_t e = cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, smc);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(ki, cudaFuncAttributeMaxDynamicSharedMemorySize, smc);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, smr);
+  cudaError_t e = set_smem(kc, smc);
+  if (e == cudaSuccess) e = set_smem(ki, smc);
+  if (e == cudaSuccess) e = set_smem(kr, smr);
   if (e != cudaSuccess) return e;
   const long long ntiles = ngroups * nseg;
-  const long long gc = ntiles * (CG::C / CB);
-  const long long gr = ngroups * ((nseg + RSEG - 1) / RSEG) * (RG::R / 2 / RP);
+  const long long gc = ntiles * (CG::C / kCB);
+  const long long gr = ngroups * ((nseg + kRSEG - 1) / kRSEG) * (RG::R / 2 / kRP);
   if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
-  kc<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  kc<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   kr<<<(unsigned)gr, RG::NT, smr, st>>>(data, hrow, nseg, lo, hi, wn1);
   ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
   return cudaGetLastError();
 }
 
-template <int MIX>
-cudaError_t f3_dispatch(float* data, const float* hrow, long long ngroups, int nseg, int logm,
-                        const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1,
-                        cudaStream_t st) {
-  switch (logm) {
-    case 10: return f3_run<5, 5, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 11: return f3_run<5, 6, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 12: return f3_run<6, 6, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 13: return f3_run<6, 7, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 14: return f3_run<7, 7, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 15: return f3_run<7, 8, MIX, 1, 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    case 16: return f3_run<8, 8, MIX, 3, 4>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
-    default: return cudaErrorInvalidValue;
+template <int LOGR, int LOGC>
+cudaError_t f3_fwd1(const float* tod, float* scratch, cplx<float>* spec, long long ntiles,
+                    long long batch, const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1,
+                    cudaStream_t st) {
+  using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
+  using RG = f3::RowSpecGeo<LOGR, LOGC, kRP1>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
+  auto kr = f3::k_f3_rowspec<LOGR, LOGC, kRP1, 1>;
+  const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
+  cudaError_t e = set_smem(kc, smc);
+  if (e == cudaSuccess) e = set_smem(kr, smr);
+  if (e != cudaSuccess) return e;
+  constexpr long long N = 2LL * CG::M;  // samples per tile
+  for (long long t0 = 0; t0 < ntiles && e == cudaSuccess; t0 += batch) {
+    const long long nb = ntiles - t0 < batch ? ntiles - t0 : batch;
+    const long long gc = nb * (CG::C / kCB1), gr = nb * (RG::R / 2 / kRP1);
+    if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
+    kc<<<(unsigned)gc, CG::NT, smc, st>>>(tod + t0 * N, scratch, lo, hi);
+    kr<<<(unsigned)gr, RG::NT, smr, st>>>(scratch, spec, t0, lo, hi, wn1);
+    e = cudaGetLastError();
   }
+  return e;
 }
+
+template <int LOGR, int LOGC, int MBC>
+cudaError_t f3_inv3(const cplx<float>* gspec, float* data, long long ngroups, int nseg,
+                    const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1, cudaStream_t st) {
+  using CG = f3::ColGeo<LOGR, LOGC, kCB, 3>;
+  using RG = f3::RowInGeo<LOGR, LOGC, kRP>;
+  auto kr = f3::k_f3_rows_specin<LOGR, LOGC, kRP, 1>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, MBC>;
+  const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
+  cudaError_t e = set_smem(ki, smc);
+  if (e == cudaSuccess) e = set_smem(kr, smr);
+  if (e != cudaSuccess) return e;
+  const long long ntiles = ngroups * nseg;
+  const long long gc = ntiles * (CG::C / kCB), gr = ntiles * (RG::R / 2 / kRP);
+  if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
+  kr<<<(unsigned)gr, RG::NT, smr, st>>>(gspec, data, nseg, lo, hi, wn1);
+  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  return cudaGetLastError();
+}
+
+// (LOGR, LOGC) = (logm / 2, logm - logm / 2); register caps for three
+// column CTAs and four row CTAs per SM, three where rows of 128 points would
+// spill at four (uncapped, the row kernel took up to 158 registers at
+// 2^13..2^15 points)
+#define SG_F3_SHAPES(X) X(10, 5, 5, 3, 4) X(11, 5, 6, 3, 4) X(12, 6, 6, 3, 4) X(13, 6, 7, 3, 3) \
+  X(14, 7, 7, 3, 3) X(15, 7, 8, 3, 4) X(16, 8, 8, 3, 4)
 
 int f3_logr(int logm) { return logm / 2; }  // R = 2^(logm/2) <= C
 }  // namespace
@@ -485,8 +737,42 @@ cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long
                               int logm, const cplx<float>* tw_lo, const cplx<float>* tw_hi,
                               cplx<float> wn1, cudaStream_t st) {
   if (!fft3_supported(logm) || ngroups < 1 || nseg < 1) return cudaErrorInvalidValue;
-  return mix ? f3_dispatch<1>(data, hrow, ngroups, nseg, logm, tw_lo, tw_hi, wn1, st)
-             : f3_dispatch<0>(data, hrow, ngroups, nseg, logm, tw_lo, tw_hi, wn1, st);
+#define SG_F3_CASE(LM, LR, LC, MBC, MBR)                                                     \
+  case LM:                                                                                  \
+    return mix ? f3_run<LR, LC, 1, MBC, MBR>(data, hrow, ngroups, nseg, tw_lo, tw_hi, wn1, st) \
+               : f3_run<LR, LC, 0, MBC, MBR>(data, hrow, ngroups, nseg, tw_lo, tw_hi, wn1, st);
+  switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
+#undef SG_F3_CASE
+  return cudaErrorInvalidValue;
+}
+
+long long fft3_rhs_batch(int logm) {
+  return std::max(1LL, (48LL << 20) / (8LL << logm));  // tiles of 2M FP32 samples in 48 MB
+}
+
+cudaError_t fft3_forward_spectra(const float* tod, float* scratch, cplx<float>* spec,
+                                 long long ntiles, int logm, const cplx<float>* tw_lo,
+                                 const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st) {
+  if (!fft3_supported(logm) || ntiles < 1) return cudaErrorInvalidValue;
+  const long long batch = fft3_rhs_batch(logm);
+#define SG_F3_CASE(LM, LR, LC, MBC, MBR) \
+  case LM:                              \
+    return f3_fwd1<LR, LC>(tod, scratch, spec, ntiles, batch, tw_lo, tw_hi, wn1, st);
+  switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
+#undef SG_F3_CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t fft3_inverse_from_spectra(const cplx<float>* gspec, float* data, long long ngroups,
+                                      int nseg, int logm, const cplx<float>* tw_lo,
+                                      const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st) {
+  if (!fft3_supported(logm) || ngroups < 1 || nseg < 1) return cudaErrorInvalidValue;
+#define SG_F3_CASE(LM, LR, LC, MBC, MBR) \
+  case LM:                              \
+    return f3_inv3<LR, LC, MBC>(gspec, data, ngroups, nseg, tw_lo, tw_hi, wn1, st);
+  switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
+#undef SG_F3_CASE
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace sg

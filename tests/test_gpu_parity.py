@@ -198,6 +198,39 @@ def test_three_pass_weighting_vs_cluster_kernels_and_oracle(ns, distinct, hwp, n
     cl.close()
 
 
+@pytest.mark.parametrize("ns,hwp", [(8192, False), (131072, True)])
+def test_three_pass_rhs_vs_cluster_kernels_and_oracle(ns, hwp, monkeypatch):
+    """the right-hand side of groups with distinct noise spectra through the
+    three-pass forward FFT (batched column and row passes, half spectra in
+    position order), the group sums and the three-pass inverse: chi^2_0 and
+    the solution against the oracle and against the cluster kernels"""
+    spec = synth.ProblemSpec("t", ndet=6, nside=32, nseg=3, ns=ns, hwp=hwp,
+                             fknee_range=(0.02, 0.2), alpha_range=(1.0, 2.0), problem=29,
+                             precision="f32")
+    prob = synth.make_problem(spec)
+    s = oracle.Setup(prob)
+    b, chi2o = s.rhs(prob["tod"])
+    xo, _, _ = s.pcg(b, precond="bj3", stop_crit=1e-15, maxiter=500)
+    out = {}
+    for f3 in ("1", "0"):
+        monkeypatch.setenv("SANEPIC_GPU_FFT3", f3)
+        mm = sg.from_problem(prob, precision="f32")
+        chi2 = mm.rhs()
+        mm.solve(precond="bj3", stop_crit=1e-14)
+        out[f3] = (chi2, mm.solution(), mm.weighting())
+        npix = mm.npix
+        mm.close()
+    assert out["1"][2] == "group-3pass" and out["0"][2] == "group"
+    for f3, (chi2, x, _) in out.items():
+        assert abs(chi2 - chi2o) <= 1e-5 * chi2o, f3
+        for c in range(3):
+            blk = slice(c * npix, (c + 1) * npix)
+            assert rel_rms(x[blk], xo[blk], remove_monopole=(c == 0)) < 1e-5, (f3, c)
+    for c in range(3):
+        blk = slice(c * npix, (c + 1) * npix)
+        assert rel_rms(out["1"][1][blk], out["0"][1][blk], remove_monopole=(c == 0)) < 2e-6, c
+
+
 def test_apply_bitwise_deterministic():
     prob = small_problem(ndet=4, nseg=4, ns=4096, precision="f32", nside=32)
     mm = sg.from_problem(prob, precision="f32", with_tod=False)
