@@ -168,6 +168,13 @@ long sg_npix(const sg_ctx *ctx);
  * number of groups.  No reference counterpart. */
 int sg_group_mode(const sg_ctx *ctx, long *ngroups);
 
+/* How the operator applies N^-1, as bits: 1 = per offset group (three
+ * timelines per group, see sg_group_mode), 2 = with the three-pass FP32 FFT
+ * through L2 (else the cluster FFT kernels).  Known once the operator was
+ * prepared by a first apply, right-hand side or solve.  No reference
+ * counterpart. */
+int sg_weighting(const sg_ctx *ctx);
+
 /* y = P^T N^-1 P x for a compact host vector [3*npix] (one operator pass,
  * sanepic.cc:1428-1448); masked != 0 applies the pol degeneracy mask
  * (sanepic.cc:1455-1459). */

@@ -35,7 +35,7 @@ MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
 
 # every symbol include/sanepic_gpu.h declares
 EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
-           "sg_group_mode",
+           "sg_group_mode", "sg_weighting",
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
@@ -130,6 +130,8 @@ def load_library(path: Optional[str] = None):
     L.sg_npix.restype = ctypes.c_long
     L.sg_group_mode.argtypes = [c_p, ctypes.POINTER(ctypes.c_long)]
     L.sg_group_mode.restype = ctypes.c_int
+    L.sg_weighting.argtypes = [c_p]
+    L.sg_weighting.restype = ctypes.c_int
     L.sg_apply.argtypes = [c_p, dp, dp, ctypes.c_int]
     L.sg_noise_filter.argtypes = [c_p, dp, dp]
     L.sg_noise_filter_noalloc.argtypes = [c_p, c_p, c_p, ctypes.c_long, ctypes.c_long,
@@ -318,11 +320,13 @@ class MapMaker:
         return on, int(n.value)
 
     def weighting(self) -> str:
-        """How the operator applies N^-1: "per-detector" (one fused filter per
-        detector timeline), "group" (cluster FFT kernels on the offset
-        groups' three timelines) or "group-3pass" (the three-pass FP32 FFT in
-        place in P^T's layout).  Known once the operator was prepared."""
-        return {0: "per-detector", 1: "group", 2: "group-3pass"}[self.L.sg_group_mode(self.h, None)]
+        """How the operator applies N^-1: "per-detector" (one fused cluster
+        filter per detector timeline), "group" (cluster FFT kernels on the
+        offset groups' three timelines), with "-3pass" where the three-pass
+        FP32 FFT through L2 runs instead.  Known once the operator was
+        prepared."""
+        w = self.L.sg_weighting(self.h)
+        return ("group" if w & 1 else "per-detector") + ("-3pass" if w & 2 else "")
 
     def autotune(self) -> dict:
         """Pick the faster compiled FFT tile shape for this problem's noise filter."""

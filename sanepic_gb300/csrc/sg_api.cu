@@ -130,6 +130,11 @@ extern "C" const char* sg_last_error(const sg_ctx* c) {
 
 extern "C" long sg_npix(const sg_ctx* c) { return c ? (long)c->npix : -1; }
 
+extern "C" int sg_weighting(const sg_ctx* c) {
+  if (!c) return SG_ERR_ARG;
+  return (c->group_mode ? 1 : 0) | (c->use_f3 ? 2 : 0);
+}
+
 extern "C" int sg_group_mode(const sg_ctx* c, long* ngroups) {
   if (!c) return 0;
   if (ngroups) *ngroups = c->ngroups;
@@ -1059,8 +1064,7 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
     } else {
       if (e == cudaSuccess) e = c->launch_project();
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
-      if (e == cudaSuccess)
-        e = c->launch_filter(kLoadTod, c->y.p, c->y.p, c->ntiles, (int)c->nseg, 0);
+      if (e == cudaSuccess) e = c->detector_weight_step(c->y.p, c->y.p);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
       if (e == cudaSuccess) e = c->launch_detsum();
     }

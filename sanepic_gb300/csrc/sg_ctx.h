@@ -295,9 +295,21 @@ struct sg_ctx {
   cudaError_t apply_map(double* out, bool masked) {
     if (group_mode) return apply_map_group(out, masked);
     cudaError_t e = launch_project();
-    if (e == cudaSuccess) e = launch_filter(kLoadTod, y.p, y.p, ntiles, (int)nseg, 0);
+    if (e == cudaSuccess) e = detector_weight_step(y.p, y.p);
     if (e == cudaSuccess) e = pt_of_y(out, masked);
     return e;
+  }
+
+  // N^-1 of the per-detector operator, out = N^-1 in (timelines [ntiles][ns],
+  // in == out allowed): the three-pass FP32 filter in batches through L2, or
+  // the fused cluster filter
+  cudaError_t detector_weight_step(const void* in, void* out) {
+    if (!use_f3) return launch_filter(kLoadTod, in, out, ntiles, (int)nseg, 0);
+    const long long nb = (ntiles + fft3_rhs_batch(logm) - 1) / fft3_rhs_batch(logm);
+    launches += 3 * nb;
+    return fft3_detector_filter((const float*)in, (float*)out, f3scratch.as<float>(),
+                                filt_pos.as<float>(), ntiles, (int)nseg, logm,
+                                tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(), wn1f, st);
   }
 
   // forward FFT of tiles to spec_out, or inverse FFT of spec_in to tiles
@@ -326,8 +338,38 @@ struct sg_ctx {
   // the per-group mixing matrices from the filter rows (before any group apply)
   // (the slot order depends on the tile shape: rebuilt when the autotuner
   // changes the cluster size)
+  // the per-detector operator's three-pass filter: the filter rows in
+  // position order and the batches' scratch (made here, not while a graph
+  // is being captured)
+  cudaError_t ensure_f3_detector() {
+    if (have_hmix) return cudaSuccess;
+    const long long M1 = ns / 2 + 1;
+    const char* f3env = getenv("SANEPIC_GPU_FFT3");
+    use_f3 = f32 && fft3_supported(logm) && !(f3env && f3env[0] == '0');
+    cudaError_t e = cudaSuccess;
+    if (use_f3) {
+      std::vector<int> kf;
+      fft3_pos_freq(logm, kf);
+      e = krow.alloc(sizeof(int) * M1);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(krow.p, kf.data(), sizeof(int) * M1, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // kf is a host temporary
+      if (e == cudaSuccess) e = filt_pos.alloc((size_t)ndet * M1 * esize);
+      if (e == cudaSuccess)
+        e = permute_rows_launch<float>(filt.as<float>(), krow.as<int>(), ndet, M1,
+                                       filt_pos.as<float>(), st);
+      if (e == cudaSuccess)
+        e = f3scratch.alloc((size_t)std::min<long long>(ntiles, fft3_rhs_batch(logm)) * ns *
+                            sizeof(float));
+      launches += 1;
+    }
+    if (e == cudaSuccess) have_hmix = true;
+    return e;
+  }
+
   cudaError_t ensure_hmix() {
-    if (!group_mode || (have_hmix && hmix_S == S)) return cudaSuccess;
+    if (!group_mode) return ensure_f3_detector();
+    if (have_hmix && hmix_S == S) return cudaSuccess;
     const long long M1 = ns / 2 + 1;
     cudaError_t e = filt_slot.alloc((size_t)ndet * M1 * esize);
     if (e == cudaSuccess && kslot_S != S) {  // the slot order depends on the tile shape only
@@ -409,6 +451,9 @@ struct sg_ctx {
       if (e == cudaSuccess)
         e = permute_rows_launch<float>(filt.as<float>(), krow.as<int>(), ndet, M1,
                                        filt_pos.as<float>(), st);
+      if (e == cudaSuccess)
+        e = f3scratch.alloc((size_t)std::min<long long>(ntiles, fft3_rhs_batch(logm)) * ns *
+                            sizeof(float));
       if (e == cudaSuccess && groups_uniform) {
         for (long long g = 0; g < ngroups && e == cudaSuccess; g++)
           e = permute_rows_launch<float>(filt.as<float>() + grp_det_h[grp_off_h[g]] * M1,
@@ -445,7 +490,8 @@ struct sg_ctx {
   // rounding differs).
   cudaError_t rhs_of(const void* d, double* bout, double* chi2_dev) {
     if (!group_mode) {
-      cudaError_t e = launch_filter(kLoadTod, d, y.p, ntiles, (int)nseg, 0, nullptr, chi2_dev);
+      cudaError_t e = chi2_dev ? launch_filter(kLoadTod, d, y.p, ntiles, (int)nseg, 0, nullptr, chi2_dev)
+                               : detector_weight_step(d, y.p);
       if (e == cudaSuccess) e = pt_of_y(bout, true);
       return e;
     }
@@ -490,11 +536,9 @@ struct sg_ctx {
       // stay in L2), the group sums (and chi^2) in position order, the
       // inverse into P^T's layout
       const long long nb = std::min<long long>(ntiles, fft3_rhs_batch(logm));
-      cudaError_t e = f3scratch.alloc((size_t)nb * ns * sizeof(float));
       const long long nbatches = (ntiles + nb - 1) / nb;
       launches += 2 * nbatches + 2 + (chi2_dev ? 1 : 0) + 2;
-      if (e == cudaSuccess)
-        e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(), dspec.as<cplx<float>>(),
+      cudaError_t e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(), dspec.as<cplx<float>>(),
                                  ntiles, logm, tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(),
                                  wn1f, st);
       if (e == cudaSuccess)

@@ -170,12 +170,14 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, NC>::NT, MINB)
   }
 }
 
-// pass 3: the conjugate four-step twiddle and the inverse column DFTs, in
-// place on group tiles
-template <int LOGR, int LOGC, int CB, int MINB = 1>
-__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, 3>::NT, MINB)
-    k_f3_colinv(float* __restrict__ data, const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi) {
-  using G = ColGeo<LOGR, LOGC, CB, 3>;
+// pass 3: the conjugate four-step twiddle and the inverse column DFTs; in
+// place on group tiles (NC = 3, in == out), or from the transformed tiles of
+// single timelines back to the timelines (NC = 1)
+template <int LOGR, int LOGC, int CB, int NC, int MINB = 1>
+__global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, NC>::NT, MINB)
+    k_f3_colinv(const float* in, float* out, const cf* __restrict__ tw_lo,
+                const cf* __restrict__ tw_hi) {
+  using G = ColGeo<LOGR, LOGC, CB, NC>;
   using S = typename G::S;
   constexpr int R1 = G::R1, R2 = G::R2, QS = G::QS, NSEQ = G::NSEQ;
   extern __shared__ __align__(16) unsigned char f3_smem[];
@@ -185,14 +187,15 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, 3>::NT, MINB)
   const int tid = threadIdx.x;
   const long long tile = blockIdx.x / (G::C / CB);
   const int c0 = (int)(blockIdx.x % (G::C / CB)) * CB;
-  cf* t = reinterpret_cast<cf*>(data + tile * 6LL * G::M);
+  const cf* ti = reinterpret_cast<const cf*>(in) + tile * NC * (long long)G::M;
+  cf* to = reinterpret_cast<cf*>(out) + tile * NC * (long long)G::M;
   // pass B': conj W_M^{n2 k1}, DFT_R2 (sign +) over kb of U[ka + R1 kb], conj W_R^{t ka}
   {
     const int q = tid % NSEQ, ka = tid / NSEQ, cc = q % CB, n2 = c0 + cc;
     cf v[R2];
 #pragma unroll
-    for (int kb = 0; kb < R2; kb++) v[kb] = t[col_elem<LOGC, CB, 3>(c0, q, ka + R1 * kb)];
-    col_tables<LOGR, LOGC, CB, 3>(twr, step, c0, tw_lo, tw_hi, tid);
+    for (int kb = 0; kb < R2; kb++) v[kb] = ti[col_elem<LOGC, CB, NC>(c0, q, ka + R1 * kb)];
+    col_tables<LOGR, LOGC, CB, NC>(twr, step, c0, tw_lo, tw_hi, tid);
     __syncthreads();
     if (n2 != 0) {
       const cf wa = twm(tw_lo, tw_hi, n2 * ka);
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(ColGeo<LOGR, LOGC, CB, 3>::NT, MINB)
     for (int ka = 0; ka < R1; ka++) a[ka] = s[q * QS + S::pad(ta + R2 * ka)];
     SgDft<R1, true, float>::run(a);
 #pragma unroll
-    for (int j = 0; j < R1; j++) t[col_elem<LOGC, CB, 3>(c0, q, ta + R2 * j)] = a[j];
+    for (int j = 0; j < R1; j++) to[col_elem<LOGC, CB, NC>(c0, q, ta + R2 * j)] = a[j];
   }
 }
 
@@ -506,6 +509,85 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   }
 }
 
+// The weighting pass of single timelines (the per-detector operator): RP
+// row pairs of RSEG consecutive tiles of one detector per CTA (sequence rr =
+// 2 pp + side), in place on the transformed tiles data [tiles][2M] (tile t of
+// the batch is tile tile0 + t of the operator, detector (tile0 + t) / nseg);
+// the spectrum of each frequency pair is scaled by the detector's filter row
+// in position order (hpos [ndet][M+1]).  Grid: ceil(tiles / RSEG) x (R/2) / RP.
+template <int LOGR, int LOGC, int RP>
+struct Row1Geo {
+  static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
+  using S = Split<LOGC>;
+  static constexpr int QS = S::QS, NSEQ = 2 * RP, NT = NSEQ * S::N1;
+  // shared: sequences, W_C twice, split table (complex) + the rows' weights
+  static constexpr int SMEM = NSEQ * QS + 3 * C + (2 * RP * C + 2) / 2;
+  static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
+};
+
+template <int LOGR, int LOGC, int RP, int RSEG, int MINB = 1>
+__global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
+    k_f3_rows1(float* __restrict__ data, long long ntiles, long long tile0, int nseg,
+               const float* __restrict__ hpos, const cf* __restrict__ tw_lo,
+               const cf* __restrict__ tw_hi, cf wn1) {
+  using G = Row1Geo<LOGR, LOGC, RP>;
+  using S = typename G::S;
+  constexpr int R = G::R, C = G::C, M = G::M, QS = G::QS, NT = G::NT, NSEQ = G::NSEQ;
+  extern __shared__ __align__(16) unsigned char f3_smem[];
+  cf* s = reinterpret_cast<cf*>(f3_smem);
+  cf* twA = s + NSEQ * QS;
+  cf* twB = twA + C;
+  cf* wsp = twB + C;
+  float* hs = reinterpret_cast<float*>(wsp + C);  // [2 RP][C], then bin M
+  const int tid = threadIdx.x;
+  constexpr int CPT = (R / 2) / RP;
+  const int p0 = (int)(blockIdx.x % CPT) * RP;
+  const long long tb = (blockIdx.x / CPT) * RSEG;  // first tile of the batch
+  row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  long long det_staged = -1;
+  const long long t_end = tb + RSEG < ntiles ? tb + RSEG : ntiles;
+  for (long long tl = tb; tl < t_end; tl++) {
+    const long long det = (tile0 + tl) / nseg;
+    cf* t = reinterpret_cast<cf*>(data) + tl * (long long)M;
+    auto elem = [&](int rr, int n) {
+      return (long long)C * row_k1(R, p0 + (rr >> 1), rr & 1) + n;
+    };
+    if (det != det_staged) {  // the detector's filter values at this CTA's rows
+      __syncthreads();  // the previous tile's last reads of hs
+      const float* h = hpos + det * (long long)(M + 1);
+      for (int i = tid; i < 2 * RP * C; i += NT)
+        hs[i] = __ldg(h + (long long)C * row_k1(R, p0 + (i / C >> 1), (i / C) & 1) + i % C);
+      if (tid == 0) hs[2 * RP * C] = __ldg(h + M);
+      det_staged = det;
+    }
+    rows_forward<LOGC, NSEQ>(s, twA, tid, [&](int rr, int n) { return t[elem(rr, n)]; });
+    for (int task = tid; task < RP * (C + 1); task += NT) {
+      const int pp = task / (C + 1), tau = task % (C + 1);
+      const int p = p0 + pp;
+      int rowA, colA, rowB, colB;
+      bool special;
+      if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
+      cf* qa = s + (2 * pp + rowA) * QS + S::pad(colA);
+      cf* qb = s + (2 * pp + rowB) * QS + S::pad(colB);
+      const float ha = hs[(2 * pp + rowA) * C + colA], hb = hs[(2 * pp + rowB) * C + colB];
+      if (special) {
+        const cf z = *qa;
+        const float y0 = ha * (z.x + z.y), yM = hs[2 * RP * C] * (z.x - z.y);
+        *qa = cf{y0 + yM, y0 - yM};
+        continue;
+      }
+      const cf wk = split_tw(row_k1(R, p, rowA), colA, wsp, tw_lo, tw_hi, wn1);
+      cf xk, xm, zk, zm;
+      split_pair(*qa, *qb, wk, xk, xm);
+      repack_pair(cscale(xk, ha), cscale(xm, hb), wk, zk, zm);
+      *qa = zk;
+      if (qb != qa) *qb = zm;
+    }
+    __syncthreads();
+    rows_inverse<LOGC, NSEQ>(s, twB, tid, [&](int rr, int n, cf v) { t[elem(rr, n)] = v; });
+  }
+}
+
 // Forward row pass of single timelines with the half spectrum out: RP row
 // pairs of one tile per CTA (sequence rr = 2 pp + side), the r2c values X[k]
 // stored at their positions pos (as above) of spec[tile0 + tile][M+1].
@@ -655,7 +737,7 @@ cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
   using RG = f3::RowGeo<LOGR, LOGC, kRP, MIX>;
   auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB, 3, MBC>;
   auto kr = f3::k_f3_rows<LOGR, LOGC, kRP, MIX, kRSEG, MBR>;
-  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, MBC>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, 3, MBC>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
   if (e == cudaSuccess) e = set_smem(ki, smc);
@@ -667,7 +749,7 @@ cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
   if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
   kc<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   kr<<<(unsigned)gr, RG::NT, smr, st>>>(data, hrow, nseg, lo, hi, wn1);
-  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   return cudaGetLastError();
 }
 
@@ -701,7 +783,7 @@ cudaError_t f3_inv3(const cplx<float>* gspec, float* data, long long ngroups, in
   using CG = f3::ColGeo<LOGR, LOGC, kCB, 3>;
   using RG = f3::RowInGeo<LOGR, LOGC, kRP>;
   auto kr = f3::k_f3_rows_specin<LOGR, LOGC, kRP, 1>;
-  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, MBC>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, 3, MBC>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(ki, smc);
   if (e == cudaSuccess) e = set_smem(kr, smr);
@@ -710,8 +792,36 @@ cudaError_t f3_inv3(const cplx<float>* gspec, float* data, long long ngroups, in
   const long long gc = ntiles * (CG::C / kCB), gr = ntiles * (RG::R / 2 / kRP);
   if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
   kr<<<(unsigned)gr, RG::NT, smr, st>>>(gspec, data, nseg, lo, hi, wn1);
-  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, lo, hi);
+  ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   return cudaGetLastError();
+}
+
+template <int LOGR, int LOGC>
+cudaError_t f3_det(const float* x, float* y, float* scratch, const float* hpos, long long ntiles,
+                   int nseg, long long batch, const cplx<float>* lo, const cplx<float>* hi,
+                   cplx<float> wn1, cudaStream_t st) {
+  constexpr int RS1 = 4;  // tiles per row CTA (consecutive segments share the filter row)
+  using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
+  using RG = f3::Row1Geo<LOGR, LOGC, kRP1>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
+  auto kr = f3::k_f3_rows1<LOGR, LOGC, kRP1, RS1, 3>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB1, 1, 1>;
+  const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
+  cudaError_t e = set_smem(kc, smc);
+  if (e == cudaSuccess) e = set_smem(ki, smc);
+  if (e == cudaSuccess) e = set_smem(kr, smr);
+  if (e != cudaSuccess) return e;
+  constexpr long long N = 2LL * CG::M;
+  for (long long t0 = 0; t0 < ntiles && e == cudaSuccess; t0 += batch) {
+    const long long nb = ntiles - t0 < batch ? ntiles - t0 : batch;
+    const long long gc = nb * (CG::C / kCB1), gr = (nb + RS1 - 1) / RS1 * (RG::R / 2 / kRP1);
+    if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
+    kc<<<(unsigned)gc, CG::NT, smc, st>>>(x + t0 * N, scratch, lo, hi);
+    kr<<<(unsigned)gr, RG::NT, smr, st>>>(scratch, nb, t0, nseg, hpos, lo, hi, wn1);
+    ki<<<(unsigned)gc, CG::NT, smc, st>>>(scratch, y + t0 * N, lo, hi);
+    e = cudaGetLastError();
+  }
+  return e;
 }
 
 // (LOGR, LOGC) = (logm / 2, logm - logm / 2); register caps for three
@@ -758,6 +868,19 @@ cudaError_t fft3_forward_spectra(const float* tod, float* scratch, cplx<float>* 
 #define SG_F3_CASE(LM, LR, LC, MBC, MBR) \
   case LM:                              \
     return f3_fwd1<LR, LC>(tod, scratch, spec, ntiles, batch, tw_lo, tw_hi, wn1, st);
+  switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
+#undef SG_F3_CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t fft3_detector_filter(const float* x, float* y, float* scratch, const float* hpos,
+                                 long long ntiles, int nseg, int logm, const cplx<float>* tw_lo,
+                                 const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st) {
+  if (!fft3_supported(logm) || ntiles < 1 || nseg < 1) return cudaErrorInvalidValue;
+  const long long batch = fft3_rhs_batch(logm);
+#define SG_F3_CASE(LM, LR, LC, MBC, MBR) \
+  case LM:                              \
+    return f3_det<LR, LC>(x, y, scratch, hpos, ntiles, nseg, batch, tw_lo, tw_hi, wn1, st);
   switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
 #undef SG_F3_CASE
   return cudaErrorInvalidValue;

@@ -233,6 +233,12 @@ cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long
 // weighted group spectra gspec [G][3][nseg][M+1] (positions pos) into the
 // group tiles in P^T's layout.
 long long fft3_rhs_batch(int logm);
+// y [ntiles][2M] <- c2r(h_d r2c(x)) per tile (detector d = tile / nseg,
+// hpos [ndet][M+1] the filter rows in position order; x == y allowed), in
+// batches through scratch [fft3_rhs_batch(logm)][2M]
+cudaError_t fft3_detector_filter(const float* x, float* y, float* scratch, const float* hpos,
+                                 long long ntiles, int nseg, int logm, const cplx<float>* tw_lo,
+                                 const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st);
 cudaError_t fft3_forward_spectra(const float* tod, float* scratch, cplx<float>* spec,
                                  long long ntiles, int logm, const cplx<float>* tw_lo,
                                  const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st);
