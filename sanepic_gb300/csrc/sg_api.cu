@@ -163,7 +163,13 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
     e = (x);                                          \
     if (e != cudaSuccess) return c->cuda_fail(e, #x); \
   } while (0)
-  DevBuf dra, ddec, dpsi, doffx, doffy, ring, psio, flag, count, scratch, gsz, gsc, gss;
+  // device scratch of the set-up, kept in the context so that a caller who
+  // sets the pointing again (one scan after another) does not pay for
+  // allocating and freeing it each time
+  sg_ctx::PointingScratch& P = c->pscr;
+  DevBuf &dra = P.ra, &ddec = P.dec, &dpsi = P.psi, &doffx = P.offx, &doffy = P.offy,
+         &ring = P.ring, &psio = P.psio, &flag = P.flag, &count = P.count, &scratch = P.scratch,
+         &gsz = P.gsz, &gsc = P.gsc, &gss = P.gss;
   SG_TRY(dra.alloc(sizeof(double) * nsd));
   SG_TRY(ddec.alloc(sizeof(double) * nsd));
   SG_TRY(dpsi.alloc(sizeof(double) * nsd));
@@ -268,9 +274,6 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
       break;
     }
   }
-  dra.release();
-  ddec.release();
-  dpsi.release();
   const int G = c->ngroups;
   const long long ng = c->ngsamp;
   std::vector<int> gsize(G);
@@ -312,7 +315,7 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   {
     const long long nf = c->npixfull, nside = c->desc.nside;
     const size_t ntb = numbering_tmp_bytes(nf);
-    DevBuf ntmp, d_i2r, d_i2rc, d_ipr, d_np;
+    DevBuf &ntmp = P.ntmp, &d_i2r = P.i2r, &d_i2rc = P.i2rc, &d_ipr = P.ipr, &d_np = P.np;
     SG_TRY(ntmp.alloc(ntb));
     SG_TRY(d_i2r.alloc(sizeof(long long) * nf));
     SG_TRY(d_i2rc.alloc(sizeof(long long) * nf));
@@ -342,7 +345,6 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(compact_launch(ring.as<int>(), c->indpix.as<int>(), ng, c->pix.as<int>(), c->st));
   SG_TRY(c->hits.alloc(sizeof(int) * npix));
   SG_TRY(hits_launch(count.as<int>(), c->indpix.as<int>(), c->npixfull, c->hits.as<int>(), c->st));
-  ring.release();
   // pixel-sorted group-sample index (CSR) for P^T
   const size_t ctb = csr_tmp_bytes(ng, npix);
   SG_TRY(scratch.alloc(ctb));
@@ -350,11 +352,10 @@ extern "C" int sg_set_pointing(sg_ctx* c, const double* ra, const double* dec,
   SG_TRY(c->csr_idx.alloc(sizeof(uint32_t) * ng));
   SG_TRY(csr_build(c->pix.as<int>(), ng, npix, c->csr_off.as<long long>(),
                    c->csr_idx.as<uint32_t>(), scratch.p, ctb, c->st));
-  scratch.release();
   // base angles (cos 2phi, sin 2phi) in time order and in CSR order
   SG_TRY(c->cs.alloc((size_t)2 * ng * c->esize));
   SG_TRY(c->csr_cs.alloc((size_t)2 * ng * c->esize));
-  DevBuf cs64;  // FP64 (cos, sin) 2 psi_o for the cross-link sums (no half-wave plate)
+  DevBuf& cs64 = P.cs64;  // FP64 (cos, sin) 2 psi_o for the cross-link sums (no half-wave plate)
   if (!hwp) SG_TRY(cs64.alloc(sizeof(double) * 2 * ng));
   if (c->f32) {
     SG_TRY(base_angles_launch<float>(psio.as<double>(), ng, ns, nsd, hwp ? 1 : 0, c->desc.omega,

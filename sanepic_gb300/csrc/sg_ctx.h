@@ -128,6 +128,12 @@ struct sg_ctx {
   int kslot_S = -1;         // the tile shape kslot was made for
   int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
+  // sg_set_pointing's device scratch (boresight, pixels, numbering and sort
+  // temporaries), kept between calls
+  struct PointingScratch {
+    DevBuf ra, dec, psi, offx, offy, ring, psio, flag, count, scratch, gsz, gsc, gss;
+    DevBuf ntmp, i2r, i2rc, ipr, np, cs64;
+  } pscr;
   DevBuf noise_stage, noise_part;  // one detector's iSpf values; g0 partial sums
   cudaEvent_t ev_copy = nullptr;   // host->device copy of a caller's array done
 
