@@ -258,16 +258,25 @@ __device__ __forceinline__ bool pair_of(int C, int p, int tau, int& rowA, int& c
   return true;
 }
 
-// W_N^k for k = k1 + R col (N = 2M): W_N^{k1} W_N^{R col}, wsp[col] = W_N^{R col}
-__device__ __forceinline__ cf split_tw(int k1, int col, const cf* wsp, const cf* lo, const cf* hi,
-                                       cf wn1) {
-  cf wk = wsp[col];
-  if (k1 != 0) {
-    cf w1 = twm(lo, hi, k1 >> 1);
-    if (k1 & 1) w1 = cmul(w1, wn1);
-    wk = cmul(w1, wk);
+// W_N^{k1} (N = 2M) of each of a CTA's 2 RP rows (row 2 pp + side of pair
+// p0 + pp), from the W_M table and wn1 = W_N; the split twiddle of
+// k = k1 + R col is then W_N^k = w1s[row] W_N^{R col} (wsp[col] = W_N^{R col};
+// exact for k1 = 0, where w1s = 1), computed once per CTA instead of once per
+// frequency pair
+__device__ __forceinline__ void row_w1_table(cf* w1s, int nrows, int p0, int R, const cf* lo,
+                                             const cf* hi, cf wn1, int tid, int nt) {
+  for (int i = tid; i < nrows; i += nt) {
+    const int k1 = row_k1(R, p0 + (i >> 1), i & 1);
+    cf w1{1.f, 0.f};
+    if (k1 != 0) {
+      w1 = twm(lo, hi, k1 >> 1);
+      if (k1 & 1) w1 = cmul(w1, wn1);
+    }
+    w1s[i] = w1;
   }
-  return wk;
+}
+__device__ __forceinline__ cf split_tw_row(const cf* w1s, int row, int col, const cf* wsp) {
+  return cmul(w1s[row], wsp[col]);
 }
 
 // r2c values X[k], X[M-k] from the packed spectrum values Z[k], Z[M-k]
@@ -392,7 +401,7 @@ struct RowGeo {
   static constexpr int NT = NSEQ * C1;
   static constexpr int HW = MIX ? 6 : 1;  // weights per frequency
   // shared: sequences, W_C twice, split table (complex) + weights (floats, padded to 8 B)
-  static constexpr int SMEM = NSEQ * QS + 3 * C + (2 * RP * C * HW + HW + 1) / 2;
+  static constexpr int SMEM = NSEQ * QS + 3 * C + 2 * RP + (2 * RP * C * HW + HW + 1) / 2;
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
@@ -409,7 +418,8 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   cf* twA = s + NSEQ * QS;
   cf* twB = twA + C;
   cf* wsp = twB + C;
-  float* hs = reinterpret_cast<float*>(wsp + C);  // [2 RP][C][HW], then bin M
+  cf* w1s = wsp + C;  // [2 RP]
+  float* hs = reinterpret_cast<float*>(w1s + 2 * RP);  // [2 RP][C][HW], then bin M
   const int tid = threadIdx.x;
   constexpr int CPT = (R / 2) / RP;  // CTAs per segment
   const int nsb = (nseg + RSEG - 1) / RSEG;
@@ -419,6 +429,7 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   const long long grp = rest / nsb;
   const float* H = hrow + grp * (long long)(M + 1) * HW;
   row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  row_w1_table(w1s, 2 * RP, p0, R, tw_lo, tw_hi, wn1, tid, NT);
   for (int i = tid; i < 2 * RP * C * HW; i += NT) {
     const int row = i / (C * HW), e = i % (C * HW);
     hs[i] = __ldg(H + (long long)C * HW * row_k1(R, p0 + (row >> 1), row & 1) + e);
@@ -473,7 +484,7 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
         for (int c = 0; c < 3; c++) qa[c * QS] = cf{y0[c] + ym[c], y0[c] - ym[c]};
         continue;
       }
-      const cf wk = split_tw(row_k1(R, p, rowA), colA, wsp, tw_lo, tw_hi, wn1);
+      const cf wk = split_tw_row(w1s, 2 * pp + rowA, colA, wsp);
       cf xk[3], xm[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) split_pair(qa[c * QS], qb[c * QS], wk, xk[c], xm[c]);
@@ -520,8 +531,8 @@ struct Row1Geo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
   using S = Split<LOGC>;
   static constexpr int QS = S::QS, NSEQ = 2 * RP, NT = NSEQ * S::N1;
-  // shared: sequences, W_C twice, split table (complex) + the rows' weights
-  static constexpr int SMEM = NSEQ * QS + 3 * C + (2 * RP * C + 2) / 2;
+  // shared: sequences, W_C twice, split tables (complex) + the rows' weights
+  static constexpr int SMEM = NSEQ * QS + 3 * C + 2 * RP + (2 * RP * C + 2) / 2;
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
@@ -538,12 +549,14 @@ __global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
   cf* twA = s + NSEQ * QS;
   cf* twB = twA + C;
   cf* wsp = twB + C;
-  float* hs = reinterpret_cast<float*>(wsp + C);  // [2 RP][C], then bin M
+  cf* w1s = wsp + C;  // [2 RP]
+  float* hs = reinterpret_cast<float*>(w1s + 2 * RP);  // [2 RP][C], then bin M
   const int tid = threadIdx.x;
   constexpr int CPT = (R / 2) / RP;
   const int p0 = (int)(blockIdx.x % CPT) * RP;
   const long long tb = (blockIdx.x / CPT) * RSEG;  // first tile of the batch
   row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  row_w1_table(w1s, 2 * RP, p0, R, tw_lo, tw_hi, wn1, tid, NT);
   long long det_staged = -1;
   const long long t_end = tb + RSEG < ntiles ? tb + RSEG : ntiles;
   for (long long tl = tb; tl < t_end; tl++) {
@@ -576,7 +589,7 @@ __global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
         *qa = cf{y0 + yM, y0 - yM};
         continue;
       }
-      const cf wk = split_tw(row_k1(R, p, rowA), colA, wsp, tw_lo, tw_hi, wn1);
+      const cf wk = split_tw_row(w1s, 2 * pp + rowA, colA, wsp);
       cf xk, xm, zk, zm;
       split_pair(*qa, *qb, wk, xk, xm);
       repack_pair(cscale(xk, ha), cscale(xm, hb), wk, zk, zm);
@@ -597,7 +610,7 @@ struct RowSpecGeo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
   using S = Split<LOGC>;
   static constexpr int QS = S::QS, NSEQ = 2 * RP, NT = NSEQ * S::N1;
-  static constexpr int SMEM = NSEQ * QS + 3 * C;
+  static constexpr int SMEM = NSEQ * QS + 3 * C + 2 * RP;
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
@@ -619,7 +632,9 @@ __global__ void __launch_bounds__(RowSpecGeo<LOGR, LOGC, RP>::NT, MINB)
   const long long tile = blockIdx.x / CPT;
   const cf* t = reinterpret_cast<const cf*>(in) + tile * (long long)M;
   cf* X = spec + (tile0 + tile) * (long long)(M + 1);
+  cf* w1s = wsp + C;
   row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  row_w1_table(w1s, 2 * RP, p0, R, tw_lo, tw_hi, wn1, tid, NT);
   rows_forward<LOGC, NSEQ>(s, twA, tid, [&](int rr, int n) {
     const float2 v = __ldcs(reinterpret_cast<const float2*>(t) +
                             (long long)C * row_k1(R, p0 + (rr >> 1), rr & 1) + n);
@@ -642,7 +657,7 @@ __global__ void __launch_bounds__(RowSpecGeo<LOGR, LOGC, RP>::NT, MINB)
     const cf zb = s[(2 * pp + rowB) * QS + S::pad(colB)];
     const int k1A = row_k1(R, p, rowA), k1B = row_k1(R, p, rowB);
     cf xk, xm;
-    split_pair(za, zb, split_tw(k1A, colA, wsp, tw_lo, tw_hi, wn1), xk, xm);
+    split_pair(za, zb, split_tw_row(w1s, 2 * pp + rowA, colA, wsp), xk, xm);
     __stcs(Xf + (long long)C * k1A + colA, make_float2(xk.x, xk.y));
     if (k1A != k1B || colA != colB) __stcs(Xf + (long long)C * k1B + colB, make_float2(xm.x, xm.y));
   }
@@ -657,7 +672,7 @@ struct RowInGeo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
   using S = Split<LOGC>;
   static constexpr int QS = S::QS, NSEQ = 6 * RP, NT = NSEQ * S::N1;
-  static constexpr int SMEM = NSEQ * QS + 3 * C;
+  static constexpr int SMEM = NSEQ * QS + 3 * C + 2 * RP;
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
@@ -679,7 +694,9 @@ __global__ void __launch_bounds__(RowInGeo<LOGR, LOGC, RP>::NT, MINB)
   const long long tile = blockIdx.x / CPT;  // group * nseg + segment
   const long long grp = tile / nseg, seg = tile % nseg;
   cf* t = reinterpret_cast<cf*>(data + tile * 6LL * M);
+  cf* w1s = wsp + C;
   row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
+  row_w1_table(w1s, 2 * RP, p0, R, tw_lo, tw_hi, wn1, tid, NT);
   __syncthreads();
   for (int task = tid; task < RP * (C + 1); task += NT) {
     const int pp = task / (C + 1), tau = task % (C + 1);
@@ -698,7 +715,7 @@ __global__ void __launch_bounds__(RowInGeo<LOGR, LOGC, RP>::NT, MINB)
         qa[c * QS] = cf{y0 + yM, y0 - yM};
         continue;
       }
-      const cf wk = split_tw(k1A, colA, wsp, tw_lo, tw_hi, wn1);
+      const cf wk = split_tw_row(w1s, 2 * pp + rowA, colA, wsp);
       const cf yk = Y[(long long)C * k1A + colA], ym = Y[(long long)C * k1B + colB];
       cf zk, zm;
       repack_pair(yk, ym, wk, zk, zm);
