@@ -52,6 +52,43 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// FP32 into P^T's interleaved layout, four group samples per thread (16-byte
+// pixel and angle loads, one float4 map gather per sample, one float4 store
+// per component: the four samples of a component are contiguous there);
+// with wmix (uniform groups) the three timelines are mixed by W as below.
+// ng and nsd are multiples of 8 (ns >= 1024).
+__global__ void __launch_bounds__(256)
+    k_group_project4(const int4* __restrict__ gpix, const float4* __restrict__ gcs,
+                     const float4* __restrict__ map, const float* __restrict__ wmix,
+                     long long n4, long long nsd, float* __restrict__ gtl) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long i0 = 4 * i, g = i0 / nsd, w = i0 - g * nsd;
+    const int4 p = __ldcs(gpix + i);
+    const float4 ca = __ldcs(gcs + 2 * i), cb = __ldcs(gcs + 2 * i + 1);
+    const float4 m0 = map[p.x], m1 = map[p.y], m2 = map[p.z], m3 = map[p.w];
+    float4 a = make_float4(m0.x, m1.x, m2.x, m3.x);
+    float4 b = make_float4(ca.x * m0.y + ca.y * m0.z, ca.z * m1.y + ca.w * m1.z,
+                           cb.x * m2.y + cb.y * m2.z, cb.z * m3.y + cb.w * m3.z);
+    float4 e = make_float4(ca.x * m0.z - ca.y * m0.y, ca.z * m1.z - ca.w * m1.y,
+                           cb.x * m2.z - cb.y * m2.y, cb.z * m3.z - cb.w * m3.y);
+    if (wmix) {
+      const float* W = wmix + 6 * g;  // W00 W01 W02 W11 W12 W22
+      const float4 a0 = a, b0 = b, e0 = e;
+      a = make_float4(W[0] * a0.x + W[1] * b0.x + W[2] * e0.x, W[0] * a0.y + W[1] * b0.y + W[2] * e0.y,
+                      W[0] * a0.z + W[1] * b0.z + W[2] * e0.z, W[0] * a0.w + W[1] * b0.w + W[2] * e0.w);
+      b = make_float4(W[1] * a0.x + W[3] * b0.x + W[4] * e0.x, W[1] * a0.y + W[3] * b0.y + W[4] * e0.y,
+                      W[1] * a0.z + W[3] * b0.z + W[4] * e0.z, W[1] * a0.w + W[3] * b0.w + W[4] * e0.w);
+      e = make_float4(W[2] * a0.x + W[4] * b0.x + W[5] * e0.x, W[2] * a0.y + W[4] * b0.y + W[5] * e0.y,
+                      W[2] * a0.z + W[4] * b0.z + W[5] * e0.z, W[2] * a0.w + W[4] * b0.w + W[5] * e0.w);
+    }
+    float* o = gtl + gtl_at(g, 0, w, nsd, 1);
+    *reinterpret_cast<float4*>(o) = a;
+    *reinterpret_cast<float4*>(o + 8) = b;
+    *reinterpret_cast<float4*>(o + 16) = e;
+  }
+}
+
 // Uniform groups (one noise spectrum h for all the group's detectors):
 // H = h W with the constant W = sum_d [1 c s]^T [1 c s], so W mixes the three
 // timelines before the filter instead of per frequency after it:
@@ -98,6 +135,14 @@ __global__ void k_group_wmix(const T* __restrict__ dcs, const int* __restrict__ 
 template <typename T>
 cudaError_t group_project_w_launch(const int* gpix, const T* gcs, const T* map, const T* wmix,
                                    long long ng, long long nsd, T* gtl, int ilv, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (ilv && nsd % 8 == 0) {
+      k_group_project4<<<blocks_for(ng / 4), 256, 0, st>>>(
+          reinterpret_cast<const int4*>(gpix), reinterpret_cast<const float4*>(gcs),
+          reinterpret_cast<const float4*>(map), wmix, ng / 4, nsd, gtl);
+      return cudaGetLastError();
+    }
+  }
   k_group_project_w<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, wmix, ng, nsd, ilv, gtl);
   return cudaGetLastError();
 }
@@ -330,6 +375,14 @@ cudaError_t group_rhs_launch(const cplx<T>* dspec, const T* filt, const T* dcs, 
 template <typename T>
 cudaError_t group_project_launch(const int* gpix, const T* gcs, const T* map, long long ng,
                                  long long nsd, T* gtl, int ilv, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    if (ilv && nsd % 8 == 0) {
+      k_group_project4<<<blocks_for(ng / 4), 256, 0, st>>>(
+          reinterpret_cast<const int4*>(gpix), reinterpret_cast<const float4*>(gcs),
+          reinterpret_cast<const float4*>(map), nullptr, ng / 4, nsd, gtl);
+      return cudaGetLastError();
+    }
+  }
   k_group_project<T><<<blocks_for(ng), 256, 0, st>>>(gpix, gcs, map, ng, nsd, ilv, gtl);
   return cudaGetLastError();
 }
