@@ -311,10 +311,9 @@ struct sg_ctx {
   // the fused cluster filter
   cudaError_t detector_weight_step(const void* in, void* out) {
     if (!use_f3) return launch_filter(kLoadTod, in, out, ntiles, (int)nseg, 0);
-    const long long nb = (ntiles + fft3_rhs_batch(logm) - 1) / fft3_rhs_batch(logm);
-    launches += 3 * nb;
+    launches += 3 * ((ntiles + f3_batch - 1) / f3_batch);
     return fft3_detector_filter((const float*)in, (float*)out, f3scratch.as<float>(),
-                                filt_pos.as<float>(), ntiles, (int)nseg, logm,
+                                filt_pos.as<float>(), ntiles, f3_batch, (int)nseg, logm,
                                 tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(), wn1f, st);
   }
 
@@ -364,9 +363,8 @@ struct sg_ctx {
       if (e == cudaSuccess)
         e = permute_rows_launch<float>(filt.as<float>(), krow.as<int>(), ndet, M1,
                                        filt_pos.as<float>(), st);
-      if (e == cudaSuccess)
-        e = f3scratch.alloc((size_t)std::min<long long>(ntiles, fft3_rhs_batch(logm)) * ns *
-                            sizeof(float));
+      f3_batch = std::min<long long>(ntiles, fft3_rhs_batch(logm));
+      if (e == cudaSuccess) e = f3scratch.alloc((size_t)f3_batch * ns * sizeof(float));
       launches += 1;
     }
     if (e == cudaSuccess) have_hmix = true;
@@ -457,9 +455,8 @@ struct sg_ctx {
       if (e == cudaSuccess)
         e = permute_rows_launch<float>(filt.as<float>(), krow.as<int>(), ndet, M1,
                                        filt_pos.as<float>(), st);
-      if (e == cudaSuccess)
-        e = f3scratch.alloc((size_t)std::min<long long>(ntiles, fft3_rhs_batch(logm)) * ns *
-                            sizeof(float));
+      f3_batch = std::min<long long>(ntiles, fft3_rhs_batch(logm));
+      if (e == cudaSuccess) e = f3scratch.alloc((size_t)f3_batch * ns * sizeof(float));
       if (e == cudaSuccess && groups_uniform) {
         for (long long g = 0; g < ngroups && e == cudaSuccess; g++)
           e = permute_rows_launch<float>(filt.as<float>() + grp_det_h[grp_off_h[g]] * M1,
@@ -486,6 +483,7 @@ struct sg_ctx {
   bool use_f3 = false;
   DevBuf krow, hrow;
   DevBuf filt_pos, f3scratch;  // filter rows in position order; the forward batches' scratch
+  long long f3_batch = 1;      // tiles per batch of the single-timeline passes
 
   // b = P^T N^-1 d for the timelines d (device, one row per detector) and
   // chi^2 of d into *chi2_dev.  Offset groups: the detectors' forward FFTs,
@@ -541,12 +539,12 @@ struct sg_ctx {
       // every detector's half spectrum (three-pass forward in batches that
       // stay in L2), the group sums (and chi^2) in position order, the
       // inverse into P^T's layout
-      const long long nb = std::min<long long>(ntiles, fft3_rhs_batch(logm));
-      const long long nbatches = (ntiles + nb - 1) / nb;
+      const long long nbatches = (ntiles + f3_batch - 1) / f3_batch;
       launches += 2 * nbatches + 2 + (chi2_dev ? 1 : 0) + 2;
-      cudaError_t e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(), dspec.as<cplx<float>>(),
-                                 ntiles, logm, tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(),
-                                 wn1f, st);
+      cudaError_t e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(),
+                                           dspec.as<cplx<float>>(), ntiles, f3_batch, logm,
+                                           tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(), wn1f,
+                                           st);
       if (e == cudaSuccess)
         e = group_rhs_launch<float>(dspec.as<cplx<float>>(), filt_pos.as<float>(), dcs.as<float>(),
                                     grp_off.as<int>(), grp_det.as<int>(), ngroups, nseg, M1,

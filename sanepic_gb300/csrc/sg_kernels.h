@@ -228,20 +228,22 @@ cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long
                               cplx<float> wn1, cudaStream_t st);
 // The right-hand side's halves: the half spectra X[k] (positions pos) of
 // single timelines tod [ntiles][2M] into spec [ntiles][M+1], in batches of
-// fft3_rhs_batch(logm) tiles through scratch [batch][2M] (sized so that a
-// batch stays in L2 between its column and row passes); and the inverse of
-// weighted group spectra gspec [G][3][nseg][M+1] (positions pos) into the
-// group tiles in P^T's layout.
+// `batch` tiles through scratch [batch][2M]; and the inverse of weighted
+// group spectra gspec [G][3][nseg][M+1] (positions pos) into the group tiles
+// in P^T's layout.  fft3_rhs_batch: tiles small enough that a batch stays in
+// L2 between its column and row passes.
 long long fft3_rhs_batch(int logm);
 // y [ntiles][2M] <- c2r(h_d r2c(x)) per tile (detector d = tile / nseg,
 // hpos [ndet][M+1] the filter rows in position order; x == y allowed), in
-// batches through scratch [fft3_rhs_batch(logm)][2M]
+// batches of `batch` tiles through scratch [batch][2M]
 cudaError_t fft3_detector_filter(const float* x, float* y, float* scratch, const float* hpos,
-                                 long long ntiles, int nseg, int logm, const cplx<float>* tw_lo,
-                                 const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st);
+                                 long long ntiles, long long batch, int nseg, int logm,
+                                 const cplx<float>* tw_lo, const cplx<float>* tw_hi,
+                                 cplx<float> wn1, cudaStream_t st);
 cudaError_t fft3_forward_spectra(const float* tod, float* scratch, cplx<float>* spec,
-                                 long long ntiles, int logm, const cplx<float>* tw_lo,
-                                 const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st);
+                                 long long ntiles, long long batch, int logm,
+                                 const cplx<float>* tw_lo, const cplx<float>* tw_hi,
+                                 cplx<float> wn1, cudaStream_t st);
 cudaError_t fft3_inverse_from_spectra(const cplx<float>* gspec, float* data, long long ngroups,
                                       int nseg, int logm, const cplx<float>* tw_lo,
                                       const cplx<float>* tw_hi, cplx<float> wn1, cudaStream_t st);
