@@ -777,7 +777,7 @@ cudaError_t f3_fwd1(const float* tod, float* scratch, cplx<float>* spec, long lo
   using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
   using RG = f3::RowSpecGeo<LOGR, LOGC, kRP1>;
   auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
-  auto kr = f3::k_f3_rowspec<LOGR, LOGC, kRP1, 1>;
+  auto kr = f3::k_f3_rowspec<LOGR, LOGC, kRP1, 4>;  // four CTAs per SM: 29.5 -> 28.4 us per 96 tiles
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
   if (e == cudaSuccess) e = set_smem(kr, smr);
