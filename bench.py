@@ -531,7 +531,8 @@ def c3_block(sg, stream, args):
                             2: "coarse space"}[learn["kind"]],
            "validation": {"plain_iterations": learn["val_plain_iters"],
                           "coarse_iterations": learn["val_coarse_iters"],
-                          "plain_ms": learn["val_plain_ms"], "coarse_ms": learn["val_coarse_ms"]}}
+                          "plain_ms": learn["val_plain_ms"], "coarse_ms": learn["val_coarse_ms"]},
+           "coarse_vectors": learn.get("coarse_k")}
     sols = {}
     for pc in ("bj3", "learned"):
         for _ in range(2):

@@ -226,7 +226,8 @@ typedef struct sg_learn_opts {
   int force;         /* 2: use the coarse space, other nonzero: the network, even
                         if validation shows no gain */
   int coarse_k;      /* coarse-space vectors, at most 32 (0: 24, and the validation also
-                        tries the first 16 and keeps the faster; < 0: no coarse space) */
+                        tries the first 16 and 8 and keeps the fastest; < 0: no coarse
+                        space) */
   int coarse_vectors; /* stored residuals the coarse space is built from (0: 256) */
 } sg_learn_opts;
 

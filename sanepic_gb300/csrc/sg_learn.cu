@@ -894,16 +894,27 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (e == cudaSuccess && c->coarse_k > 0) {
     c->set_learned_kind(2);
     e = val_solve(c, 2, vcrit, vc);
-    if (e == cudaSuccess && coarse_auto && c->coarse_k > 16) {
+    // the automatic size also tries the first 16 and 8 Ritz vectors and keeps
+    // the fastest: smaller spaces cost less per iteration (at NSIDE 512 each
+    // basis vector set is read three times an iteration), larger ones save
+    // iterations
+    if (e == cudaSuccess && coarse_auto && c->coarse_k > 8) {
       const int k_full = c->coarse_k;
-      ValSolve v16;
-      rc = coarse_combine(c, cbasis, 16);
-      if (rc) return rc;
-      if (c->coarse_k > 0) e = val_solve(c, 2, vcrit, v16);
-      if (e == cudaSuccess && v16.converged && (!vc.converged || v16.ms < vc.ms)) {
-        vc = v16;  // keep the smaller space
-      } else if (e == cudaSuccess) {
-        rc = coarse_combine(c, cbasis, k_full);
+      int k_best = k_full;
+      for (const int kk : {16, 8}) {
+        if (kk >= k_full) continue;
+        ValSolve vk;
+        rc = coarse_combine(c, cbasis, kk);
+        if (rc) return rc;
+        if (c->coarse_k > 0) e = val_solve(c, 2, vcrit, vk);
+        if (e != cudaSuccess) break;
+        if (c->coarse_k > 0 && vk.converged && (!vc.converged || vk.ms < vc.ms)) {
+          vc = vk;
+          k_best = kk;
+        }
+      }
+      if (e == cudaSuccess && c->coarse_k != k_best) {
+        rc = coarse_combine(c, cbasis, k_best);
         if (rc) return rc;
       }
     }
