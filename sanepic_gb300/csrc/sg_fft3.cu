@@ -392,7 +392,7 @@ __device__ __forceinline__ void rows_inverse(cf* s, const cf* twB, int tid, St s
 // MIX 0: one spectrum h per group, hrow[g][pos].  pos = C k1 + k2 for
 // k = k1 + R k2 < M, pos = M for k = M.  Grid: groups x ceil(nseg / RSEG) x
 // (R/2) / RP.
-template <int LOGR, int LOGC, int RP, int MIX>
+template <int LOGR, int LOGC, int RP, int MIX, bool HSTAGE = true>
 struct RowGeo {
   static constexpr int R = 1 << LOGR, C = 1 << LOGC, M = R * C;
   using S = Split<LOGC>;
@@ -400,16 +400,18 @@ struct RowGeo {
   static constexpr int NSEQ = 6 * RP;
   static constexpr int NT = NSEQ * C1;
   static constexpr int HW = MIX ? 6 : 1;  // weights per frequency
-  // shared: sequences, W_C twice, split table (complex) + weights (floats, padded to 8 B)
-  static constexpr int SMEM = NSEQ * QS + 3 * C + 2 * RP + (2 * RP * C * HW + HW + 1) / 2;
+  // shared: sequences, W_C twice, split tables (complex) + with HSTAGE the
+  // rows' weights (floats, padded to 8 B)
+  static constexpr int SMEM =
+      NSEQ * QS + 3 * C + 2 * RP + (HSTAGE ? (2 * RP * C * HW + HW + 1) / 2 : 0);
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
-template <int LOGR, int LOGC, int RP, int MIX, int RSEG, int MINB = 1>
-__global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
+template <int LOGR, int LOGC, int RP, int MIX, int RSEG, int MINB = 1, bool HSTAGE = true>
+__global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX, HSTAGE>::NT, MINB)
     k_f3_rows(float* __restrict__ data, const float* __restrict__ hrow, int nseg,
               const cf* __restrict__ tw_lo, const cf* __restrict__ tw_hi, cf wn1) {
-  using G = RowGeo<LOGR, LOGC, RP, MIX>;
+  using G = RowGeo<LOGR, LOGC, RP, MIX, HSTAGE>;
   using S = typename G::S;
   constexpr int R = G::R, C = G::C, M = G::M, QS = S::QS, NT = G::NT, HW = G::HW;
   constexpr int NSEQ = G::NSEQ;
@@ -430,11 +432,13 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
   const float* H = hrow + grp * (long long)(M + 1) * HW;
   row_tables<LOGR, LOGC>(twA, twB, wsp, tw_lo, tw_hi, tid, NT);
   row_w1_table(w1s, 2 * RP, p0, R, tw_lo, tw_hi, wn1, tid, NT);
-  for (int i = tid; i < 2 * RP * C * HW; i += NT) {
-    const int row = i / (C * HW), e = i % (C * HW);
-    hs[i] = __ldg(H + (long long)C * HW * row_k1(R, p0 + (row >> 1), row & 1) + e);
+  if constexpr (HSTAGE) {
+    for (int i = tid; i < 2 * RP * C * HW; i += NT) {
+      const int row = i / (C * HW), e = i % (C * HW);
+      hs[i] = __ldg(H + (long long)C * HW * row_k1(R, p0 + (row >> 1), row & 1) + e);
+    }
+    if (tid < HW) hs[2 * RP * C * HW + tid] = __ldg(H + (long long)M * HW + tid);
   }
-  if (tid < HW) hs[2 * RP * C * HW + tid] = __ldg(H + (long long)M * HW + tid);
   const int s_end = min(nseg, (sb + 1) * RSEG);
   auto elem = [&](int rr, int n) {
     const int row = rr / 3;
@@ -454,10 +458,28 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX>::NT, MINB)
       if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
       cf* qa = s + ((2 * pp + rowA) * 3) * QS + S::pad(colA);
       cf* qb = s + ((2 * pp + rowB) * 3) * QS + S::pad(colB);
-      const float* ha = hs + ((2 * pp + rowA) * C + colA) * HW;
-      const float* hb = hs + ((2 * pp + rowB) * C + colB) * HW;
+      // the weights: staged rows, or straight from L2 (read-only path)
+      float hva[HW], hvb[HW];
+      if constexpr (HSTAGE) {
+        const float* sb = special ? hs + 2 * RP * C * HW : hs + ((2 * pp + rowB) * C + colB) * HW;
+#pragma unroll
+        for (int i = 0; i < HW; i++) {
+          hva[i] = hs[((2 * pp + rowA) * C + colA) * HW + i];
+          hvb[i] = sb[i];
+        }
+      } else {
+        const long long pa = (long long)C * row_k1(R, p, rowA) + colA;
+        const long long pb = special ? M : (long long)C * row_k1(R, p, rowB) + colB;
+#pragma unroll
+        for (int i = 0; i < HW; i++) {
+          hva[i] = __ldg(H + pa * HW + i);
+          hvb[i] = __ldg(H + pb * HW + i);
+        }
+      }
+      const float* ha = hva;
+      const float* hb = hvb;
       if (special) {
-        const float* hm = hs + 2 * RP * C * HW;
+        const float* hm = hvb;  // bin M
         float x0[3], xm[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -740,20 +762,24 @@ __global__ void __launch_bounds__(RowInGeo<LOGR, LOGC, RP>::NT, MINB)
 // application of 48 tiles on a GB300).  Single timelines (the right-hand
 // side's detectors): 16 columns per column CTA, 8 row pairs per row CTA.
 namespace {
-constexpr int kCB = 8, kRP = 2, kRSEG = 3, kCB1 = 16, kRP1 = 8;
+constexpr int kCB = 8, kRP = 2, kCB1 = 16, kRP1 = 8;
 
 template <class K>
 cudaError_t set_smem(K k, int bytes) {
   return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-template <int LOGR, int LOGC, int MIX, int MBC, int MBR>
+// The weighting pass reads H straight from L2 (staging a CTA's rows of H in
+// shared memory for three segments had been slower: 56 -> 47.7 us for the
+// 3 x 3 mixing at 48 x 131072 samples, 47.3 -> 43.6 us for one spectrum, with
+// more CTAs per SM in the freed shared memory).  RPR row pairs per CTA.
+template <int LOGR, int LOGC, int MIX, int MBC, int RPR, int MBR>
 cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
                    const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1, cudaStream_t st) {
   using CG = f3::ColGeo<LOGR, LOGC, kCB, 3>;
-  using RG = f3::RowGeo<LOGR, LOGC, kRP, MIX>;
+  using RG = f3::RowGeo<LOGR, LOGC, RPR, MIX, false>;
   auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB, 3, MBC>;
-  auto kr = f3::k_f3_rows<LOGR, LOGC, kRP, MIX, kRSEG, MBR>;
+  auto kr = f3::k_f3_rows<LOGR, LOGC, RPR, MIX, 1, MBR, false>;
   auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB, 3, MBC>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
@@ -762,12 +788,25 @@ cudaError_t f3_run(float* data, const float* hrow, long long ngroups, int nseg,
   if (e != cudaSuccess) return e;
   const long long ntiles = ngroups * nseg;
   const long long gc = ntiles * (CG::C / kCB);
-  const long long gr = ngroups * ((nseg + kRSEG - 1) / kRSEG) * (RG::R / 2 / kRP);
+  const long long gr = ntiles * (RG::R / 2 / RPR);
   if (gc > 0x7fffffffLL || gr > 0x7fffffffLL) return cudaErrorInvalidValue;
   kc<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   kr<<<(unsigned)gr, RG::NT, smr, st>>>(data, hrow, nseg, lo, hi, wn1);
   ki<<<(unsigned)gc, CG::NT, smc, st>>>(data, data, lo, hi);
   return cudaGetLastError();
+}
+
+// row pass shape per MIX: (row pairs per CTA, register cap); the 3 x 3
+// mixing at 2^15..2^16 points runs one row pair per CTA
+template <int LOGR, int LOGC, int MBC, int MBR>
+cudaError_t f3_run_mix(int mix, float* data, const float* hrow, long long ngroups, int nseg,
+                       const cplx<float>* lo, const cplx<float>* hi, cplx<float> wn1,
+                       cudaStream_t st) {
+  constexpr bool big = LOGR + LOGC >= 15;
+  if (mix)
+    return f3_run<LOGR, LOGC, 1, MBC, big ? 1 : 2, big ? 2 * MBR : MBR>(data, hrow, ngroups, nseg,
+                                                                       lo, hi, wn1, st);
+  return f3_run<LOGR, LOGC, 0, MBC, 2, MBR + 1>(data, hrow, ngroups, nseg, lo, hi, wn1, st);
 }
 
 template <int LOGR, int LOGC>
@@ -864,10 +903,9 @@ cudaError_t fft3_group_weight(float* data, const float* hrow, int mix, long long
                               int logm, const cplx<float>* tw_lo, const cplx<float>* tw_hi,
                               cplx<float> wn1, cudaStream_t st) {
   if (!fft3_supported(logm) || ngroups < 1 || nseg < 1) return cudaErrorInvalidValue;
-#define SG_F3_CASE(LM, LR, LC, MBC, MBR)                                                     \
-  case LM:                                                                                  \
-    return mix ? f3_run<LR, LC, 1, MBC, MBR>(data, hrow, ngroups, nseg, tw_lo, tw_hi, wn1, st) \
-               : f3_run<LR, LC, 0, MBC, MBR>(data, hrow, ngroups, nseg, tw_lo, tw_hi, wn1, st);
+#define SG_F3_CASE(LM, LR, LC, MBC, MBR) \
+  case LM:                              \
+    return f3_run_mix<LR, LC, MBC, MBR>(mix, data, hrow, ngroups, nseg, tw_lo, tw_hi, wn1, st);
   switch (logm) { SG_F3_SHAPES(SG_F3_CASE) }
 #undef SG_F3_CASE
   return cudaErrorInvalidValue;
