@@ -558,7 +558,7 @@ struct Row1Geo {
   static_assert((R / 2) % RP == 0, "row pairs per CTA divide R/2");
 };
 
-template <int LOGR, int LOGC, int RP, int RSEG, int MINB = 1>
+template <int LOGR, int LOGC, int RP, int RSEG, int MINB = 1, bool HSTAGE = true>
 __global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
     k_f3_rows1(float* __restrict__ data, long long ntiles, long long tile0, int nseg,
                const float* __restrict__ hpos, const cf* __restrict__ tw_lo,
@@ -587,7 +587,8 @@ __global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
     auto elem = [&](int rr, int n) {
       return (long long)C * row_k1(R, p0 + (rr >> 1), rr & 1) + n;
     };
-    if (det != det_staged) {  // the detector's filter values at this CTA's rows
+    const float* hdet = hpos + det * (long long)(M + 1);
+    if (HSTAGE && det != det_staged) {  // the detector's filter values at this CTA's rows
       __syncthreads();  // the previous tile's last reads of hs
       const float* h = hpos + det * (long long)(M + 1);
       for (int i = tid; i < 2 * RP * C; i += NT)
@@ -604,10 +605,17 @@ __global__ void __launch_bounds__(Row1Geo<LOGR, LOGC, RP>::NT, MINB)
       if (!pair_of(C, p, tau, rowA, colA, rowB, colB, special)) continue;
       cf* qa = s + (2 * pp + rowA) * QS + S::pad(colA);
       cf* qb = s + (2 * pp + rowB) * QS + S::pad(colB);
-      const float ha = hs[(2 * pp + rowA) * C + colA], hb = hs[(2 * pp + rowB) * C + colB];
+      float ha, hb;
+      if constexpr (HSTAGE) {
+        ha = hs[(2 * pp + rowA) * C + colA];
+        hb = special ? hs[2 * RP * C] : hs[(2 * pp + rowB) * C + colB];
+      } else {  // straight from L2
+        ha = __ldg(hdet + (long long)C * row_k1(R, p, rowA) + colA);
+        hb = __ldg(hdet + (special ? (long long)M : (long long)C * row_k1(R, p, rowB) + colB));
+      }
       if (special) {
         const cf z = *qa;
-        const float y0 = ha * (z.x + z.y), yM = hs[2 * RP * C] * (z.x - z.y);
+        const float y0 = ha * (z.x + z.y), yM = hb * (z.x - z.y);
         *qa = cf{y0 + yM, y0 - yM};
         continue;
       }
@@ -856,11 +864,14 @@ template <int LOGR, int LOGC>
 cudaError_t f3_det(const float* x, float* y, float* scratch, const float* hpos, long long ntiles,
                    int nseg, long long batch, const cplx<float>* lo, const cplx<float>* hi,
                    cplx<float> wn1, cudaStream_t st) {
-  constexpr int RS1 = 4;  // tiles per row CTA (consecutive segments share the filter row)
+  // four tiles per row CTA (consecutive segments of one detector share the
+  // filter row, staged once; one tile per CTA with the filter values read
+  // from L2 measured the same, 2.57 against 2.64 ms at C2)
+  constexpr int RS1 = 4;
   using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
   using RG = f3::Row1Geo<LOGR, LOGC, kRP1>;
   auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
-  auto kr = f3::k_f3_rows1<LOGR, LOGC, kRP1, RS1, 3>;
+  auto kr = f3::k_f3_rows1<LOGR, LOGC, kRP1, RS1, 3, true>;
   auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB1, 1, 1>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
