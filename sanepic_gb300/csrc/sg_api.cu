@@ -963,15 +963,20 @@ extern "C" int sg_get_map(sg_ctx* c, int kind, double* out) {
     case SG_MAP_I:
     case SG_MAP_Q:
     case SG_MAP_U: {
-      // only the requested component, through page-locked memory
+      // only the requested component, expanded to the full-sky RING map on
+      // the device (the int -> RING table kept from sg_set_pointing) and
+      // copied out once
       if (!c->have_solution) return c->fail(SG_ERR_STATE, "no solution yet");
-      e = c->map_stage.reserve(sizeof(double) * npix);
+      const size_t fb = sizeof(double) * c->npixfull;
+      e = c->map_full.alloc(fb);
+      if (e == cudaSuccess) e = cudaMemsetAsync(c->map_full.p, 0, fb, c->st);
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(c->map_stage.p, c->x.as<double>() + (kind - SG_MAP_I) * npix,
-                            sizeof(double) * npix, cudaMemcpyDeviceToHost, c->st);
+        e = expand_launch(c->x.as<double>() + (kind - SG_MAP_I) * npix,
+                          c->pscr.i2r.as<long long>(), npix, c->map_full.as<double>(), c->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(out, c->map_full.p, fb, cudaMemcpyDeviceToHost, c->st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-      blk = static_cast<const double*>(c->map_stage.p);
-      break;
+      if (e != cudaSuccess) return c->cuda_fail(e, "get_map");
+      return SG_OK;
     }
     case SG_MAP_NVAR:
     case SG_MAP_Q_NVAR:

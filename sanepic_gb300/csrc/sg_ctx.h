@@ -55,27 +55,6 @@ struct DevBuf {
   }
 };
 
-// page-locked host memory for device->host reads of results (grown on demand)
-struct HostStage {
-  void* p = nullptr;
-  size_t bytes = 0;
-  HostStage() = default;
-  HostStage(const HostStage&) = delete;
-  HostStage& operator=(const HostStage&) = delete;
-  ~HostStage() {
-    if (p) cudaFreeHost(p);
-  }
-  cudaError_t reserve(size_t n) {
-    if (p && bytes >= n) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    const cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocDefault);
-    if (e == cudaSuccess) bytes = n;
-    return e;
-  }
-};
-
 inline double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
       .count();
@@ -97,7 +76,6 @@ struct sg_ctx {
   long long npix = 0;
   std::vector<int> indpix_host;        // RING pixel -> RING-order compact index (reference)
   std::vector<long long> int2ring;     // internal index -> RING pixel
-  HostStage map_stage;                 // one map component on its way to the caller
   std::vector<long long> int2ringc;    // internal index -> RING-order compact index
   std::vector<long long> isampmin;
 
@@ -128,6 +106,7 @@ struct sg_ctx {
   int kslot_S = -1;         // the tile shape kslot was made for
   int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
   DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
+  DevBuf map_full;        // a full-sky RING map being read out
   // sg_set_pointing's device scratch (boresight, pixels, numbering and sort
   // temporaries), kept between calls
   struct PointingScratch {

@@ -75,6 +75,9 @@ cudaError_t hist_launch(const int* ring_pix, long long n, long long nsd, const i
 cudaError_t compact_launch(const int* ring_pix, const int* indpix, long long n, int* pix,
                            cudaStream_t st);
 // hits_true[m] = count[ring(m)] via indpix
+// full[i2r[m]] = compact[m] for the npix observed pixels (full zeroed before)
+cudaError_t expand_launch(const double* compact, const long long* i2r, long long npix,
+                          double* full, cudaStream_t st);
 cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull,
                         int* hits_true, cudaStream_t st);
 // pixel numbering from the per-RING-pixel sample counts [n = 12 nside^2]:

@@ -63,6 +63,21 @@ cudaError_t hits_launch(const int* count, const int* indpix, long long npixfull,
   return cudaGetLastError();
 }
 
+// full[int2ring[m]] = compact[m]: a compact map into the full-sky RING map
+// (the caller zeroes full first; unobserved pixels stay 0)
+__global__ void k_expand(const double* __restrict__ compact, const long long* __restrict__ i2r,
+                         long long npix, double* __restrict__ full) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < npix;
+       m += (long long)gridDim.x * blockDim.x)
+    full[i2r[m]] = compact[m];
+}
+
+cudaError_t expand_launch(const double* compact, const long long* i2r, long long npix,
+                          double* full, cudaStream_t st) {
+  k_expand<<<grid_for(npix, 256), 256, 0, st>>>(compact, i2r, npix, full);
+  return cudaGetLastError();
+}
+
 // ---- pixel numbering -------------------------------------------------------
 // The reference's indpix (rank of each observed pixel in ascending RING order,
 // sanepic.cc:904-915) and the library's internal numbering (rank in NESTED
