@@ -22,13 +22,21 @@
 // A frequency k = k1 + R k2 (k1 > 0) has its real-FFT partner M - k =
 // (R - k1) + R (C - 1 - k2), so pass 2 takes the rows k1 and R - k1 of all
 // three components together (rows 0 and R/2 pair with themselves and share
-// one CTA).  Between the passes the tile goes through L2 (74 MB for 48
-// segments of 131,072 samples, which stays resident in the 129 MB L2); each
-// pass reads and writes it once, with 16-byte accesses to contiguous 96-byte
-// blocks.
+// one CTA).  Between the passes the tiles go through L2 (75 MB for 48
+// segments of 131,072 samples: with L2 warm the three passes read 54 MB from
+// DRAM); each pass reads and writes every tile once.
 //
 // Every sub-DFT of length R or C is two in-register radix passes (R = R1 R2,
-// sizes <= 16) through shared memory, one unit (one small DFT) per thread.
+// sizes <= 16) with one exchange through shared memory, one unit (one small
+// DFT) per thread; the first radix pass's units load straight from the tile
+// and the last pass's units store straight to it, the lanes of a warp over
+// columns (or row positions), so that every global access is a run of whole
+// 32-byte sectors.
+//
+// The same passes serve single timelines (NC = 1): the right-hand side's
+// per-detector half spectra (column pass + a forward row pass that stores
+// the r2c values) and the per-detector operator's filter, both in batches of
+// tiles through an L2-sized scratch.
 // Conventions are FFTW's unnormalised r2c (sign -1) and c2r (sign +1), as in
 // the reference's noise weighting (sanepic.cc:2390-2445, 2522-2582): the
 // output is c2r(H r2c(x)) per group and segment, the same linear map as the
