@@ -394,8 +394,9 @@ __device__ __forceinline__ void rows_inverse(cf* s, const cf* twB, int tid, St s
 }
 
 // The weighting pass: RP row pairs of RSEG consecutive segments of one group
-// per CTA, three components (sequence rr = (2 pp + side) 3 + c).  The weights
-// of its rows are staged in shared memory once and serve all RSEG segments.
+// per CTA, three components (sequence rr = (2 pp + side) 3 + c).  With HSTAGE
+// the weights of its rows are staged in shared memory once and serve all RSEG
+// segments; otherwise each frequency pair reads its weights from L2.
 // MIX 1: the group's 3 x 3 H, hrow[g][pos][6] (H00 H01 H02 H11 H12 H22);
 // MIX 0: one spectrum h per group, hrow[g][pos].  pos = C k1 + k2 for
 // k = k1 + R k2 < M, pos = M for k = M.  Grid: groups x ceil(nseg / RSEG) x
@@ -469,11 +470,12 @@ __global__ void __launch_bounds__(RowGeo<LOGR, LOGC, RP, MIX, HSTAGE>::NT, MINB)
       // the weights: staged rows, or straight from L2 (read-only path)
       float hva[HW], hvb[HW];
       if constexpr (HSTAGE) {
-        const float* sb = special ? hs + 2 * RP * C * HW : hs + ((2 * pp + rowB) * C + colB) * HW;
+        const float* hsb =
+            special ? hs + 2 * RP * C * HW : hs + ((2 * pp + rowB) * C + colB) * HW;
 #pragma unroll
         for (int i = 0; i < HW; i++) {
           hva[i] = hs[((2 * pp + rowA) * C + colA) * HW + i];
-          hvb[i] = sb[i];
+          hvb[i] = hsb[i];
         }
       } else {
         const long long pa = (long long)C * row_k1(R, p, rowA) + colA;
