@@ -238,9 +238,10 @@ typedef struct sg_learn_report {
   float loss_first, loss_last;  /* batch MSE (normalised units) at the first / last step */
   double gen_seconds, train_seconds;
   double gemm_tflop;            /* tensor-core work of the training, TFLOP */
-  /* validation on a held-out synthetic sky and noise realisation */
+  /* validation on two held-out synthetic skies and noise realisations:
+   * iterations and CUDA-event time of a solve, the mean of the two */
   int val_plain_iters, val_learned_iters;
-  double val_plain_ms, val_learned_ms;  /* CUDA-event time of each solve */
+  double val_plain_ms, val_learned_ms;
   int enabled;  /* 1: SG_PRECOND_LEARNED uses a learned part; 0: it runs plain
                    block-Jacobi PCG because neither part beat it */
   int coarse_k, coarse_vectors;  /* coarse-space vectors kept, residuals used */
@@ -259,7 +260,7 @@ typedef struct sg_learn_report {
  * forward/backward kernels: each step maximises the A-cosine
  * (r^T z)^2 / ((z^T A z)(r^T M_bj3 r)) of the corrected direction z for one
  * stored residual, differentiated through one application of A.  Plain PCG
- * then judges both on a held-out problem (report->kind, report->enabled).
+ * then judges both on two held-out problems (report->kind, report->enabled).
  * The coarse space belongs to this operator: a context with other pointing
  * or noise must be trained again.  `batch` is unused (one residual's patches
  * per step).  Overwrites b and the solution: call sg_rhs again before
