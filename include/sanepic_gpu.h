@@ -175,6 +175,11 @@ int sg_group_mode(const sg_ctx *ctx, long *ngroups);
  * counterpart. */
 int sg_weighting(const sg_ctx *ctx);
 
+/* Kernels this context has launched so far (a CUDA graph's kernel nodes
+ * counted one by one), for callers that account for device work; -1 for a
+ * null context.  No reference counterpart. */
+long sg_kernel_launches(const sg_ctx *ctx);
+
 /* y = P^T N^-1 P x for a compact host vector [3*npix] (one operator pass,
  * sanepic.cc:1428-1448); masked != 0 applies the pol degeneracy mask
  * (sanepic.cc:1455-1459). */

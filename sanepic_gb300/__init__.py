@@ -35,7 +35,7 @@ MAPS = {"I": 0, "Q": 1, "U": 2, "NVAR": 3, "Q_NVAR": 4, "U_NVAR": 5, "HITS": 6,
 
 # every symbol include/sanepic_gpu.h declares
 EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_set_tod", "sg_rhs", "sg_npix",
-           "sg_group_mode", "sg_weighting",
+           "sg_group_mode", "sg_weighting", "sg_kernel_launches",
            "sg_apply", "sg_noise_filter", "sg_noise_filter_noalloc", "sg_solve", "sg_get_map", "sg_get_solution",
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
@@ -132,6 +132,8 @@ def load_library(path: Optional[str] = None):
     L.sg_group_mode.restype = ctypes.c_int
     L.sg_weighting.argtypes = [c_p]
     L.sg_weighting.restype = ctypes.c_int
+    L.sg_kernel_launches.argtypes = [c_p]
+    L.sg_kernel_launches.restype = ctypes.c_long
     L.sg_apply.argtypes = [c_p, dp, dp, ctypes.c_int]
     L.sg_noise_filter.argtypes = [c_p, dp, dp]
     L.sg_noise_filter_noalloc.argtypes = [c_p, c_p, c_p, ctypes.c_long, ctypes.c_long,
@@ -318,6 +320,10 @@ class MapMaker:
         n = ctypes.c_long(0)
         on = bool(self.L.sg_group_mode(self.h, ctypes.byref(n)))
         return on, int(n.value)
+
+    def kernel_launches(self) -> int:
+        """Kernels this context has launched so far (graph nodes one by one)."""
+        return int(self.L.sg_kernel_launches(self.h))
 
     def weighting(self) -> str:
         """How the operator applies N^-1: "per-detector" (one fused cluster

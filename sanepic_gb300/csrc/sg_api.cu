@@ -130,6 +130,8 @@ extern "C" const char* sg_last_error(const sg_ctx* c) {
 
 extern "C" long sg_npix(const sg_ctx* c) { return c ? (long)c->npix : -1; }
 
+extern "C" long sg_kernel_launches(const sg_ctx* c) { return c ? (long)c->launches : -1; }
+
 extern "C" int sg_weighting(const sg_ctx* c) {
   if (!c) return SG_ERR_ARG;
   return (c->group_mode ? 1 : 0) | (c->use_f3 ? 2 : 0);

@@ -481,8 +481,9 @@ struct sg_ctx {
     const long long nsd = ns * nseg, M1 = ns / 2 + 1, gt = 3LL * ngroups * nseg;
     if (!chi2_dev && groups_uniform && use_f3) {
       // the detectors' timelines summed per group into P^T's layout, weighted
-      // there by the group's one spectrum in place
-      launches += 4;
+      // there by the group's one spectrum in place (the passes and P^T count
+      // their own launches)
+      launches += 1;
       cudaError_t e = group_tod_rhs_launch<float>((const float*)d, nsd, grp_off.as<int>(),
                                                   grp_det.as<int>(), dcs.as<float>(), ngroups,
                                                   ys.as<float>(), 1, st);
@@ -519,7 +520,9 @@ struct sg_ctx {
       // stay in L2), the group sums (and chi^2) in position order, the
       // inverse into P^T's layout
       const long long nbatches = (ntiles + f3_batch - 1) / f3_batch;
-      launches += 2 * nbatches + 2 + (chi2_dev ? 1 : 0) + 2;
+      // the batches' column and row passes, the group sums (and the chi^2
+      // sum), the inverse row and column passes; P^T counts itself
+      launches += 2 * nbatches + 1 + (chi2_dev ? 1 : 0) + 2;
       cudaError_t e = fft3_forward_spectra((const float*)d, f3scratch.as<float>(),
                                            dspec.as<cplx<float>>(), ntiles, f3_batch, logm,
                                            tw_lo.as<cplx<float>>(), tw_hi.as<cplx<float>>(), wn1f,
