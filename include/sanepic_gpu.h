@@ -110,6 +110,8 @@ typedef struct sg_report {
                              r^T M r <= 0 (bit 1) -- the residual reached rounding level */
   int fallback_iter;      /* SG_PRECOND_LEARNED: iteration at which the solve fell back
                              to plain block-Jacobi PCG, or -1 */
+  double crit0;           /* sg_solve: |r0|^2/|b|^2 of the start map, the reference's
+                             var0/var00 (sanepic.cc:1362-1384); sg_solve_batch: 0 */
 } sg_report;
 
 /* Creates a context on desc->device.  Replaces the parameter handling of
@@ -156,6 +158,36 @@ int sg_set_tod(sg_ctx *ctx, long det, const double *tod, long nsamp_total);
  * their timelines before the FFTs (three FFT pairs per group and segment
  * instead of one FFT per detector; the same b up to rounding). */
 int sg_rhs(sg_ctx *ctx, double *chi2);
+
+/* Detector gains of the recalibration loop (-r / -R, sanepic.cc:1041-1130,
+ * 2123-2316): one gain per (detector, segment) tile, gains[idet + iseg *
+ * ndet] (the layout of the reference's relCalib and of its relCalib.dat<n>
+ * files), every gain finite and > 0; NULL restores 1.  The operator then
+ * solves P^T G N^-1 G P m = P^T G N^-1 d with G = diag(g) tile by tile (the
+ * reference's calibrated data d/g with its noise weights times g^2,
+ * sanepic.cc:1044-1053, 2545).  While gains other than 1 are set the
+ * operator runs per detector (gains break the sums of an offset group).
+ * Invalidates b (call sg_rhs again) and any learned part; the current map
+ * stays readable and the preconditioners are kept, as the reference keeps
+ * those of its first loop (sanepic.cc:1352). */
+int sg_set_gains(sg_ctx *ctx, const double *gains);
+
+/* Gain fit with the current map m held fixed (after sg_solve), the
+ * reference's relCalib = sPNd / cPNPc (sanepic.cc:2166-2226) as the
+ * weighted least-squares gain of d = g P m + n per tile:
+ *   g = (P m)^T N^-1 d / (P m)^T N^-1 (P m),
+ * per_detector != 0 (-R): one gain per detector from the sums over its
+ * segments (sanepic.cc:2254-2271).  The new gains are scaled so that their
+ * mean equals the mean of the gains m was made with (the common factor the
+ * map absorbs; the reference's absrecal, sanepic.cc:2281-2291).  gains_out
+ * [nseg * ndet] as sg_set_gains takes them (not applied: pass them to
+ * sg_set_gains); chi2_before / chi2_after (may be NULL): the reference's
+ * chi^2 of d - g P m with the old and the new gains (sanepic.cc:3206-3260).
+ * Differences from the reference (whose -r diverges): its fits carry a
+ * factor 4 (sPNd x 2, cPNPc x 1/2), its absrecal reads arrays only -R fills,
+ * and the orbital dipole (-o) is taken as zero here. */
+int sg_fit_gains(sg_ctx *ctx, int per_detector, double *gains_out, double *chi2_before,
+                 double *chi2_after);
 
 /* Number of observed pixels (npix, sanepic.cc:915). */
 long sg_npix(const sg_ctx *ctx);

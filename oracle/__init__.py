@@ -38,6 +38,7 @@ def lib():
         _LIB.orc_ang2pix_ring.restype = ctypes.c_long
         _LIB.orc_indpix.restype = ctypes.c_long
         _LIB.orc_rhs.restype = ctypes.c_double
+        _LIB.orc_gain_chi2.restype = ctypes.c_double
         _LIB.orc_pcg.restype = ctypes.c_int
         _LIB.orc_expand_detector.restype = ctypes.c_int
         _LIB.cp_run.restype = ctypes.c_int
@@ -172,6 +173,104 @@ class Setup:
                            ctypes.c_double(stop_crit), ctypes.c_int(maxiter),
                            ctypes.c_int(int(verbose)), _pd(x), _pd(hist))
         return x, it, hist[:it]
+
+    # ---- recalibration: per-tile gains (sanepic.cc:1041-1130, 2123-2316) --
+    # A tile (det, seg) is its own one-segment "detector": the [det][seg]
+    # sample layout is already [tile][sample], so the operator with gains is
+    # orc_apply / orc_rhs / orc_pcg over ndet * nseg one-segment detectors,
+    # each with its detector's weights times g^2 (A) or g (b = P^T G N^-1 d).
+    def _tile_spn(self, scale):
+        """spn of every tile [det][seg] times scale[det][seg]."""
+        sc = np.asarray(scale, np.float64).reshape(self.ndet, self.nseg, 1)
+        return np.ascontiguousarray((self.spn.reshape(self.ndet, 1, self.ns) * sc).reshape(-1))
+
+    def _gains_ds(self, gains):
+        """gains in the reference's [seg][det] layout -> [det][seg]."""
+        return np.ascontiguousarray(np.asarray(gains, np.float64).reshape(self.nseg, self.ndet).T)
+
+    def apply_gains(self, x, gains):
+        g = self._gains_ds(gains)
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty(3 * self.npix)
+        lib().orc_apply(ctypes.c_long(self.ns), ctypes.c_long(1),
+                        ctypes.c_long(self.ndet * self.nseg), ctypes.c_long(self.npix),
+                        _pl(self.indpix), _pl(self.pix), _pd(self.psip),
+                        _pd(self._tile_spn(g * g)), _pd(x), _pd(y))
+        return y
+
+    def rhs_gains(self, tod, gains):
+        g = self._gains_ds(gains)
+        tod = np.ascontiguousarray(tod, np.float64).reshape(-1)
+        b = np.empty(3 * self.npix)
+        lib().orc_rhs(ctypes.c_long(self.ns), ctypes.c_long(1),
+                      ctypes.c_long(self.ndet * self.nseg), ctypes.c_long(self.npix),
+                      _pl(self.indpix), _pl(self.pix), _pd(self.psip), _pd(self._tile_spn(g)),
+                      _pd(tod), _pd(b))
+        return b
+
+    def pcg_gains(self, b, gains, precond="diag", x0=None, stop_crit=1e-15, maxiter=2000,
+                  Mp=None, minv=None):
+        """PCG on P^T G N^-1 G P with the preconditioner made without gains
+        (the reference keeps that of its first loop, sanepic.cc:1352)."""
+        g = self._gains_ds(gains)
+        n = 3 * self.npix
+        x = np.empty(n)
+        hist = np.zeros(maxiter + 1)
+        pc = {"diag": 0, "bj3": 1}[precond]
+        if pc == 0 and Mp is None:
+            Mp = self.diag_precond()
+        if pc == 1 and minv is None:
+            minv = self.block_jacobi()
+        Mp_arr = np.ascontiguousarray(Mp if Mp is not None else np.zeros(n))
+        minv_arr = np.ascontiguousarray(minv if minv is not None else np.zeros(9 * self.npix))
+        x0p = _pd(np.ascontiguousarray(x0, np.float64)) if x0 is not None else None
+        it = lib().orc_pcg(ctypes.c_long(self.ns), ctypes.c_long(1),
+                           ctypes.c_long(self.ndet * self.nseg), ctypes.c_long(self.npix),
+                           _pl(self.indpix), _pl(self.pix), _pd(self.psip),
+                           _pd(self._tile_spn(g * g)),
+                           _pd(np.ascontiguousarray(b, np.float64)), _pl(self.hits),
+                           _pd(Mp_arr), _pd(minv_arr), ctypes.c_int(pc), x0p,
+                           ctypes.c_double(stop_crit), ctypes.c_int(maxiter), ctypes.c_int(0),
+                           _pd(x), _pd(hist))
+        return x, it, hist[:it]
+
+    def gain_dots(self, x, tod):
+        """(b, c) per tile [det][seg]: 2 sum_k Re(D conj S) spn and
+        2 sum_k |S|^2 spn over the half spectrum, S = r2c(P x), D = r2c(d)."""
+        tod = np.ascontiguousarray(tod, np.float64).reshape(-1)
+        nt = self.ndet * self.nseg
+        dots = np.empty(2 * nt)
+        lib().orc_gain_dots(ctypes.c_long(self.ns), ctypes.c_long(self.nseg),
+                            ctypes.c_long(self.ndet), ctypes.c_long(self.npix),
+                            _pl(self.indpix), _pl(self.pix), _pd(self.psip), _pd(self.spn),
+                            _pd(tod), _pd(np.ascontiguousarray(x, np.float64)), _pd(dots))
+        return (dots[:nt].reshape(self.ndet, self.nseg), dots[nt:].reshape(self.ndet, self.nseg))
+
+    def gain_chi2(self, x, tod, gains=None):
+        tod = np.ascontiguousarray(tod, np.float64).reshape(-1)
+        gp = _pd(self._gains_ds(gains)) if gains is not None else None
+        return lib().orc_gain_chi2(ctypes.c_long(self.ns), ctypes.c_long(self.nseg),
+                                   ctypes.c_long(self.ndet), ctypes.c_long(self.npix),
+                                   _pl(self.indpix), _pl(self.pix), _pd(self.psip),
+                                   _pd(self.spn), _pd(tod),
+                                   _pd(np.ascontiguousarray(x, np.float64)), gp)
+
+    def fit_gains(self, x, tod, gains_old, per_detector=False):
+        """The recalibration fit with the map x fixed (sanepic.cc:2166-2291):
+        g = b / c per tile (per detector with -R: sums over its segments),
+        then scaled so that the mean gain equals that of gains_old.  Returns
+        (gains [nseg][ndet], chi2 before, chi2 after)."""
+        bd, cs = self.gain_dots(x, tod)
+        g0 = self._gains_ds(gains_old)
+        if per_detector:
+            zeta, gamma = bd.sum(axis=1, keepdims=True), cs.sum(axis=1, keepdims=True)
+            g = np.where(gamma > 0, zeta / np.where(gamma > 0, gamma, 1.0), g0)
+            g = np.broadcast_to(g, g0.shape).copy()
+        else:
+            g = np.where(cs > 0, bd / np.where(cs > 0, cs, 1.0), g0)
+        g *= g0.sum() / g.sum()
+        gr = np.ascontiguousarray(g.T)
+        return gr, self.gain_chi2(x, tod, gains_old), self.gain_chi2(x, tod, gr)
 
     def expand(self, compact):
         compact = np.ascontiguousarray(compact, np.float64)

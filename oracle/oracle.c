@@ -270,6 +270,68 @@ double orc_rhs(long ns, long nseg, long ndet, long npix, const long *indpix,
   return chi20;
 }
 
+/* The gain fit's sums with the map x held fixed, as the reference forms
+ * sPNd and cPNPc (sanepic.cc:2166-2226) but with one factor on both: for
+ * tile t = idet * nseg + iseg, s = P x on the tile (deproject,
+ * sanepic.cc:2173-2176), S = r2c(s), D = r2c(d) and
+ *   dots[t]          = 2 sum_{k <= ns/2} Re(D_k conj S_k) spn[k]
+ *   dots[ntiles + t] = 2 sum_{k <= ns/2} |S_k|^2 spn[k]
+ * (the reference's sPNd carries 2, its cPNPc 1/2: its ratio is 4x this). */
+void orc_gain_dots(long ns, long nseg, long ndet, long npix, const long *indpix,
+                   const long *pix, const double *psip, const double *spn,
+                   const double *tod, const double *x, double *dots) {
+  long nt = ndet * nseg, nk = ns / 2 + 1;
+  double *s = (double *)malloc(sizeof(double) * ns);
+  double *fs = (double *)malloc(sizeof(double) * 2 * nk);
+  double *fd = (double *)malloc(sizeof(double) * 2 * nk);
+  for (long idet = 0; idet < ndet; idet++)
+    for (long iseg = 0; iseg < nseg; iseg++) {
+      long off = ns * iseg + ns * nseg * idet, t = idet * nseg + iseg;
+      const double *sp = spn + ns * idet;
+      orc_deproject(x, indpix, pix + off, psip + off, ns, npix, s);
+      fft64_r2c(ns, s, fs);
+      fft64_r2c(ns, tod + off, fd);
+      double bd = 0.0, cs = 0.0;
+      for (long k = 0; k < nk; k++) {
+        bd += (fd[2 * k] * fs[2 * k] + fd[2 * k + 1] * fs[2 * k + 1]) * sp[k] * 2.0;
+        cs += (fs[2 * k] * fs[2 * k] + fs[2 * k + 1] * fs[2 * k + 1]) * sp[k] * 2.0;
+      }
+      dots[t] = bd;
+      dots[nt + t] = cs;
+    }
+  free(s);
+  free(fs);
+  free(fd);
+}
+
+/* chi^2 of d - g P x over every tile as MPI_compute_chi2 forms it
+ * (sanepic.cc:3206-3260, the orbital dipole zero): 2 sum_{k <= ns/2}
+ * |F(d - g s)_k|^2 spn[k]; gains per tile [idet][iseg], NULL for 1. */
+double orc_gain_chi2(long ns, long nseg, long ndet, long npix, const long *indpix,
+                     const long *pix, const double *psip, const double *spn,
+                     const double *tod, const double *x, const double *gains) {
+  long nk = ns / 2 + 1;
+  double *s = (double *)malloc(sizeof(double) * ns);
+  double *f = (double *)malloc(sizeof(double) * 2 * nk);
+  double chi2 = 0.0;
+  for (long iseg = 0; iseg < nseg; iseg++)
+    for (long idet = 0; idet < ndet; idet++) {
+      long off = ns * iseg + ns * nseg * idet;
+      double g = gains ? gains[idet * nseg + iseg] : 1.0;
+      orc_deproject(x, indpix, pix + off, psip + off, ns, npix, s);
+      for (long i = 0; i < ns; i++) s[i] = tod[off + i] - g * s[i];
+      fft64_r2c(ns, s, f);
+      const double *sp = spn + ns * idet;
+      for (long k = 0; k < nk; k++) {
+        double fr = f[2 * k] * sqrt(sp[k]), fi = f[2 * k + 1] * sqrt(sp[k]);
+        chi2 += (fr * fr + fi * fi) * 2.0;
+      }
+    }
+  free(s);
+  free(f);
+  return chi2;
+}
+
 /* sanepic.cc:2613-2626, run twice (sanepic.cc:1258-1266) */
 void orc_hits(long nsamp, long npix, const long *indpix, const long *pix,
               long *hits) {

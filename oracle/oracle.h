@@ -76,6 +76,21 @@ double orc_rhs(long ns, long nseg, long ndet, long npix, const long *indpix,
                const long *pix, const double *psip, const double *spn,
                const double *tod, double *b);
 
+/* Gain fit of the recalibration loop with the map x held fixed
+ * (sanepic.cc:2166-2226, one factor 2 on both sums where the reference has
+ * 2 on sPNd and 1/2 on cPNPc): per tile t = idet * nseg + iseg, s = P x,
+ * dots[t] = 2 sum_{k <= ns/2} Re(D_k conj S_k) spn[k] and
+ * dots[ndet * nseg + t] = 2 sum_{k <= ns/2} |S_k|^2 spn[k]. */
+void orc_gain_dots(long ns, long nseg, long ndet, long npix, const long *indpix,
+                   const long *pix, const double *psip, const double *spn,
+                   const double *tod, const double *x, double *dots);
+
+/* chi^2 of d - g P x (MPI_compute_chi2, sanepic.cc:3206-3260, no dipole);
+ * gains per tile [idet][iseg], NULL for 1. */
+double orc_gain_chi2(long ns, long nseg, long ndet, long npix, const long *indpix,
+                     const long *pix, const double *psip, const double *spn,
+                     const double *tod, const double *x, const double *gains);
+
 /* Hit counts as the reference accumulates them: do_PtNd runs twice with
  * hits != NULL (sanepic.cc:1258-1266), so every count is doubled.
  * hits has 2*npix entries (I then pol), sanepic.cc:2613-2626. */

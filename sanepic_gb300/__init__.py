@@ -40,7 +40,7 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
            "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
-           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes",
+           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes", "sg_set_gains", "sg_fit_gains",
            "sg_last_error", "sg_destroy"]
 
 
@@ -79,7 +79,7 @@ class SgReport(ctypes.Structure):
                 ("solve_seconds", ctypes.c_double), ("iter_per_sec", ctypes.c_double),
                 ("setup_seconds", ctypes.c_double), ("device_seconds", ctypes.c_double),
                 ("kernel_launches", ctypes.c_long), ("breakdown", ctypes.c_int),
-                ("fallback_iter", ctypes.c_int)]
+                ("fallback_iter", ctypes.c_int), ("crit0", ctypes.c_double)]
 
 
 class SgLearnOpts(ctypes.Structure):
@@ -126,6 +126,8 @@ def load_library(path: Optional[str] = None):
     L.sg_tile_shapes.argtypes = [c_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.sg_set_tod.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
     L.sg_rhs.argtypes = [c_p, dp]
+    L.sg_set_gains.argtypes = [c_p, dp]
+    L.sg_fit_gains.argtypes = [c_p, ctypes.c_int, dp, dp, dp]
     L.sg_npix.argtypes = [c_p]
     L.sg_npix.restype = ctypes.c_long
     L.sg_group_mode.argtypes = [c_p, ctypes.POINTER(ctypes.c_long)]
@@ -242,6 +244,28 @@ class MapMaker:
     def set_tod(self, det: int, tod):
         tod = _f64(tod)
         self._check(self.L.sg_set_tod(self.h, det, _dp(tod), tod.size))
+
+    # ---- recalibration (sanepic.cc:1041-1130, 2123-2316) ---------------------
+    def set_gains(self, gains) -> None:
+        """Per-tile gains [nseg][ndet] (the reference's relCalib layout), or
+        None for 1; the next rhs() and solve() use them."""
+        if gains is None:
+            self._check(self.L.sg_set_gains(self.h, None))
+            return
+        g = _f64(gains)
+        if g.size != self.nseg * self.ndet:
+            raise ValueError(f"gains: {g.size} values for {self.nseg} x {self.ndet} tiles")
+        self._check(self.L.sg_set_gains(self.h, _dp(g)))
+
+    def fit_gains(self, per_detector: bool = False):
+        """Gains refitted to the current map: (gains [nseg][ndet], chi2 before,
+        chi2 after).  Not applied; pass them to set_gains()."""
+        g = np.empty(self.nseg * self.ndet)
+        b = ctypes.c_double(0.0)
+        a = ctypes.c_double(0.0)
+        self._check(self.L.sg_fit_gains(self.h, int(per_detector), _dp(g), ctypes.byref(b),
+                                        ctypes.byref(a)))
+        return g.reshape(self.nseg, self.ndet), b.value, a.value
 
     # ---- operator -----------------------------------------------------------
     def rhs(self, chi2: bool = True) -> Optional[float]:

@@ -30,6 +30,7 @@ UNITS = {
     "sg_pt.cu": [],
     "sg_group.cu": [],
     "sg_fft3.cu": [],
+    "sg_recal.cu": [],
     "sg_cg.cu": [],
     "sg_api.cu": [],
     "sg_noalloc.cu": [],

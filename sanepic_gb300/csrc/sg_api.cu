@@ -134,13 +134,13 @@ extern "C" long sg_kernel_launches(const sg_ctx* c) { return c ? (long)c->launch
 
 extern "C" int sg_weighting(const sg_ctx* c) {
   if (!c) return SG_ERR_ARG;
-  return (c->group_mode ? 1 : 0) | (c->use_f3 ? 2 : 0);
+  return (c->grouped() ? 1 : 0) | (c->use_f3 ? 2 : 0);
 }
 
 extern "C" int sg_group_mode(const sg_ctx* c, long* ngroups) {
   if (!c) return 0;
   if (ngroups) *ngroups = c->ngroups;
-  return c->group_mode ? (c->use_f3 ? 2 : 1) : 0;
+  return c->grouped() ? (c->use_f3 ? 2 : 1) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -492,6 +492,11 @@ extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) 
   if (e == cudaSuccess) e = cudaEventSynchronize(c->ev_copy);  // the caller's array is read
   if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
   c->launches += 2;
+  // the weights of bins 0 and ns/2 in FP64 (sanepic.cc:533-537), which the
+  // gain fit's half-spectrum sums count twice (sg_recal.cu)
+  if (c->spn_edge.size() != (size_t)(2 * c->ndet)) c->spn_edge.assign(2 * c->ndet, 0.0);
+  c->spn_edge[2 * det] = ispf[1] * 1e-6 / (double)ns / (double)ns;
+  c->spn_edge[2 * det + 1] = ispf[idx_max] / (double)ns / (double)ns;
   c->have_noise[det] = 1;
   c->have_bj3 = c->have_diag = c->have_rhs = c->have_hmix = false;
   return SG_OK;
@@ -837,6 +842,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
   const double t1 = now_s();
   const double var00 = c->sc_host->var00, delta0 = c->sc_host->delta0;
   double crit = c->sc_host->var / var00;
+  const double crit0 = crit;
   const int refresh_every = o->refresh_every > 0 ? o->refresh_every : 10;
   // the reference's diagonal mode, and any solve that prints or reports chi2,
   // keeps the reference's true residual at iteration 0
@@ -942,6 +948,7 @@ extern "C" int sg_solve(sg_ctx* c, const sg_solve_opts* o, sg_report* rep) {
     rep->kernel_launches = (long)(c->launches - launches0);
     rep->breakdown = c->sc_host->flag;
     rep->fallback_iter = fallback_iter;
+    rep->crit0 = crit0;
   }
   return SG_OK;
 }
@@ -1061,7 +1068,7 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
   float tot[4] = {0.f, 0.f, 0.f, 0.f};
   for (int i = 0; i < reps && e == cudaSuccess; i++) {
     e = cudaEventRecord(ev[0], c->st);
-    if (c->group_mode) {
+    if (c->grouped()) {
       // projection = (a, b1, b2) (mixed by W for uniform groups); N^-1 into
       // P^T's layout (the three-pass weighting, or the cluster FFT kernels);
       // no detector sums
@@ -1070,7 +1077,7 @@ extern "C" int sg_profile_operator(sg_ctx* c, int reps, double* ms) {
       if (e == cudaSuccess) e = c->group_weight_step();
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);
     } else {
-      if (e == cudaSuccess) e = c->launch_project();
+      if (e == cudaSuccess) e = c->launch_project(c->gains_on ? &c->gain2_t : nullptr);
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], c->st);
       if (e == cudaSuccess) e = c->detector_weight_step(c->y.p, c->y.p);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], c->st);

@@ -66,7 +66,7 @@ extern "C" int sg_autotune(sg_ctx* c, int* cluster_size, double* ms) {
     for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {  // first launch warms up
       if (rep == 1) e = cudaEventRecord(a, c->st);
       if (e != cudaSuccess) break;
-      e = c->group_mode
+      e = c->grouped()
               ? c->apply_dev(c->x.as<double>(), c->q.as<double>(), true)
               : c->launch_filter(kLoadTod, c->tod.p, c->y.p, c->ntiles, (int)c->nseg, 0);
     }

@@ -8,9 +8,14 @@
 //  * errors print a message and exit(1) instead of undefined behaviour
 //    (missing or short input files, segment lists that do not match -l/-n);
 //  * options of code paths that are not part of the map-maker's hot path
-//    (-o dipole, -r/-R/-c recalibration, -b galactic leakage) are refused
+//    (-o dipole, -c leakage recalibration, -b galactic leakage) are refused
 //    when switched on; -E 1 stops like the reference ("NOT IMPLEMENTED YET");
 //    the other options are accepted and ignored, as the reference ignores them;
+//  * -r (with -R: one gain per detector) runs the reference's outer loop of
+//    map-making and gain fits (sanepic.cc:1041-1042, 2123-2316) with its fit
+//    corrected (sg_fit_gains: the reference's fits carry a factor 4 and its
+//    loop diverges); the orbital-dipole timelines orbdip_<detector> it reads
+//    must be absent or zero (the -o path is not implemented);
 //  * SANEPIC_GPU_PRECISION (f64 | f32), SANEPIC_GPU_PRECOND (diag | bj3),
 //    SANEPIC_GPU_DEVICE and SANEPIC_GPU_STOP select what the reference fixes:
 //    FP64 and its diagonal preconditioner by default, stop at 1e-15;
@@ -65,6 +70,7 @@ struct Args {
   bool have_pointing_dir = false, have_init = false;
   long ndet = 0, nseg = 0, ns = 0, nssp = 0, nside = 0;
   int pol = 0, hwp = 0, iterw = 10, write_iter = 1;
+  bool recalib = false, recal_global = false;  // -r, -R (sanepic.cc:364, 388)
   double omega = 0.0;
   std::vector<std::string> bolos;
 };
@@ -170,10 +176,12 @@ Args parse(int argc, char** argv) {
           exit(0);
         }
         break;
-      case 'o': case 'r': case 'R': case 'c': case 'b':
+      case 'r': a.recalib = atoi(optarg) != 0; break;
+      case 'R': a.recal_global = atoi(optarg) != 0; break;
+      case 'o': case 'c': case 'b':
         if (atoi(optarg))
           die("option -%c %s selects a path this executable does not implement "
-              "(dipole / recalibration / galactic leakage)", c, optarg);
+              "(dipole / leakage recalibration / galactic leakage)", c, optarg);
         break;
       case 'H': case 'J': case 'G': case 'A': case 'm': case 'K': case 'L': case 'g':
       case 'M': case 'z':
@@ -202,6 +210,7 @@ struct Run {
   sg_ctx* ctx;
   long npixfull;
   std::vector<double> full;
+  int rloop = 1;  // the outer loop of -r (sanepic.cc:1041)
 
   void check(int rc, const char* what) {
     if (rc != SG_OK) die("%s failed (%d): %s", what, rc, sg_last_error(ctx));
@@ -222,6 +231,7 @@ int on_iteration(void* user, int iter, double crit, double crit2, double chi2) {
   fflush(stdout);
   const std::string& O = a.outdir;
   const std::string& e = a.termin;
+  if (r->rloop != 1) return 0;  // the maps below only in the first loop (sanepic.cc:1616, 1711)
   if (iter == 1) {
     r->write_map(SG_MAP_NVAR, O + "_NVAR" + e);
     r->write_map(SG_MAP_HITS, O + "_HITS" + e);
@@ -339,6 +349,22 @@ int main(int argc, char** argv) {
     run.check(sg_set_tod(run.ctx, i, buf.data(), nsamp_total), "sg_set_tod");
   }
 
+  // -r reads the orbital dipole of every detector (sanepic.cc:702-712): this
+  // executable takes it as zero, so a file that holds anything else is refused
+  if (a.recalib) {
+    for (long i = 0; i < a.ndet; i++) {
+      const std::string df = a.dirfile + "/orbdip_" + a.bolos[i];
+      FILE* fp = fopen(df.c_str(), "rb");
+      if (!fp) continue;
+      fclose(fp);
+      read_vector(df, 0, nsamp_total, buf);
+      for (long g = 0; g < a.nseg; g++)
+        for (long s = isampmin[g]; s < isampmin[g] + a.ns; s++)
+          if (buf[s] != 0.0)
+            die("%s: nonzero orbital dipole (the -o path is not implemented)", df.c_str());
+    }
+  }
+
   double chi20 = 0.0;
   run.check(sg_rhs(run.ctx, &chi20), "sg_rhs");
   printf("PtNd Computed...\n");
@@ -359,17 +385,55 @@ int main(int argc, char** argv) {
   run.check(sg_solve(run.ctx, &o, &rep), "sg_solve");
   printf("\n");
 
-  // final maps (sanepic.cc:1770-1801)
+  // final maps of each loop (sanepic.cc:1770-1801)
   const std::string& O = a.outdir;
-  const std::string tail = "_" + a.termin + "_1";
   std::vector<double> sol(3 * npix);
-  run.check(sg_get_solution(run.ctx, sol.data()), "sg_get_solution");
-  write_vector(O + "_A" + tail, sol.data(), 3 * npix);
-  run.write_map(SG_MAP_I, O + "_I" + tail);
-  run.write_map(SG_MAP_Q, O + "_Q" + tail);
-  run.write_map(SG_MAP_U, O + "_U" + tail);
-  fprintf(stderr, "sanepic (GPU): %d iterations, crit %.3e, %.3f s solve (%.1f it/s)\n",
-          rep.iterations, rep.crit, rep.solve_seconds, rep.iter_per_sec);
+  auto write_loop_maps = [&]() {
+    const std::string tail = "_" + a.termin + "_" + std::to_string(run.rloop);
+    run.check(sg_get_solution(run.ctx, sol.data()), "sg_get_solution");
+    write_vector(O + "_A" + tail, sol.data(), 3 * npix);
+    run.write_map(SG_MAP_I, O + "_I" + tail);
+    run.write_map(SG_MAP_Q, O + "_Q" + tail);
+    run.write_map(SG_MAP_U, O + "_U" + tail);
+  };
+  write_loop_maps();
+  int total_iters = rep.iterations;
+
+  if (a.recalib) {
+    // the outer loop (sanepic.cc:1041-1042, 2123-2316): fit the gains to the
+    // map, write them (relCalib.dat<loop>, in the working directory as the
+    // reference does), and make the map again from the previous one with the
+    // new gains, until a loop starts already converged (its var0 / var00 at
+    // most the stop criterion) or the 500th loop
+    const double stop_crit = o.stop_crit;
+    const double var00_1 = rep.var00;
+    double var0_ratio = rep.crit0;  // var0 / var00 of the loop just made
+    std::vector<double> gains(a.ndet * a.nseg, 1.0);
+    while (true) {
+      double x2b = 0.0, x2a = 0.0;
+      run.check(sg_fit_gains(run.ctx, a.recal_global ? 1 : 0, gains.data(), &x2b, &x2a),
+                "sg_fit_gains");
+      printf("Before recal chi2 = %10.15g\n", x2b);
+      if (a.recal_global)
+        for (long d = 0; d < a.ndet; d++) printf("Coef calib det %ld is %10.15g\n", d, gains[d]);
+      printf("After recal chi2 = %10.15g\n", x2a);
+      fflush(stdout);
+      write_vector("relCalib.dat" + std::to_string(run.rloop), gains.data(), a.ndet * a.nseg);
+      run.rloop += 1;
+      if (!(run.rloop < 500 && var0_ratio > stop_crit)) break;
+      run.check(sg_set_gains(run.ctx, gains.data()), "sg_set_gains");
+      run.check(sg_rhs(run.ctx, nullptr), "sg_rhs");
+      o.x0 = sol.data();  // the previous loop's map (sanepic.cc:1226-1232)
+      run.check(sg_solve(run.ctx, &o, &rep), "sg_solve");
+      printf("\n");
+      var0_ratio = rep.crit0 * rep.var00 / var00_1;
+      total_iters += rep.iterations;
+      write_loop_maps();
+    }
+  }
+  fprintf(stderr, "sanepic (GPU): %d loop(s), %d iterations, crit %.3e, %.3f s last solve (%.1f it/s)\n",
+          a.recalib ? run.rloop - 1 : 1, total_iters, rep.crit, rep.solve_seconds,
+          rep.iter_per_sec);
   sg_destroy(run.ctx);
   return 0;
 }

@@ -101,6 +101,17 @@ struct sg_ctx {
   // hmix [G][M+1][6]
   static constexpr int kGroupMin = 4;
   bool group_mode = false, have_hmix = false;
+  // per (detector, segment) gains of the recalibration loop (sg_set_gains,
+  // sanepic.cc:1044-1053 and 2508-2510): A = P^T G N^-1 G P and
+  // b = P^T G N^-1 d with G = diag(g) tile by tile.  Gains of one tile break
+  // the sums of an offset group, so the operator runs per detector while
+  // they are set.
+  bool gains_on = false;
+  DevBuf gain_t, gain2_t;       // g and g^2 per tile [det][seg], in the operator's type
+  std::vector<double> gains_h;  // g per tile [det][seg]
+  DevBuf yb, tdots;             // the gain fit's second timeline buffer and per-tile sums
+  std::vector<double> spn_edge;  // per detector: the weights of bins 0 and ns/2 (FP64)
+  bool grouped() const { return group_mode && !gains_on; }
   DevBuf gtl, gspec, hmix, dspec, rhs_part;  // + data spectra [ndet][nseg][M+1], chi^2 partials
   DevBuf kslot, filt_slot;  // frequency of each spectrum slot; filter rows in slot order
   int kslot_S = -1;         // the tile shape kslot was made for
@@ -265,21 +276,31 @@ struct sg_ctx {
     return to_map4<double>(v, npix, dmap.as<double>(), st);
   }
 
-  // y = P map (time order, every detector), then N^-1 in place on y
-  cudaError_t launch_project() {
+  // y = P map (time order, every detector), each tile times tsc[tile] when
+  // tsc is set (the gains: g^2 in A, g in the residual d - G P x)
+  cudaError_t launch_project(const DevBuf* tsc = nullptr, void* out = nullptr) {
     launches++;
+    void* o = out ? out : y.p;
     if (f32)
       return project_launch<float>(pix.as<int>(), cs.as<float>(), dmap.as<float>(), ngsamp,
                                    ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
-                                   dcs.as<float>(), y.as<float>(), st);
+                                   dcs.as<float>(), (float*)o, tsc ? tsc->as<float>() : nullptr,
+                                   ns, st);
     return project_launch<double>(pix.as<int>(), cs.as<double>(), dmap.as<double>(), ngsamp,
                                   ns * nseg, grp_off.as<int>(), grp_det.as<int>(),
-                                  dcs.as<double>(), y.as<double>(), st);
+                                  dcs.as<double>(), (double*)o, tsc ? tsc->as<double>() : nullptr,
+                                  ns, st);
+  }
+  // y *= g per tile (G after N^-1: b = P^T G N^-1 d, r = P^T G N^-1 (d - G P x))
+  cudaError_t scale_by_gain(void* t) {
+    launches++;
+    return f32 ? tile_scale_launch<float>((float*)t, gain_t.as<float>(), ntiles, ns, st)
+               : tile_scale_launch<double>((double*)t, gain_t.as<double>(), ntiles, ns, st);
   }
 
   cudaError_t apply_map(double* out, bool masked) {
-    if (group_mode) return apply_map_group(out, masked);
-    cudaError_t e = launch_project();
+    if (grouped()) return apply_map_group(out, masked);
+    cudaError_t e = launch_project(gains_on ? &gain2_t : nullptr);
     if (e == cudaSuccess) e = detector_weight_step(y.p, y.p);
     if (e == cudaSuccess) e = pt_of_y(out, masked);
     return e;
@@ -472,9 +493,13 @@ struct sg_ctx {
   // instead of one forward FFT per detector and segment (same map; only the
   // rounding differs).
   cudaError_t rhs_of(const void* d, double* bout, double* chi2_dev) {
-    if (!group_mode) {
+    if (!grouped()) {
+      // with gains, G N^-1 d: chi^2_0 stays that of the raw data, as the
+      // reference's calibrated data times its g^2 weights give
+      // (sanepic.cc:1044-1053, 1089-1110)
       cudaError_t e = chi2_dev ? launch_filter(kLoadTod, d, y.p, ntiles, (int)nseg, 0, nullptr, chi2_dev)
                                : detector_weight_step(d, y.p);
+      if (e == cudaSuccess && gains_on) e = scale_by_gain(y.p);
       if (e == cudaSuccess) e = pt_of_y(bout, true);
       return e;
     }
@@ -663,7 +688,7 @@ struct sg_ctx {
   // no chi^2 wanted (no printed line, no callback) r = b - A x through the
   // group operator instead, a few percent of the cost.
   bool refresh_chi2 = true;
-  int refresh_kind() const { return (group_mode && !refresh_chi2) ? 2 : 1; }
+  int refresh_kind() const { return (grouped() && !refresh_chi2) ? 2 : 1; }
   cudaError_t enqueue_true_residual(const CgVecs& v, int flexible) {
     cudaError_t e = to_map(x.as<double>());
     launches++;  // cg_refresh_r
@@ -672,10 +697,12 @@ struct sg_ctx {
       if (e == cudaSuccess) e = cg_refresh_r(v, flexible, 0, st);
       return e;
     }
-    if (e == cudaSuccess) e = launch_project();
+    // with gains: chi^2 of d - G P x (sanepic.cc:1500-1535), then G N^-1
+    if (e == cudaSuccess) e = launch_project(gains_on ? &gain_t : nullptr);
     if (e == cudaSuccess)
       e = launch_filter(kLoadTodMinus, tod_active(), y.p, ntiles, (int)nseg, 0, y.p,
                         &sc.as<CgScalars>()->chi2);
+    if (e == cudaSuccess && gains_on) e = scale_by_gain(y.p);
     if (e == cudaSuccess) e = pt_of_y(q.as<double>(), true);
     if (e == cudaSuccess) e = cg_refresh_r(v, flexible, 1, st);
     return e;

@@ -149,7 +149,15 @@ cudaError_t nan_patch_launch(T* v, long long ns, long long nseg, cudaStream_t st
 template <typename T>
 cudaError_t project_launch(const int* gpix, const T* gcs, const T* map, long long n,
                            long long nsd, const int* grp_off, const int* grp_det, const T* dcs,
-                           T* t, cudaStream_t st);
+                           T* t, const T* tsc, long long ns, cudaStream_t st);
+// per (detector, segment) tile of ns samples (tile = det * nseg + seg):
+// y[tile][:] *= tsc[tile]
+template <typename T>
+cudaError_t tile_scale_launch(T* y, const T* tsc, long long ntiles, long long ns, cudaStream_t st);
+// out[tile] = sum over the tile's samples of a * b (FP64, fixed order)
+template <typename T>
+cudaError_t tile_dots_launch(const T* a, const T* b, long long ntiles, long long ns, double* out,
+                             cudaStream_t st);
 // detector sums per group sample: ys[gs] = (sum y, sum cos2d' y, sum sin2d' y, 0)
 template <typename T>
 cudaError_t detsum_launch(const T* y, long long n, long long nsd, const int* grp_off,

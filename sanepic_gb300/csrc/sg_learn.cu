@@ -732,6 +732,8 @@ extern "C" int sg_learn_train(sg_ctx* c, const sg_learn_opts* o, sg_learn_report
   if (!c->have_pointing) return c->fail(SG_ERR_STATE, "pointing not set");
   for (long long d = 0; d < c->ndet; d++)
     if (!c->have_noise[d]) return c->fail(SG_ERR_STATE, "noise of detector %lld not set", d);
+  if (c->gains_on)  // the training problems are made without gains
+    return c->fail(SG_ERR_UNSUPPORTED, "learned part with detector gains set (sg_set_gains)");
   const int npairs = o->npairs > 0 ? o->npairs : 512;
   const uint64_t seed0 = o->seed > 0 ? (uint64_t)o->seed : 5000;
   const int steps = o->steps > 0 ? o->steps : (o->steps < 0 ? 0 : 1500);  // 0: no network

@@ -47,6 +47,8 @@ struct alignas(4 * sizeof(T)) pmap4 {
 
 // Four group samples per thread: one pixel/angle load and one map gather per
 // sample, then the P value of every detector of the group (coalesced writes).
+// tsc (or null): one factor per (detector, segment) tile -- the squared gains
+// of a recalibrated operator, G N^-1 G = g^2 N^-1 on a tile.
 __global__ void __launch_bounds__(256) k_project_f32(const int4* __restrict__ gpix,
                                                      const float4* __restrict__ gcs,
                                                      const pmap4<float>* __restrict__ map,
@@ -54,7 +56,9 @@ __global__ void __launch_bounds__(256) k_project_f32(const int4* __restrict__ gp
                                                      const int* __restrict__ grp_off,
                                                      const int* __restrict__ grp_det,
                                                      const float2* __restrict__ dcs,
-                                                     float4* __restrict__ t) {
+                                                     float4* __restrict__ t,
+                                                     const float* __restrict__ tsc,
+                                                     long long ns4) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
        i += (long long)gridDim.x * blockDim.x) {
     const int g = (int)(i / nsd4);
@@ -76,6 +80,13 @@ __global__ void __launch_bounds__(256) k_project_f32(const int4* __restrict__ gp
       o.y = a.y + r.x * b.y + r.y * e.y;
       o.z = a.z + r.x * b.z + r.y * e.z;
       o.w = a.w + r.x * b.w + r.y * e.w;
+      if (tsc) {
+        const float f = tsc[(long long)d * (nsd4 / ns4) + w4 / ns4];
+        o.x *= f;
+        o.y *= f;
+        o.z *= f;
+        o.w *= f;
+      }
       __stcs(t + (long long)d * nsd4 + w4, o);
     }
   }
@@ -88,7 +99,9 @@ __global__ void __launch_bounds__(256) k_project_f64(const int* __restrict__ gpi
                                                      const int* __restrict__ grp_off,
                                                      const int* __restrict__ grp_det,
                                                      const double2* __restrict__ dcs,
-                                                     double* __restrict__ t) {
+                                                     double* __restrict__ t,
+                                                     const double* __restrict__ tsc,
+                                                     long long ns) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const int g = (int)(i / nsd);
@@ -99,7 +112,8 @@ __global__ void __launch_bounds__(256) k_project_f64(const int* __restrict__ gpi
     for (int k = grp_off[g]; k < grp_off[g + 1]; k++) {
       const int d = grp_det[k];
       const double2 r = dcs[d];
-      t[(long long)d * nsd + w] = m.I + (r.x * b + r.y * e);
+      const double v = m.I + (r.x * b + r.y * e);
+      t[(long long)d * nsd + w] = tsc ? v * tsc[(long long)d * (nsd / ns) + w / ns] : v;
     }
   }
 }
@@ -108,14 +122,14 @@ template <>
 cudaError_t project_launch<float>(const int* gpix, const float* gcs, const float* map,
                                   long long n, long long nsd, const int* grp_off,
                                   const int* grp_det, const float* dcs, float* t,
-                                  cudaStream_t st) {
+                                  const float* tsc, long long ns, cudaStream_t st) {
   const long long n4 = n / 4;  // nsd is a multiple of 4 (ns >= 256)
   long long blocks = (n4 + 255) / 256;
   if (blocks > 152LL * 16) blocks = 152LL * 16;
   k_project_f32<<<(unsigned)blocks, 256, 0, st>>>(
       reinterpret_cast<const int4*>(gpix), reinterpret_cast<const float4*>(gcs),
       reinterpret_cast<const pmap4<float>*>(map), n4, nsd / 4, grp_off, grp_det,
-      reinterpret_cast<const float2*>(dcs), reinterpret_cast<float4*>(t));
+      reinterpret_cast<const float2*>(dcs), reinterpret_cast<float4*>(t), tsc, ns / 4);
   return cudaGetLastError();
 }
 
@@ -123,12 +137,12 @@ template <>
 cudaError_t project_launch<double>(const int* gpix, const double* gcs, const double* map,
                                    long long n, long long nsd, const int* grp_off,
                                    const int* grp_det, const double* dcs, double* t,
-                                   cudaStream_t st) {
+                                   const double* tsc, long long ns, cudaStream_t st) {
   long long blocks = (n + 255) / 256;
   if (blocks > 152LL * 16) blocks = 152LL * 16;
   k_project_f64<<<(unsigned)blocks, 256, 0, st>>>(
       gpix, reinterpret_cast<const double2*>(gcs), reinterpret_cast<const pmap4<double>*>(map),
-      n, nsd, grp_off, grp_det, reinterpret_cast<const double2*>(dcs), t);
+      n, nsd, grp_off, grp_det, reinterpret_cast<const double2*>(dcs), t, tsc, ns);
   return cudaGetLastError();
 }
 

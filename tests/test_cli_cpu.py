@@ -45,7 +45,7 @@ def test_unknown_option_is_rejected(tree):
     assert r.returncode == 1 and "not valid" in r.stderr
 
 
-@pytest.mark.parametrize("flag", ["-o", "-r", "-b"])
+@pytest.mark.parametrize("flag", ["-o", "-c", "-b"])
 def test_unsupported_paths_are_refused(tree, flag):
     r = run(tree[1] + [flag, "1"])
     assert r.returncode == 1 and "does not implement" in r.stderr

@@ -37,7 +37,7 @@ def test_struct_layouts_match_header():
     # sizes of the by-value structs shared with C (LP64)
     assert ctypes.sizeof(sg.SgDesc) == 8 * 4 + 4 + 4 + 8 + 4 + 4
     assert ctypes.sizeof(sg.SgDet) == 24
-    assert ctypes.sizeof(sg.SgReport) == 4 + 4 + 8 * 6 + 8 + 8
+    assert ctypes.sizeof(sg.SgReport) == 4 + 4 + 8 * 6 + 8 + 8 + 8
     # precond, stop_crit, maxiter, refresh_every, verbose, x0, use_graph,
     # on_iteration, user (natural alignment, LP64)
     assert ctypes.sizeof(sg.SgSolveOpts) == 64

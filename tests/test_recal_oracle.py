@@ -1,0 +1,109 @@
+"""The oracle's gain recalibration (sanepic.cc:2123-2316, 3206-3260) against
+the reference's own first gain fit (tests/golden/recal_4det_nside16_ref.*,
+made by tests/golden/make_recal_golden.py), and its corrected outer loop on a
+problem with known gains.
+
+The reference's fit returns four times the least-squares gain (sPNd carries
+a factor 2, cPNPc a factor 1/2); the fixture's numbers are checked with that
+factor put back, so the pin covers every other step of the fit."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import GOLDEN_DIR, load_problem
+from sanepic_gb300 import synth
+
+REF_FACTOR = 4.0  # sanepic.cc:2196-2201 (x 2) over 2217-2220 (x 1/2)
+
+
+def recal_problem():
+    z = np.load(os.path.join(GOLDEN_DIR, "recal_4det_nside16_ref.npz"))
+    with open(os.path.join(GOLDEN_DIR, "recal_4det_nside16_ref.json")) as f:
+        log = json.load(f)
+    prob = load_problem(log["problem"])
+    spec = prob["spec"]
+    g = z["gains"]
+    tod = prob["tod"].copy()
+    for d in range(spec.ndet):
+        for s in range(spec.nseg):
+            tod[d, s * spec.ns:(s + 1) * spec.ns] *= g[d, s]
+    prob["tod"] = tod
+    return prob, z["A_1"], log
+
+
+def test_gain_fit_matches_the_references_first_fit():
+    prob, a1, log = recal_problem()
+    spec = prob["spec"]
+    s = oracle.Setup(prob)
+    tod = prob["tod"].reshape(-1)
+    assert a1.size == 3 * s.npix
+    # chi^2 with the gains the first map was made with (all 1)
+    assert s.gain_chi2(a1, tod) == pytest.approx(log["per_tile"]["before"], rel=1e-12)
+    bd, cs = s.gain_dots(a1, tod)  # [det][seg]
+    # -r: one gain per tile; the reference's chi^2 with its (x4) gains
+    g_tile = REF_FACTOR * bd / cs
+    assert s.gain_chi2(a1, tod, g_tile.T) == pytest.approx(log["per_tile"]["after"], rel=1e-12)
+    # -R: one gain per detector, printed as "Coef calib det"
+    g_det = REF_FACTOR * bd.sum(axis=1) / cs.sum(axis=1)
+    np.testing.assert_allclose(g_det, log["per_detector"]["coef"], rtol=1e-12)
+    gd = np.repeat(g_det[None, :], spec.nseg, axis=0)
+    assert s.gain_chi2(a1, tod, gd) == pytest.approx(log["per_detector"]["after"], rel=1e-12)
+
+
+def test_fit_normalises_to_the_previous_mean_gain():
+    prob, a1, _ = recal_problem()
+    s = oracle.Setup(prob)
+    tod = prob["tod"].reshape(-1)
+    g0 = np.full((prob["spec"].nseg, prob["spec"].ndet), 1.1)
+    g, before, after = s.fit_gains(a1, tod, g0)
+    assert g.mean() == pytest.approx(1.1, rel=1e-14)
+    gd, _, _ = s.fit_gains(a1, tod, g0, per_detector=True)
+    assert np.ptp(gd, axis=0).max() == 0.0  # one gain per detector
+    assert gd.mean() == pytest.approx(1.1, rel=1e-14)
+
+
+def recal_loop(prob, gtrue, nloop, per_detector=False):
+    spec = prob["spec"]
+    tod = prob["tod"].copy()
+    for d in range(spec.ndet):
+        for s in range(spec.nseg):
+            tod[d, s * spec.ns:(s + 1) * spec.ns] *= gtrue[d, s]
+    st = oracle.Setup(prob)
+    tod = tod.reshape(-1)
+    g = np.ones((spec.nseg, spec.ndet))
+    x = None
+    Mp = st.diag_precond()
+    hist = []
+    for _ in range(nloop):
+        b = st.rhs_gains(tod, g)
+        x, _, _ = st.pcg_gains(b, g, precond="diag", x0=x, stop_crit=1e-15, Mp=Mp)
+        g, before, after = st.fit_gains(x, tod, g, per_detector=per_detector)
+        hist.append((before, after))
+    return g, hist
+
+
+@pytest.mark.parametrize("per_detector", [False, True])
+def test_corrected_loop_recovers_the_injected_gains(per_detector):
+    spec = synth.ProblemSpec("recal_4det_nside16", ndet=4, nside=16, nseg=8, ns=2048,
+                             fknee=0.02, alpha=1.0, problem=5, sigma_uk=5.0)
+    prob = synth.make_problem(spec)
+    rng = np.random.default_rng(2)
+    if per_detector:
+        gtrue = np.repeat(1.0 + 0.02 * rng.standard_normal((4, 1)), 8, axis=1)
+    else:
+        gtrue = 1.0 + 0.02 * rng.standard_normal((4, 8))
+    # one gain per detector is nearly degenerate with Q and U (a gain
+    # mismatch between detectors at different angles looks like
+    # polarisation), so that loop converges more slowly
+    g, hist = recal_loop(prob, gtrue, 32 if per_detector else 6, per_detector)
+    # chi^2 never rises: each fit lowers it, and each map made with the new
+    # gains lowers it again
+    chi = [h for pair in hist for h in pair]
+    assert all(b <= a * (1 + 1e-12) for a, b in zip(chi, chi[1:]))
+    # the gains up to the common factor the map absorbs: from 2 % off to
+    # below 0.5 %, the noise floor of this problem
+    ratio = g.T / gtrue
+    assert np.std(ratio / ratio.mean()) < 0.005
