@@ -148,9 +148,19 @@ int sg_set_pol_rcond(sg_ctx *ctx, double rcond_min);
  * Replaces sanepic.cc:507-539 (including the bin-0 override, 536-537). */
 int sg_set_noise(sg_ctx *ctx, long det, const double *ispf, long nssp);
 
+/* The same for every detector at once: ispf holds ndet rows of nssp values
+ * (detector d's -u file in row d).  One copy and one wait instead of one
+ * per detector; the rows are the ones sg_set_noise makes. */
+int sg_set_noise_all(sg_ctx *ctx, const double *ispf, long nssp);
+
 /* TOD of one detector (full timeline; NaNs patched as sanepic.cc:784-790).
  * Replaces sanepic.cc:776-803. */
 int sg_set_tod(sg_ctx *ctx, long det, const double *tod, long nsamp_total);
+
+/* The same for every detector at once: tod holds ndet rows of nsamp_total
+ * samples (detector d's timeline in row d).  One wait for all detectors
+ * instead of one per detector. */
+int sg_set_tod_all(sg_ctx *ctx, const double *tod, long nsamp_total);
 
 /* b = P^T N^-1 d (sanepic.cc:1069-1125).  chi2 (may be NULL) receives the
  * reference's chi2_0 = 2 sum |F d|^2 SpN (sanepic.cc:1089-1110).  Without

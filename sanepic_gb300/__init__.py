@@ -40,7 +40,7 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
            "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
-           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes", "sg_set_gains", "sg_fit_gains",
+           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes", "sg_set_gains", "sg_fit_gains", "sg_set_noise_all", "sg_set_tod_all",
            "sg_last_error", "sg_destroy"]
 
 
@@ -122,6 +122,8 @@ def load_library(path: Optional[str] = None):
     L.sg_set_stream.argtypes = [c_p, c_p]
     L.sg_set_pointing.argtypes = [c_p, dp, dp, dp, ctypes.c_long, lp, ctypes.POINTER(SgDet)]
     L.sg_set_noise.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
+    L.sg_set_noise_all.argtypes = [c_p, dp, ctypes.c_long]
+    L.sg_set_tod_all.argtypes = [c_p, dp, ctypes.c_long]
     L.sg_set_pol_rcond.argtypes = [c_p, ctypes.c_double]
     L.sg_tile_shapes.argtypes = [c_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.sg_set_tod.argtypes = [c_p, ctypes.c_long, dp, ctypes.c_long]
@@ -241,9 +243,23 @@ class MapMaker:
         ispf = _f64(ispf)
         self._check(self.L.sg_set_noise(self.h, det, _dp(ispf), ispf.size))
 
+    def set_noise_all(self, ispf):
+        """Every detector's iSpf at once: ispf [ndet][nssp]."""
+        ispf = _f64(ispf)
+        if ispf.ndim != 2 or ispf.shape[0] != self.ndet:
+            raise ValueError(f"ispf: want [{self.ndet}][nssp], got {ispf.shape}")
+        self._check(self.L.sg_set_noise_all(self.h, _dp(ispf), ispf.shape[1]))
+
     def set_tod(self, det: int, tod):
         tod = _f64(tod)
         self._check(self.L.sg_set_tod(self.h, det, _dp(tod), tod.size))
+
+    def set_tod_all(self, tod):
+        """Every detector's timeline at once: tod [ndet][nsamp_total]."""
+        tod = _f64(tod)
+        if tod.ndim != 2 or tod.shape[0] != self.ndet:
+            raise ValueError(f"tod: want [{self.ndet}][nsamp], got {tod.shape}")
+        self._check(self.L.sg_set_tod_all(self.h, _dp(tod), tod.shape[1]))
 
     # ---- recalibration (sanepic.cc:1041-1130, 2123-2316) ---------------------
     def set_gains(self, gains) -> None:

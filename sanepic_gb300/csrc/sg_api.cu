@@ -462,103 +462,136 @@ extern "C" int sg_set_pol_rcond(sg_ctx* c, double rcond_min) {
   return c->have_pointing ? build_polmask(c) : SG_OK;
 }
 
-extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) {
-  if (!c) return SG_ERR_ARG;
-  if (det < 0 || det >= c->ndet || !ispf || nssp < 2)
-    return c->fail(SG_ERR_ARG, "bad detector index or noise spectrum");
-  cudaSetDevice(c->desc.device);
+// the filter rows of detectors d0 .. d0 + n - 1 from their iSpf values (n
+// rows of nssp values, ispf_host: the caller's array), one copy and one wait
+static int set_noise_rows(sg_ctx* c, long d0, long n, const double* ispf, long nssp) {
   const long long ns = c->ns, M = ns / 2;
   // the largest index read (sanepic.cc:535; monotonic in k)
   const long long idx_max = (long long)((double)M / nssp * ns);
   if (idx_max < 0 || idx_max >= nssp)
     return c->fail(SG_ERR_ARG, "noise spectrum of %ld values is too short for ns=%lld", nssp, ns);
+  cudaSetDevice(c->desc.device);
   // the iSpf values go to the device as they are; the row, its 1/ns^2 scale,
   // the bin-0 override (sanepic.cc:536-537) and g0 are computed there
+  const size_t bytes = sizeof(double) * (size_t)n * nssp;
   cudaError_t e = cudaSuccess;
-  if (c->noise_stage.bytes < sizeof(double) * nssp) e = c->noise_stage.alloc(sizeof(double) * nssp);
+  if (c->noise_stage.bytes < bytes) e = c->noise_stage.alloc(bytes);
   if (e == cudaSuccess && !c->noise_part.p) e = c->noise_part.alloc(sizeof(double) * kNoiseRowBlocks);
   if (e == cudaSuccess && !c->ev_copy) e = cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(c->noise_stage.p, ispf, sizeof(double) * nssp, cudaMemcpyHostToDevice, c->st);
+    e = cudaMemcpyAsync(c->noise_stage.p, ispf, bytes, cudaMemcpyHostToDevice, c->st);
   if (e == cudaSuccess) e = cudaEventRecord(c->ev_copy, c->st);
-  if (e == cudaSuccess)
-    e = c->f32 ? noise_row_launch<float>(c->noise_stage.as<double>(), nssp, ns,
-                                         c->filt.as<float>() + det * (M + 1),
+  for (long k = 0; k < n && e == cudaSuccess; k++) {
+    const long det = d0 + k;
+    const double* row = c->noise_stage.as<double>() + (size_t)k * nssp;
+    e = c->f32 ? noise_row_launch<float>(row, nssp, ns, c->filt.as<float>() + det * (M + 1),
                                          c->g0.as<double>() + det, c->noise_part.as<double>(), c->st)
-               : noise_row_launch<double>(c->noise_stage.as<double>(), nssp, ns,
-                                          c->filt.as<double>() + det * (M + 1),
+               : noise_row_launch<double>(row, nssp, ns, c->filt.as<double>() + det * (M + 1),
                                           c->g0.as<double>() + det, c->noise_part.as<double>(),
                                           c->st);
+    c->launches += 2;
+  }
   if (e == cudaSuccess) e = cudaEventSynchronize(c->ev_copy);  // the caller's array is read
   if (e != cudaSuccess) return c->cuda_fail(e, "set_noise");
-  c->launches += 2;
   // the weights of bins 0 and ns/2 in FP64 (sanepic.cc:533-537), which the
   // gain fit's half-spectrum sums count twice (sg_recal.cu)
   if (c->spn_edge.size() != (size_t)(2 * c->ndet)) c->spn_edge.assign(2 * c->ndet, 0.0);
-  c->spn_edge[2 * det] = ispf[1] * 1e-6 / (double)ns / (double)ns;
-  c->spn_edge[2 * det + 1] = ispf[idx_max] / (double)ns / (double)ns;
-  c->have_noise[det] = 1;
+  for (long k = 0; k < n; k++) {
+    const double* r = ispf + (size_t)k * nssp;
+    c->spn_edge[2 * (d0 + k)] = r[1] * 1e-6 / (double)ns / (double)ns;
+    c->spn_edge[2 * (d0 + k) + 1] = r[idx_max] / (double)ns / (double)ns;
+    c->have_noise[d0 + k] = 1;
+  }
   c->have_bj3 = c->have_diag = c->have_rhs = c->have_hmix = false;
   return SG_OK;
 }
 
-extern "C" int sg_set_tod(sg_ctx* c, long det, const double* tod, long nsamp_total) {
+extern "C" int sg_set_noise(sg_ctx* c, long det, const double* ispf, long nssp) {
   if (!c) return SG_ERR_ARG;
+  if (det < 0 || det >= c->ndet || !ispf || nssp < 2)
+    return c->fail(SG_ERR_ARG, "bad detector index or noise spectrum");
+  return set_noise_rows(c, det, 1, ispf, nssp);
+}
+
+extern "C" int sg_set_noise_all(sg_ctx* c, const double* ispf, long nssp) {
+  if (!c) return SG_ERR_ARG;
+  if (!ispf || nssp < 2) return c->fail(SG_ERR_ARG, "bad noise spectra");
+  return set_noise_rows(c, 0, c->ndet, ispf, nssp);
+}
+
+// TOD of detectors d0 .. d0 + n - 1 (rows of nsamp_total samples in the
+// caller's array): each detector's segments go to the device as they are,
+// are converted there and NaN-patched (sanepic.cc:776-803); one wait for all
+static int set_tod_rows(sg_ctx* c, long d0, long n, const double* tod, long nsamp_total) {
   if (!c->have_pointing) return c->fail(SG_ERR_STATE, "set the pointing before the TOD");
-  if (det < 0 || det >= c->ndet || !tod) return c->fail(SG_ERR_ARG, "bad detector or TOD");
   cudaSetDevice(c->desc.device);
   const long long ns = c->ns, nseg = c->nseg, nsd = ns * nseg;
   for (long long g = 0; g < nseg; g++)
     if (c->isampmin[g] + ns > nsamp_total)
       return c->fail(SG_ERR_ARG, "TOD shorter than the segment list");
-  // the segments' raw FP64 samples go to the device as they are (one copy if
-  // the segments are contiguous); conversion and the NaN rule of
-  // sanepic.cc:784-790 run there
   cudaError_t e = cudaSuccess;
-  if (!c->nanflag.p) e = c->nanflag.alloc(sizeof(int));
+  if (c->nanflag.bytes < sizeof(int) * (size_t)c->ndet) e = c->nanflag.alloc(sizeof(int) * c->ndet);
   bool contiguous = true;
   for (long long g = 1; g < nseg; g++) contiguous &= c->isampmin[g] == c->isampmin[0] + g * ns;
-  // pinned (page-locked, device-mapped) caller memory is read by the ingest
-  // kernel itself over the CPU-GPU link; other memory is staged by a copy
-  const double* src = nullptr;
-  if (contiguous) {
-    cudaPointerAttributes pa{};
-    if (cudaPointerGetAttributes(&pa, tod + c->isampmin[0]) == cudaSuccess &&
-        pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
-      src = static_cast<const double*>(pa.devicePointer);
-    else
-      (void)cudaGetLastError();
-  }
-  if (!src) {
-    if (e == cudaSuccess && c->stage.bytes < sizeof(double) * nsd)
-      e = c->stage.alloc(sizeof(double) * nsd);
-    if (e == cudaSuccess && contiguous) {
-      e = cudaMemcpyAsync(c->stage.p, tod + c->isampmin[0], sizeof(double) * nsd,
-                          cudaMemcpyHostToDevice, c->st);
-    } else {
-      for (long long g = 0; g < nseg && e == cudaSuccess; g++)
-        e = cudaMemcpyAsync(c->stage.as<double>() + g * ns, tod + c->isampmin[g],
-                            sizeof(double) * ns, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->nanflag.p, 0, sizeof(int) * n, c->st);
+  for (long k = 0; k < n && e == cudaSuccess; k++) {
+    const double* row = tod + (size_t)k * nsamp_total;
+    const long det = d0 + k;
+    // pinned (page-locked, device-mapped) caller memory is read by the
+    // ingest kernel itself over the CPU-GPU link; other memory is staged by
+    // a copy (one staging buffer: the copy of the next detector waits for
+    // this one's ingest, in stream order)
+    const double* src = nullptr;
+    if (contiguous) {
+      cudaPointerAttributes pa{};
+      if (cudaPointerGetAttributes(&pa, row + c->isampmin[0]) == cudaSuccess &&
+          pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr)
+        src = static_cast<const double*>(pa.devicePointer);
+      else
+        (void)cudaGetLastError();
     }
-    src = c->stage.as<double>();
+    if (!src) {
+      if (c->stage.bytes < sizeof(double) * nsd) e = c->stage.alloc(sizeof(double) * nsd);
+      if (e == cudaSuccess && contiguous) {
+        e = cudaMemcpyAsync(c->stage.p, row + c->isampmin[0], sizeof(double) * nsd,
+                            cudaMemcpyHostToDevice, c->st);
+      } else {
+        for (long long g = 0; g < nseg && e == cudaSuccess; g++)
+          e = cudaMemcpyAsync(c->stage.as<double>() + g * ns, row + c->isampmin[g],
+                              sizeof(double) * ns, cudaMemcpyHostToDevice, c->st);
+      }
+      src = c->stage.as<double>();
+    }
+    if (e == cudaSuccess)
+      e = c->f32 ? ingest_launch<float>(src, nsd, c->tod.as<float>() + det * nsd,
+                                        c->nanflag.as<int>() + k, c->st)
+                 : ingest_launch<double>(src, nsd, c->tod.as<double>() + det * nsd,
+                                         c->nanflag.as<int>() + k, c->st);
   }
-  if (e == cudaSuccess) e = cudaMemsetAsync(c->nanflag.p, 0, sizeof(int), c->st);
+  std::vector<int> nan(n, 0);
   if (e == cudaSuccess)
-    e = c->f32 ? ingest_launch<float>(src, nsd, c->tod.as<float>() + det * nsd,
-                                      c->nanflag.as<int>(), c->st)
-               : ingest_launch<double>(src, nsd, c->tod.as<double>() + det * nsd,
-                                       c->nanflag.as<int>(), c->st);
-  int nan = 0;
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&nan, c->nanflag.p, sizeof(int), cudaMemcpyDeviceToHost, c->st);
+    e = cudaMemcpyAsync(nan.data(), c->nanflag.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-  if (e == cudaSuccess && nan)
-    e = c->f32 ? nan_patch_launch<float>(c->tod.as<float>() + det * nsd, ns, nseg, c->st)
-               : nan_patch_launch<double>(c->tod.as<double>() + det * nsd, ns, nseg, c->st);
+  for (long k = 0; k < n && e == cudaSuccess; k++)
+    if (nan[k])
+      e = c->f32 ? nan_patch_launch<float>(c->tod.as<float>() + (d0 + k) * nsd, ns, nseg, c->st)
+                 : nan_patch_launch<double>(c->tod.as<double>() + (d0 + k) * nsd, ns, nseg, c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "set_tod");
-  c->have_tod[det] = 1;
+  for (long k = 0; k < n; k++) c->have_tod[d0 + k] = 1;
   c->have_rhs = false;
   return SG_OK;
+}
+
+extern "C" int sg_set_tod(sg_ctx* c, long det, const double* tod, long nsamp_total) {
+  if (!c) return SG_ERR_ARG;
+  if (det < 0 || det >= c->ndet || !tod) return c->fail(SG_ERR_ARG, "bad detector or TOD");
+  return set_tod_rows(c, det, 1, tod, nsamp_total);
+}
+
+extern "C" int sg_set_tod_all(sg_ctx* c, const double* tod, long nsamp_total) {
+  if (!c) return SG_ERR_ARG;
+  if (!tod) return c->fail(SG_ERR_ARG, "null TOD");
+  return set_tod_rows(c, 0, c->ndet, tod, nsamp_total);
 }
 
 static int check_ready(sg_ctx* c, bool need_tod) {

@@ -778,9 +778,12 @@ __global__ void __launch_bounds__(RowInGeo<LOGR, LOGC, RP>::NT, MINB)
 // M = 65536 the column kernels are capped for three CTAs per SM and the row
 // kernel for four (fewer registers, more CTAs in flight: 149 -> 107 us per
 // application of 48 tiles on a GB300).  Single timelines (the right-hand
-// side's detectors): 16 columns per column CTA, 8 row pairs per row CTA.
+// side's detectors): 16 columns per column CTA, 8 row pairs per row CTA,
+// the column kernels capped for four CTAs per SM (64 registers, no spills;
+// at 131072 samples 20.8 -> 20.5 us forward and 20.6 -> 19.3 us inverse per
+// 96 tiles on a GB300, against three CTAs at 80 registers).
 namespace {
-constexpr int kCB = 8, kRP = 2, kCB1 = 16, kRP1 = 8;
+constexpr int kCB = 8, kRP = 2, kCB1 = 16, kRP1 = 8, kMB1 = 4;
 
 template <class K>
 cudaError_t set_smem(K k, int bytes) {
@@ -833,7 +836,7 @@ cudaError_t f3_fwd1(const float* tod, float* scratch, cplx<float>* spec, long lo
                     cudaStream_t st) {
   using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
   using RG = f3::RowSpecGeo<LOGR, LOGC, kRP1>;
-  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, kMB1>;
   auto kr = f3::k_f3_rowspec<LOGR, LOGC, kRP1, 4>;  // four CTAs per SM: 29.5 -> 28.4 us per 96 tiles
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
@@ -880,9 +883,9 @@ cudaError_t f3_det(const float* x, float* y, float* scratch, const float* hpos, 
   constexpr int RS1 = 4;
   using CG = f3::ColGeo<LOGR, LOGC, kCB1, 1>;
   using RG = f3::Row1Geo<LOGR, LOGC, kRP1>;
-  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, 1>;
+  auto kc = f3::k_f3_colfwd<LOGR, LOGC, kCB1, 1, kMB1>;
   auto kr = f3::k_f3_rows1<LOGR, LOGC, kRP1, RS1, 3, true>;
-  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB1, 1, 1>;
+  auto ki = f3::k_f3_colinv<LOGR, LOGC, kCB1, 1, kMB1>;
   const int smc = CG::SMEM * (int)sizeof(cplx<float>), smr = RG::SMEM * (int)sizeof(cplx<float>);
   cudaError_t e = set_smem(kc, smc);
   if (e == cudaSuccess) e = set_smem(ki, smc);

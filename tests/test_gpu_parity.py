@@ -117,6 +117,30 @@ def test_noise_filter_vs_cufft(ns):
     assert rel_rms(got, want) < 2e-6
 
 
+def test_noise_of_every_detector_in_one_call():
+    """sg_set_noise_all makes the rows sg_set_noise makes, detector by detector"""
+    prob = small_problem(ndet=3, nseg=2, ns=4096, precision="f32", nside=16)
+    one = sg.from_problem(prob, precision="f32")
+    allm = sg.from_problem(prob, precision="f32")
+    allm.set_noise_all(np.asarray(prob["ispf"]))
+    x = np.random.default_rng(4).standard_normal(3 * one.npix)
+    assert np.array_equal(one.apply(x), allm.apply(x))
+    assert one.rhs() == allm.rhs()
+    with pytest.raises(ValueError):
+        allm.set_noise_all(np.asarray(prob["ispf"])[:2])
+    # and every detector's timeline in one call, one of them with NaNs
+    tod = np.array(prob["tod"], dtype=np.float64)
+    tod[1, 100] = np.nan
+    tod[2, 4096 + 7] = np.nan
+    for d in range(3):
+        one.set_tod(d, tod[d])
+    allm.set_tod_all(tod)
+    assert one.rhs() == allm.rhs()
+    one.solve(precond="bj3", stop_crit=1e-10)
+    allm.solve(precond="bj3", stop_crit=1e-10)
+    assert np.array_equal(one.solution(), allm.solution())
+
+
 # ---- operator ---------------------------------------------------------------------
 # ndet >= 4 on one pointing: the offset-group operator (three timelines per
 # group, 3 x 3 spectral mixing); ndet = 2: one filter per detector
