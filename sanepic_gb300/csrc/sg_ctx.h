@@ -116,7 +116,11 @@ struct sg_ctx {
   DevBuf kslot, filt_slot;  // frequency of each spectrum slot; filter rows in slot order
   int kslot_S = -1;         // the tile shape kslot was made for
   int hmix_S = 0;           // the tile shape (cluster size) the slot order was built for
-  DevBuf stage, nanflag;  // FP64 staging of one detector's timeline, NaN flag
+  DevBuf stage, nanflag;  // FP64 staging of two detectors' timelines, NaN flags
+  // the timelines' copies run on their own stream, two staging buffers deep
+  // (sg_set_tod_all: the copy of detector k + 1 overlaps the conversion of k)
+  cudaStream_t copy_st = nullptr;
+  cudaEvent_t ev_staged[2] = {nullptr, nullptr}, ev_ingested[2] = {nullptr, nullptr};
   DevBuf map_full;        // a full-sky RING map being read out
   // sg_set_pointing's device scratch (boresight, pixels, numbering and sort
   // temporaries), kept between calls
@@ -176,6 +180,11 @@ struct sg_ctx {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     if (ev0) cudaEventDestroy(ev0);
     if (ev_copy) cudaEventDestroy(ev_copy);
+    for (int b = 0; b < 2; b++) {
+      if (ev_staged[b]) cudaEventDestroy(ev_staged[b]);
+      if (ev_ingested[b]) cudaEventDestroy(ev_ingested[b]);
+    }
+    if (copy_st) cudaStreamDestroy(copy_st);
     if (ev1) cudaEventDestroy(ev1);
     if (sc_host) cudaFreeHost(sc_host);
     if (own_st) cudaStreamDestroy(own_st);
