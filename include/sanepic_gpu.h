@@ -199,6 +199,16 @@ int sg_set_gains(sg_ctx *ctx, const double *gains);
 int sg_fit_gains(sg_ctx *ctx, int per_detector, double *gains_out, double *chi2_before,
                  double *chi2_after);
 
+/* The host arithmetic of sg_fit_gains on given per-tile sums (no GPU; for
+ * checking): tile t = idet * nseg + iseg, dots_ds[t] = (N^-1 d)^T s,
+ * dots_ss[t] = (N^-1 s)^T s with s = P m, edges_s[2t..2t+1] = (sum s_i,
+ * sum (-1)^i s_i), edges_d likewise for d, spn_edge[2 idet..] the detector's
+ * weights of bins 0 and ns/2; g_old / g_new per tile [idet][iseg].  Returns
+ * SG_ERR_NOT_CONVERGED when the new gains have no positive mean. */
+int sg_gains_from_sums(long ndet, long nseg, int per_detector, const double *dots_ds,
+                       const double *dots_ss, const double *edges_s, const double *edges_d,
+                       const double *spn_edge, const double *g_old, double *g_new);
+
 /* Number of observed pixels (npix, sanepic.cc:915). */
 long sg_npix(const sg_ctx *ctx);
 /* 1 if the operator runs per offset group (detectors with identical

@@ -40,7 +40,7 @@ EXPORTS = ["sg_create", "sg_set_stream", "sg_set_pointing", "sg_set_noise", "sg_
            "sg_get_pixels", "sg_get_indpix", "sg_get_crit_history", "sg_profile_operator",
            "sg_learn_train", "sg_learn_nparams", "sg_learn_get_params", "sg_learn_set_params",
            "sg_coarse_from_gram", "sg_mlp_gemm_host", "sg_mlp_grad_host", "sg_solve_batch",
-           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes", "sg_set_gains", "sg_fit_gains", "sg_set_noise_all", "sg_set_tod_all",
+           "sg_autotune", "sg_set_pol_rcond", "sg_tile_shapes", "sg_set_gains", "sg_fit_gains", "sg_set_noise_all", "sg_set_tod_all", "sg_gains_from_sums",
            "sg_last_error", "sg_destroy"]
 
 
@@ -130,6 +130,8 @@ def load_library(path: Optional[str] = None):
     L.sg_rhs.argtypes = [c_p, dp]
     L.sg_set_gains.argtypes = [c_p, dp]
     L.sg_fit_gains.argtypes = [c_p, ctypes.c_int, dp, dp, dp]
+    L.sg_gains_from_sums.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, dp, dp, dp, dp,
+                                     dp, dp, dp]
     L.sg_npix.argtypes = [c_p]
     L.sg_npix.restype = ctypes.c_long
     L.sg_group_mode.argtypes = [c_p, ctypes.POINTER(ctypes.c_long)]
@@ -457,6 +459,21 @@ def from_problem(prob, precision: Optional[str] = None, device: int = 0,
         if with_tod and "tod" in prob:
             mm.set_tod(d, prob["tod"][d])
     return mm
+
+
+def gains_from_sums(dots_ds, dots_ss, edges_s, edges_d, spn_edge, g_old, per_detector=False):
+    """sg_fit_gains' host arithmetic on given per-tile sums (no GPU): arrays
+    [ndet][nseg] (edges [ndet][nseg][2], spn_edge [ndet][2]); returns the new
+    gains [ndet][nseg]."""
+    g_old = _f64(g_old)
+    ndet, nseg = g_old.shape
+    out = np.empty_like(g_old)
+    args = [_f64(a) for a in (dots_ds, dots_ss, edges_s, edges_d, spn_edge)]
+    rc = load_library().sg_gains_from_sums(ndet, nseg, int(per_detector), *[_dp(a) for a in args],
+                                           _dp(g_old), _dp(out))
+    if rc != SG_OK:
+        raise SanepicError(rc, "no positive mean gain")
+    return out
 
 
 # ---- tensor-core GEMM and network gradients on host arrays (tests, measurements) ----

@@ -187,6 +187,49 @@ cudaError_t chi2_of(sg_ctx* c, const DevBuf* g, double* out) {
 
 }  // namespace
 
+extern "C" int sg_gains_from_sums(long ndet, long nseg, int per_detector, const double* dots_ds,
+                                  const double* dots_ss, const double* edges_s,
+                                  const double* edges_d, const double* spn_edge,
+                                  const double* g_old, double* g_new) {
+  if (ndet < 1 || nseg < 1 || !dots_ds || !dots_ss || !edges_s || !edges_d || !spn_edge || !g_old ||
+      !g_new)
+    return SG_ERR_ARG;
+  const long long nt = (long long)ndet * nseg;
+  // the half-spectrum sums (bins 0 and ns/2 counted twice, as the reference)
+  std::vector<double> bd(nt), cs(nt);
+  for (long long t = 0; t < nt; t++) {
+    const long long d = t / nseg;
+    const double w0 = spn_edge[2 * d], wm = spn_edge[2 * d + 1];
+    const double s0 = edges_s[2 * t], sm = edges_s[2 * t + 1];
+    const double d0 = edges_d[2 * t], dm = edges_d[2 * t + 1];
+    bd[t] = dots_ds[t] + w0 * s0 * d0 + wm * sm * dm;
+    cs[t] = dots_ss[t] + w0 * s0 * s0 + wm * sm * sm;
+  }
+  if (per_detector) {  // -R: one gain per detector (sanepic.cc:2254-2271)
+    for (long long d = 0; d < ndet; d++) {
+      double zeta = 0.0, gamma = 0.0;
+      for (long long s = 0; s < nseg; s++) {
+        zeta += bd[d * nseg + s];
+        gamma += cs[d * nseg + s];
+      }
+      for (long long s = 0; s < nseg; s++)
+        g_new[d * nseg + s] = gamma > 0.0 ? zeta / gamma : g_old[d * nseg + s];
+    }
+  } else {
+    for (long long t = 0; t < nt; t++) g_new[t] = cs[t] > 0.0 ? bd[t] / cs[t] : g_old[t];
+  }
+  // the mean gain held at that of the gains the map was made with
+  double m0 = 0.0, m1 = 0.0;
+  for (long long t = 0; t < nt; t++) {
+    m0 += g_old[t];
+    m1 += g_new[t];
+  }
+  if (!(m1 > 0.0 && std::isfinite(m1))) return SG_ERR_NOT_CONVERGED;
+  const double f = m0 / m1;
+  for (long long t = 0; t < nt; t++) g_new[t] *= f;
+  return SG_OK;
+}
+
 extern "C" int sg_set_gains(sg_ctx* c, const double* gains) {
   if (!c) return SG_ERR_ARG;
   const long long nd = c->ndet, nsg = c->nseg, nt = nd * nsg;
@@ -273,41 +316,11 @@ extern "C" int sg_fit_gains(sg_ctx* c, int per_detector, double* gains_out, doub
     e = cudaMemcpyAsync(h.data(), dots, sizeof(double) * 6 * nt, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return c->cuda_fail(e, "gain fit");
-  // the half-spectrum sums (bins 0 and ns/2 counted twice, as the reference)
-  std::vector<double> bd(nt), cs(nt);
-  for (long long t = 0; t < nt; t++) {
-    const long long d = t / nsg;
-    const double w0 = c->spn_edge[2 * d], wm = c->spn_edge[2 * d + 1];
-    const double s0 = h[2 * nt + 2 * t], sm = h[2 * nt + 2 * t + 1];
-    const double d0 = h[4 * nt + 2 * t], dm = h[4 * nt + 2 * t + 1];
-    bd[t] = h[t] + w0 * s0 * d0 + wm * sm * dm;
-    cs[t] = h[nt + t] + w0 * s0 * s0 + wm * sm * sm;
-  }
-  const std::vector<double>& g0 = c->gains_h;
   std::vector<double> g(nt);
-  if (per_detector) {  // -R: one gain per detector (sanepic.cc:2254-2271)
-    for (long long d = 0; d < nd; d++) {
-      double zeta = 0.0, gamma = 0.0;
-      for (long long s = 0; s < nsg; s++) {
-        zeta += bd[d * nsg + s];
-        gamma += cs[d * nsg + s];
-      }
-      for (long long s = 0; s < nsg; s++)
-        g[d * nsg + s] = gamma > 0.0 ? zeta / gamma : g0[d * nsg + s];
-    }
-  } else {
-    for (long long t = 0; t < nt; t++) g[t] = cs[t] > 0.0 ? bd[t] / cs[t] : g0[t];
-  }
-  double m0 = 0.0, m1 = 0.0;
-  for (long long t = 0; t < nt; t++) {
-    m0 += g0[t];
-    m1 += g[t];
-  }
-  if (!(m1 > 0.0 && std::isfinite(m1)))
-    return c->fail(SG_ERR_NOT_CONVERGED, "gain fit: mean gain %g (the map does not fit the data)",
-                   m1 / (double)nt);
-  const double f = m0 / m1;
-  for (long long t = 0; t < nt; t++) g[t] *= f;
+  if (sg_gains_from_sums(nd, nsg, per_detector, h.data(), h.data() + nt, h.data() + 2 * nt,
+                         h.data() + 4 * nt, c->spn_edge.data(), c->gains_h.data(), g.data()) != SG_OK)
+    return c->fail(SG_ERR_NOT_CONVERGED,
+                   "gain fit: no positive mean gain (the map does not fit the data)");
   // chi^2 with the gains the map was made with, and with the new ones
   double x2b = 0.0, x2a = 0.0;
   DevBuf gnew;

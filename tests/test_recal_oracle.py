@@ -107,3 +107,49 @@ def test_corrected_loop_recovers_the_injected_gains(per_detector):
     # below 0.5 %, the noise floor of this problem
     ratio = g.T / gtrue
     assert np.std(ratio / ratio.mean()) < 0.005
+
+
+def tile_sums(s, x, tod):
+    """The per-tile sums sg_fit_gains forms on the GPU, here on the host from
+    the oracle's pieces: (N^-1 d)^T s and (N^-1 s)^T s in the time domain
+    (s = P x), and the bins 0 and ns/2 of s and d."""
+    import ctypes
+    L = oracle.lib()
+    ns, nseg, ndet = s.ns, s.nseg, s.ndet
+    dots_ds = np.empty((ndet, nseg))
+    dots_ss = np.empty((ndet, nseg))
+    edges_s = np.empty((ndet, nseg, 2))
+    edges_d = np.empty((ndet, nseg, 2))
+    sign = np.where(np.arange(ns) % 2 == 0, 1.0, -1.0)
+    xs = np.ascontiguousarray(x, np.float64)
+    for d in range(ndet):
+        for g in range(nseg):
+            off = ns * g + ns * nseg * d
+            pv = np.empty(ns)
+            L.orc_deproject(oracle._pd(xs), oracle._pl(s.indpix),
+                            oracle._pl(np.ascontiguousarray(s.pix[off:off + ns])),
+                            oracle._pd(np.ascontiguousarray(s.psip[off:off + ns])),
+                            ctypes.c_long(ns), ctypes.c_long(s.npix), oracle._pd(pv))
+            dv = tod[off:off + ns]
+            dots_ds[d, g] = s.noise_filter(d, dv) @ pv
+            dots_ss[d, g] = s.noise_filter(d, pv) @ pv
+            edges_s[d, g] = (pv.sum(), sign @ pv)
+            edges_d[d, g] = (dv.sum(), sign @ dv)
+    spn_edge = np.stack([s.spn[np.arange(ndet) * ns], s.spn[np.arange(ndet) * ns + ns // 2]], 1)
+    return dots_ds, dots_ss, edges_s, edges_d, spn_edge
+
+
+@pytest.mark.parametrize("per_detector", [False, True])
+def test_library_gain_arithmetic_matches_the_oracle_fit(per_detector):
+    """the library's host arithmetic (sg_gains_from_sums) on time-domain sums
+    plus the bins 0 and ns/2 gives the oracle's half-spectrum fit"""
+    import sanepic_gb300 as sg
+    prob, a1, _ = recal_problem()
+    s = oracle.Setup(prob)
+    tod = prob["tod"].reshape(-1)
+    spec = prob["spec"]
+    g0 = 1.0 + 0.01 * np.random.default_rng(7).standard_normal((spec.nseg, spec.ndet))
+    want, _, _ = s.fit_gains(a1, tod, g0, per_detector=per_detector)  # [nseg][ndet]
+    sums = tile_sums(s, a1, tod)
+    got = sg.gains_from_sums(*sums, g0.T, per_detector=per_detector)  # [ndet][nseg]
+    np.testing.assert_allclose(got.T, want, rtol=1e-12)
