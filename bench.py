@@ -137,6 +137,19 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(sec, device):
+    """The slowest rank's time: every rank runs its own replica of the
+    workload (the path has no exchange step), and the job takes as long as
+    its slowest replica.  One process: sec itself."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return sec
+    t = torch.tensor([sec], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 def run_ours(args):
     import torch
@@ -205,11 +218,7 @@ def run_ours(args):
         launches = mm.kernel_launches() - launches0
         torch.cuda.nvtx.range_pop()
         barrier()
-        sec = ev0.elapsed_time(ev1) / args.steps / 1e3
-        if world > 1:
-            t = torch.tensor([sec], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            sec = float(t.item())
+        sec = max_over_ranks(ev0.elapsed_time(ev1) / args.steps / 1e3, "cuda")
         return sec, reps, launches
 
     # ---- value: inputs resident, CUDA events on the launching stream -------
