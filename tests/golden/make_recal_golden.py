@@ -2,19 +2,18 @@
 
 Runs the UNMODIFIED reference (patanch/SANEPIC src/sanepic.cc, built by
 `make -C oracle ref` against the project-written FFTW/MPI shims) with -r 1
-and with -r 1 -R 1 on the 4-detector NSIDE-16 golden problem whose
-(detector, segment) timelines were multiplied by gains 1 + 0.02 N(0, 1)
-(numpy default_rng(1), shape [ndet][nseg]), with all-zero orbital-dipole
-timelines (the reference reads orbdip_<detector> whenever -r is set,
-sanepic.cc:702-712), and stores what its first gain fit prints before its
-loop diverges:
+and with -r 1 -R 1 on golden problems (the 4-detector NSIDE-16 one, and the
+2-detector one with a half-wave plate) whose (detector, segment) timelines
+were multiplied by gains 1 + 0.02 N(0, 1) (numpy default_rng(1), shape
+[ndet][nseg]), with all-zero orbital-dipole timelines (the reference reads
+orbdip_<detector> whenever -r is set, sanepic.cc:702-712), and stores what
+its first gain fit prints before its loop diverges:
 
-  recal_4det_nside16_ref.npz   A_1: the compact map of its first loop
-                               (map_A_..._1, made with gains 1), and the
-                               gains applied to the timelines
-  recal_4det_nside16_ref.json  per run: the first "Before recal chi2",
-                               "After recal chi2" and (-R) the ndet
-                               "Coef calib det" lines
+  recal_<tag>_ref.npz   A_1: the compact map of its first loop
+                        (map_A_..._1, made with gains 1), and the gains
+                        applied to the timelines
+  recal_<tag>_ref.json  per run: the first "Before recal chi2", "After
+                        recal chi2" and (-R) the ndet "Coef calib det" lines
 
 Usage (needs the reference checkout, this container only):
     python tests/golden/make_recal_golden.py --ref-src <checkout>/src/sanepic.cc
@@ -39,13 +38,15 @@ sys.path.insert(0, os.path.dirname(HERE))
 from golden_util import load_problem  # noqa: E402
 from sanepic_gb300 import synth  # noqa: E402
 
-NAME = "golden_4det_nside16"
+# fixture tag -> golden problem
+PROBLEMS = {"4det_nside16": "golden_4det_nside16",
+            "2det_nside16_hwp": "golden_2det_nside16_hwp"}
 NPROC = 3  # 1 master + 2 workers, as the other golden runs
 
 
-def recal_problem():
+def recal_problem(name="golden_4det_nside16"):
     """The golden problem with its timelines times the seeded gains."""
-    prob = load_problem(NAME)
+    prob = load_problem(name)
     spec = prob["spec"]
     g = 1.0 + 0.02 * np.random.default_rng(1).standard_normal((spec.ndet, spec.nseg))
     tod = prob["tod"].copy()
@@ -90,18 +91,19 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref",
                            f"REFERENCE_SRC={a.ref_src}"])
     exe = os.path.join(ROOT, "oracle", "_ref", "sanepic")
-    prob, g = recal_problem()
-    a_tile, tile = run(prob, exe, ["-r", "1"])
-    a_det, det = run(prob, exe, ["-r", "1", "-R", "1"])
-    if not np.array_equal(a_tile, a_det):
-        raise RuntimeError("the first loop's map differs between the two runs")
-    np.savez_compressed(os.path.join(HERE, "recal_4det_nside16_ref.npz"), A_1=a_tile, gains=g)
-    with open(os.path.join(HERE, "recal_4det_nside16_ref.json"), "w") as f:
-        json.dump({"problem": NAME, "gain_seed": 1, "gain_sigma": 0.02, "nproc": NPROC,
-                   "per_tile": tile, "per_detector": det,
-                   "generator": "tests/golden/make_recal_golden.py"}, f, indent=1)
-    print("per tile", tile)
-    print("per detector", det)
+    for tag, name in PROBLEMS.items():
+        prob, g = recal_problem(name)
+        a_tile, tile = run(prob, exe, ["-r", "1"])
+        a_det, det = run(prob, exe, ["-r", "1", "-R", "1"])
+        if not np.array_equal(a_tile, a_det):
+            raise RuntimeError("the first loop's map differs between the two runs")
+        np.savez_compressed(os.path.join(HERE, f"recal_{tag}_ref.npz"), A_1=a_tile, gains=g)
+        with open(os.path.join(HERE, f"recal_{tag}_ref.json"), "w") as f:
+            json.dump({"problem": name, "gain_seed": 1, "gain_sigma": 0.02, "nproc": NPROC,
+                       "per_tile": tile, "per_detector": det,
+                       "generator": "tests/golden/make_recal_golden.py"}, f, indent=1)
+        print(tag, "per tile", tile)
+        print(tag, "per detector", det)
 
 
 if __name__ == "__main__":

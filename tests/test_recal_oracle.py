@@ -1,7 +1,7 @@
 """The oracle's gain recalibration (sanepic.cc:2123-2316, 3206-3260) against
-the reference's own first gain fit (tests/golden/recal_4det_nside16_ref.*,
-made by tests/golden/make_recal_golden.py), and its corrected outer loop on a
-problem with known gains.
+the reference's own first gain fit (tests/golden/recal_*_ref.*, made by
+tests/golden/make_recal_golden.py: 4 detectors, and 2 with a half-wave
+plate), and its corrected outer loop on a problem with known gains.
 
 The reference's fit returns four times the least-squares gain (sPNd carries
 a factor 2, cPNPc a factor 1/2); the fixture's numbers are checked with that
@@ -19,9 +19,12 @@ from sanepic_gb300 import synth
 REF_FACTOR = 4.0  # sanepic.cc:2196-2201 (x 2) over 2217-2220 (x 1/2)
 
 
-def recal_problem():
-    z = np.load(os.path.join(GOLDEN_DIR, "recal_4det_nside16_ref.npz"))
-    with open(os.path.join(GOLDEN_DIR, "recal_4det_nside16_ref.json")) as f:
+RECAL_TAGS = ["4det_nside16", "2det_nside16_hwp"]
+
+
+def recal_problem(tag="4det_nside16"):
+    z = np.load(os.path.join(GOLDEN_DIR, f"recal_{tag}_ref.npz"))
+    with open(os.path.join(GOLDEN_DIR, f"recal_{tag}_ref.json")) as f:
         log = json.load(f)
     prob = load_problem(log["problem"])
     spec = prob["spec"]
@@ -34,8 +37,9 @@ def recal_problem():
     return prob, z["A_1"], log
 
 
-def test_gain_fit_matches_the_references_first_fit():
-    prob, a1, log = recal_problem()
+@pytest.mark.parametrize("tag", RECAL_TAGS)
+def test_gain_fit_matches_the_references_first_fit(tag):
+    prob, a1, log = recal_problem(tag)
     spec = prob["spec"]
     s = oracle.Setup(prob)
     tod = prob["tod"].reshape(-1)
