@@ -13,7 +13,7 @@ import oracle
 import sanepic_gb300 as sg
 from golden_util import rel_rms
 from sanepic_gb300 import build, synth
-from test_recal_oracle import REF_FACTOR, recal_loop, recal_problem
+from test_recal_oracle import RECAL_TAGS, REF_FACTOR, recal_loop, recal_problem
 
 pytestmark = pytest.mark.gpu
 
@@ -34,11 +34,12 @@ def comp_err(x, y, npix):
                        remove_monopole=(c == 0)) for c in range(3))
 
 
-def test_first_fit_vs_reference():
+@pytest.mark.parametrize("tag", RECAL_TAGS)
+def test_first_fit_vs_reference(tag):
     """the map of the first loop (gains 1) and the fit to it: chi^2 before as
     the reference prints it, the per-detector coefficients it prints (/4,
     normalised to mean 1), and the oracle's fit to the GPU's own map"""
-    prob, a1, log = recal_problem()
+    prob, a1, log = recal_problem(tag)
     spec = prob["spec"]
     tod = prob["tod"].reshape(-1)
     mm = sg.from_problem(prob, precision="f64")
