@@ -772,6 +772,12 @@ int build_bj3(sg_ctx* c) {
                              c->gconst.as<double>(), c->polmask.as<int>(), 0.0, nullptr,
                              c->minv.as<double>(), c->st);
   }
+  if (e == cudaSuccess && c->f32) {
+    e = c->minv32.alloc(sizeof(float) * 6 * c->npix);
+    if (e == cudaSuccess) e = to_f32_launch(c->minv.as<double>(), c->minv32.as<float>(),
+                                            6 * c->npix, c->st);
+    c->launches++;
+  }
   if (e != cudaSuccess) return c->cuda_fail(e, "bj3 build");
   c->have_bj3 = true;
   return SG_OK;

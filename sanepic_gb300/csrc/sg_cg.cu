@@ -82,6 +82,21 @@ __device__ __forceinline__ void store_map(T* dmap, long long m, double a, double
   dmap[4 * m + 3] = (T)0;
 }
 
+__global__ void __launch_bounds__(256) k_to_f32(const double* __restrict__ in,
+                                                float* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+cudaError_t to_f32_launch(const double* in, float* out, long long n, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152LL * 16) blocks = 152LL * 16;
+  if (blocks < 1) return cudaSuccess;
+  k_to_f32<<<(unsigned)blocks, 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
+}
+
 // ---- init: r = b - r (r holds the masked A x0), z = M r, d = z ------------
 __global__ void __launch_bounds__(kCgThreads) k_init_a(CgVecs v) {
   const long long n = v.npix;
@@ -649,8 +664,11 @@ __device__ __forceinline__ void coarse_solve_block(const float2* __restrict__ pa
 
 // c = E^-1 U^T r (from part1); z = M (r - AU c); block 0 keeps c in coef;
 // part2[k][block] = partial sums of AU[i][k] z[i] (the rows are read once for
-// both: the second use hits L1)
-template <int KP>
+// both: the second use hits L1).  With the FP32 blocks (FP32 operators),
+// r - AU c and M_bj3 run on the FP32 pipe: GB300's FP64 pipe had bounded
+// this kernel (18 FP64 instructions a pixel, 6 this way), and flexible PCG
+// takes the FP32-rounded preconditioner as it is (its residual stays FP64).
+template <int KP, bool M32>
 __global__ void __launch_bounds__(kCgThreads, 2)
     k_coarse_pre(CgVecs v, const uint16_t* __restrict__ AU, const float2* __restrict__ part1,
                  const double* __restrict__ einv, int kc, double* coef, float2* part2) {
@@ -669,6 +687,7 @@ __global__ void __launch_bounds__(kCgThreads, 2)
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
        m += (long long)gridDim.x * blockDim.x) {
     double t[3];
+    float tf[3];
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
@@ -681,15 +700,28 @@ __global__ void __launch_bounds__(kCgThreads, 2)
 #pragma unroll
         for (int t2 = 0; t2 < 8; t2++) s = fmaf(a[t2], c[8 * q + t2], s);
       }
-      t[cc] = v.r[i] - (double)s;
+      if constexpr (M32)
+        tf[cc] = (float)v.r[i] - s;
+      else
+        t[cc] = v.r[i] - (double)s;
     }
     double z[3];
-    apply_m(v, m, t[0], t[1], t[2], z[0], z[1], z[2]);
+    float zq[3];
+    if constexpr (M32) {
+      const float* o = v.minv32;  // 00 01 02 11 12 22
+      const float o00 = o[m], o01 = o[n + m], o02 = o[2 * n + m];
+      const float o11 = o[3 * n + m], o12 = o[4 * n + m], o22 = o[5 * n + m];
+      zq[0] = fmaf(o00, tf[0], fmaf(o01, tf[1], o02 * tf[2]));
+      zq[1] = fmaf(o01, tf[0], fmaf(o11, tf[1], o12 * tf[2]));
+      zq[2] = fmaf(o02, tf[0], fmaf(o12, tf[1], o22 * tf[2]));
+    } else {
+      apply_m(v, m, t[0], t[1], t[2], z[0], z[1], z[2]);
+    }
 #pragma unroll
     for (int cc = 0; cc < 3; cc++) {
       const long long i = cc * n + m;
-      v.z[i] = z[cc];
-      const float zf = (float)z[cc];
+      v.z[i] = M32 ? (double)zq[cc] : z[cc];
+      const float zf = M32 ? zq[cc] : (float)z[cc];
       const uint4* row = reinterpret_cast<const uint4*>(AU + i * KP);
 #pragma unroll
       for (int q = 0; q < KP / 8; q++) {
@@ -764,8 +796,12 @@ static cudaError_t coarse_apply_kp(const CgVecs& v, const CoarseSpace& cs, int f
   float2* part1 = reinterpret_cast<float2*>(cs.part);  // same 8 bytes per partial
   float2* part2 = part1 + (size_t)kCoarseMax * kCgBlocks;
   k_coarse_dots<KP><<<kCgBlocks, kCgThreads, 0, st>>>(cs.u, n3, v.r, part1);
-  k_coarse_pre<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc, cs.coef,
-                                                      part2);
+  if (v.minv32 && v.precond == 1)
+    k_coarse_pre<KP, true><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc,
+                                                             cs.coef, part2);
+  else
+    k_coarse_pre<KP, false><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.au, part1, cs.einv, cs.kc,
+                                                              cs.coef, part2);
   k_coarse_post<KP><<<kCgBlocks, kCgThreads, 0, st>>>(v, cs.u, part2, cs.einv, cs.kc, cs.coef,
                                                        flexible);
   return cudaGetLastError();

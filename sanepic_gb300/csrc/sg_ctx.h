@@ -95,6 +95,7 @@ struct sg_ctx {
   DevBuf grp_off, grp_det, dcs, ys, gconst;
   DevBuf filt, tw_lo, tw_hi, g0, ntab;
   DevBuf x, r, d, q, z, rprev, b, minv, mdiag, mp_raw, part, sc, dmap;
+  DevBuf minv32;  // FP32 operators: the bj3 blocks in FP32 as well
   DevBuf chi2p;  // per-CTA chi^2 partials of the noise filter
   // offset-group operator (sg_group.cu): used when every group has at least
   // kGroupMin detectors; gtl [G][3][nsd], gspec [G][3][nseg][M+1] complex,
@@ -668,6 +669,7 @@ struct sg_ctx {
     v.rprev = rprev.as<double>();
     v.b = b.as<double>();
     v.minv = minv.as<double>();
+    v.minv32 = f32 ? minv32.as<float>() : nullptr;
     v.mdiag = mdiag.as<double>();
     v.hits_true = polmask.as<int>();
     v.precond = precond;

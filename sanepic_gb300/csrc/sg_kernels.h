@@ -284,6 +284,9 @@ struct CgVecs {
   double* rprev;        // flexible PCG: previous residual (or nullptr)
   const double* b;
   const double* minv;   // bj3 [6][npix] (00 01 02 11 12 22)
+  // the same blocks in FP32 (FP32 operators only, else null): the coarse
+  // space's pre-smoothing applies M_bj3 on the FP32 pipe (flexible PCG)
+  const float* minv32;
   const double* mdiag;  // reference diagonal, inverted [3][npix]
   const int* hits_true;
   int precond;          // 0 diag, 1 bj3, 2 z supplied externally
@@ -297,6 +300,8 @@ cudaError_t cg_step_a(const CgVecs& v, cudaStream_t st);  // partial q.d
 cudaError_t cg_step_b(const CgVecs& v, int refresh, int flexible, cudaStream_t st);
 // refresh: r = b - q, or r = q when q already holds the residual (direct)
 cudaError_t cg_refresh_r(const CgVecs& v, int flexible, int direct, cudaStream_t st);
+// out[i] = (float)in[i]
+cudaError_t to_f32_launch(const double* in, float* out, long long n, cudaStream_t st);
 // out = 2 * sum of n per-CTA chi^2 partials (fixed order)
 cudaError_t chi2_sum(const double* part, int n, double* out, cudaStream_t st);
 cudaError_t cg_dots(const CgVecs& v, int flexible, cudaStream_t st);
