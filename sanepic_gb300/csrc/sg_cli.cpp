@@ -58,6 +58,7 @@ void usage(const char* prog) {
           "          -k <iSpf prefix> -u <iSpf length> -N <nside> -p 1 -O <output prefix>\n"
           "          -e <output id> [-h <hwp> -w <hwp rad/sample>] [-I <start map>]\n"
           "          [-i <write iteration maps> -j <every>] [-P <pointing suffix>]\n"
+          "          [-r 1 [-R 1]]  gain recalibration loop (per tile; -R: per detector)\n"
           "environment: SANEPIC_GPU_PRECISION=f64|f32  SANEPIC_GPU_PRECOND=diag|bj3\n"
           "             SANEPIC_GPU_DEVICE=<ordinal>   SANEPIC_GPU_STOP=<crit>\n"
           "             SANEPIC_GPU_POL_RCOND=<min reciprocal condition of a pixel's Q/U>\n",
