@@ -157,3 +157,69 @@ def test_library_gain_arithmetic_matches_the_oracle_fit(per_detector):
     sums = tile_sums(s, a1, tod)
     got = sg.gains_from_sums(*sums, g0.T, per_detector=per_detector)  # [ndet][nseg]
     np.testing.assert_allclose(got.T, want, rtol=1e-12)
+
+
+def test_operator_with_gains_is_the_tile_sum():
+    """the oracle's operator with gains (every tile a one-segment detector
+    with weights g^2 spn) equals sum_t P_t^T g_t^2 N_d^-1 P_t written out
+    tile by tile from the oracle's pieces; b likewise with g"""
+    import ctypes
+    spec = synth.ProblemSpec("t", ndet=2, nside=8, nseg=3, ns=512, fknee=0.05, alpha=1.0,
+                             problem=9)
+    prob = synth.make_problem(spec)
+    s = oracle.Setup(prob)
+    L = oracle.lib()
+    rng = np.random.default_rng(3)
+    g = 1.0 + 0.1 * rng.standard_normal((spec.nseg, spec.ndet))  # [seg][det]
+    x = rng.standard_normal(3 * s.npix)
+    tod = np.ascontiguousarray(prob["tod"], np.float64).reshape(-1)
+    ns = spec.ns
+    want_a = np.zeros(3 * s.npix)
+    want_b = np.zeros(3 * s.npix)
+    for d in range(spec.ndet):
+        for sg_ in range(spec.nseg):
+            off = ns * sg_ + ns * spec.nseg * d
+            pix = np.ascontiguousarray(s.pix[off:off + ns])
+            psip = np.ascontiguousarray(s.psip[off:off + ns])
+            pv = np.empty(ns)
+            L.orc_deproject(oracle._pd(x), oracle._pl(s.indpix), oracle._pl(pix),
+                            oracle._pd(psip), ctypes.c_long(ns), ctypes.c_long(s.npix),
+                            oracle._pd(pv))
+            gt = g[sg_, d]
+            ya = gt * gt * s.noise_filter(d, pv)
+            yb = gt * s.noise_filter(d, np.ascontiguousarray(tod[off:off + ns]))
+            for y, acc in ((ya, want_a), (yb, want_b)):
+                y = np.ascontiguousarray(y)
+                L.orc_backproject(oracle._pd(acc), oracle._pl(s.indpix), oracle._pl(pix),
+                                  oracle._pd(psip), ctypes.c_long(ns), ctypes.c_long(s.npix),
+                                  oracle._pd(y))
+    np.testing.assert_allclose(s.apply_gains(x, g), want_a, rtol=1e-12,
+                               atol=1e-12 * np.abs(want_a).max())
+    np.testing.assert_allclose(s.rhs_gains(tod, g), want_b, rtol=1e-12,
+                               atol=1e-12 * np.abs(want_b).max())
+    # gains 1: the operator without gains
+    ones = np.ones_like(g)
+    np.testing.assert_allclose(s.apply_gains(x, ones), s.apply(x), rtol=1e-12,
+                               atol=1e-12 * np.abs(want_a).max())
+
+
+def test_gain_arithmetic_edge_cases():
+    """a tile without signal keeps its gain; no positive mean is an error"""
+    import sanepic_gb300 as sg
+    nd, nsg = 2, 3
+    z2 = np.zeros((nd, nsg, 2))
+    spn = np.zeros((nd, 2))
+    g0 = np.full((nd, nsg), 1.2)
+    bd = np.full((nd, nsg), 2.0)
+    cs = np.full((nd, nsg), 1.0)
+    cs[1, 2] = 0.0  # no signal in this tile
+    got = sg.gains_from_sums(bd, cs, z2, z2, spn, g0)
+    # raw gains 2 (and the old 1.2 where c = 0), scaled to mean 1.2
+    raw = np.full((nd, nsg), 2.0)
+    raw[1, 2] = 1.2
+    np.testing.assert_allclose(got, raw * (1.2 / raw.mean()), rtol=1e-15)
+    # -R sums a detector's segments
+    got_d = sg.gains_from_sums(bd, cs, z2, z2, spn, g0, per_detector=True)
+    assert np.ptp(got_d, axis=1).max() == 0.0
+    with pytest.raises(sg.SanepicError):
+        sg.gains_from_sums(-bd, cs, z2, z2, spn, g0)
