@@ -285,6 +285,37 @@ class MapMaker:
                                         ctypes.byref(a)))
         return g.reshape(self.nseg, self.ndet), b.value, a.value
 
+    def recalibrate(self, precond: str = "bj3", stop_crit: float = 1e-15, maxiter: int = 2000,
+                    per_detector: bool = False, max_loops: int = 499) -> dict:
+        """The reference's -r (-R: per_detector) outer loop (sanepic.cc:1041-1042,
+        2123-2316), as the drop-in executable runs it: make the map with gains
+        1, fit the gains to it, make the map again from the previous one with
+        the new gains, until a loop starts already converged (its var0 / var00
+        at most stop_crit, var00 of the first loop) or after max_loops loops.
+        Returns the last fitted gains [nseg][ndet], the loops made, chi^2
+        (before, after) of every fit and the iterations of every solve; the
+        map is the last loop's."""
+        self.set_gains(None)
+        self.rhs(chi2=False)
+        rep = self.solve(precond=precond, stop_crit=stop_crit, maxiter=maxiter)
+        var00 = rep["var00"]
+        ratio = rep["crit0"]
+        chi2, iters = [], [rep["iterations"]]
+        loops = 1
+        while True:
+            g, before, after = self.fit_gains(per_detector)
+            chi2.append((before, after))
+            if not (loops < max_loops and ratio > stop_crit):
+                break
+            loops += 1
+            self.set_gains(g)
+            self.rhs(chi2=False)
+            rep = self.solve(precond=precond, stop_crit=stop_crit, maxiter=maxiter,
+                             x0=self.solution())
+            ratio = rep["crit0"] * rep["var00"] / var00
+            iters.append(rep["iterations"])
+        return {"gains": g, "loops": loops, "chi2": chi2, "iterations": iters}
+
     # ---- operator -----------------------------------------------------------
     def rhs(self, chi2: bool = True) -> Optional[float]:
         """b = P^T N^-1 d; returns chi2_0, or None with chi2=False (then groups

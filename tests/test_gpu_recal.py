@@ -141,6 +141,25 @@ def test_recalibration_loop_vs_oracle(prec):
     assert all(b <= a * (1 + 1e-9) for a, b in zip(chi, chi[1:]))
 
 
+def test_recalibrate_loop_of_the_python_api():
+    """MapMaker.recalibrate: the outer loop with its stop rule, loop by loop
+    the oracle's (six loops here, the rule does not stop it earlier)"""
+    spec = synth.ProblemSpec("recal_4det_nside16", ndet=4, nside=16, nseg=8, ns=2048,
+                             fknee=0.02, alpha=1.0, problem=5, sigma_uk=5.0)
+    prob = synth.make_problem(spec)
+    gtrue = 1.0 + 0.02 * np.random.default_rng(2).standard_normal((4, 8))
+    tod = prob["tod"].copy()
+    for d in range(4):
+        for sgi in range(8):
+            tod[d, sgi * spec.ns:(sgi + 1) * spec.ns] *= gtrue[d, sgi]
+    mm = sg.from_problem(dict(prob, tod=tod), precision="f64")
+    out = mm.recalibrate(precond="diag", stop_crit=1e-15, max_loops=6)
+    assert out["loops"] == 6 and len(out["chi2"]) == 6 and len(out["iterations"]) == 6
+    g_o, hist_o = recal_loop(prob, gtrue, 6)
+    np.testing.assert_allclose(out["gains"], g_o, rtol=1e-7)
+    np.testing.assert_allclose(np.array(out["chi2"]), np.array(hist_o), rtol=1e-7)
+
+
 def test_gain_arguments_and_learned_part_refused():
     prob = problem(2, nseg=2, ns=2048)
     mm = sg.from_problem(prob, precision="f64")
