@@ -20,7 +20,7 @@
 // absrecal turns NaN):
 //  * sPNd carries a factor 2 and cPNPc a factor 1/2 (sanepic.cc:2196-2201,
 //    2217-2220), so each of its fits returns four times the gain; here both
-//    are the quadratic forms of N^-1 in the time domain;
+//    sums carry the same factor (below);
 //  * absrecal divides by gamma_all, which only -R fills (997-998, 2254-2271):
 //    here the mean of the new gains is scaled to the mean of the old ones in
 //    closed form instead of its fixed-point reruns;
